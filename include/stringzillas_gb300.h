@@ -1,0 +1,406 @@
+/**
+ *  @file include/stringzillas_gb300.h
+ *  @brief C-ABI of the GB300 batched scoring engine: a drop-in for StringZillas' `szs_*` scoring path.
+ *
+ *  The declarations below keep the reference's names, argument order, argument meaning, status codes and ownership
+ *  rules, so a program (or FFI binding) written against the reference's `include/stringzillas/stringzillas.h`
+ *  links against `libszs_gb300.so` unchanged. Each declaration cites the reference line it replaces.
+ *
+ *  Scope of the engine: Levenshtein distances, Needleman-Wunsch global scores and Smith-Waterman local scores over
+ *  bytes, with linear or affine gaps and a class-folded int8 substitution table, computed on an NVIDIA GB300
+ *  (sm_103a). There is no CPU backend: a CPU-cores scope is rejected with `sz_device_code_mismatch_k`, exactly as
+ *  the reference rejects a CPU scope for a CUDA engine (`c/stringzillas/levenshtein.cuh:60-90`).
+ *
+ *  Inputs and outputs may live in host memory (pageable or pinned), device memory or managed memory; the engine
+ *  stages whatever is not device-resident. Engines are not thread-safe (one call at a time per engine, as in the
+ *  reference); scopes may be driven from any thread.
+ *
+ *  Functions under "Extensions" have no counterpart in the reference; each says so.
+ */
+#ifndef STRINGZILLAS_GB300_H_
+#define STRINGZILLAS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define SZS_GB300_API __declspec(dllexport)
+#else
+#define SZS_GB300_API __attribute__((visibility("default")))
+#endif
+
+/*  Core types. Layout-identical to `include/stringzilla/types.h` of the reference (lines cited); skipped when the
+ *  reference's own types header was included first, so both headers can coexist in one translation unit. */
+#ifndef STRINGZILLA_TYPES_H_
+typedef int8_t sz_i8_t;                /* types.h:530 */
+typedef uint8_t sz_u8_t;               /* types.h:531 */
+typedef uint32_t sz_u32_t;             /* types.h:535 */
+typedef uint64_t sz_u64_t;             /* types.h:536 */
+typedef size_t sz_size_t;              /* types.h:538 */
+typedef ptrdiff_t sz_ssize_t;          /* types.h:539 */
+typedef char const *sz_cptr_t;         /* types.h:632 */
+typedef sz_i8_t sz_error_cost_t;       /* types.h:634 */
+typedef sz_size_t sz_sorted_idx_t;     /* types.h:644 */
+
+/** Status codes, values as in types.h:699-721. */
+typedef enum sz_status_t {
+    sz_success_k = 0,
+    sz_bad_alloc_k = -10,
+    sz_invalid_utf8_k = -12,
+    sz_contains_duplicates_k = -13,
+    sz_overflow_risk_k = -14,
+    sz_unexpected_dimensions_k = -15,
+    sz_missing_gpu_k = -16,
+    sz_device_code_mismatch_k = -17,
+    sz_device_memory_mismatch_k = -18,
+    sz_authentication_failed_k = -19,
+    sz_status_unknown_k = -1,
+} sz_status_t;
+
+/** Capability bits, values as in types.h:728-766 (only the bits this library reports or accepts are named). */
+typedef enum sz_capability_t {
+    sz_cap_serial_k = 1,
+    sz_cap_parallel_k = 1 << 2,
+    sz_cap_any_k = 0x7FFFFFFF,
+    sz_cap_cuda_k = 1 << 21,
+    sz_cap_kepler_k = 1 << 22,
+    sz_cap_hopper_k = 1 << 23,
+    sz_caps_none_k = 0,
+    sz_caps_ckh_k = (1 << 21) | (1 << 22) | (1 << 23),
+} sz_capability_t;
+
+typedef sz_cptr_t (*sz_sequence_member_start_t)(void const *, sz_sorted_idx_t);  /* types.h:1168 */
+typedef sz_size_t (*sz_sequence_member_length_t)(void const *, sz_sorted_idx_t); /* types.h:1170 */
+
+/** A collection of strings reached through callbacks (types.h:1177-1182). */
+typedef struct sz_sequence_t {
+    void const *handle;
+    sz_size_t count;
+    sz_sequence_member_start_t get_start;
+    sz_sequence_member_length_t get_length;
+} sz_sequence_t;
+
+typedef void *(*sz_memory_allocate_t)(sz_size_t, void *); /* types.h:859 */
+typedef void (*sz_memory_free_t)(void *, sz_size_t, void *);
+
+/** Allocator hooks (types.h:866-870). Accepted and ignored by every `*_init`, as in the reference. */
+typedef struct sz_memory_allocator_t {
+    sz_memory_allocate_t allocate;
+    sz_memory_free_t free;
+    void *handle;
+} sz_memory_allocator_t;
+#endif /* STRINGZILLA_TYPES_H_ */
+
+#ifndef STRINGZILLAS_H_
+/** Arrow-like tape with 32-bit offsets, `count + 1` of them (stringzillas.h:68-72). */
+typedef struct sz_sequence_u32tape_t {
+    sz_cptr_t data;
+    sz_u32_t const *offsets;
+    sz_size_t count;
+} sz_sequence_u32tape_t;
+
+/** Arrow-like tape with 64-bit offsets, `count + 1` of them (stringzillas.h:78-82). */
+typedef struct sz_sequence_u64tape_t {
+    sz_cptr_t data;
+    sz_u64_t const *offsets;
+    sz_size_t count;
+} sz_sequence_u64tape_t;
+
+typedef void *szs_device_scope_t;             /* stringzillas.h:101 */
+typedef void *szs_levenshtein_distances_t;    /* stringzillas.h:153 */
+typedef void *szs_levenshtein_distances_utf8_t;
+typedef void *szs_needleman_wunsch_scores_t;  /* stringzillas.h:293 */
+typedef void *szs_smith_waterman_scores_t;
+typedef void *szs_fingerprints_t;
+typedef void *szs_fingerprints_utf8_t;
+#endif /* STRINGZILLAS_H_ */
+
+/* ---- Metadata (replaces stringzillas.h:33-62) ------------------------------------------------------------------ */
+
+/** Version of the reference release this ABI mirrors (5.3.2). Replaces stringzillas.h:37. */
+SZS_GB300_API int szs_version_major(void);
+/** Replaces stringzillas.h:42. */
+SZS_GB300_API int szs_version_minor(void);
+/** Replaces stringzillas.h:47. */
+SZS_GB300_API int szs_version_patch(void);
+/** `cuda | kepler | hopper` (the engine is compiled for sm_103a). Replaces stringzillas.h:52. */
+SZS_GB300_API sz_capability_t szs_capabilities_comptime(void);
+/** The same bits when a CUDA device is visible, else `sz_caps_none_k`. Replaces stringzillas.h:57. */
+SZS_GB300_API sz_capability_t szs_capabilities_runtime(void);
+/** `comptime & runtime`, cached. Replaces stringzillas.h:62. */
+SZS_GB300_API sz_capability_t szs_capabilities(void);
+
+/** Fills @p alloc with managed-memory hooks. Replaces stringzillas.h:88. */
+SZS_GB300_API sz_status_t sz_memory_allocator_init_unified(sz_memory_allocator_t *alloc, char const **error_message);
+
+/* ---- Device scopes (replaces stringzillas.h:107-152) ----------------------------------------------------------- */
+
+/** Default scope: GPU engines run on device 0. Replaces stringzillas.h:107. */
+SZS_GB300_API sz_status_t szs_device_scope_init_default(szs_device_scope_t *scope, char const **error_message);
+/** CPU-cores scope: accepted, but every scoring call on it returns `sz_device_code_mismatch_k`. Replaces :115. */
+SZS_GB300_API sz_status_t szs_device_scope_init_cpu_cores(sz_size_t cpu_cores, szs_device_scope_t *scope,
+                                                          char const **error_message);
+/** GPU scope with its own non-blocking stream; `sz_missing_gpu_k` if the device does not exist. Replaces :123. */
+SZS_GB300_API sz_status_t szs_device_scope_init_gpu_device(sz_size_t gpu_device, szs_device_scope_t *scope,
+                                                           char const **error_message);
+/** Replaces stringzillas.h:131. */
+SZS_GB300_API sz_status_t szs_device_scope_get_cpu_cores(szs_device_scope_t scope, sz_size_t *cpu_cores,
+                                                         char const **error_message);
+/** Replaces stringzillas.h:139. */
+SZS_GB300_API sz_status_t szs_device_scope_get_gpu_device(szs_device_scope_t scope, sz_size_t *gpu_device,
+                                                          char const **error_message);
+/** Replaces stringzillas.h:147. */
+SZS_GB300_API sz_status_t szs_device_scope_get_capabilities(szs_device_scope_t scope, sz_capability_t *capabilities,
+                                                            char const **error_message);
+/** Replaces stringzillas.h:152. */
+SZS_GB300_API void szs_device_scope_free(szs_device_scope_t scope);
+
+/* ---- Levenshtein distances (replaces stringzillas.h:153-223) --------------------------------------------------- */
+
+/**
+ *  Creates an engine for `min` edit costs: `match`/`mismatch` per substitution, a gap of length k costing
+ *  `open + (k-1)*extend`; `open == extend` selects linear gaps. `*engine` must be NULL on entry. Costs must be
+ *  non-negative (the reference's unsigned cells wrap on negative costs; here they are rejected with
+ *  `sz_overflow_risk_k`). Replaces stringzillas.h:170-173.
+ */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_init(sz_error_cost_t match, sz_error_cost_t mismatch,
+                                                         sz_error_cost_t open, sz_error_cost_t extend,
+                                                         sz_memory_allocator_t const *alloc,
+                                                         sz_capability_t capabilities,
+                                                         szs_levenshtein_distances_t *engine,
+                                                         char const **error_message);
+/**
+ *  Fills `results[q * results_row_stride + c]` with the distance of `queries[q]` to `candidates[c]`; with
+ *  `candidates == NULL`, the symmetric self-distance matrix of `queries`. Replaces stringzillas.h:184-188.
+ */
+SZS_GB300_API sz_status_t szs_levenshtein_distances(szs_levenshtein_distances_t engine, szs_device_scope_t device,
+                                                    sz_sequence_t const *queries, sz_sequence_t const *candidates,
+                                                    sz_size_t *results, sz_size_t results_row_stride,
+                                                    char const **error_message);
+/** Tape form with 32-bit offsets. Replaces stringzillas.h:199-203. */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_u32tape(szs_levenshtein_distances_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u32tape_t const *queries,
+                                                            sz_sequence_u32tape_t const *candidates,
+                                                            sz_size_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message);
+/** Tape form with 64-bit offsets. Replaces stringzillas.h:214-218. */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_u64tape(szs_levenshtein_distances_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u64tape_t const *queries,
+                                                            sz_sequence_u64tape_t const *candidates,
+                                                            sz_size_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message);
+/** Replaces stringzillas.h:223. */
+SZS_GB300_API void szs_levenshtein_distances_free(szs_levenshtein_distances_t engine);
+
+/* ---- UTF-8 Levenshtein: out of this engine's scope; present so bindings load (stringzillas.h:224-292) ---------- */
+
+/** Always fails with `sz_status_unknown_k` ("not implemented by the GB300 engine"). Replaces stringzillas.h:239. */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_init(sz_error_cost_t match, sz_error_cost_t mismatch,
+                                                              sz_error_cost_t open, sz_error_cost_t extend,
+                                                              sz_memory_allocator_t const *alloc,
+                                                              sz_capability_t capabilities,
+                                                              szs_levenshtein_distances_utf8_t *engine,
+                                                              char const **error_message);
+/** Replaces stringzillas.h:255. */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8(szs_levenshtein_distances_utf8_t engine,
+                                                         szs_device_scope_t device, sz_sequence_t const *queries,
+                                                         sz_sequence_t const *candidates, sz_size_t *results,
+                                                         sz_size_t results_row_stride, char const **error_message);
+/** Replaces stringzillas.h:270. */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u32tape(szs_levenshtein_distances_utf8_t engine,
+                                                                 szs_device_scope_t device,
+                                                                 sz_sequence_u32tape_t const *queries,
+                                                                 sz_sequence_u32tape_t const *candidates,
+                                                                 sz_size_t *results, sz_size_t results_row_stride,
+                                                                 char const **error_message);
+/** Replaces stringzillas.h:285. */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u64tape(szs_levenshtein_distances_utf8_t engine,
+                                                                 szs_device_scope_t device,
+                                                                 sz_sequence_u64tape_t const *queries,
+                                                                 sz_sequence_u64tape_t const *candidates,
+                                                                 sz_size_t *results, sz_size_t results_row_stride,
+                                                                 char const **error_message);
+/** Replaces stringzillas.h:292. */
+SZS_GB300_API void szs_levenshtein_distances_utf8_free(szs_levenshtein_distances_utf8_t engine);
+
+/* ---- Needleman-Wunsch scores (replaces stringzillas.h:293-364) ------------------------------------------------- */
+
+/**
+ *  Creates a global-alignment engine maximising `sum(table[byte_to_class[a]][byte_to_class[b]]) + gaps`, the table
+ *  being 32x32 row-major int8 (first string's class selects the row). Gap of length k: `open + (k-1)*extend`
+ *  (pass negative values). `open == extend` selects linear gaps. Replaces stringzillas.h:310-314.
+ */
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_init(sz_u8_t const *byte_to_class,
+                                                           sz_error_cost_t const *class_substitution_costs,
+                                                           sz_error_cost_t open, sz_error_cost_t extend,
+                                                           sz_memory_allocator_t const *alloc,
+                                                           sz_capability_t capabilities,
+                                                           szs_needleman_wunsch_scores_t *engine,
+                                                           char const **error_message);
+/** Replaces stringzillas.h:325-329. */
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores(szs_needleman_wunsch_scores_t engine, szs_device_scope_t device,
+                                                      sz_sequence_t const *queries, sz_sequence_t const *candidates,
+                                                      sz_ssize_t *results, sz_size_t results_row_stride,
+                                                      char const **error_message);
+/** Replaces stringzillas.h:340-344. */
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_u32tape(szs_needleman_wunsch_scores_t engine,
+                                                              szs_device_scope_t device,
+                                                              sz_sequence_u32tape_t const *queries,
+                                                              sz_sequence_u32tape_t const *candidates,
+                                                              sz_ssize_t *results, sz_size_t results_row_stride,
+                                                              char const **error_message);
+/** Replaces stringzillas.h:355-359. */
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_u64tape(szs_needleman_wunsch_scores_t engine,
+                                                              szs_device_scope_t device,
+                                                              sz_sequence_u64tape_t const *queries,
+                                                              sz_sequence_u64tape_t const *candidates,
+                                                              sz_ssize_t *results, sz_size_t results_row_stride,
+                                                              char const **error_message);
+/** Replaces stringzillas.h:364. */
+SZS_GB300_API void szs_needleman_wunsch_scores_free(szs_needleman_wunsch_scores_t engine);
+
+/* ---- Smith-Waterman scores (replaces stringzillas.h:365-434) --------------------------------------------------- */
+
+/** Local alignment, same arguments as Needleman-Wunsch; an empty side scores 0. Replaces stringzillas.h:380-384. */
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_init(sz_u8_t const *byte_to_class,
+                                                         sz_error_cost_t const *class_substitution_costs,
+                                                         sz_error_cost_t open, sz_error_cost_t extend,
+                                                         sz_memory_allocator_t const *alloc,
+                                                         sz_capability_t capabilities,
+                                                         szs_smith_waterman_scores_t *engine,
+                                                         char const **error_message);
+/** Replaces stringzillas.h:395-399. */
+SZS_GB300_API sz_status_t szs_smith_waterman_scores(szs_smith_waterman_scores_t engine, szs_device_scope_t device,
+                                                    sz_sequence_t const *queries, sz_sequence_t const *candidates,
+                                                    sz_ssize_t *results, sz_size_t results_row_stride,
+                                                    char const **error_message);
+/** Replaces stringzillas.h:410-414. */
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_u32tape(szs_smith_waterman_scores_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u32tape_t const *queries,
+                                                            sz_sequence_u32tape_t const *candidates,
+                                                            sz_ssize_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message);
+/** Replaces stringzillas.h:425-429. */
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_u64tape(szs_smith_waterman_scores_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u64tape_t const *queries,
+                                                            sz_sequence_u64tape_t const *candidates,
+                                                            sz_ssize_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message);
+/** Replaces stringzillas.h:434. */
+SZS_GB300_API void szs_smith_waterman_scores_free(szs_smith_waterman_scores_t engine);
+
+/* ---- Fingerprints: out of this engine's scope; present so bindings load (stringzillas.h:435-536) --------------- */
+
+/** Always fails with `sz_status_unknown_k`. Replaces stringzillas.h:476-480. */
+SZS_GB300_API sz_status_t szs_fingerprints_init(sz_size_t dimensions, sz_size_t alphabet_size,
+                                                sz_size_t const *window_widths, sz_size_t window_widths_count,
+                                                sz_u64_t seed, sz_memory_allocator_t const *alloc,
+                                                sz_capability_t capabilities, szs_fingerprints_t *engine,
+                                                char const **error_message);
+/** Replaces stringzillas.h:495. */
+SZS_GB300_API sz_status_t szs_fingerprints_sequence(szs_fingerprints_t engine, szs_device_scope_t device,
+                                                    sz_sequence_t const *texts, sz_u32_t *min_hashes,
+                                                    sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                    sz_size_t min_counts_stride, char const **error_message);
+/** Replaces stringzillas.h:509. */
+SZS_GB300_API sz_status_t szs_fingerprints_u64tape(szs_fingerprints_t engine, szs_device_scope_t device,
+                                                   sz_sequence_u64tape_t const *texts, sz_u32_t *min_hashes,
+                                                   sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                   sz_size_t min_counts_stride, char const **error_message);
+/** Replaces stringzillas.h:523. */
+SZS_GB300_API sz_status_t szs_fingerprints_u32tape(szs_fingerprints_t engine, szs_device_scope_t device,
+                                                   sz_sequence_u32tape_t const *texts, sz_u32_t *min_hashes,
+                                                   sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                   sz_size_t min_counts_stride, char const **error_message);
+/** Replaces stringzillas.h:536. */
+SZS_GB300_API void szs_fingerprints_free(szs_fingerprints_t engine);
+
+/* ---- Unified memory (replaces stringzillas.h:545-551) ---------------------------------------------------------- */
+
+/** `cudaMallocManaged`, NULL on failure. Replaces stringzillas.h:545. */
+SZS_GB300_API void *szs_unified_alloc(sz_size_t size_bytes);
+/** Replaces stringzillas.h:551. */
+SZS_GB300_API void szs_unified_free(void *ptr, sz_size_t size_bytes);
+
+/* ==== Extensions (no counterpart in the reference) ============================================================== */
+
+/**
+ *  Pairwise ("zip") scoring: `results[i] = score(first[i], second[i])` for `i < first->count`; both tapes must hold
+ *  the same count (else `sz_unexpected_dimensions_k`). The reference only offers the cross-product, whose diagonal
+ *  gives the same numbers at quadratic cost. Results are written densely (stride 1).
+ */
+SZS_GB300_API sz_status_t szs_levenshtein_distances_pairwise_u32tape(szs_levenshtein_distances_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u32tape_t const *first,
+                                                                     sz_sequence_u32tape_t const *second,
+                                                                     sz_size_t *results, char const **error_message);
+SZS_GB300_API sz_status_t szs_levenshtein_distances_pairwise_u64tape(szs_levenshtein_distances_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u64tape_t const *first,
+                                                                     sz_sequence_u64tape_t const *second,
+                                                                     sz_size_t *results, char const **error_message);
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_pairwise_u32tape(szs_needleman_wunsch_scores_t engine,
+                                                                       szs_device_scope_t device,
+                                                                       sz_sequence_u32tape_t const *first,
+                                                                       sz_sequence_u32tape_t const *second,
+                                                                       sz_ssize_t *results,
+                                                                       char const **error_message);
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_pairwise_u64tape(szs_needleman_wunsch_scores_t engine,
+                                                                       szs_device_scope_t device,
+                                                                       sz_sequence_u64tape_t const *first,
+                                                                       sz_sequence_u64tape_t const *second,
+                                                                       sz_ssize_t *results,
+                                                                       char const **error_message);
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_pairwise_u32tape(szs_smith_waterman_scores_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u32tape_t const *first,
+                                                                     sz_sequence_u32tape_t const *second,
+                                                                     sz_ssize_t *results, char const **error_message);
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_pairwise_u64tape(szs_smith_waterman_scores_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u64tape_t const *first,
+                                                                     sz_sequence_u64tape_t const *second,
+                                                                     sz_ssize_t *results, char const **error_message);
+
+/** Scheduling forms an engine can run a batch in. */
+typedef enum szs_gb300_schedule_t {
+    /** Length-binned plan, persistent kernels per bin, cached CUDA graph when inputs are device-resident. */
+    szs_gb300_schedule_batched_k = 0,
+    /** One launch of one kernel shape over all pairs in input order: the "plain one-launch-per-batch" form. */
+    szs_gb300_schedule_plain_k = 1,
+} szs_gb300_schedule_t;
+
+/**
+ *  Selects the scheduling form for later calls on @p engine (any of the three engine kinds). No counterpart in the
+ *  reference, which always runs its own tier router.
+ */
+SZS_GB300_API sz_status_t szs_gb300_engine_set_schedule(void *engine, szs_gb300_schedule_t schedule,
+                                                        char const **error_message);
+
+/** Per-engine counters of the last call. No counterpart in the reference (its timer is dropped at the ABI). */
+typedef struct szs_gb300_stats_t {
+    double last_call_ms;       /**< CUDA-event time of the last call's device work */
+    sz_u64_t last_cells;       /**< sum of len(a)*len(b) over the scored pairs */
+    sz_u64_t last_pairs;       /**< number of scored pairs (a symmetric call counts the triangle once) */
+    sz_u64_t last_launches;    /**< kernels launched by the last call (graph nodes count one each) */
+    sz_u64_t graph_replays;    /**< calls served by replaying a cached CUDA graph */
+    sz_u64_t kernel_launches;  /**< kernels launched over the engine's lifetime */
+} szs_gb300_stats_t;
+
+/** Copies the engine's counters into @p stats. No counterpart in the reference. */
+SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine, szs_gb300_stats_t *stats,
+                                                     char const **error_message);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STRINGZILLAS_GB300_H_ */

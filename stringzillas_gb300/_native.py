@@ -1,0 +1,135 @@
+"""Loads ``libszs_gb300.so`` and declares the C-ABI prototypes (include/stringzillas_gb300.h).
+
+The library is the product: there is no CPU fallback. If it cannot be loaded (not built, no CUDA runtime), importing
+the package raises, so nothing silently runs elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+c_size_t = ctypes.c_size_t
+c_void_p = ctypes.c_void_p
+c_int = ctypes.c_int
+c_int8 = ctypes.c_int8
+c_char_p = ctypes.c_char_p
+c_status = ctypes.c_int
+
+
+class U32Tape(ctypes.Structure):
+    """``sz_sequence_u32tape_t``"""
+    _fields_ = [("data", c_void_p), ("offsets", c_void_p), ("count", c_size_t)]
+
+
+class U64Tape(ctypes.Structure):
+    """``sz_sequence_u64tape_t``"""
+    _fields_ = [("data", c_void_p), ("offsets", c_void_p), ("count", c_size_t)]
+
+
+class Stats(ctypes.Structure):
+    """``szs_gb300_stats_t``"""
+    _fields_ = [
+        ("last_call_ms", ctypes.c_double),
+        ("last_cells", ctypes.c_uint64),
+        ("last_pairs", ctypes.c_uint64),
+        ("last_launches", ctypes.c_uint64),
+        ("graph_replays", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+    ]
+
+
+def _load() -> ctypes.CDLL:
+    path = _build.LIBRARY
+    if not os.path.exists(path):
+        path = _build.build()
+    return ctypes.CDLL(path)
+
+
+lib = _load()
+LIBRARY_PATH = _build.LIBRARY
+
+_err = ctypes.POINTER(c_char_p)
+
+for _name in ("szs_version_major", "szs_version_minor", "szs_version_patch"):
+    getattr(lib, _name).restype = c_int
+    getattr(lib, _name).argtypes = []
+for _name in ("szs_capabilities", "szs_capabilities_comptime", "szs_capabilities_runtime"):
+    getattr(lib, _name).restype = ctypes.c_uint32
+    getattr(lib, _name).argtypes = []
+
+lib.szs_device_scope_init_default.restype = c_status
+lib.szs_device_scope_init_default.argtypes = [ctypes.POINTER(c_void_p), _err]
+lib.szs_device_scope_init_cpu_cores.restype = c_status
+lib.szs_device_scope_init_cpu_cores.argtypes = [c_size_t, ctypes.POINTER(c_void_p), _err]
+lib.szs_device_scope_init_gpu_device.restype = c_status
+lib.szs_device_scope_init_gpu_device.argtypes = [c_size_t, ctypes.POINTER(c_void_p), _err]
+lib.szs_device_scope_get_cpu_cores.restype = c_status
+lib.szs_device_scope_get_cpu_cores.argtypes = [c_void_p, ctypes.POINTER(c_size_t), _err]
+lib.szs_device_scope_get_gpu_device.restype = c_status
+lib.szs_device_scope_get_gpu_device.argtypes = [c_void_p, ctypes.POINTER(c_size_t), _err]
+lib.szs_device_scope_get_capabilities.restype = c_status
+lib.szs_device_scope_get_capabilities.argtypes = [c_void_p, ctypes.POINTER(ctypes.c_uint32), _err]
+lib.szs_device_scope_free.restype = None
+lib.szs_device_scope_free.argtypes = [c_void_p]
+
+lib.szs_unified_alloc.restype = c_void_p
+lib.szs_unified_alloc.argtypes = [c_size_t]
+lib.szs_unified_free.restype = None
+lib.szs_unified_free.argtypes = [c_void_p, c_size_t]
+
+lib.szs_levenshtein_distances_init.restype = c_status
+lib.szs_levenshtein_distances_init.argtypes = [c_int8, c_int8, c_int8, c_int8, c_void_p, ctypes.c_uint32,
+                                               ctypes.POINTER(c_void_p), _err]
+for _algo in ("needleman_wunsch_scores", "smith_waterman_scores"):
+    fn = getattr(lib, f"szs_{_algo}_init")
+    fn.restype = c_status
+    fn.argtypes = [c_void_p, c_void_p, c_int8, c_int8, c_void_p, ctypes.c_uint32, ctypes.POINTER(c_void_p), _err]
+for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterman_scores"):
+    for _suffix in ("_u32tape", "_u64tape", ""):
+        fn = getattr(lib, f"szs_{_algo}{_suffix}")
+        fn.restype = c_status
+        fn.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, _err]
+    for _suffix in ("_pairwise_u32tape", "_pairwise_u64tape"):
+        fn = getattr(lib, f"szs_{_algo}{_suffix}")
+        fn.restype = c_status
+        fn.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, _err]
+    fn = getattr(lib, f"szs_{_algo}_free")
+    fn.restype = None
+    fn.argtypes = [c_void_p]
+
+lib.szs_gb300_engine_set_schedule.restype = c_status
+lib.szs_gb300_engine_set_schedule.argtypes = [c_void_p, c_int, _err]
+lib.szs_gb300_engine_get_stats.restype = c_status
+lib.szs_gb300_engine_get_stats.argtypes = [c_void_p, ctypes.POINTER(Stats), _err]
+
+# Status codes (include/stringzillas_gb300.h; values of the reference's types.h:699-721).
+SUCCESS = 0
+BAD_ALLOC = -10
+INVALID_UTF8 = -12
+OVERFLOW_RISK = -14
+UNEXPECTED_DIMENSIONS = -15
+MISSING_GPU = -16
+DEVICE_CODE_MISMATCH = -17
+DEVICE_MEMORY_MISMATCH = -18
+UNKNOWN = -1
+
+CAP_CUDA, CAP_KEPLER, CAP_HOPPER = 1 << 21, 1 << 22, 1 << 23
+CAP_SERIAL, CAP_PARALLEL = 1, 1 << 2
+
+
+def raise_for(status: int, message, context: str) -> None:
+    """Maps a status onto the exception type the reference's binding raises
+    (python/stringzillas/stringzillas.c:21-32)."""
+    if status == SUCCESS:
+        return
+    detail = message.decode() if isinstance(message, bytes) else (message or "Unknown error")
+    text = f"{context}: {detail}"
+    if status == BAD_ALLOC:
+        raise MemoryError(text)
+    if status in (INVALID_UTF8, UNEXPECTED_DIMENSIONS):
+        raise ValueError(text)
+    if status == OVERFLOW_RISK:
+        raise OverflowError(text)
+    raise RuntimeError(text)

@@ -1,0 +1,1092 @@
+/**
+ *  @file engine.cu
+ *  @brief Host orchestration of the GB300 scoring engine and its `szs_*` C-ABI.
+ *
+ *  One call = stage inputs that are not device-resident -> plan on the device (planner.cu) -> read the bin
+ *  counts back -> launch one persistent kernel per non-empty route -> scatter results into the caller's matrix.
+ *  The reference's equivalent orchestration is `cuda_weighted_cross_` / the Levenshtein cross driver
+ *  (include/stringzillas/similarities/cuda.cuh:5395-5505, :3806-3936) behind the shims in
+ *  c/stringzillas/{levenshtein,needleman_wunsch,smith_waterman}.cuh.
+ */
+#include "stringzillas_gb300.h"
+#include "launchers.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+namespace szs_gb300 {
+
+constexpr std::uint32_t engine_magic_k = 0x53475a45u; // "EZGS"
+constexpr std::uint32_t scope_magic_k = 0x50435353u;
+constexpr int max_devices_k = 64;
+
+/* ---- errors --------------------------------------------------------------------------------------------------- */
+
+struct status_t {
+    sz_status_t code = sz_success_k;
+    char const *message = nullptr;
+    bool ok() const noexcept { return code == sz_success_k; }
+};
+
+static status_t from_cuda(cudaError_t error) noexcept {
+    if (error == cudaSuccess) return {};
+    if (error == cudaErrorMemoryAllocation) return {sz_bad_alloc_k, cudaGetErrorName(error)};
+    if (error == cudaErrorNoDevice || error == cudaErrorInsufficientDriver || error == cudaErrorInvalidDevice)
+        return {sz_missing_gpu_k, cudaGetErrorName(error)};
+    return {sz_status_unknown_k, cudaGetErrorName(error)};
+}
+
+static sz_status_t report(status_t status, char const **error_message) noexcept {
+    if (error_message) {
+        if (status.ok()) *error_message = nullptr;
+        else if (status.message) *error_message = status.message;
+        else {
+            switch (status.code) {
+            case sz_bad_alloc_k: *error_message = "Memory allocation failed"; break;
+            case sz_overflow_risk_k: *error_message = "Overflow risk detected"; break;
+            case sz_unexpected_dimensions_k: *error_message = "Input/output size mismatch"; break;
+            case sz_missing_gpu_k: *error_message = "GPU device not available or CUDA not initialized"; break;
+            case sz_device_code_mismatch_k: *error_message = "Backend and executor mismatch"; break;
+            case sz_device_memory_mismatch_k: *error_message = "Use device-reachable or unified memory"; break;
+            default: *error_message = "Unknown error"; break;
+            }
+        }
+    }
+    return status.code;
+}
+
+#define SZS_TRY_CUDA(expression)                                                                                     \
+    do {                                                                                                             \
+        cudaError_t const szs_error_ = (expression);                                                                 \
+        if (szs_error_ != cudaSuccess) return from_cuda(szs_error_);                                                 \
+    } while (0)
+
+/* ---- scopes --------------------------------------------------------------------------------------------------- */
+
+enum scope_kind_t { scope_default_k, scope_cpu_k, scope_gpu_k };
+
+struct scope_t {
+    std::uint32_t magic = scope_magic_k;
+    scope_kind_t kind = scope_default_k;
+    std::size_t cpu_cores = 1;
+    int device = 0;
+    cudaStream_t stream = nullptr; // GPU scopes own a non-blocking stream
+};
+
+static scope_t *as_scope(void *handle) noexcept {
+    auto *scope = static_cast<scope_t *>(handle);
+    return scope && scope->magic == scope_magic_k ? scope : nullptr;
+}
+
+static int visible_devices() noexcept {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return count;
+}
+
+/* ---- device memory ---------------------------------------------------------------------------------------------- */
+
+/** A grow-only device buffer, reused across calls. */
+struct device_buffer_t {
+    void *data = nullptr;
+    std::size_t bytes = 0;
+    status_t reserve(std::size_t needed, cudaStream_t stream) noexcept {
+        if (needed <= bytes) return {};
+        if (data) {
+            cudaStreamSynchronize(stream);
+            cudaFree(data);
+            data = nullptr, bytes = 0;
+        }
+        std::size_t const grown = std::max(needed, std::size_t(1) << 20);
+        SZS_TRY_CUDA(cudaMalloc(&data, grown));
+        bytes = grown;
+        return {};
+    }
+    void release() noexcept {
+        if (data) cudaFree(data);
+        data = nullptr, bytes = 0;
+    }
+};
+
+/** A grow-only pinned host buffer. */
+struct pinned_buffer_t {
+    void *data = nullptr;
+    std::size_t bytes = 0;
+    status_t reserve(std::size_t needed) noexcept {
+        if (needed <= bytes) return {};
+        if (data) cudaFreeHost(data);
+        data = nullptr, bytes = 0;
+        SZS_TRY_CUDA(cudaMallocHost(&data, needed));
+        bytes = needed;
+        return {};
+    }
+    void release() noexcept {
+        if (data) cudaFreeHost(data);
+        data = nullptr, bytes = 0;
+    }
+};
+
+static bool device_accessible(void const *pointer) noexcept {
+    if (!pointer) return false;
+    cudaPointerAttributes attributes;
+    if (cudaPointerGetAttributes(&attributes, pointer) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attributes.type == cudaMemoryTypeDevice || attributes.type == cudaMemoryTypeManaged;
+}
+
+/** Per-device state of an engine: its stream for the default scope, buffers, plan readback, timers. */
+struct device_context_t {
+    bool ready = false;
+    int device = -1;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    device_buffer_t control; // plan bins + alphabet
+    device_buffer_t inputs;  // staged tapes
+    device_buffer_t work;    // tasks + dense results
+    device_buffer_t scratch; // wavefront scratch rows
+    pinned_buffer_t readback;
+    pinned_buffer_t results_host;
+    cudaEvent_t start = nullptr, stop = nullptr;
+
+    status_t prepare(int device_index) noexcept {
+        if (ready) return {};
+        device = device_index;
+        SZS_TRY_CUDA(cudaSetDevice(device));
+        SZS_TRY_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+        SZS_TRY_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+        SZS_TRY_CUDA(cudaEventCreate(&start));
+        SZS_TRY_CUDA(cudaEventCreate(&stop));
+        status_t status = control.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256, own_stream);
+        if (!status.ok()) return status;
+        status = readback.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256);
+        if (!status.ok()) return status;
+        ready = true;
+        return {};
+    }
+    plan_bins_t *bins_device() const noexcept { return static_cast<plan_bins_t *>(control.data); }
+    batch_alphabet_t *alphabet_device() const noexcept {
+        return reinterpret_cast<batch_alphabet_t *>(static_cast<unsigned char *>(control.data) + sizeof(plan_bins_t));
+    }
+    plan_bins_t *bins_host() const noexcept { return static_cast<plan_bins_t *>(readback.data); }
+    batch_alphabet_t *alphabet_host() const noexcept {
+        return reinterpret_cast<batch_alphabet_t *>(static_cast<unsigned char *>(readback.data) + sizeof(plan_bins_t));
+    }
+    void release() noexcept {
+        if (!ready) return;
+        cudaSetDevice(device);
+        cudaStreamSynchronize(own_stream);
+        control.release(), inputs.release(), work.release(), scratch.release();
+        readback.release(), results_host.release();
+        if (start) cudaEventDestroy(start);
+        if (stop) cudaEventDestroy(stop);
+        if (own_stream) cudaStreamDestroy(own_stream);
+        ready = false;
+    }
+};
+
+/* ---- engines ---------------------------------------------------------------------------------------------------- */
+
+struct engine_t {
+    std::uint32_t magic = engine_magic_k;
+    int kind = kind_levenshtein_k;
+    int schedule = szs_gb300_schedule_batched_k;
+    score_costs_t costs {};
+    int magnitude = 1;
+    bool unit_levenshtein = false;
+    device_context_t devices[max_devices_k];
+    szs_gb300_stats_t stats {};
+    ~engine_t() {
+        for (auto &context : devices) context.release();
+    }
+};
+
+static engine_t *as_engine(void *handle, int kind) noexcept {
+    auto *engine = static_cast<engine_t *>(handle);
+    if (!engine || engine->magic != engine_magic_k) return nullptr;
+    if (kind >= 0 && engine->kind != kind) return nullptr;
+    return engine;
+}
+
+static int cost_abs(int x) noexcept { return x < 0 ? -x : x; }
+
+cudaError_t launch_myers_planes2(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
+                                 std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_planes3(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
+                                 std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_planes5(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
+                                 std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_planes8(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
+                                 std::int64_t *, int, cudaStream_t);
+
+int myers_planes_for(int bits_needed) {
+    if (bits_needed <= 2) return 2;
+    if (bits_needed <= 3) return 3;
+    if (bits_needed <= 5) return 5;
+    return 8;
+}
+
+int myers_threads_per_cta() { return 128; }
+
+cudaError_t launch_myers(int words, int planes, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
+                         batch_alphabet_t const *alphabet, std::int64_t *results, int ctas, cudaStream_t stream) {
+    switch (planes) {
+    case 2: return launch_myers_planes2(words, exact, tasks, bins, alphabet, results, ctas, stream);
+    case 3: return launch_myers_planes3(words, exact, tasks, bins, alphabet, results, ctas, stream);
+    case 5: return launch_myers_planes5(words, exact, tasks, bins, alphabet, results, ctas, stream);
+    case 8: return launch_myers_planes8(words, exact, tasks, bins, alphabet, results, ctas, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+/** Builds the compact column classes and both orientations of the profile table from the reference's inputs. */
+static void prepare_class_costs(score_costs_t &costs, std::uint8_t const *byte_to_class, std::int8_t const *table) {
+    std::memcpy(costs.byte_to_class, byte_to_class, 256);
+    int compact_of_class[32];
+    for (int &c : compact_of_class) c = -1;
+    int classes = 0;
+    int class_of_compact[32];
+    for (int b = 0; b < 256; ++b) {
+        int const cls = byte_to_class[b] & 31; // the reference indexes a 32x32 table with the raw value
+        if (compact_of_class[cls] < 0) class_of_compact[classes] = cls, compact_of_class[cls] = classes++;
+        costs.byte_to_compact[b] = (std::uint8_t)compact_of_class[cls];
+    }
+    costs.classes = classes;
+    std::memset(costs.profile_table, 0, sizeof(costs.profile_table));
+    std::memset(costs.profile_table_t, 0, sizeof(costs.profile_table_t));
+    for (int cc = 0; cc < classes; ++cc)
+        for (int row_class = 0; row_class < 32; ++row_class) {
+            int const column_class = class_of_compact[cc];
+            // rows = first string: cost(first = row, second = column)
+            costs.profile_table[cc * 32 + row_class] = table[row_class * 32 + column_class];
+            // rows = second string: cost(first = column, second = row)
+            costs.profile_table_t[cc * 32 + row_class] = table[column_class * 32 + row_class];
+        }
+}
+
+/* ---- inputs ----------------------------------------------------------------------------------------------------- */
+
+/** A caller's tape in any memory, before staging. */
+struct tape_view_t {
+    char const *data = nullptr;
+    void const *offsets = nullptr;
+    std::size_t count = 0;
+    int offset_bits = 64;
+};
+
+/** Owns host-side copies made for `sz_sequence_t` inputs (callbacks are host functions). */
+struct gathered_tape_t {
+    std::vector<char> data;
+    std::vector<std::uint64_t> offsets;
+    tape_view_t view() const noexcept {
+        tape_view_t v;
+        v.data = data.empty() ? nullptr : data.data();
+        v.offsets = offsets.data();
+        v.count = offsets.empty() ? 0 : offsets.size() - 1;
+        v.offset_bits = 64;
+        return v;
+    }
+};
+
+static status_t gather_sequence(sz_sequence_t const *sequence, gathered_tape_t &out) noexcept {
+    try {
+        out.offsets.assign(1, 0);
+        out.offsets.reserve(sequence->count + 1);
+        for (sz_size_t i = 0; i < sequence->count; ++i) {
+            sz_cptr_t const start = sequence->get_start(sequence->handle, i);
+            sz_size_t const length = sequence->get_length(sequence->handle, i);
+            out.data.insert(out.data.end(), start, start + length);
+            out.offsets.push_back(out.data.size());
+        }
+    }
+    catch (std::bad_alloc const &) {
+        return {sz_bad_alloc_k, nullptr};
+    }
+    return {};
+}
+
+static std::uint64_t host_offset(tape_view_t const &tape, std::size_t index) noexcept {
+    return tape.offset_bits == 32 ? static_cast<std::uint32_t const *>(tape.offsets)[index]
+                                  : static_cast<std::uint64_t const *>(tape.offsets)[index];
+}
+
+/** Bytes of device memory staging @p tape needs (0 when fully device-resident). */
+struct staging_plan_t {
+    bool offsets_on_device = false, data_on_device = false;
+    std::uint64_t first = 0, last = 0; // data range [first, last)
+    std::size_t offsets_bytes = 0, data_bytes = 0;
+};
+
+static status_t plan_staging(tape_view_t const &tape, staging_plan_t &plan, cudaStream_t stream) noexcept {
+    plan.offsets_on_device = device_accessible(tape.offsets);
+    plan.data_on_device = tape.data == nullptr || device_accessible(tape.data);
+    std::size_t const offset_size = tape.offset_bits == 32 ? 4 : 8;
+    plan.offsets_bytes = plan.offsets_on_device ? 0 : (tape.count + 1) * offset_size;
+    if (plan.offsets_on_device) {
+        if (!plan.data_on_device) {
+            // Read the data range from device-resident offsets.
+            std::uint64_t ends[2] = {0, 0};
+            if (tape.offset_bits == 32) {
+                std::uint32_t e32[2];
+                SZS_TRY_CUDA(cudaMemcpyAsync(&e32[0], tape.offsets, 4, cudaMemcpyDeviceToHost, stream));
+                SZS_TRY_CUDA(cudaMemcpyAsync(&e32[1], static_cast<std::uint32_t const *>(tape.offsets) + tape.count,
+                                             4, cudaMemcpyDeviceToHost, stream));
+                SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+                ends[0] = e32[0], ends[1] = e32[1];
+            }
+            else {
+                SZS_TRY_CUDA(cudaMemcpyAsync(&ends[0], tape.offsets, 8, cudaMemcpyDeviceToHost, stream));
+                SZS_TRY_CUDA(cudaMemcpyAsync(&ends[1], static_cast<std::uint64_t const *>(tape.offsets) + tape.count,
+                                             8, cudaMemcpyDeviceToHost, stream));
+                SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+            }
+            plan.first = ends[0], plan.last = ends[1];
+        }
+    }
+    else {
+        plan.first = host_offset(tape, 0), plan.last = host_offset(tape, tape.count);
+    }
+    if (plan.last < plan.first) return {sz_unexpected_dimensions_k, "Tape offsets must be non-decreasing"};
+    plan.data_bytes = plan.data_on_device ? 0 : (std::size_t)(plan.last - plan.first);
+    return {};
+}
+
+static std::size_t align_up(std::size_t x, std::size_t a) noexcept { return (x + a - 1) / a * a; }
+
+/** Copies what is not device-resident into @p area (which has at least the planned bytes) and describes the
+ *  result for the kernels. */
+static status_t stage_tape(tape_view_t const &tape, staging_plan_t const &plan, unsigned char *area,
+                           tape_t &staged, cudaStream_t stream) noexcept {
+    staged.count = tape.count;
+    staged.offset_bits = tape.offset_bits;
+    unsigned char *cursor = area;
+    if (plan.offsets_on_device) staged.offsets = tape.offsets;
+    else {
+        SZS_TRY_CUDA(cudaMemcpyAsync(cursor, tape.offsets, plan.offsets_bytes, cudaMemcpyHostToDevice, stream));
+        staged.offsets = cursor;
+        cursor += align_up(plan.offsets_bytes, 256);
+    }
+    if (plan.data_on_device) staged.base = reinterpret_cast<std::uint8_t const *>(tape.data);
+    else {
+        if (plan.data_bytes)
+            SZS_TRY_CUDA(cudaMemcpyAsync(cursor, tape.data + plan.first, plan.data_bytes, cudaMemcpyHostToDevice,
+                                         stream));
+        // Kernels address `base + offsets[i]`; the staged copy starts at offsets[0].
+        staged.base = reinterpret_cast<std::uint8_t const *>(cursor) - plan.first;
+    }
+    return {};
+}
+
+/* ---- one call ----------------------------------------------------------------------------------------------------- */
+
+struct call_t {
+    tape_view_t queries;
+    tape_view_t candidates;
+    bool has_candidates = false;
+    int mode = mode_cross_k;
+    std::int64_t *out = nullptr;
+    std::size_t stride = 0;
+};
+
+static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &stream, engine_t &engine,
+                              device_context_t *&context) noexcept {
+    scope_t *scope = as_scope(scope_handle);
+    if (scope_handle && !scope) return {sz_status_unknown_k, "Invalid device scope handle"};
+    if (scope && scope->kind == scope_cpu_k) return {sz_device_code_mismatch_k, nullptr};
+    device = scope ? scope->device : 0;
+    if (device < 0 || device >= max_devices_k || device >= visible_devices()) return {sz_missing_gpu_k, nullptr};
+    context = &engine.devices[device];
+    status_t status = context->prepare(device);
+    if (!status.ok()) return status;
+    SZS_TRY_CUDA(cudaSetDevice(device));
+    stream = scope && scope->kind == scope_gpu_k ? scope->stream : context->own_stream;
+    return {};
+}
+
+static status_t run_call(engine_t &engine, void *scope_handle, call_t const &call) noexcept {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    device_context_t *context = nullptr;
+    status_t status = resolve_scope(scope_handle, device, stream, engine, context);
+    if (!status.ok()) return status;
+
+    std::uint64_t const queries_count = call.queries.count;
+    std::uint64_t const candidates_count = call.has_candidates ? call.candidates.count : queries_count;
+    plan_args_t args {};
+    args.mode = call.mode;
+    if (call.mode == mode_pairwise_k) {
+        if (call.candidates.count != call.queries.count) return {sz_unexpected_dimensions_k, nullptr};
+        args.pairs = queries_count;
+    }
+    else if (call.mode == mode_cross_k) args.pairs = queries_count * candidates_count;
+    else args.pairs = queries_count * (queries_count + 1) / 2;
+    args.candidates_count = candidates_count;
+    engine.stats.last_pairs = args.pairs;
+    engine.stats.last_cells = 0;
+    engine.stats.last_launches = 0;
+    engine.stats.last_call_ms = 0;
+    if (args.pairs == 0) return {};
+    if (args.pairs > 0xFFFFFFFFull) return {sz_overflow_risk_k, "More than 2^32 pairs in one call"};
+
+    // Stage inputs.
+    staging_plan_t query_plan, candidate_plan;
+    status = plan_staging(call.queries, query_plan, stream);
+    if (!status.ok()) return status;
+    if (call.has_candidates) {
+        status = plan_staging(call.candidates, candidate_plan, stream);
+        if (!status.ok()) return status;
+    }
+    std::size_t const query_area = align_up(query_plan.offsets_bytes, 256) + align_up(query_plan.data_bytes, 256);
+    std::size_t const candidate_area =
+        call.has_candidates ? align_up(candidate_plan.offsets_bytes, 256) + align_up(candidate_plan.data_bytes, 256)
+                            : 0;
+    status = context->inputs.reserve(query_area + candidate_area + 512, stream);
+    if (!status.ok()) return status;
+    unsigned char *inputs_area = static_cast<unsigned char *>(context->inputs.data);
+    status = stage_tape(call.queries, query_plan, inputs_area, args.queries, stream);
+    if (!status.ok()) return status;
+    if (call.has_candidates) {
+        status = stage_tape(call.candidates, candidate_plan, inputs_area + query_area, args.candidates, stream);
+        if (!status.ok()) return status;
+    }
+    else args.candidates = args.queries;
+
+    // Work buffers: tasks, then dense results.
+    std::size_t const tasks_bytes = align_up(args.pairs * sizeof(pair_task_t), 256);
+    std::size_t const results_bytes = align_up(args.pairs * sizeof(std::int64_t), 256);
+    status = context->work.reserve(tasks_bytes + results_bytes, stream);
+    if (!status.ok()) return status;
+    auto *tasks = static_cast<pair_task_t *>(context->work.data);
+    auto *results = reinterpret_cast<std::int64_t *>(static_cast<unsigned char *>(context->work.data) + tasks_bytes);
+
+    score_costs_t const &costs = engine.costs;
+    args.kind = engine.kind;
+    args.affine = costs.affine;
+    args.open = costs.open, args.extend = costs.extend;
+    args.match = costs.match, args.mismatch = costs.mismatch;
+    args.unit_levenshtein = engine.unit_levenshtein ? 1 : 0;
+    args.magnitude = engine.magnitude;
+    args.steps_beyond_span = costs.affine ? 3 : 1;
+    args.force_route = engine.schedule == szs_gb300_schedule_plain_k ? 1 : -1;
+
+    SZS_TRY_CUDA(cudaEventRecord(context->start, stream));
+    std::uint64_t launches = 0;
+    plan_bins_t *bins = context->bins_device();
+    SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, stream));
+    launches += 3;
+    // Read the plan back: which bins are non-empty and how long the columns get.
+    SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t), cudaMemcpyDeviceToHost, stream));
+    SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+    plan_bins_t const &plan = *context->bins_host();
+    engine.stats.last_cells = plan.cells;
+
+    // Bit-parallel routes.
+    if (engine.unit_levenshtein) {
+        bool any_myers = false;
+        for (int key = bin_myers_begin_k; key < bin_dp32_begin_k; ++key) any_myers |= plan.count[key] != 0;
+        if (any_myers) {
+            // Alphabet of the batch, marked over every pair's bytes.
+            SZS_TRY_CUDA(cudaMemsetAsync(bins->symbol_mask, 0, sizeof(plan.symbol_mask), stream));
+            auto mark_range = [&](tape_t const &tape, staging_plan_t const &plan_of) -> cudaError_t {
+                std::uint64_t first = plan_of.first, last = plan_of.last;
+                if (plan_of.offsets_on_device && plan_of.data_on_device) {
+                    // Device-resident tape: read its range.
+                    std::uint64_t ends[2] = {0, 0};
+                    if (tape.offset_bits == 32) {
+                        std::uint32_t e32[2];
+                        cudaMemcpyAsync(&e32[0], tape.offsets, 4, cudaMemcpyDeviceToHost, stream);
+                        cudaMemcpyAsync(&e32[1], static_cast<std::uint32_t const *>(tape.offsets) + tape.count, 4,
+                                        cudaMemcpyDeviceToHost, stream);
+                        cudaStreamSynchronize(stream);
+                        ends[0] = e32[0], ends[1] = e32[1];
+                    }
+                    else {
+                        cudaMemcpyAsync(&ends[0], tape.offsets, 8, cudaMemcpyDeviceToHost, stream);
+                        cudaMemcpyAsync(&ends[1], static_cast<std::uint64_t const *>(tape.offsets) + tape.count, 8,
+                                        cudaMemcpyDeviceToHost, stream);
+                        cudaStreamSynchronize(stream);
+                    }
+                    first = ends[0], last = ends[1];
+                }
+                return launch_alphabet(tape.base + first, last - first, bins->symbol_mask, context->sm_count, stream);
+            };
+            SZS_TRY_CUDA(mark_range(args.queries, query_plan));
+            if (call.has_candidates) SZS_TRY_CUDA(mark_range(args.candidates, candidate_plan));
+            SZS_TRY_CUDA(launch_alphabet_codes(bins->symbol_mask, context->alphabet_device(), stream));
+            SZS_TRY_CUDA(cudaMemcpyAsync(context->alphabet_host(), context->alphabet_device(),
+                                         sizeof(batch_alphabet_t), cudaMemcpyDeviceToHost, stream));
+            SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+            launches += 2;
+            int const planes = myers_planes_for((int)context->alphabet_host()->bits);
+            for (int words = 1; words <= myers_max_words_k; ++words) {
+                std::uint64_t pairs_here = 0;
+                for (int k = 0; k < 16; ++k) pairs_here += plan.count[bin_myers_begin_k + words * 16 + k];
+                if (!pairs_here) continue;
+                int const threads = myers_threads_per_cta();
+                std::uint64_t const needed = (pairs_here + threads - 1) / threads;
+                int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
+                bool const exact = engine.schedule != szs_gb300_schedule_plain_k;
+                SZS_TRY_CUDA(launch_myers(words, planes, exact, tasks, bins, context->alphabet_device(), results,
+                                          ctas, stream));
+                ++launches;
+            }
+        }
+    }
+
+    // Wavefront routes.
+    for (int cell_bits : {32, 64}) {
+        int const key_begin = cell_bits == 32 ? bin_dp32_begin_k : bin_dp64_begin_k;
+        int const key_end = key_begin + bin_dp_classes_k;
+        std::uint64_t pairs_here = 0;
+        for (int key = key_begin; key < key_end; ++key) pairs_here += plan.count[key];
+        if (!pairs_here) continue;
+        dp_launch_shape_t const shape = dp_shape(engine.kind, costs.affine != 0, cell_bits, costs.classes);
+        if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Wavefront kernel cannot be resident"};
+        std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
+        int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+        std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
+        std::size_t const scratch_bytes = cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta;
+        status = context->scratch.reserve(scratch_bytes, stream);
+        if (!status.ok()) return status;
+        SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, cell_bits, key_begin, key_end, tasks, bins, costs,
+                               results, context->scratch.data, cells_per_warp, ctas, stream));
+        ++launches;
+    }
+
+    // Results into the caller's matrix.
+    bool const out_on_device = device_accessible(call.out);
+    if (out_on_device) {
+        SZS_TRY_CUDA(launch_scatter_output(args, results, call.out, call.stride, context->sm_count, stream));
+        ++launches;
+        SZS_TRY_CUDA(cudaEventRecord(context->stop, stream));
+        SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+    }
+    else {
+        if (call.mode == mode_pairwise_k) {
+            SZS_TRY_CUDA(cudaMemcpyAsync(call.out, results, args.pairs * sizeof(std::int64_t), cudaMemcpyDeviceToHost,
+                                         stream));
+            SZS_TRY_CUDA(cudaEventRecord(context->stop, stream));
+            SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+        }
+        else {
+            status = context->results_host.reserve(args.pairs * sizeof(std::int64_t));
+            if (!status.ok()) return status;
+            auto *dense = static_cast<std::int64_t *>(context->results_host.data);
+            SZS_TRY_CUDA(cudaMemcpyAsync(dense, results, args.pairs * sizeof(std::int64_t), cudaMemcpyDeviceToHost,
+                                         stream));
+            SZS_TRY_CUDA(cudaEventRecord(context->stop, stream));
+            SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+            if (call.mode == mode_cross_k) {
+                for (std::uint64_t q = 0; q < queries_count; ++q)
+                    std::memcpy(call.out + q * call.stride, dense + q * candidates_count,
+                                candidates_count * sizeof(std::int64_t));
+            }
+            else {
+                std::uint64_t p = 0;
+                for (std::uint64_t q = 0; q < queries_count; ++q)
+                    for (std::uint64_t c = 0; c <= q; ++c, ++p) {
+                        call.out[q * call.stride + c] = dense[p];
+                        call.out[c * call.stride + q] = dense[p];
+                    }
+            }
+        }
+    }
+    SZS_TRY_CUDA(cudaGetLastError());
+    float elapsed = 0;
+    cudaEventElapsedTime(&elapsed, context->start, context->stop);
+    engine.stats.last_call_ms = elapsed;
+    engine.stats.last_launches = launches;
+    engine.stats.kernel_launches += launches;
+    return {};
+}
+
+} // namespace szs_gb300
+
+using namespace szs_gb300;
+
+/* ---- C-ABI ------------------------------------------------------------------------------------------------------ */
+
+namespace {
+
+tape_view_t view_of(sz_sequence_u32tape_t const *tape) {
+    tape_view_t v;
+    v.data = tape->data, v.offsets = tape->offsets, v.count = tape->count, v.offset_bits = 32;
+    return v;
+}
+tape_view_t view_of(sz_sequence_u64tape_t const *tape) {
+    tape_view_t v;
+    v.data = tape->data, v.offsets = tape->offsets, v.count = tape->count, v.offset_bits = 64;
+    return v;
+}
+
+template <typename tape_type_>
+sz_status_t score_cross(int kind, void *engine_handle, void *scope, tape_type_ const *queries,
+                        tape_type_ const *candidates, void *results, sz_size_t stride, char const **error_message) {
+    engine_t *engine = as_engine(engine_handle, kind);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!queries || !results) return report({sz_unexpected_dimensions_k, "Queries and results must not be NULL"},
+                                            error_message);
+    call_t call;
+    call.queries = view_of(queries);
+    call.has_candidates = candidates != nullptr;
+    if (candidates) call.candidates = view_of(candidates);
+    call.mode = candidates ? mode_cross_k : mode_symmetric_k;
+    call.out = static_cast<std::int64_t *>(results);
+    call.stride = stride;
+    std::size_t const columns = candidates ? candidates->count : queries->count;
+    if (queries->count > 0 && columns > 0 && stride < columns)
+        return report({sz_unexpected_dimensions_k, "results_row_stride is smaller than the candidates count"},
+                      error_message);
+    return report(run_call(*engine, scope, call), error_message);
+}
+
+sz_status_t score_cross_sequence(int kind, void *engine_handle, void *scope, sz_sequence_t const *queries,
+                                 sz_sequence_t const *candidates, void *results, sz_size_t stride,
+                                 char const **error_message) {
+    engine_t *engine = as_engine(engine_handle, kind);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!queries || !results) return report({sz_unexpected_dimensions_k, "Queries and results must not be NULL"},
+                                            error_message);
+    gathered_tape_t q, c;
+    status_t status = gather_sequence(queries, q);
+    if (status.ok() && candidates) status = gather_sequence(candidates, c);
+    if (!status.ok()) return report(status, error_message);
+    call_t call;
+    call.queries = q.view();
+    call.has_candidates = candidates != nullptr;
+    if (candidates) call.candidates = c.view();
+    call.mode = candidates ? mode_cross_k : mode_symmetric_k;
+    call.out = static_cast<std::int64_t *>(results);
+    call.stride = stride;
+    std::size_t const columns = candidates ? candidates->count : queries->count;
+    if (queries->count > 0 && columns > 0 && stride < columns)
+        return report({sz_unexpected_dimensions_k, "results_row_stride is smaller than the candidates count"},
+                      error_message);
+    return report(run_call(*engine, scope, call), error_message);
+}
+
+template <typename tape_type_>
+sz_status_t score_pairwise(int kind, void *engine_handle, void *scope, tape_type_ const *first,
+                           tape_type_ const *second, void *results, char const **error_message) {
+    engine_t *engine = as_engine(engine_handle, kind);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!first || !second || !results)
+        return report({sz_unexpected_dimensions_k, "Inputs and results must not be NULL"}, error_message);
+    if (first->count != second->count)
+        return report({sz_unexpected_dimensions_k, "Pairwise inputs must hold the same count"}, error_message);
+    call_t call;
+    call.queries = view_of(first);
+    call.candidates = view_of(second);
+    call.has_candidates = true;
+    call.mode = mode_pairwise_k;
+    call.out = static_cast<std::int64_t *>(results);
+    call.stride = 1;
+    return report(run_call(*engine, scope, call), error_message);
+}
+
+sz_status_t create_engine(int kind, int match, int mismatch, int open, int extend, std::uint8_t const *byte_to_class,
+                          std::int8_t const *table, void **engine_out, char const **error_message) {
+    if (!engine_out) return report({sz_status_unknown_k, "Engine output pointer must not be NULL"}, error_message);
+    if (*engine_out) return report({sz_status_unknown_k, "Engine must be uninitialized (NULL) on entry"}, error_message);
+    if (kind == kind_levenshtein_k && (match < 0 || mismatch < 0 || open < 0 || extend < 0))
+        return report({sz_overflow_risk_k, "Levenshtein costs must be non-negative"}, error_message);
+    if (kind != kind_levenshtein_k && (!byte_to_class || !table))
+        return report({sz_unexpected_dimensions_k, "Substitution tables must not be NULL"}, error_message);
+    engine_t *engine = new (std::nothrow) engine_t();
+    if (!engine) return report({sz_bad_alloc_k, "Failed to allocate the engine"}, error_message);
+    engine->kind = kind;
+    score_costs_t &costs = engine->costs;
+    std::memset(&costs, 0, sizeof(costs));
+    costs.kind = kind;
+    costs.open = open, costs.extend = extend;
+    costs.affine = open != extend; // `open == extend` selects the linear engine, as the reference's init does
+    costs.match = match, costs.mismatch = mismatch;
+    int magnitude = std::max(cost_abs(open), cost_abs(extend));
+    if (kind == kind_levenshtein_k) {
+        magnitude = std::max({magnitude, cost_abs(match), cost_abs(mismatch)});
+        costs.classes = 0;
+        engine->unit_levenshtein = match == 0 && mismatch == 1 && open == 1 && extend == 1;
+    }
+    else {
+        prepare_class_costs(costs, byte_to_class, table);
+        for (int i = 0; i < 1024; ++i) magnitude = std::max(magnitude, cost_abs(table[i]));
+    }
+    engine->magnitude = std::max(magnitude, 1);
+    *engine_out = engine;
+    return report({}, error_message);
+}
+
+void free_engine(void *handle) {
+    engine_t *engine = as_engine(handle, -1);
+    if (!engine) return;
+    engine->magic = 0;
+    delete engine;
+}
+
+sz_status_t not_in_scope(char const **error_message) {
+    return report({sz_status_unknown_k, "Not implemented by the GB300 engine (outside its scoring scope)"},
+                  error_message);
+}
+
+} // namespace
+
+extern "C" {
+
+SZS_GB300_API int szs_version_major(void) { return 5; }
+SZS_GB300_API int szs_version_minor(void) { return 3; }
+SZS_GB300_API int szs_version_patch(void) { return 2; }
+
+SZS_GB300_API sz_capability_t szs_capabilities_comptime(void) { return sz_caps_ckh_k; }
+SZS_GB300_API sz_capability_t szs_capabilities_runtime(void) {
+    return visible_devices() > 0 ? sz_caps_ckh_k : sz_caps_none_k;
+}
+SZS_GB300_API sz_capability_t szs_capabilities(void) {
+    static std::once_flag once;
+    static sz_capability_t cached = sz_caps_none_k;
+    std::call_once(once, [] { cached = (sz_capability_t)(szs_capabilities_comptime() & szs_capabilities_runtime()); });
+    return cached;
+}
+
+static void *unified_allocate_(sz_size_t size, void *) { return szs_unified_alloc(size); }
+static void unified_free_(void *p, sz_size_t size, void *) { szs_unified_free(p, size); }
+
+SZS_GB300_API sz_status_t sz_memory_allocator_init_unified(sz_memory_allocator_t *alloc, char const **error_message) {
+    if (!alloc) return report({sz_status_unknown_k, "Allocator must not be NULL"}, error_message);
+    alloc->allocate = &unified_allocate_;
+    alloc->free = &unified_free_;
+    alloc->handle = nullptr;
+    return report({}, error_message);
+}
+
+SZS_GB300_API void *szs_unified_alloc(sz_size_t size_bytes) {
+    void *p = nullptr;
+    if (cudaMallocManaged(&p, size_bytes ? size_bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+SZS_GB300_API void szs_unified_free(void *ptr, sz_size_t) {
+    if (ptr) cudaFree(ptr);
+}
+
+SZS_GB300_API sz_status_t szs_device_scope_init_default(szs_device_scope_t *scope, char const **error_message) {
+    if (!scope) return report({sz_status_unknown_k, "Scope must not be NULL"}, error_message);
+    auto *s = new (std::nothrow) scope_t();
+    if (!s) return report({sz_bad_alloc_k, "Failed to allocate device scope"}, error_message);
+    *scope = s;
+    return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_device_scope_init_cpu_cores(sz_size_t cpu_cores, szs_device_scope_t *scope,
+                                                          char const **error_message) {
+    if (!scope) return report({sz_status_unknown_k, "Scope must not be NULL"}, error_message);
+    // One core is the default scope, as in the reference (c/stringzillas/runtime.cuh:85-90).
+    if (cpu_cores == 1) return szs_device_scope_init_default(scope, error_message);
+    auto *s = new (std::nothrow) scope_t();
+    if (!s) return report({sz_bad_alloc_k, "Failed to allocate device scope"}, error_message);
+    s->kind = scope_cpu_k;
+    s->cpu_cores = cpu_cores;
+    *scope = s;
+    return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_device_scope_init_gpu_device(sz_size_t gpu_device, szs_device_scope_t *scope,
+                                                           char const **error_message) {
+    if (!scope) return report({sz_status_unknown_k, "Scope must not be NULL"}, error_message);
+    if ((int)gpu_device >= visible_devices() || gpu_device >= (sz_size_t)max_devices_k)
+        return report({sz_missing_gpu_k, nullptr}, error_message);
+    auto *s = new (std::nothrow) scope_t();
+    if (!s) return report({sz_bad_alloc_k, "Failed to allocate device scope"}, error_message);
+    s->kind = scope_gpu_k;
+    s->device = (int)gpu_device;
+    if (cudaSetDevice(s->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaError_t const error = cudaGetLastError();
+        delete s;
+        return report(from_cuda(error == cudaSuccess ? cudaErrorUnknown : error), error_message);
+    }
+    *scope = s;
+    return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_device_scope_get_cpu_cores(szs_device_scope_t scope, sz_size_t *cpu_cores,
+                                                         char const **error_message) {
+    scope_t *s = as_scope(scope);
+    if (!s || !cpu_cores) return report({sz_status_unknown_k, "Invalid device scope handle"}, error_message);
+    if (s->kind == scope_gpu_k) return report({sz_device_code_mismatch_k, nullptr}, error_message);
+    *cpu_cores = s->kind == scope_cpu_k ? s->cpu_cores : 1;
+    return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_device_scope_get_gpu_device(szs_device_scope_t scope, sz_size_t *gpu_device,
+                                                          char const **error_message) {
+    scope_t *s = as_scope(scope);
+    if (!s || !gpu_device) return report({sz_status_unknown_k, "Invalid device scope handle"}, error_message);
+    if (s->kind != scope_gpu_k) return report({sz_device_code_mismatch_k, nullptr}, error_message);
+    *gpu_device = (sz_size_t)s->device;
+    return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_device_scope_get_capabilities(szs_device_scope_t scope, sz_capability_t *capabilities,
+                                                            char const **error_message) {
+    scope_t *s = as_scope(scope);
+    if (!s || !capabilities) return report({sz_status_unknown_k, "Invalid device scope handle"}, error_message);
+    if (s->kind == scope_cpu_k) *capabilities = (sz_capability_t)(sz_cap_serial_k | sz_cap_parallel_k);
+    else if (s->kind == scope_gpu_k) *capabilities = sz_caps_ckh_k;
+    else *capabilities = (sz_capability_t)(sz_cap_serial_k | szs_capabilities());
+    return report({}, error_message);
+}
+
+SZS_GB300_API void szs_device_scope_free(szs_device_scope_t scope) {
+    scope_t *s = as_scope(scope);
+    if (!s) return;
+    if (s->stream) {
+        cudaSetDevice(s->device);
+        cudaStreamSynchronize(s->stream);
+        cudaStreamDestroy(s->stream);
+    }
+    s->magic = 0;
+    delete s;
+}
+
+/* Levenshtein */
+
+SZS_GB300_API sz_status_t szs_levenshtein_distances_init(sz_error_cost_t match, sz_error_cost_t mismatch,
+                                                         sz_error_cost_t open, sz_error_cost_t extend,
+                                                         sz_memory_allocator_t const *, sz_capability_t,
+                                                         szs_levenshtein_distances_t *engine,
+                                                         char const **error_message) {
+    return create_engine(kind_levenshtein_k, match, mismatch, open, extend, nullptr, nullptr, engine, error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances(szs_levenshtein_distances_t engine, szs_device_scope_t device,
+                                                    sz_sequence_t const *queries, sz_sequence_t const *candidates,
+                                                    sz_size_t *results, sz_size_t results_row_stride,
+                                                    char const **error_message) {
+    return score_cross_sequence(kind_levenshtein_k, engine, device, queries, candidates, results, results_row_stride,
+                                error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances_u32tape(szs_levenshtein_distances_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u32tape_t const *queries,
+                                                            sz_sequence_u32tape_t const *candidates,
+                                                            sz_size_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message) {
+    return score_cross(kind_levenshtein_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances_u64tape(szs_levenshtein_distances_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u64tape_t const *queries,
+                                                            sz_sequence_u64tape_t const *candidates,
+                                                            sz_size_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message) {
+    return score_cross(kind_levenshtein_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message);
+}
+SZS_GB300_API void szs_levenshtein_distances_free(szs_levenshtein_distances_t engine) { free_engine(engine); }
+
+/* UTF-8 Levenshtein: outside the engine's scope */
+
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_init(sz_error_cost_t, sz_error_cost_t, sz_error_cost_t,
+                                                              sz_error_cost_t, sz_memory_allocator_t const *,
+                                                              sz_capability_t, szs_levenshtein_distances_utf8_t *,
+                                                              char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8(szs_levenshtein_distances_utf8_t, szs_device_scope_t,
+                                                         sz_sequence_t const *, sz_sequence_t const *, sz_size_t *,
+                                                         sz_size_t, char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u32tape(szs_levenshtein_distances_utf8_t,
+                                                                 szs_device_scope_t, sz_sequence_u32tape_t const *,
+                                                                 sz_sequence_u32tape_t const *, sz_size_t *,
+                                                                 sz_size_t, char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u64tape(szs_levenshtein_distances_utf8_t,
+                                                                 szs_device_scope_t, sz_sequence_u64tape_t const *,
+                                                                 sz_sequence_u64tape_t const *, sz_size_t *,
+                                                                 sz_size_t, char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API void szs_levenshtein_distances_utf8_free(szs_levenshtein_distances_utf8_t) {}
+
+/* Needleman-Wunsch */
+
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_init(sz_u8_t const *byte_to_class,
+                                                           sz_error_cost_t const *class_substitution_costs,
+                                                           sz_error_cost_t open, sz_error_cost_t extend,
+                                                           sz_memory_allocator_t const *, sz_capability_t,
+                                                           szs_needleman_wunsch_scores_t *engine,
+                                                           char const **error_message) {
+    return create_engine(kind_needleman_wunsch_k, 0, 0, open, extend, byte_to_class, class_substitution_costs, engine,
+                         error_message);
+}
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores(szs_needleman_wunsch_scores_t engine, szs_device_scope_t device,
+                                                      sz_sequence_t const *queries, sz_sequence_t const *candidates,
+                                                      sz_ssize_t *results, sz_size_t results_row_stride,
+                                                      char const **error_message) {
+    return score_cross_sequence(kind_needleman_wunsch_k, engine, device, queries, candidates, results,
+                                results_row_stride, error_message);
+}
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_u32tape(szs_needleman_wunsch_scores_t engine,
+                                                              szs_device_scope_t device,
+                                                              sz_sequence_u32tape_t const *queries,
+                                                              sz_sequence_u32tape_t const *candidates,
+                                                              sz_ssize_t *results, sz_size_t results_row_stride,
+                                                              char const **error_message) {
+    return score_cross(kind_needleman_wunsch_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message);
+}
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_u64tape(szs_needleman_wunsch_scores_t engine,
+                                                              szs_device_scope_t device,
+                                                              sz_sequence_u64tape_t const *queries,
+                                                              sz_sequence_u64tape_t const *candidates,
+                                                              sz_ssize_t *results, sz_size_t results_row_stride,
+                                                              char const **error_message) {
+    return score_cross(kind_needleman_wunsch_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message);
+}
+SZS_GB300_API void szs_needleman_wunsch_scores_free(szs_needleman_wunsch_scores_t engine) { free_engine(engine); }
+
+/* Smith-Waterman */
+
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_init(sz_u8_t const *byte_to_class,
+                                                         sz_error_cost_t const *class_substitution_costs,
+                                                         sz_error_cost_t open, sz_error_cost_t extend,
+                                                         sz_memory_allocator_t const *, sz_capability_t,
+                                                         szs_smith_waterman_scores_t *engine,
+                                                         char const **error_message) {
+    return create_engine(kind_smith_waterman_k, 0, 0, open, extend, byte_to_class, class_substitution_costs, engine,
+                         error_message);
+}
+SZS_GB300_API sz_status_t szs_smith_waterman_scores(szs_smith_waterman_scores_t engine, szs_device_scope_t device,
+                                                    sz_sequence_t const *queries, sz_sequence_t const *candidates,
+                                                    sz_ssize_t *results, sz_size_t results_row_stride,
+                                                    char const **error_message) {
+    return score_cross_sequence(kind_smith_waterman_k, engine, device, queries, candidates, results,
+                                results_row_stride, error_message);
+}
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_u32tape(szs_smith_waterman_scores_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u32tape_t const *queries,
+                                                            sz_sequence_u32tape_t const *candidates,
+                                                            sz_ssize_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message) {
+    return score_cross(kind_smith_waterman_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message);
+}
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_u64tape(szs_smith_waterman_scores_t engine,
+                                                            szs_device_scope_t device,
+                                                            sz_sequence_u64tape_t const *queries,
+                                                            sz_sequence_u64tape_t const *candidates,
+                                                            sz_ssize_t *results, sz_size_t results_row_stride,
+                                                            char const **error_message) {
+    return score_cross(kind_smith_waterman_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message);
+}
+SZS_GB300_API void szs_smith_waterman_scores_free(szs_smith_waterman_scores_t engine) { free_engine(engine); }
+
+/* Fingerprints: outside the engine's scope */
+
+SZS_GB300_API sz_status_t szs_fingerprints_init(sz_size_t, sz_size_t, sz_size_t const *, sz_size_t, sz_u64_t,
+                                                sz_memory_allocator_t const *, sz_capability_t, szs_fingerprints_t *,
+                                                char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API sz_status_t szs_fingerprints_sequence(szs_fingerprints_t, szs_device_scope_t, sz_sequence_t const *,
+                                                    sz_u32_t *, sz_size_t, sz_u32_t *, sz_size_t,
+                                                    char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API sz_status_t szs_fingerprints_u64tape(szs_fingerprints_t, szs_device_scope_t,
+                                                   sz_sequence_u64tape_t const *, sz_u32_t *, sz_size_t, sz_u32_t *,
+                                                   sz_size_t, char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API sz_status_t szs_fingerprints_u32tape(szs_fingerprints_t, szs_device_scope_t,
+                                                   sz_sequence_u32tape_t const *, sz_u32_t *, sz_size_t, sz_u32_t *,
+                                                   sz_size_t, char const **error_message) {
+    return not_in_scope(error_message);
+}
+SZS_GB300_API void szs_fingerprints_free(szs_fingerprints_t) {}
+
+/* Extensions */
+
+SZS_GB300_API sz_status_t szs_levenshtein_distances_pairwise_u32tape(szs_levenshtein_distances_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u32tape_t const *first,
+                                                                     sz_sequence_u32tape_t const *second,
+                                                                     sz_size_t *results, char const **error_message) {
+    return score_pairwise(kind_levenshtein_k, engine, device, first, second, results, error_message);
+}
+SZS_GB300_API sz_status_t szs_levenshtein_distances_pairwise_u64tape(szs_levenshtein_distances_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u64tape_t const *first,
+                                                                     sz_sequence_u64tape_t const *second,
+                                                                     sz_size_t *results, char const **error_message) {
+    return score_pairwise(kind_levenshtein_k, engine, device, first, second, results, error_message);
+}
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_pairwise_u32tape(szs_needleman_wunsch_scores_t engine,
+                                                                       szs_device_scope_t device,
+                                                                       sz_sequence_u32tape_t const *first,
+                                                                       sz_sequence_u32tape_t const *second,
+                                                                       sz_ssize_t *results,
+                                                                       char const **error_message) {
+    return score_pairwise(kind_needleman_wunsch_k, engine, device, first, second, results, error_message);
+}
+SZS_GB300_API sz_status_t szs_needleman_wunsch_scores_pairwise_u64tape(szs_needleman_wunsch_scores_t engine,
+                                                                       szs_device_scope_t device,
+                                                                       sz_sequence_u64tape_t const *first,
+                                                                       sz_sequence_u64tape_t const *second,
+                                                                       sz_ssize_t *results,
+                                                                       char const **error_message) {
+    return score_pairwise(kind_needleman_wunsch_k, engine, device, first, second, results, error_message);
+}
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_pairwise_u32tape(szs_smith_waterman_scores_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u32tape_t const *first,
+                                                                     sz_sequence_u32tape_t const *second,
+                                                                     sz_ssize_t *results, char const **error_message) {
+    return score_pairwise(kind_smith_waterman_k, engine, device, first, second, results, error_message);
+}
+SZS_GB300_API sz_status_t szs_smith_waterman_scores_pairwise_u64tape(szs_smith_waterman_scores_t engine,
+                                                                     szs_device_scope_t device,
+                                                                     sz_sequence_u64tape_t const *first,
+                                                                     sz_sequence_u64tape_t const *second,
+                                                                     sz_ssize_t *results, char const **error_message) {
+    return score_pairwise(kind_smith_waterman_k, engine, device, first, second, results, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_engine_set_schedule(void *engine_handle, szs_gb300_schedule_t schedule,
+                                                        char const **error_message) {
+    engine_t *engine = as_engine(engine_handle, -1);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (schedule != szs_gb300_schedule_batched_k && schedule != szs_gb300_schedule_plain_k)
+        return report({sz_status_unknown_k, "Unknown schedule"}, error_message);
+    engine->schedule = schedule;
+    return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine_handle, szs_gb300_stats_t *stats,
+                                                     char const **error_message) {
+    engine_t *engine = as_engine(engine_handle, -1);
+    if (!engine || !stats) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    *stats = engine->stats;
+    return report({}, error_message);
+}
+
+} // extern "C"

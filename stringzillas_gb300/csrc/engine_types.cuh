@@ -1,0 +1,60 @@
+/**
+ *  @file engine_types.cuh
+ *  @brief Types shared by the host orchestration and the device kernels of the GB300 scoring engine.
+ *
+ *  Terminology: a "pair" is one (first, second) string pair whose score lands in one output cell. Inside the DP
+ *  kernels the pair is laid out as a matrix of `rows` (the shorter string, held in registers, 32 lanes x R rows per
+ *  "strip") by `cols` (the longer string, streamed column by column). `transposed` records that rows came from the
+ *  second string, so class-table lookups swap their operands back and scores stay `cost(first[i], second[j])`,
+ *  as the reference's walkers guarantee (include/stringzillas/similarities/serial.hpp:1179, :721-722).
+ */
+#pragma once
+#include <cstdint>
+
+namespace szs_gb300 {
+
+enum score_kind_t : int {
+    kind_levenshtein_k = 0,      // minimise, uniform match / mismatch
+    kind_needleman_wunsch_k = 1, // maximise, global, class table
+    kind_smith_waterman_k = 2,   // maximise, local, class table
+};
+
+/** How a pair is scored; chosen per pair by the planner. */
+enum pair_route_t : int {
+    route_trivial_k = 0, // an empty side: answered by the closed form, no kernel
+    route_myers_k = 1,   // unit-cost Levenshtein, bit-parallel, thread per pair
+    route_dp32_k = 2,    // wavefront DP, 32-bit cells, warp per pair
+    route_dp64_k = 3,    // wavefront DP, 64-bit cells, warp per pair (only when 32-bit could overflow)
+};
+
+/** One scheduled pair. 32 bytes; the planner writes these in scheduled order. */
+struct pair_task_t {
+    std::uint8_t const *rows;  // the string laid along DP rows (the shorter one)
+    std::uint8_t const *cols;  // the string laid along DP columns
+    std::uint32_t rows_length; // n >= 1 for DP routes
+    std::uint32_t cols_length; // m >= 1 for DP routes
+    std::uint32_t slot;        // index into the dense per-pair results array
+    std::uint32_t transposed;  // 1 if rows came from the second string
+};
+
+/** Costs as the kernels see them. Copied into shared memory by every CTA that needs the tables. */
+struct score_costs_t {
+    int kind;                       // score_kind_t
+    int affine;                     // 0: linear gaps (open == extend), 1: affine
+    int open, extend;               // gap costs; a gap of length k costs open + (k-1)*extend
+    int match, mismatch;            // Levenshtein substitution costs
+    int classes;                    // number of compact column classes (NW / SW), <= 32
+    std::uint8_t byte_to_compact[256];  // byte -> compact class, indexing `profile_table` rows
+    std::int8_t profile_table[32 * 32]; // [compact column class][row class] cost, already oriented for rows=first
+    std::int8_t profile_table_t[32 * 32]; // same for rows=second (transposed lookups)
+    std::uint8_t byte_to_class[256];      // byte -> full class of the reference's 32x32 table
+};
+
+/** Alphabet of a batch: byte -> dense code, and the number of code bits the bit-parallel kernel needs. */
+struct batch_alphabet_t {
+    std::uint8_t code[256];
+    std::uint32_t symbols;
+    std::uint32_t bits;
+};
+
+} // namespace szs_gb300

@@ -1,0 +1,52 @@
+/**
+ *  @file launchers.h
+ *  @brief Host-side launch entry points of the engine's kernels, one translation unit per kernel family so the
+ *         template instantiations compile in parallel.
+ */
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "engine_types.cuh"
+#include "planner.cuh"
+
+namespace szs_gb300 {
+
+cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t *tasks, std::int64_t *results,
+                        int sm_count, cudaStream_t stream);
+cudaError_t launch_alphabet(std::uint8_t const *data, std::uint64_t length, std::uint32_t *symbol_mask, int sm_count,
+                            cudaStream_t stream);
+cudaError_t launch_alphabet_codes(std::uint32_t const *symbol_mask, batch_alphabet_t *alphabet, cudaStream_t stream);
+cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
+                                  std::uint64_t stride, int sm_count, cudaStream_t stream);
+
+/** Shape of a wavefront-DP launch for one engine configuration. */
+struct dp_launch_shape_t {
+    int threads_per_cta;
+    int warps_per_cta;
+    int shared_bytes;
+    int ctas_per_sm; // from the occupancy calculator
+    int rows_per_lane;
+};
+
+/** Launch shape of the wavefront kernel for (kind, affine, cell bits, classes); ctas_per_sm = 0 if unsupported. */
+dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes);
+
+/** Runs the wavefront kernel over bins [key_begin, key_end). `scratch` holds `ctas * warps_per_cta` rows of
+ *  `scratch_cells_per_warp` cells of `cell_bits` bits. */
+cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int key_end, pair_task_t const *tasks,
+                      plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                      std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
+
+/** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
+ *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be
+ *  shorter (the plain schedule puts every bit-parallel pair in the 16-word bin). */
+cudaError_t launch_myers(int words, int planes, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
+                         batch_alphabet_t const *alphabet, std::int64_t *results, int ctas, cudaStream_t stream);
+int myers_threads_per_cta();
+/** Planes actually instantiated for a requested minimum. */
+int myers_planes_for(int bits_needed);
+
+} // namespace szs_gb300

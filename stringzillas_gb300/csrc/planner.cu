@@ -1,0 +1,303 @@
+/**
+ *  @file planner.cu
+ *  @brief Planning kernels: pair enumeration, routing, binning, the batch alphabet, and the output scatter.
+ */
+#include "launchers.h"
+#include "planner.cuh"
+
+#include <cuda_runtime.h>
+
+namespace szs_gb300 {
+
+__device__ __forceinline__ void tape_string(tape_t const &tape, std::uint64_t index, std::uint8_t const *&start,
+                                            std::uint64_t &length) {
+    std::uint64_t begin, end;
+    if (tape.offset_bits == 32) {
+        auto const *offsets = static_cast<std::uint32_t const *>(tape.offsets);
+        begin = offsets[index], end = offsets[index + 1];
+    }
+    else {
+        auto const *offsets = static_cast<std::uint64_t const *>(tape.offsets);
+        begin = offsets[index], end = offsets[index + 1];
+    }
+    start = tape.base + begin;
+    length = end - begin;
+}
+
+/** Maps a flat pair index onto (query, candidate); the symmetric form walks the lower triangle row by row, the
+ *  order `cross_sequentially_` uses (serial.hpp:2565-2576). */
+__device__ __forceinline__ void pair_indices(plan_args_t const &args, std::uint64_t p, std::uint64_t &q,
+                                             std::uint64_t &c) {
+    if (args.mode == mode_pairwise_k) q = c = p;
+    else if (args.mode == mode_cross_k) q = p / args.candidates_count, c = p % args.candidates_count;
+    else {
+        std::uint64_t row = (std::uint64_t)((sqrt(8.0 * (double)p + 1.0) - 1.0) / 2.0);
+        while (row * (row + 1) / 2 > p) --row;
+        while ((row + 1) * (row + 2) / 2 <= p) ++row;
+        q = row, c = p - row * (row + 1) / 2;
+    }
+}
+
+/** Closed form of a pair with an empty side (serial.hpp:142-151, :2493-2496). */
+__device__ __forceinline__ std::int64_t trivial_score(plan_args_t const &args, std::uint64_t n, std::uint64_t m) {
+    if (args.kind == kind_smith_waterman_k) return 0;
+    std::uint64_t const length = n > m ? n : m;
+    if (!args.affine) return (std::int64_t)args.open * (std::int64_t)length;
+    return length == 0 ? 0 : (std::int64_t)args.open + (std::int64_t)args.extend * (std::int64_t)(length - 1);
+}
+
+__device__ __forceinline__ int floor_log2_u64(std::uint64_t x) { return x ? 63 - __clzll((long long)x) : 0; }
+
+struct pair_route_info_t {
+    int key; // -1 for trivial
+    std::uint8_t const *rows, *cols;
+    std::uint32_t n, m;
+    std::uint32_t transposed;
+};
+
+/** Routing decision for one pair. The 32-bit bound mirrors the reference's `worst_case_reach` (serial.hpp:117-140)
+ *  with one extra step of headroom for the E/F intermediates. */
+__device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args, std::uint8_t const *first,
+                                                        std::uint64_t first_length, std::uint8_t const *second,
+                                                        std::uint64_t second_length) {
+    pair_route_info_t info;
+    info.key = -1;
+    // Rows take the shorter string; equal lengths keep the first string on rows.
+    bool const swap = second_length < first_length;
+    info.rows = swap ? second : first;
+    info.cols = swap ? first : second;
+    info.n = (std::uint32_t)(swap ? second_length : first_length);
+    info.m = (std::uint32_t)(swap ? first_length : second_length);
+    info.transposed = swap ? 1u : 0u;
+    if (first_length == 0 || second_length == 0) return info;
+    std::uint64_t const n = info.n, m = info.m;
+    if (args.unit_levenshtein && n <= 32u * myers_max_words_k) {
+        if (args.force_route >= 0) {
+            info.key = bin_myers_begin_k + myers_max_words_k * 16; // plain form: one bin, one kernel shape
+            return info;
+        }
+        int const words = int((n + 31) / 32);
+        int text_class;
+        if (m < 512) text_class = int(m / 64);
+        else text_class = min(15, 8 + floor_log2_u64(m) - 9);
+        info.key = bin_myers_begin_k + words * 16 + text_class;
+        return info;
+    }
+    bool const maximize = args.kind != kind_levenshtein_k;
+    std::uint64_t const span = maximize ? n + m : (n > m ? n : m);
+    std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;
+    bool const fits32 = reach < (1ull << 31) - 1;
+    int const base = fits32 ? bin_dp32_begin_k : bin_dp64_begin_k;
+    if (args.force_route >= 0) {
+        info.key = base; // one bin, input order is kept by the caller's launch
+        return info;
+    }
+    int size_class = floor_log2_u64(n * m) - 10;
+    size_class = size_class < 0 ? 0 : (size_class > bin_dp_classes_k - 1 ? bin_dp_classes_k - 1 : size_class);
+    info.key = base + (bin_dp_classes_k - 1 - size_class);
+    return info;
+}
+
+__device__ __forceinline__ pair_route_info_t route_of_pair(plan_args_t const &args, std::uint64_t p) {
+    std::uint64_t q, c;
+    pair_indices(args, p, q, c);
+    std::uint8_t const *first, *second;
+    std::uint64_t first_length, second_length;
+    tape_string(args.queries, q, first, first_length);
+    tape_string(args.mode == mode_symmetric_k ? args.queries : args.candidates, c, second, second_length);
+    return route_pair(args, first, first_length, second, second_length);
+}
+
+/** Pass 1: answer trivial pairs, count pairs per bin, track the longest column string and total cells. */
+__global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restrict__ bins,
+                                  std::int64_t *__restrict__ results) {
+    __shared__ std::uint32_t histogram[bin_keys_k];
+    __shared__ unsigned long long block_cells;
+    __shared__ std::uint32_t block_max_cols;
+    for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x) histogram[i] = 0;
+    if (threadIdx.x == 0) block_cells = 0, block_max_cols = 0;
+    __syncthreads();
+    std::uint64_t thread_cells = 0;
+    std::uint32_t thread_max_cols = 0;
+    for (std::uint64_t p = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < args.pairs;
+         p += (std::uint64_t)gridDim.x * blockDim.x) {
+        pair_route_info_t const info = route_of_pair(args, p);
+        thread_cells += (std::uint64_t)info.n * info.m;
+        if (info.key < 0) {
+            results[p] = trivial_score(args, info.n, info.m);
+            continue;
+        }
+        atomicAdd(&histogram[info.key], 1u);
+        if (info.key >= bin_dp32_begin_k) thread_max_cols = max(thread_max_cols, info.m);
+    }
+    atomicAdd(&block_cells, (unsigned long long)thread_cells);
+    atomicMax(&block_max_cols, thread_max_cols);
+    __syncthreads();
+    for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x)
+        if (histogram[i]) atomicAdd(&bins->count[i], histogram[i]);
+    if (threadIdx.x == 0) {
+        atomicAdd((unsigned long long *)&bins->cells, block_cells);
+        atomicMax(&bins->max_cols, block_max_cols);
+    }
+}
+
+/** Pass 2: exclusive scan of bin counts (one CTA of `bin_keys_k` threads). */
+__global__ void plan_scan_kernel(plan_bins_t *__restrict__ bins) {
+    __shared__ std::uint32_t scan[bin_keys_k];
+    int const i = threadIdx.x;
+    std::uint32_t const own = bins->count[i];
+    scan[i] = own;
+    __syncthreads();
+    for (int offset = 1; offset < bin_keys_k; offset <<= 1) {
+        std::uint32_t const add = i >= offset ? scan[i - offset] : 0u;
+        __syncthreads();
+        scan[i] += add;
+        __syncthreads();
+    }
+    bins->begin[i] = scan[i] - own;
+    bins->fill[i] = 0;
+    bins->cursor[i] = 0;
+    if (i == bin_keys_k - 1) bins->scheduled = scan[i];
+}
+
+/** Pass 3: write each routed pair into its bin; lanes sharing a bin reserve their slots with one atomic. */
+__global__ void plan_scatter_kernel(plan_args_t const args, plan_bins_t *__restrict__ bins,
+                                    pair_task_t *__restrict__ tasks) {
+    int const lane = threadIdx.x & 31;
+    std::uint64_t const warps = (std::uint64_t)gridDim.x * (blockDim.x / 32);
+    std::uint64_t const warp = (std::uint64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    for (std::uint64_t base = warp * 32; base < args.pairs; base += warps * 32) {
+        std::uint64_t const p = base + lane;
+        pair_route_info_t info;
+        info.key = -1;
+        if (p < args.pairs) info = route_of_pair(args, p);
+        unsigned const key = info.key < 0 ? 0xFFFFFFFFu : (unsigned)info.key;
+        unsigned const peers = __match_any_sync(0xFFFFFFFFu, key);
+        int const leader = __ffs(peers) - 1;
+        unsigned const rank = __popc(peers & ((1u << lane) - 1u));
+        std::uint32_t slot_base = 0;
+        if (lane == leader && key != 0xFFFFFFFFu) slot_base = atomicAdd(&bins->fill[key], (unsigned)__popc(peers));
+        slot_base = __shfl_sync(0xFFFFFFFFu, slot_base, leader);
+        if (key != 0xFFFFFFFFu) {
+            pair_task_t task;
+            task.rows = info.rows, task.cols = info.cols;
+            task.rows_length = info.n, task.cols_length = info.m;
+            task.slot = (std::uint32_t)p;
+            task.transposed = info.transposed;
+            tasks[bins->begin[key] + slot_base + rank] = task;
+        }
+    }
+}
+
+/** Marks every byte value present in a tape's data range, 16 bytes per load where aligned. */
+__global__ void alphabet_mark_kernel(std::uint8_t const *__restrict__ data, std::uint64_t length,
+                                     std::uint32_t *__restrict__ symbol_mask) {
+    __shared__ std::uint32_t mask[8];
+    if (threadIdx.x < 8) mask[threadIdx.x] = 0;
+    __syncthreads();
+    std::uint32_t local[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // Head bytes up to 16-byte alignment, then aligned 16-byte loads, then the tail.
+    std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(data);
+    std::uint64_t head = (16 - (address & 15)) & 15;
+    if (head > length) head = length;
+    std::uint64_t const thread = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    std::uint64_t const threads = (std::uint64_t)gridDim.x * blockDim.x;
+    if (thread < head) {
+        std::uint32_t const b = data[thread];
+        local[b >> 5] |= 1u << (b & 31);
+    }
+    std::uint64_t const body = (length - head) / 16;
+    uint4 const *vectors = reinterpret_cast<uint4 const *>(data + head);
+    for (std::uint64_t v = thread; v < body; v += threads) {
+        uint4 const x = __ldg(vectors + v);
+        std::uint32_t const words[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int s = 0; s < 32; s += 8) {
+                std::uint32_t const b = (words[k] >> s) & 0xFF;
+                local[b >> 5] |= 1u << (b & 31);
+            }
+    }
+    std::uint64_t const tail_begin = head + body * 16;
+    if (thread < length - tail_begin) {
+        std::uint32_t const b = data[tail_begin + thread];
+        local[b >> 5] |= 1u << (b & 31);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (local[k]) atomicOr(&mask[k], local[k]);
+    __syncthreads();
+    if (threadIdx.x < 8 && mask[threadIdx.x]) atomicOr(&symbol_mask[threadIdx.x], mask[threadIdx.x]);
+}
+
+/** Dense codes for the marked bytes; `bits` = planes the Myers kernel needs (1..8). */
+__global__ void alphabet_codes_kernel(std::uint32_t const *__restrict__ symbol_mask,
+                                      batch_alphabet_t *__restrict__ alphabet) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    std::uint32_t next = 0;
+    for (int b = 0; b < 256; ++b) {
+        bool const present = (symbol_mask[b >> 5] >> (b & 31)) & 1u;
+        alphabet->code[b] = present ? (std::uint8_t)next : 0;
+        next += present;
+    }
+    std::uint32_t bits = 1;
+    while ((1u << bits) < next) ++bits;
+    alphabet->symbols = next;
+    alphabet->bits = bits;
+}
+
+/** Dense per-pair results into the caller's matrix (device-resident output). */
+__global__ void scatter_output_kernel(plan_args_t const args, std::int64_t const *__restrict__ results,
+                                      std::int64_t *__restrict__ out, std::uint64_t stride) {
+    for (std::uint64_t p = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < args.pairs;
+         p += (std::uint64_t)gridDim.x * blockDim.x) {
+        std::int64_t const value = results[p];
+        if (args.mode == mode_pairwise_k) {
+            out[p] = value;
+            continue;
+        }
+        std::uint64_t q, c;
+        pair_indices(args, p, q, c);
+        out[q * stride + c] = value;
+        if (args.mode == mode_symmetric_k && q != c) out[c * stride + q] = value;
+    }
+}
+
+static int grid_for(std::uint64_t items, int block, int sm_count, int per_sm = 8) {
+    std::uint64_t const needed = (items + block - 1) / block;
+    std::uint64_t const cap = (std::uint64_t)sm_count * per_sm;
+    return (int)(needed < cap ? (needed ? needed : 1) : cap);
+}
+
+cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t *tasks, std::int64_t *results,
+                        int sm_count, cudaStream_t stream) {
+    cudaError_t status = cudaMemsetAsync(bins, 0, sizeof(plan_bins_t), stream);
+    if (status != cudaSuccess) return status;
+    if (args.pairs == 0) return cudaSuccess;
+    plan_count_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, bins, results);
+    plan_scan_kernel<<<1, bin_keys_k, 0, stream>>>(bins);
+    plan_scatter_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, bins, tasks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alphabet(std::uint8_t const *data, std::uint64_t length, std::uint32_t *symbol_mask, int sm_count,
+                            cudaStream_t stream) {
+    if (length == 0) return cudaSuccess;
+    alphabet_mark_kernel<<<grid_for(length / 16 + 1, 256, sm_count, 4), 256, 0, stream>>>(data, length, symbol_mask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alphabet_codes(std::uint32_t const *symbol_mask, batch_alphabet_t *alphabet, cudaStream_t stream) {
+    alphabet_codes_kernel<<<1, 32, 0, stream>>>(symbol_mask, alphabet);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
+                                  std::uint64_t stride, int sm_count, cudaStream_t stream) {
+    if (args.pairs == 0) return cudaSuccess;
+    scatter_output_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, results, out, stride);
+    return cudaGetLastError();
+}
+
+} // namespace szs_gb300

@@ -1,0 +1,70 @@
+/**
+ *  @file planner.cuh
+ *  @brief Device-side planning of one batch: enumerate the pairs of a call, answer the trivial ones, choose a
+ *         route and a length bin for the rest, and counting-sort them into bins.
+ *
+ *  The reference does this with a materialisation kernel, a min/max probe, a histogram, a scan and a scatter,
+ *  syncing the host between stages (include/stringzillas/similarities/cuda.cuh:1583-1747, :1859-1914). Here the
+ *  whole plan stays on the device: three kernels, no host round trip until the launch list is read back, and
+ *  bins are ordered so persistent kernels meet the longest pairs first (longest-processing-time order).
+ *
+ *  Bin keys:
+ *    [0, 272)    Myers: key = words * 16 + text-length class (words 1..16)
+ *    [272, 304)  32-bit wavefront DP: key = 272 + (31 - size class), size class ~ log2(n * m)
+ *    [304, 336)  64-bit wavefront DP: same layout
+ */
+#pragma once
+#include "engine_types.cuh"
+
+namespace szs_gb300 {
+
+constexpr int bin_keys_k = 512;
+constexpr int bin_myers_begin_k = 0;
+constexpr int bin_dp32_begin_k = 272;
+constexpr int bin_dp64_begin_k = 304;
+constexpr int bin_dp_classes_k = 32;
+constexpr int myers_max_words_k = 16;
+
+/** Which pairs a call scores. */
+enum pair_mode_t : int {
+    mode_pairwise_k = 0,  // (i, i)
+    mode_cross_k = 1,     // (q, c) for all q, c
+    mode_symmetric_k = 2, // (q, c) for c <= q, mirrored on output
+};
+
+/** A tape as the kernels see it: `base + offsets[i]` is the start of string i. */
+struct tape_t {
+    std::uint8_t const *base;
+    void const *offsets;
+    std::uint64_t count;
+    int offset_bits; // 32 or 64
+};
+
+/** Everything the planning kernels need. */
+struct plan_args_t {
+    tape_t queries, candidates;
+    int mode;
+    std::uint64_t pairs;
+    std::uint64_t candidates_count; // columns of the cross product
+    int kind, affine;
+    int open, extend, match, mismatch;
+    int unit_levenshtein;   // 0/1/1/1 Levenshtein: bit-parallel route
+    int magnitude;          // max |cost| over substitution and gap costs, at least 1
+    int steps_beyond_span;  // 1 linear, 3 affine (serial.hpp:126-140)
+    int force_route;        // -1: normal planning; otherwise every non-trivial pair takes this DP route
+};
+
+/** Per-bin counters the planner fills. */
+struct plan_bins_t {
+    std::uint32_t count[bin_keys_k];
+    std::uint32_t begin[bin_keys_k];
+    std::uint32_t fill[bin_keys_k];
+    std::uint32_t cursor[bin_keys_k];
+    std::uint32_t max_cols;
+    std::uint32_t error_flags;
+    std::uint32_t symbol_mask[8]; // bytes seen in Myers pairs
+    std::uint64_t cells;
+    std::uint64_t scheduled;
+};
+
+} // namespace szs_gb300

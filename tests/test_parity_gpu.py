@@ -1,0 +1,221 @@
+"""GPU parity: every route of the engine against the oracle, bit for bit, through the C-ABI."""
+import numpy as np
+import pytest
+
+from conftest import tape
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+DNA = np.frombuffer(b"ACGT", dtype=np.uint8)
+PROTEIN = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+
+
+@pytest.fixture(scope="module")
+def szs():
+    import stringzillas_gb300
+    if "cuda" not in stringzillas_gb300.__capabilities__:
+        pytest.fail("no CUDA device visible: GPU tests must run on a GPU")
+    return stringzillas_gb300
+
+
+def random_strings(rng, count, low, high, alphabet):
+    return [bytes(rng.choice(alphabet, size=int(rng.integers(low, high + 1)))) for _ in range(count)]
+
+
+def dna_tables():
+    b2c = np.zeros(256, dtype=np.uint8)
+    b2c[DNA] = [1, 2, 3, 4]
+    table = np.zeros((32, 32), dtype=np.int8)
+    table[1:5, 1:5] = -3
+    np.fill_diagonal(table[1:5, 1:5], 2)
+    return b2c, table
+
+
+def protein_tables(rng, symmetric=True):
+    b2c = np.zeros(256, dtype=np.uint8)
+    b2c[PROTEIN] = np.arange(1, 21, dtype=np.uint8)
+    table = np.zeros((32, 32), dtype=np.int8)
+    core = rng.integers(-4, 4, size=(20, 20))
+    if symmetric:
+        core = np.triu(core) + np.triu(core, 1).T
+        np.fill_diagonal(core, rng.integers(4, 12, size=20))
+    table[1:21, 1:21] = core
+    return b2c, table
+
+
+ENGINES = [
+    ("lev-unit", "lev", (0, 1, 1, 1)),
+    ("lev-linear", "lev", (0, 3, 2, 2)),
+    ("lev-affine", "lev", (0, 4, 5, 2)),
+    ("lev-match-cost", "lev", (1, 3, 4, 1)),
+    ("nw-linear", "nw", (-5, -5)),
+    ("nw-affine", "nw", (-11, -1)),
+    ("sw-linear", "sw", (-5, -5)),
+    ("sw-affine", "sw", (-5, -2)),
+    ("nw-positive-gaps", "nw", (3, 1)),
+]
+
+
+def make_engine(szs, family, costs, b2c, table):
+    if family == "lev":
+        return szs.LevenshteinDistances(*costs), oracle.levenshtein_costs(*costs)
+    kind = oracle.NEEDLEMAN_WUNSCH if family == "nw" else oracle.SMITH_WATERMAN
+    cls = szs.NeedlemanWunschScores if family == "nw" else szs.SmithWatermanScores
+    return cls(b2c, table, open=costs[0], extend=costs[1]), oracle.alignment_costs(kind, b2c, table, *costs)
+
+
+@pytest.mark.parametrize("name,family,costs", ENGINES, ids=[e[0] for e in ENGINES])
+@pytest.mark.parametrize("lengths", [(0, 6), (1, 40), (50, 600), (900, 2100)], ids=["tiny", "short", "strips", "long"])
+def test_pairwise_matches_oracle(szs, port, name, family, costs, lengths):
+    rng = np.random.default_rng(abs(hash((name, lengths))) % 2**32)
+    alphabet = DNA if family != "nw" or name == "nw-positive-gaps" else PROTEIN
+    b2c, table = dna_tables() if alphabet is DNA else protein_tables(rng)
+    count = 200 if lengths[1] <= 600 else 24
+    first = random_strings(rng, count, *lengths, alphabet)
+    second = random_strings(rng, count, *lengths, alphabet)
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    bad = np.flatnonzero(got != want)
+    assert bad.size == 0, f"{name}: {bad.size} mismatches, first {bad[:5]}: got {got[bad[:5]]} want {want[bad[:5]]}"
+
+
+@pytest.mark.parametrize("family,costs", [("nw", (-3, -1)), ("sw", (-3, -1)), ("nw", (-2, -2)), ("sw", (-4, -4))])
+def test_asymmetric_table_orientation(szs, port, family, costs):
+    """Cost lookups must stay cost(first[i], second[j]) whichever string the kernel lays along its rows."""
+    rng = np.random.default_rng(11)
+    b2c, table = protein_tables(rng, symmetric=False)
+    first = random_strings(rng, 150, 1, 400, PROTEIN)
+    second = random_strings(rng, 150, 1, 400, PROTEIN)
+    second[:20] = [bytes(rng.choice(PROTEIN, size=len(f))) for f in first[:20]]  # equal lengths too
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("name,family,costs", ENGINES[:1] + ENGINES[2:3] + ENGINES[5:6] + ENGINES[7:8],
+                         ids=["lev-unit", "lev-affine", "nw-affine", "sw-affine"])
+def test_cross_and_symmetric_matrices(szs, port, name, family, costs):
+    rng = np.random.default_rng(5)
+    alphabet = DNA if family != "nw" else PROTEIN
+    b2c, table = dna_tables() if alphabet is DNA else protein_tables(rng)
+    queries = random_strings(rng, 9, 0, 300, alphabet)
+    candidates = random_strings(rng, 13, 0, 300, alphabet)
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    got = engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64)
+    want = port.cross(oracle_costs, tape(queries), tape(candidates))
+    np.testing.assert_array_equal(got, want)
+    got_sym = engine(szs.Strs(queries)).astype(np.int64)
+    want_sym = port.cross(oracle_costs, tape(queries))
+    np.testing.assert_array_equal(got_sym, want_sym)
+    # out= with a wider row stride keeps the padding untouched
+    out = np.full((9, 20), 7, dtype=engine._dtype)
+    returned = engine(szs.Strs(queries), szs.Strs(candidates), out=out)
+    assert returned is out
+    np.testing.assert_array_equal(out[:, :13].astype(np.int64), want)
+    assert (out[:, 13:] == 7).all()
+
+
+def test_myers_every_word_count(szs, port):
+    """Unit-cost Levenshtein takes the bit-parallel route for shorter sides up to 512, the DP route above."""
+    rng = np.random.default_rng(3)
+    first, second = [], []
+    for n in list(range(1, 70)) + list(range(90, 530, 7)):
+        first.append(bytes(rng.choice(DNA, size=n)))
+        second.append(bytes(rng.choice(DNA, size=int(rng.integers(n, n + 400)))))
+    engine = szs.LevenshteinDistances()
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle.levenshtein_costs(), tape(first), tape(second))
+    np.testing.assert_array_equal(got, want)
+    # Large alphabets need more code planes.
+    text = np.arange(256, dtype=np.uint8)
+    first = [bytes(rng.choice(text, size=int(rng.integers(1, 300)))) for _ in range(100)]
+    second = [bytes(rng.choice(text, size=int(rng.integers(1, 300)))) for _ in range(100)]
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle.levenshtein_costs(), tape(first), tape(second))
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("schedule", ["batched", "plain"])
+def test_schedules_agree(szs, port, schedule):
+    rng = np.random.default_rng(21)
+    b2c, table = protein_tables(rng)
+    first = random_strings(rng, 300, 0, 700, PROTEIN)
+    second = random_strings(rng, 300, 0, 700, PROTEIN)
+    for family, costs in (("nw", (-11, -1)), ("sw", (-5, -2)), ("lev", (0, 1, 1, 1))):
+        engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+def test_device_resident_and_sliced_inputs(szs, port):
+    rng = np.random.default_rng(8)
+    strings = random_strings(rng, 40, 0, 200, DNA)
+    engine = szs.LevenshteinDistances(0, 2, 3, 1)
+    host = szs.Strs(strings)
+    sliced = host[5:25]  # first offset is not zero
+    want = port.cross(oracle.levenshtein_costs(0, 2, 3, 1), tape(strings[5:25]), tape(strings[:10]))
+    np.testing.assert_array_equal(engine(sliced, host[:10]).astype(np.int64), want)
+    device = szs.to_device(szs.Strs(strings))
+    np.testing.assert_array_equal(engine(device[5:25], device[:10]).astype(np.int64), want)
+
+
+def test_reference_known_answers(szs):
+    """Hand-checked cases of the reference's own tests (test/similarities.py:124-143, :170-197)."""
+    unit = szs.LevenshteinDistances()
+
+    def d(engine, a, b):
+        return int(engine(szs.Strs([a]), szs.Strs([b]))[0, 0])
+
+    assert d(unit, "hello", "hello") == 0
+    assert d(unit, "hello", "hell") == 1
+    assert d(unit, "", "") == 0
+    assert d(unit, "", "abc") == 3
+    assert d(unit, "abc", "") == 3
+    assert d(unit, "abc", "ac") == 1
+    assert d(unit, "abc", "a_bc") == 1
+    assert d(unit, "abc", "adc") == 1
+    assert d(unit, "ggbuzgjux{}l", "gbuzgjux{}l") == 1
+    assert d(unit, "abcdefgABCDEFG", "ABCDEFGabcdefg") == 14
+    mismatch, opening, extension = 4, 3, 2
+    custom = szs.LevenshteinDistances(open=opening, extend=extension, mismatch=mismatch)
+    assert d(custom, "hello", "hello") == 0
+    assert d(custom, "hello", "hell") == opening
+    assert d(custom, "", "") == 0
+    assert d(custom, "", "abc") == opening + 2 * extension
+    assert d(custom, "abc", "") == opening + 2 * extension
+    assert d(custom, "abc", "ac") == opening
+    assert d(custom, "abc", "a_bc") == opening
+    assert d(custom, "abc", "adc") == mismatch
+    assert d(custom, "ggbuzgjux{}l", "gbuzgjux{}l") == opening
+    assert d(custom, "abcdefgABCDEFG", "ABCDEFGabcdefg") == min(14 * mismatch, 2 * opening + 12 * extension)
+
+
+def test_insertion_ladder(szs):
+    """Each random insertion raises the distance by exactly one (test/similarities.py:105-122)."""
+    rng = np.random.default_rng(42)
+    engine = szs.LevenshteinDistances()
+    a = bytes(rng.choice(np.frombuffer(b"abcdefghijklmnopqrstuvwxyz", np.uint8), size=20))
+    b = a
+    for i in range(150):
+        pos = int(rng.integers(0, len(b)))
+        b = b[:pos] + bytes([int(rng.integers(97, 123))]) + b[pos:]
+        assert int(engine(szs.Strs([a]), szs.Strs([b]))[0, 0]) == i + 1
+
+
+def test_needleman_wunsch_is_negative_levenshtein(szs, port):
+    """NW with a -1/0 class table and -1 gaps equals minus the unit edit distance (test/similarities.py:290-319)."""
+    rng = np.random.default_rng(4)
+    b2c = (np.arange(256) % 32).astype(np.uint8)
+    table = np.full((32, 32), -1, dtype=np.int8)
+    np.fill_diagonal(table, 0)
+    letters = np.frombuffer(b"abcdefghijklmnopqrstuvwxyz", np.uint8)
+    first = random_strings(rng, 300, 10, 400, letters)
+    second = random_strings(rng, 300, 10, 400, letters)
+    nw = szs.NeedlemanWunschScores(b2c, table, open=-1, extend=-1)
+    lev = szs.LevenshteinDistances()
+    np.testing.assert_array_equal(nw.pairwise(szs.Strs(first), szs.Strs(second)),
+                                  -lev.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64))
