@@ -1,0 +1,425 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 batched scoring engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload c2|c1|c3|c4]
+
+One step = one pass of the engine over one whole batch: every pair of the workload scored through the C-ABI
+(`szs_*_pairwise_u64tape`). The headline workload is the batched-Levenshtein configuration: 1,048,576 DNA pairs,
+lengths U[100,300], partner = 3% substitutions + 1% indels, unit costs. Inputs are seeded synthetic data.
+
+* `value`: GCUPS (sum of len(a)*len(b) over pairs / seconds) with inputs resident in HBM, timed with CUDA events on the
+  stream the engine runs on (a scope bound to torch's current stream), K steps between barriers.
+* `e2e`: the same through the same C-ABI call with pinned HOST tapes and a host result array: the engine's H2D copy
+  of the inputs and D2H copy of the results are inside the timed region.
+* `plain`: the same device-resident measurement with the engine's plain schedule (one launch of one kernel shape
+  over the pairs in input order).
+* `roofline`: the scoring kernels' algorithmic HBM bytes per step over their event-timed duration, against the
+  measured copy bandwidth; `roofline_int`: their algorithmic integer operations against the integer issue rate
+  measured live by `szs_gb300_measure_integer_peaks` (the bound that actually applies to this path).
+* `cpu_baseline`: the oracle's C restatement (bit-parallel for unit costs) on all host cores.
+
+`--impl reference` times that CPU implementation alone and prints its line (rank 0 only under torchrun).
+Multi-GPU (torchrun): every rank scores its own batch (seed + rank), no data-path collective; the time is the
+maximum over ranks and `value` aggregates all ranks' cells (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "GCUPS batched Levenshtein/NW/SW, 1 GB300, vs plain launch; serving p50/p99 ms"
+
+# Algorithmic integer operations per DP cell of each route, counted from the kernels' recurrences:
+#  - bit-parallel (unit Levenshtein): per 32-cell word and column, B code-plane LOP3s + 11 ops of the Myers step
+#    (Xv, Eq&Pv, 2-op carried add, Xh, Ph, Mh, two funnel shifts, Pv, Mv); DNA needs B = 2 -> 13 / 32 per cell.
+#  - wavefront, 32-bit cells: linear 4 = opt(up, left) + (diag + s) + fused add-opt + cost unpack;
+#    affine 7 = E (add + fused add-opt) + F (add + fused add-opt) + (diag + s) + 3-way opt + cost unpack.
+OPS_PER_CELL = {"myers_dna": 13.0 / 32.0, "dp_linear": 4.0, "dp_affine": 7.0}
+
+WORKLOADS = {
+    "c1": "plain Levenshtein: 1,024 DNA pairs, len U[64,256], partner 5% subs + 2% indels, unit costs",
+    "c2": "batched Levenshtein: 1,048,576 DNA pairs, len U[100,300], partner 3% subs + 1% indels, unit costs",
+    "c3": "Needleman-Wunsch affine protein: 262,144 pairs, len lognormal(350, 0.6) in [50,2000], 70% identity, "
+          "seeded symmetric int8 table (diag 4..11, off -4..3), open -11 extend -1",
+    "c4": "Smith-Waterman affine DNA: 8,192 pairs, len log-uniform [1,000, 30,000], planted 500-5,000 bp shared "
+          "segment with 10% divergence, match +2 mismatch -3 open -5 extend -2",
+}
+
+
+def parse_args():
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=10)
+    parser.add_argument("--warmup", type=int, default=3)
+    parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    parser.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    parser.add_argument("--no-extra", action="store_true", help="skip the other workloads' lines")
+    parser.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    return parser.parse_args()
+
+
+def make_workload(name, seed):
+    from stringzillas_gb300 import workloads as w
+    if name == "c1":
+        first, second = w.levenshtein_reads(1024, 64, 256, 0.05, 0.02, seed=seed)
+        return first, second, ("lev", None)
+    if name == "c2":
+        first, second = w.levenshtein_reads(1 << 20, 100, 300, 0.03, 0.01, seed=seed)
+        return first, second, ("lev", None)
+    if name == "c3":
+        first, second = w.protein_pairs(262144, seed=seed)
+        return first, second, ("nw", w.protein_table(seed=seed))
+    first, second = w.local_dna_pairs(8192, seed=seed)
+    return first, second, ("sw", w.dna_table(2, -3))
+
+
+def make_engine(kind_and_tables):
+    import stringzillas_gb300 as szs
+    kind, tables = kind_and_tables
+    if kind == "lev":
+        return szs.LevenshteinDistances()
+    if kind == "nw":
+        return szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
+    return szs.SmithWatermanScores(*tables, open=-5, extend=-2)
+
+
+def oracle_costs(kind_and_tables):
+    from oracle import oracle
+    kind, tables = kind_and_tables
+    if kind == "lev":
+        return oracle.levenshtein_costs()
+    if kind == "nw":
+        return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables, -11, -1)
+    return oracle.alignment_costs(oracle.SMITH_WATERMAN, *tables, -5, -2)
+
+
+def ops_per_cell(kind_and_tables):
+    kind = kind_and_tables[0]
+    return OPS_PER_CELL["myers_dna"] if kind == "lev" else OPS_PER_CELL["dp_affine"]
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.device_index = device_index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.process = None
+
+    def __enter__(self):
+        try:
+            self.process = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.device_index)], stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.process = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.process:
+            self.process.terminate()
+            try:
+                self.process.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.process.kill()
+        self.file.flush()
+
+    def summary(self):
+        self.file.seek(0)
+        rows = [line.strip().split(", ") for line in self.file.read().splitlines() if line.strip()]
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        sm_max = [float(r[2]) for r in rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            for name, flag in zip(names, r[5:9]):
+                if flag.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(sm_max) if sm_max else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        return float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def integer_peaks(device):
+    from stringzillas_gb300._native import lib
+    rates = (ctypes.c_double * 5)()
+    err = ctypes.c_char_p()
+    status = lib.szs_gb300_measure_integer_peaks(device, rates, 5, ctypes.byref(err))
+    if status != 0:
+        return None
+    return {"lop3": rates[0], "iadd3": rates[1], "dpx_viaddmax_s32": rates[2], "dpx_vimax3_s32": rates[3],
+            "dpx_viaddmax_s16x2": rates[4]}
+
+
+class DeviceBatch:
+    """A workload's tapes in HBM plus the C-ABI structs that point at them."""
+
+    def __init__(self, first, second, torch):
+        from stringzillas_gb300 import _native
+        self.tensors = []
+        self.tapes = []
+        for data, offsets in (first, second):
+            d = torch.from_numpy(data).cuda()
+            o = torch.from_numpy(offsets.astype(np.int64)).cuda()
+            self.tensors += [d, o]
+            self.tapes.append(_native.U64Tape(d.data_ptr(), o.data_ptr(), len(offsets) - 1))
+        self.count = len(first[1]) - 1
+        self.out = torch.empty(self.count, dtype=torch.int64, device="cuda")
+
+
+class HostBatch:
+    """The same tapes in pinned host memory, with a pinned host result array."""
+
+    def __init__(self, first, second, torch):
+        from stringzillas_gb300 import _native
+        self.tensors = []
+        self.tapes = []
+        self.bytes_in = 0
+        for data, offsets in (first, second):
+            d = torch.from_numpy(data).pin_memory()
+            o = torch.from_numpy(offsets.astype(np.int64)).pin_memory()
+            self.tensors += [d, o]
+            self.bytes_in += d.numel() + o.numel() * 8
+            self.tapes.append(_native.U64Tape(d.data_ptr(), o.data_ptr(), len(offsets) - 1))
+        self.count = len(first[1]) - 1
+        self.out = torch.empty(self.count, dtype=torch.int64).pin_memory()
+        self.bytes_out = self.count * 8
+
+
+def call_pairwise(engine, scope, batch):
+    from stringzillas_gb300._native import lib
+    err = ctypes.c_char_p()
+    fn = getattr(lib, f"szs_{engine._algo}_pairwise_u64tape")
+    status = fn(engine.handle, scope.handle, ctypes.byref(batch.tapes[0]), ctypes.byref(batch.tapes[1]),
+                ctypes.c_void_p(batch.out.data_ptr()), ctypes.byref(err))
+    if status != 0:
+        raise RuntimeError(f"engine call failed ({status}): {err.value}")
+    return engine.stats()
+
+
+def timed_steps(engine, scope, batch, steps, warmup, torch, barrier):
+    for _ in range(warmup):
+        call_pairwise(engine, scope, batch)
+    stream = torch.cuda.current_stream()
+    begin, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    begin.record(stream)
+    compute_ms, launches, cells = 0.0, 0, 0
+    for _ in range(steps):
+        stats = call_pairwise(engine, scope, batch)
+        compute_ms += stats["last_compute_ms"]
+        launches += stats["last_launches"]
+        cells += stats["last_cells"]
+    end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    return begin.elapsed_time(end), compute_ms, launches, cells
+
+
+def cpu_baseline(first, second, kind_and_tables, seconds_budget):
+    """The oracle's C restatement on all host cores over a bounded prefix of the same pairs."""
+    from oracle import oracle
+    port = oracle.Port()
+    costs = oracle_costs(kind_and_tables)
+    threads = os.cpu_count() or 1
+    count = len(first[1]) - 1
+
+    def sample(k):
+        a = (first[0], first[1][:k + 1])
+        b = (second[0], second[1][:k + 1])
+        t0 = time.perf_counter()
+        port.pairs(costs, a, b, threads)
+        elapsed = time.perf_counter() - t0
+        cells = int(np.dot(np.diff(a[1]).astype(np.int64), np.diff(b[1]).astype(np.int64)))
+        return elapsed, cells
+
+    k = max(1, count // 256)
+    elapsed, cells = sample(k)
+    if elapsed < seconds_budget / 4 and k < count:
+        k = min(count, max(k + 1, int(k * seconds_budget / max(elapsed, 1e-3))))
+        elapsed, cells = sample(k)
+    return {"value": cells / elapsed / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
+            "sample": f"first {k} of {count} pairs ({cells:.3e} cells, {elapsed:.2f} s), oracle C restatement"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    first, second, kind_and_tables = make_workload(args.workload, 42)
+    values = []
+    baseline = None
+    for step in range(args.warmup + args.steps):
+        baseline = cpu_baseline(first, second, kind_and_tables, args.cpu_seconds / max(1, args.warmup + args.steps))
+        if step >= args.warmup:
+            values.append(baseline["value"])
+    value = statistics.median(values)
+    cells = int(np.dot(np.diff(first[1]).astype(np.int64), np.diff(second[1]).astype(np.int64)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / (value * 1e9) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit-vectors / int64",
+        "data": "synthetic (seeded)", "config": {"workload": WORKLOADS[args.workload], "pairs": len(first[1]) - 1},
+        "cpu_baseline": dict(baseline, value=value),
+        "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    import stringzillas_gb300 as szs
+    first, second, kind_and_tables = make_workload(args.workload, 42 + rank)
+    engine = make_engine(kind_and_tables)
+    scope = szs.DeviceScope(gpu_device=local_rank, stream=torch.cuda.current_stream())
+    device_batch = DeviceBatch(first, second, torch)
+    pairs = device_batch.count
+    input_bytes = int(first[0].shape[0] + second[0].shape[0])
+
+    peaks = integer_peaks(local_rank)
+    with Clocks(local_rank) as clocks:
+        elapsed_ms, compute_ms, launches, cells_total = timed_steps(engine, scope, device_batch, args.steps,
+                                                                    args.warmup, torch, barrier)
+    clock_summary = clocks.summary()
+
+    slowest_ms = elapsed_ms
+    all_cells = cells_total
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        slowest_ms = float(t.item())
+        c = torch.tensor([float(cells_total)], device="cuda", dtype=torch.float64)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        all_cells = float(c.item())
+    value = all_cells / (slowest_ms * 1e-3) / 1e9
+    cells_per_step = cells_total / args.steps
+
+    # The plain one-launch-per-batch form of the same kernels.
+    engine.set_schedule("plain")
+    plain_steps = max(1, min(args.steps, 5))
+    plain_ms, plain_compute_ms, _, plain_cells = timed_steps(engine, scope, device_batch, plain_steps, 1, torch,
+                                                             barrier)
+    engine.set_schedule("batched")
+
+    # End to end through the same C-ABI with host buffers: copies in the timed region.
+    del device_batch
+    host_batch = HostBatch(first, second, torch)
+    e2e_steps = max(1, min(args.steps, 5))
+    e2e_ms, _, _, e2e_cells = timed_steps(engine, scope, host_batch, e2e_steps, 1, torch, barrier)
+
+    line = None
+    if rank == 0:
+        hbm_peak, peak_source = measured_peaks()
+        step_compute_s = compute_ms / args.steps * 1e-3
+        algorithmic_bytes = input_bytes + 8 * pairs
+        achieved_gbs = algorithmic_bytes / step_compute_s / 1e9
+        int_ops = cells_per_step * ops_per_cell(kind_and_tables)
+        int_peak = None
+        if peaks:
+            int_peak = peaks["lop3"] if kind_and_tables[0] == "lev" else peaks["dpx_viaddmax_s32"]
+        line = {
+            "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32" if kind_and_tables[0] == "lev" else "int32",
+            "data": "synthetic (seeded numpy PCG64)",
+            "config": {"workload": WORKLOADS[args.workload], "pairs": pairs, "cells_per_step": cells_per_step,
+                       "input_bytes_per_step": input_bytes,
+                       "l2": "inputs larger than L2 (129 MB), no flush between steps",
+                       "parallelism": f"pairs: each of {world} ranks scores its own batch, no collective"},
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm_peak, "traffic": None,
+                         "note": f"peak of {peak_source}; the path is integer-issue bound, see roofline_int"},
+            "roofline_int": {"bound": "int_pipe", "achieved": int_ops / step_compute_s / 1e12,
+                             "peak": None if int_peak is None else int_peak / 1e12, "unit": "Tops/s",
+                             "frac": None if int_peak is None else int_ops / step_compute_s / int_peak,
+                             "ops_per_cell": ops_per_cell(kind_and_tables), "measured_peaks_tops":
+                                 None if peaks is None else {k: v / 1e12 for k, v in peaks.items()}},
+            "plain": {"value": plain_cells / (plain_ms * 1e-3) / 1e9, "unit": "GCUPS",
+                      "ms_per_step": plain_ms / plain_steps, "compute_ms_per_step": plain_compute_ms / plain_steps},
+            "e2e": {"value": e2e_cells / (e2e_ms * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": e2e_ms / e2e_steps,
+                    "h2d_bytes_per_step": host_batch.bytes_in, "d2h_bytes_per_step": host_batch.bytes_out},
+            "clocks": clock_summary,
+            "gpu_launches": launches,
+            "compute_ms_per_step": compute_ms / args.steps,
+        }
+    del host_batch
+
+    if rank == 0 and world == 1 and not args.no_extra:
+        line["cpu_baseline"] = cpu_baseline(first, second, kind_and_tables, args.cpu_seconds)
+        extra = {}
+        for name in ("c3", "c4"):
+            if name == args.workload:
+                continue
+            f, s, kt = make_workload(name, 42)
+            eng = make_engine(kt)
+            batch = DeviceBatch(f, s, torch)
+            row = {"workload": WORKLOADS[name]}
+            for schedule in ("batched", "plain"):
+                eng.set_schedule(schedule)
+                ms, cms, _, cells = timed_steps(eng, scope, batch, 2, 1, torch, barrier)
+                row[schedule] = {"GCUPS": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms / 2,
+                                 "compute_ms_per_step": cms / 2}
+            row["batched_over_plain"] = row["batched"]["GCUPS"] / row["plain"]["GCUPS"]
+            extra[name] = row
+            del batch
+        line["extra"] = extra
+    elif rank == 0:
+        line["cpu_baseline"] = None
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

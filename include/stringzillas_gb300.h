@@ -387,7 +387,8 @@ SZS_GB300_API sz_status_t szs_gb300_engine_set_schedule(void *engine, szs_gb300_
 
 /** Per-engine counters of the last call. No counterpart in the reference (its timer is dropped at the ABI). */
 typedef struct szs_gb300_stats_t {
-    double last_call_ms;       /**< CUDA-event time of the last call's device work */
+    double last_call_ms;       /**< CUDA-event time of the last call's device work (copies included) */
+    double last_compute_ms;    /**< CUDA-event time from the first to the end of the last scoring kernel */
     sz_u64_t last_cells;       /**< sum of len(a)*len(b) over the scored pairs */
     sz_u64_t last_pairs;       /**< number of scored pairs (a symmetric call counts the triangle once) */
     sz_u64_t last_launches;    /**< kernels launched by the last call (graph nodes count one each) */
@@ -395,9 +396,26 @@ typedef struct szs_gb300_stats_t {
     sz_u64_t kernel_launches;  /**< kernels launched over the engine's lifetime */
 } szs_gb300_stats_t;
 
+/**
+ *  GPU scope that runs every call on the caller's CUDA stream (`cudaStream_t` passed as `void *`), so callers can
+ *  order the engine's work with their own and time it with events on that stream. The stream stays owned by the
+ *  caller and must outlive the scope. No counterpart in the reference (its scopes always create their own stream).
+ */
+SZS_GB300_API sz_status_t szs_gb300_device_scope_init_stream(sz_size_t gpu_device, void *cuda_stream,
+                                                             szs_device_scope_t *scope, char const **error_message);
+
 /** Copies the engine's counters into @p stats. No counterpart in the reference. */
 SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine, szs_gb300_stats_t *stats,
                                                      char const **error_message);
+
+/**
+ *  Measures the device's sustained integer issue rates (operations per second, whole GPU) into
+ *  @p ops_per_second[0..4]: LOP3, IADD3, DPX `max(a + b, c)` (32-bit), DPX `max(a, b, c)` (32-bit) and DPX
+ *  `max(a + b, c)` on 16x2 lanes. These are the roofline denominators of the scoring kernels, which are bound by the
+ *  integer pipes rather than by HBM or tensor cores. No counterpart in the reference.
+ */
+SZS_GB300_API sz_status_t szs_gb300_measure_integer_peaks(sz_size_t gpu_device, double *ops_per_second,
+                                                          sz_size_t count, char const **error_message);
 
 #ifdef __cplusplus
 }

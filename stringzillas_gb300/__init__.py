@@ -198,9 +198,18 @@ def to_device(strs: Strs) -> Strs:
 class DeviceScope:
     """``DeviceScope(cpu_cores=None, gpu_device=None)`` (python/stringzillas/device_scope.c:17-61)."""
 
-    def __init__(self, cpu_cores=None, gpu_device=None):
+    def __init__(self, cpu_cores=None, gpu_device=None, stream=None):
         self.handle = ctypes.c_void_p()
         err = ctypes.c_char_p()
+        if stream is not None:
+            # Extension: run on a caller-owned CUDA stream (an int handle, or an object with `.cuda_stream`).
+            handle = int(getattr(stream, "cuda_stream", stream))
+            status = lib.szs_gb300_device_scope_init_stream(gpu_device or 0, ctypes.c_void_p(handle),
+                                                            ctypes.byref(self.handle), ctypes.byref(err))
+            self.description = f"GPU:{gpu_device or 0}:stream"
+            self._stream = stream
+            _native.raise_for(status, err.value, "DeviceScope initialization")
+            return
         if cpu_cores is not None and gpu_device is not None:
             raise ValueError("Cannot specify both cpu_cores and gpu_device")
         if cpu_cores is not None:

@@ -32,6 +32,7 @@ class Stats(ctypes.Structure):
     """``szs_gb300_stats_t``"""
     _fields_ = [
         ("last_call_ms", ctypes.c_double),
+        ("last_compute_ms", ctypes.c_double),
         ("last_cells", ctypes.c_uint64),
         ("last_pairs", ctypes.c_uint64),
         ("last_launches", ctypes.c_uint64),
@@ -41,9 +42,11 @@ class Stats(ctypes.Structure):
 
 
 def _load() -> ctypes.CDLL:
-    path = _build.LIBRARY
+    # Rebuilds only when the sources changed since the last build (content digest), so a stale library with
+    # missing entry points is never loaded.
+    path = _build.build() if _build.nvcc_available() else _build.LIBRARY
     if not os.path.exists(path):
-        path = _build.build()
+        raise ImportError(f"{path} is missing and nvcc is unavailable to build it")
     return ctypes.CDLL(path)
 
 
@@ -71,6 +74,8 @@ lib.szs_device_scope_get_gpu_device.restype = c_status
 lib.szs_device_scope_get_gpu_device.argtypes = [c_void_p, ctypes.POINTER(c_size_t), _err]
 lib.szs_device_scope_get_capabilities.restype = c_status
 lib.szs_device_scope_get_capabilities.argtypes = [c_void_p, ctypes.POINTER(ctypes.c_uint32), _err]
+lib.szs_gb300_device_scope_init_stream.restype = c_status
+lib.szs_gb300_device_scope_init_stream.argtypes = [c_size_t, c_void_p, ctypes.POINTER(c_void_p), _err]
 lib.szs_device_scope_free.restype = None
 lib.szs_device_scope_free.argtypes = [c_void_p]
 
@@ -101,6 +106,8 @@ for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterma
 
 lib.szs_gb300_engine_set_schedule.restype = c_status
 lib.szs_gb300_engine_set_schedule.argtypes = [c_void_p, c_int, _err]
+lib.szs_gb300_measure_integer_peaks.restype = c_status
+lib.szs_gb300_measure_integer_peaks.argtypes = [c_size_t, ctypes.POINTER(ctypes.c_double), c_size_t, _err]
 lib.szs_gb300_engine_get_stats.restype = c_status
 lib.szs_gb300_engine_get_stats.argtypes = [c_void_p, ctypes.POINTER(Stats), _err]
 

@@ -29,6 +29,7 @@ UNITS = [
     ("engine", "engine.cu", []),
     ("planner", "planner.cu", []),
     ("kernels_dp", "kernels_dp.cu", []),
+    ("probe", "probe.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),
     ("myers_p3", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=3"]),
     ("myers_p5", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=5"]),
@@ -44,6 +45,14 @@ def nvcc() -> str:
     if os.path.exists(fallback):
         return fallback
     raise RuntimeError("nvcc not found: the GB300 engine has no CPU fallback and must be compiled with CUDA")
+
+
+def nvcc_available() -> bool:
+    try:
+        nvcc()
+        return True
+    except RuntimeError:
+        return False
 
 
 def _sources_digest() -> str:

@@ -77,7 +77,8 @@ struct scope_t {
     scope_kind_t kind = scope_default_k;
     std::size_t cpu_cores = 1;
     int device = 0;
-    cudaStream_t stream = nullptr; // GPU scopes own a non-blocking stream
+    cudaStream_t stream = nullptr; // GPU scopes own a non-blocking stream, or borrow the caller's
+    bool borrowed_stream = false;
 };
 
 static scope_t *as_scope(void *handle) noexcept {
@@ -159,6 +160,7 @@ struct device_context_t {
     pinned_buffer_t readback;
     pinned_buffer_t results_host;
     cudaEvent_t start = nullptr, stop = nullptr;
+    cudaEvent_t compute_start = nullptr, compute_stop = nullptr;
 
     status_t prepare(int device_index) noexcept {
         if (ready) return {};
@@ -168,6 +170,8 @@ struct device_context_t {
         SZS_TRY_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
         SZS_TRY_CUDA(cudaEventCreate(&start));
         SZS_TRY_CUDA(cudaEventCreate(&stop));
+        SZS_TRY_CUDA(cudaEventCreate(&compute_start));
+        SZS_TRY_CUDA(cudaEventCreate(&compute_stop));
         status_t status = control.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256, own_stream);
         if (!status.ok()) return status;
         status = readback.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256);
@@ -191,6 +195,8 @@ struct device_context_t {
         readback.release(), results_host.release();
         if (start) cudaEventDestroy(start);
         if (stop) cudaEventDestroy(stop);
+        if (compute_start) cudaEventDestroy(compute_start);
+        if (compute_stop) cudaEventDestroy(compute_stop);
         if (own_stream) cudaStreamDestroy(own_stream);
         ready = false;
     }
@@ -436,6 +442,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     engine.stats.last_cells = 0;
     engine.stats.last_launches = 0;
     engine.stats.last_call_ms = 0;
+    engine.stats.last_compute_ms = 0;
     if (args.pairs == 0) return {};
     if (args.pairs > 0xFFFFFFFFull) return {sz_overflow_risk_k, "More than 2^32 pairs in one call"};
 
@@ -491,6 +498,14 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     plan_bins_t const &plan = *context->bins_host();
     engine.stats.last_cells = plan.cells;
 
+    // Scoring kernels are bracketed by their own events so the stats isolate them from planning and copies.
+    bool compute_recorded = false;
+    auto mark_compute_start = [&]() -> cudaError_t {
+        if (compute_recorded) return cudaSuccess;
+        compute_recorded = true;
+        return cudaEventRecord(context->compute_start, stream);
+    };
+
     // Bit-parallel routes.
     if (engine.unit_levenshtein) {
         bool any_myers = false;
@@ -537,6 +552,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
                 std::uint64_t const needed = (pairs_here + threads - 1) / threads;
                 int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
                 bool const exact = engine.schedule != szs_gb300_schedule_plain_k;
+                SZS_TRY_CUDA(mark_compute_start());
                 SZS_TRY_CUDA(launch_myers(words, planes, exact, tasks, bins, context->alphabet_device(), results,
                                           ctas, stream));
                 ++launches;
@@ -559,10 +575,13 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
         std::size_t const scratch_bytes = cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta;
         status = context->scratch.reserve(scratch_bytes, stream);
         if (!status.ok()) return status;
+        SZS_TRY_CUDA(mark_compute_start());
         SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, cell_bits, key_begin, key_end, tasks, bins, costs,
                                results, context->scratch.data, cells_per_warp, ctas, stream));
         ++launches;
     }
+
+    if (compute_recorded) SZS_TRY_CUDA(cudaEventRecord(context->compute_stop, stream));
 
     // Results into the caller's matrix.
     bool const out_on_device = device_accessible(call.out);
@@ -606,6 +625,9 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     float elapsed = 0;
     cudaEventElapsedTime(&elapsed, context->start, context->stop);
     engine.stats.last_call_ms = elapsed;
+    float compute = 0;
+    if (compute_recorded) cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
+    engine.stats.last_compute_ms = compute;
     engine.stats.last_launches = launches;
     engine.stats.kernel_launches += launches;
     return {};
@@ -849,10 +871,25 @@ SZS_GB300_API sz_status_t szs_device_scope_get_capabilities(szs_device_scope_t s
     return report({}, error_message);
 }
 
+SZS_GB300_API sz_status_t szs_gb300_device_scope_init_stream(sz_size_t gpu_device, void *cuda_stream,
+                                                             szs_device_scope_t *scope, char const **error_message) {
+    if (!scope) return report({sz_status_unknown_k, "Scope must not be NULL"}, error_message);
+    if ((int)gpu_device >= visible_devices() || gpu_device >= (sz_size_t)max_devices_k)
+        return report({sz_missing_gpu_k, nullptr}, error_message);
+    auto *s = new (std::nothrow) scope_t();
+    if (!s) return report({sz_bad_alloc_k, "Failed to allocate device scope"}, error_message);
+    s->kind = scope_gpu_k;
+    s->device = (int)gpu_device;
+    s->stream = static_cast<cudaStream_t>(cuda_stream);
+    s->borrowed_stream = true;
+    *scope = s;
+    return report({}, error_message);
+}
+
 SZS_GB300_API void szs_device_scope_free(szs_device_scope_t scope) {
     scope_t *s = as_scope(scope);
     if (!s) return;
-    if (s->stream) {
+    if (s->stream && !s->borrowed_stream) {
         cudaSetDevice(s->device);
         cudaStreamSynchronize(s->stream);
         cudaStreamDestroy(s->stream);

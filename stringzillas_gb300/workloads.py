@@ -1,0 +1,136 @@
+"""Seeded synthetic workloads with the shapes of the engine's benchmark configurations.
+
+No public dataset is named for these workloads; every input is generated here from a ``numpy`` PCG64 seed.
+Each generator returns tapes as ``(data: uint8[], offsets: int64[count + 1])`` pairs.
+
+* ``levenshtein_reads``: DNA pairs, first string length uniform in [low, high], second derived from the first by
+  per-base substitutions and single-character insertions/deletions (configs "plain Levenshtein" 1,024 pairs
+  U[64,256] 5%/2%, and "batched Levenshtein" 1,048,576 pairs U[100,300] 3%/1%).
+* ``protein_pairs``: 20 amino acids at background frequencies, length log-normal (median 350, sigma 0.6) clipped to
+  [50, 2000], partner = a mutant with the requested identity (substitutions plus a small indel rate).
+* ``protein_table``: symmetric int8 20x20 scores, diagonal U{4..11}, off-diagonal U{-4..3}, folded into the
+  reference's 256-byte class map + 32x32 table (letters -> classes 1..20, everything else -> class 0).
+* ``local_dna_pairs``: DNA strings with log-uniform lengths in [1,000, 30,000], each pair sharing one planted
+  segment of U{500..5000} bp at random offsets with 10% divergence, random flanks.
+* ``dna_table``: match +2 / mismatch -3 over A, C, G, T (classes 1..4), class 0 for other bytes.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+DNA = np.frombuffer(b"ACGT", dtype=np.uint8)
+AMINO_ACIDS = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+AMINO_FREQUENCIES = np.array([.074, .052, .045, .054, .025, .034, .054, .074, .026, .068,
+                              .099, .058, .025, .047, .039, .057, .051, .013, .032, .073])
+
+
+def _offsets(lengths) -> np.ndarray:
+    offsets = np.zeros(len(lengths) + 1, dtype=np.int64)
+    np.cumsum(lengths, out=offsets[1:])
+    return offsets
+
+
+def _letters(rng, alphabet, size, probabilities=None):
+    """`size` letters drawn from `alphabet` (uniform, or by `probabilities` at 1/65536 resolution)."""
+    if probabilities is None:
+        return alphabet[rng.integers(0, len(alphabet), size=size, dtype=np.uint8)]
+    edges = np.cumsum(probabilities / np.sum(probabilities)) * 65536.0
+    lut = alphabet[np.minimum(np.searchsorted(edges, np.arange(65536) + 0.5), len(alphabet) - 1)]
+    return lut[rng.integers(0, 65536, size=size, dtype=np.uint16)]
+
+
+def _chance(rng, size, rate):
+    """Boolean mask with each entry set with probability `rate` (32-bit threshold)."""
+    return rng.integers(0, 1 << 32, size=size, dtype=np.uint64) < np.uint64(int(rate * (1 << 32)))
+
+
+def _mutate(rng, data, offsets, alphabet, substitution_rate, indel_rate, probabilities=None):
+    """Per-base substitutions (always to a different letter) then single-character insertions and deletions.
+    Returns the mutated tape; pair i of the result derives from pair i of the input."""
+    letters = np.sort(alphabet)
+    data = data.copy()
+    substitute = np.flatnonzero(_chance(rng, data.shape[0], substitution_rate))
+    if substitute.size:
+        codes = np.searchsorted(letters, data[substitute])
+        shift = rng.integers(1, len(letters), size=codes.shape[0])
+        data[substitute] = letters[(codes + shift) % len(letters)]
+    delete = _chance(rng, data.shape[0], indel_rate / 2)
+    insert = _chance(rng, data.shape[0], indel_rate / 2) & ~delete
+    copies = 1 - delete.astype(np.int64) + insert.astype(np.int64)
+    mutated = np.repeat(data, copies)
+    inserted_at = np.cumsum(copies)[insert] - 1
+    mutated[inserted_at] = _letters(rng, alphabet, inserted_at.shape[0], probabilities)
+    per_base = np.zeros(data.shape[0] + 1, dtype=np.int64)
+    np.cumsum(copies, out=per_base[1:])
+    return mutated, per_base[offsets]
+
+
+def levenshtein_reads(count, low, high, substitution_rate, indel_rate, seed=42):
+    """DNA pairs for the Levenshtein configurations."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = rng.integers(low, high + 1, size=count)
+    offsets = _offsets(lengths)
+    first = _letters(rng, DNA, int(offsets[-1]))
+    second, second_offsets = _mutate(rng, first, offsets, DNA, substitution_rate, indel_rate)
+    return (first, offsets), (second, second_offsets)
+
+
+def protein_pairs(count, median=350.0, sigma=0.6, low=50, high=2000, identity=0.70, indel_rate=0.02, seed=42):
+    """Protein pairs for the Needleman-Wunsch configuration."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = np.clip(np.rint(rng.lognormal(np.log(median), sigma, size=count)), low, high).astype(np.int64)
+    offsets = _offsets(lengths)
+    p = AMINO_FREQUENCIES / AMINO_FREQUENCIES.sum()
+    first = _letters(rng, AMINO_ACIDS, int(offsets[-1]), p)
+    second, second_offsets = _mutate(rng, first, offsets, AMINO_ACIDS, 1.0 - identity, indel_rate, probabilities=p)
+    return (first, offsets), (second, second_offsets)
+
+
+def protein_table(seed=42):
+    """(byte_to_class[256] uint8, class_costs[32, 32] int8) of a seeded symmetric 20x20 score matrix."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    core = rng.integers(-4, 4, size=(20, 20))
+    core = np.triu(core, 1)
+    core = core + core.T
+    np.fill_diagonal(core, rng.integers(4, 12, size=20))
+    byte_to_class = np.zeros(256, dtype=np.uint8)
+    byte_to_class[AMINO_ACIDS] = np.arange(1, 21, dtype=np.uint8)
+    table = np.zeros((32, 32), dtype=np.int8)
+    table[1:21, 1:21] = core
+    return byte_to_class, table
+
+
+def dna_table(match=2, mismatch=-3):
+    byte_to_class = np.zeros(256, dtype=np.uint8)
+    byte_to_class[DNA] = np.arange(1, 5, dtype=np.uint8)
+    table = np.zeros((32, 32), dtype=np.int8)
+    table[1:5, 1:5] = mismatch
+    np.fill_diagonal(table[1:5, 1:5], match)
+    return byte_to_class, table
+
+
+def local_dna_pairs(count, low=1000, high=30000, segment_low=500, segment_high=5000, divergence=0.10, seed=42):
+    """Long DNA pairs sharing one planted, diverged segment, for the Smith-Waterman configuration."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    log_low, log_high = np.log(low), np.log(high)
+    first_lengths = np.exp(rng.uniform(log_low, log_high, size=count)).astype(np.int64)
+    second_lengths = np.exp(rng.uniform(log_low, log_high, size=count)).astype(np.int64)
+    first_offsets, second_offsets = _offsets(first_lengths), _offsets(second_lengths)
+    first = _letters(rng, DNA, int(first_offsets[-1]))
+    second = _letters(rng, DNA, int(second_offsets[-1]))
+    segment_lengths = np.minimum(rng.integers(segment_low, segment_high + 1, size=count),
+                                 np.minimum(first_lengths, second_lengths))
+    for i in range(count):
+        length = int(segment_lengths[i])
+        a_at = int(first_offsets[i] + rng.integers(0, first_lengths[i] - length + 1))
+        b_at = int(second_offsets[i] + rng.integers(0, second_lengths[i] - length + 1))
+        segment = first[a_at:a_at + length].copy()
+        diverge = rng.random(length) < divergence
+        segment[diverge] = _letters(rng, DNA, int(diverge.sum()))
+        second[b_at:b_at + length] = segment
+    return (first, first_offsets), (second, second_offsets)
+
+
+def cells(first, second) -> int:
+    """Sum over pairs of len(first_i) * len(second_i): the cell count GCUPS divides by."""
+    return int(np.dot(np.diff(first[1]).astype(np.int64), np.diff(second[1]).astype(np.int64)))
