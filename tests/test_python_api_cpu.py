@@ -1,0 +1,94 @@
+"""Host-side behaviour of the Python callables (argument validation, containers); no GPU needed."""
+import numpy as np
+import pytest
+
+import stringzillas_gb300 as szs
+
+
+def test_device_scope_validation():
+    with pytest.raises(ValueError):
+        szs.DeviceScope(cpu_cores=4, gpu_device=0)
+    with pytest.raises(TypeError):
+        szs.DeviceScope(cpu_cores="invalid")
+    with pytest.raises(TypeError):
+        szs.DeviceScope(gpu_device="invalid")
+    assert repr(szs.DeviceScope(cpu_cores=2)) == "DeviceScope(CPUs:2)"
+    assert repr(szs.DeviceScope(cpu_cores=1)) == "DeviceScope(default)"
+    if "cuda" not in szs.__capabilities__:
+        with pytest.raises(RuntimeError):
+            szs.DeviceScope(gpu_device=0)
+
+
+def test_cpu_scope_rejects_the_gpu_engine():
+    engine = szs.LevenshteinDistances()
+    with pytest.raises(RuntimeError):
+        engine(szs.Strs(["hello", "world"]), szs.Strs(["hallo", "word"]), device=szs.DeviceScope(cpu_cores=2))
+
+
+def test_levenshtein_constructor_validation():
+    with pytest.raises(ValueError):
+        szs.LevenshteinDistances(mismatch=300)
+    with pytest.raises(TypeError):
+        szs.LevenshteinDistances(capabilities="cuda")
+    assert "LevenshteinDistances" in repr(szs.LevenshteinDistances(0, 2, 3, 1))
+
+
+def test_alignment_constructor_validation():
+    b2c = np.zeros(256, np.uint8)
+    table = np.zeros((32, 32), np.int8)
+    with pytest.raises(TypeError):
+        szs.NeedlemanWunschScores()
+    with pytest.raises(TypeError):
+        szs.NeedlemanWunschScores(list(b2c), table)
+    with pytest.raises(ValueError):
+        szs.NeedlemanWunschScores(np.zeros(255, np.uint8), table)
+    with pytest.raises(TypeError):
+        szs.SmithWatermanScores(b2c.astype(np.int8), table)
+    with pytest.raises(ValueError):
+        szs.SmithWatermanScores(b2c, np.zeros((16, 16), np.int8))
+    with pytest.raises(TypeError):
+        szs.SmithWatermanScores(b2c, table.astype(np.int16))
+    with pytest.raises(ValueError):
+        szs.SmithWatermanScores(b2c, np.asfortranarray(np.arange(1024, dtype=np.int8).reshape(32, 32)))
+    with pytest.raises(ValueError):
+        szs.NeedlemanWunschScores(b2c, table, open=-200)
+
+
+def test_strs_container():
+    s = szs.Strs(["hello", "", "world", "café"])
+    assert len(s) == 4
+    assert list(s) == ["hello", "", "world", "café"]
+    view = s[1:3]
+    assert len(view) == 2 and list(view) == ["", "world"]
+    assert s[-1] == "café"
+    b = szs.Strs([b"\x00\xff", b"x"])
+    assert list(b) == [b"\x00\xff", b"x"]
+    with pytest.raises(TypeError):
+        szs.Strs([1, 2])
+    tape, bits = s[2:4].tape()
+    assert bits == 64 and tape.count == 2
+
+
+def test_strs_from_pyarrow():
+    pa = pytest.importorskip("pyarrow")
+    arrow = pa.array(["hello", "", "world", "a"])
+    s = szs.Strs(arrow)
+    assert list(s) == ["hello", "", "world", "a"]
+    assert list(szs.Strs(arrow.slice(1, 2))) == ["", "world"]
+
+
+def test_calls_validate_before_running():
+    engine = szs.LevenshteinDistances()
+    with pytest.raises(TypeError):
+        engine("not strs")
+    with pytest.raises(TypeError):
+        engine(szs.Strs(["a"]), device="gpu")
+    with pytest.raises(ValueError):
+        engine(szs.Strs(["a", "b"]), szs.Strs(["c"]), out=np.zeros((1, 1), np.uint64))
+    with pytest.raises(TypeError):
+        engine(szs.Strs(["a"]), szs.Strs(["c"]), out=np.zeros((1, 1), np.int64))
+    with pytest.raises(ValueError):
+        engine.pairwise(szs.Strs(["a", "b"]), szs.Strs(["c"]))
+    # Empty inputs return empty matrices without touching a device.
+    assert engine(szs.Strs([]), szs.Strs([])).shape == (0, 0)
+    assert engine(szs.Strs(["a"]), szs.Strs([])).shape == (1, 0)
