@@ -409,6 +409,26 @@ SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine, szs_gb300_sta
                                                      char const **error_message);
 
 /**
+ *  Pairwise scoring that allocates no memory: `results[i] = score(first[i], second[i])` for any engine made by the
+ *  `*_init` functions above (8-byte results: `sz_size_t` for Levenshtein, `sz_ssize_t` for alignments). No counterpart
+ *  in the reference. For callers that cannot call `cudaMalloc` / `cudaFree` - for example a host application whose
+ *  own allocator already reserves the device memory, or a latency-bound loop that cannot afford the device-wide
+ *  synchronisation of `cudaFree`.
+ *  - Tapes (data and offsets) and `results` must already be in device or managed memory, else
+ *    `sz_device_memory_mismatch_k`. The engine's staging buffers are not used.
+ *  - Scratch comes from a fixed 16 MiB (+ 256 B) device array inside the library, held by every GPU that loads it
+ *    until exit. A pair whose two sides both exceed 256 bytes must have both sides below 2,048 bytes; longer ones
+ *    fail the call with `sz_overflow_risk_k` (other pairs' results are still written).
+ *  - The first call on each device resolves the array's address with that device current; make that first call
+ *    before any stream capture. Every call shares the array: calls whose kernels overlap on the GPU race.
+ *  The default scope runs on the legacy default stream; GPU scopes use their own stream. Synchronous, like the rest.
+ */
+SZS_GB300_API sz_status_t szs_gb300_score_pairwise_noalloc_u64tape(void *engine, szs_device_scope_t device,
+                                                                   sz_sequence_u64tape_t const *first,
+                                                                   sz_sequence_u64tape_t const *second, void *results,
+                                                                   char const **error_message);
+
+/**
  *  Measures the device's sustained integer issue rates (operations per second, whole GPU) into
  *  @p ops_per_second[0..4]: LOP3, IADD3, DPX `max(a + b, c)` (32-bit), DPX `max(a, b, c)` (32-bit) and DPX
  *  `max(a + b, c)` on 16x2 lanes. These are the roofline denominators of the scoring kernels, which are bound by the

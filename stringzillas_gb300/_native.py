@@ -104,6 +104,8 @@ for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterma
     fn.restype = None
     fn.argtypes = [c_void_p]
 
+lib.szs_gb300_score_pairwise_noalloc_u64tape.restype = c_status
+lib.szs_gb300_score_pairwise_noalloc_u64tape.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, _err]
 lib.szs_gb300_engine_set_schedule.restype = c_status
 lib.szs_gb300_engine_set_schedule.argtypes = [c_void_p, c_int, _err]
 lib.szs_gb300_measure_integer_peaks.restype = c_status

@@ -30,6 +30,7 @@ UNITS = [
     ("planner", "planner.cu", []),
     ("kernels_dp", "kernels_dp.cu", []),
     ("probe", "probe.cu", []),
+    ("static_scratch", "static_scratch.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),
     ("myers_p3", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=3"]),
     ("myers_p5", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=5"]),

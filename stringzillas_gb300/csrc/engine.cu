@@ -204,6 +204,17 @@ struct device_context_t {
 
 /* ---- engines ---------------------------------------------------------------------------------------------------- */
 
+struct static_call_t {
+    score_costs_t const *costs;
+    int kind;
+    int magnitude;
+    int device;
+    cudaStream_t stream;
+};
+sz_status_t static_scratch_pairwise(static_call_t const &call, sz_sequence_u64tape_t const *first,
+                                    sz_sequence_u64tape_t const *second, std::int64_t *results,
+                                    char const **error_message);
+
 struct engine_t {
     std::uint32_t magic = engine_magic_k;
     int kind = kind_levenshtein_k;
@@ -1106,6 +1117,28 @@ SZS_GB300_API sz_status_t szs_smith_waterman_scores_pairwise_u64tape(szs_smith_w
                                                                      sz_sequence_u64tape_t const *second,
                                                                      sz_ssize_t *results, char const **error_message) {
     return score_pairwise(kind_smith_waterman_k, engine, device, first, second, results, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_score_pairwise_noalloc_u64tape(void *engine_handle, szs_device_scope_t device,
+                                                                   sz_sequence_u64tape_t const *first,
+                                                                   sz_sequence_u64tape_t const *second, void *results,
+                                                                   char const **error_message) {
+    engine_t *engine = as_engine(engine_handle, -1);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!first || !second || !results)
+        return report({sz_unexpected_dimensions_k, "Inputs and results must not be NULL"}, error_message);
+    // Resolve the device and stream without touching the engine's per-device buffers (which would allocate).
+    scope_t *scope = as_scope(device);
+    if (device && !scope) return report({sz_status_unknown_k, "Invalid device scope handle"}, error_message);
+    if (scope && scope->kind == scope_cpu_k) return report({sz_device_code_mismatch_k, nullptr}, error_message);
+    static_call_t call;
+    call.costs = &engine->costs;
+    call.kind = engine->kind;
+    call.magnitude = engine->magnitude;
+    call.device = scope ? scope->device : 0;
+    call.stream = scope && scope->kind == scope_gpu_k ? scope->stream : nullptr;
+    if (call.device >= visible_devices()) return report({sz_missing_gpu_k, nullptr}, error_message);
+    return static_scratch_pairwise(call, first, second, static_cast<std::int64_t *>(results), error_message);
 }
 
 SZS_GB300_API sz_status_t szs_gb300_engine_set_schedule(void *engine_handle, szs_gb300_schedule_t schedule,
