@@ -29,6 +29,7 @@ UNITS = [
     ("engine", "engine.cu", []),
     ("planner", "planner.cu", []),
     ("kernels_dp", "kernels_dp.cu", []),
+    ("kernels_dp16", "kernels_dp16.cu", []),
     ("probe", "probe.cu", []),
     ("static_scratch", "static_scratch.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),

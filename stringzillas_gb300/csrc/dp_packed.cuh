@@ -1,0 +1,367 @@
+/**
+ *  @file dp_packed.cuh
+ *  @brief Wavefront DP with 16x2 packed cells: one warp scores two pairs at once, pair A in the low halves and pair
+ *         B in the high halves of every register, with DPX 16x2 instructions.
+ *
+ *  Taken only when the length bound proves every value of both pairs fits int16 (the planner checks
+ *  `(span + steps + 1) * magnitude < 32767` per pair). Cells of rows or columns beyond a pair's own length are
+ *  computed but never flow into that pair's real cells (information only moves down and right), and the two halves
+ *  never interact (16x2 instructions have no carries between halves), so such filler cannot change a result even
+ *  when it wraps.
+ *
+ *  Gap tracks are kept shifted by the gap-open cost, `Ê = E - open` and `F̂ = F - open`, which turns the affine
+ *  recurrence into fused DPX operations without separate additions:
+ *
+ *      Ê = max(Ê_left + extend, H_left)        (was max(E_left + extend, H_left + open))
+ *      F̂ = max(F̂_up + extend, H_up)
+ *      H = max(max(Ê, F̂) + open, diag + s)      (local: also max(., 0))
+ *
+ *  (min for Levenshtein). Substitution costs come from two per-warp int8 profiles, one per pair, and one byte-permute
+ *  with sign replication builds the packed cost of both pairs for a row.
+ *
+ *  The layout of a pair inside the warp is the one of dp_wavefront.cuh: strips of 32 x R rows, lane L owns rows
+ *  L*R..L*R+R-1, column j = t + 1 - L at step t, bottom values passed down with `__shfl_up_sync`, lane 0 fed by the
+ *  closed-form row 0 or by the previous strip's bottom row in the warp's scratch row.
+ */
+#pragma once
+#include "dp_cells.cuh"
+#include "dp_wavefront.cuh"
+#include "engine_types.cuh"
+#include "planner.cuh"
+
+namespace szs_gb300 {
+
+template <int kind_, bool affine_, int rows_per_lane_>
+struct dp16_policy_t {
+    static constexpr int kind_k = kind_;
+    static constexpr bool affine_k = affine_;
+    static constexpr bool maximize_k = kind_ != kind_levenshtein_k;
+    static constexpr bool local_k = kind_ == kind_smith_waterman_k;
+    static constexpr int rows_per_lane_k = rows_per_lane_;
+    static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
+};
+
+/** Per-warp shared profile bytes: two pairs x classes x strip rows, plus lane 0's column staging area. */
+template <typename policy_>
+__host__ __device__ constexpr int dp16_profile_bytes_per_warp(int classes) {
+    return 2 * classes * policy_::strip_rows_k;
+}
+
+constexpr int dp16_chunk_bytes_k = 3 * 64 * 4;
+
+template <typename policy_>
+__host__ __device__ constexpr int dp16_shared_bytes(int warps_per_cta, int classes) {
+    return int((sizeof(score_costs_t) + 15) / 16 * 16) +
+           warps_per_cta * (dp16_profile_bytes_per_warp<policy_>(classes) + dp16_chunk_bytes_k);
+}
+
+constexpr std::uint32_t packed_floor_k = 0x80008000u; // -32768 in both halves: max(x + y, floor) == x + y
+
+__device__ __forceinline__ std::uint32_t pack16(std::int32_t lo, std::int32_t hi) {
+    return (std::uint32_t(lo) & 0xFFFFu) | (std::uint32_t(hi) << 16);
+}
+__device__ __forceinline__ std::int32_t low16(std::uint32_t x) { return std::int32_t(std::int16_t(x & 0xFFFFu)); }
+__device__ __forceinline__ std::int32_t high16(std::uint32_t x) { return std::int32_t(std::int16_t(x >> 16)); }
+
+/** Byte `b` of `x` and byte `b` of `y`, each sign-extended to 16 bits: {lo: x.b, hi: y.b}. */
+template <int b_>
+__device__ __forceinline__ std::uint32_t interleave_signed_bytes(std::uint32_t x, std::uint32_t y) {
+    constexpr std::uint32_t selector = std::uint32_t(b_) | (std::uint32_t(8 + b_) << 4) | (std::uint32_t(4 + b_) << 8) |
+                                       (std::uint32_t(12 + b_) << 12);
+    std::uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(y), "r"(selector));
+    return r;
+}
+
+template <bool maximize_>
+struct packed_ops_t {
+    __device__ __forceinline__ static std::uint32_t add(std::uint32_t a, std::uint32_t b) {
+        return maximize_ ? __viaddmax_s16x2(a, b, packed_floor_k) : __viaddmin_s16x2(a, b, 0x7FFF7FFFu);
+    }
+    __device__ __forceinline__ static std::uint32_t opt2(std::uint32_t a, std::uint32_t b) {
+        return maximize_ ? __vimax3_s16x2(a, b, b) : __vimin3_s16x2(a, b, b);
+    }
+    __device__ __forceinline__ static std::uint32_t add_opt(std::uint32_t a, std::uint32_t b, std::uint32_t c) {
+        return maximize_ ? __viaddmax_s16x2(a, b, c) : __viaddmin_s16x2(a, b, c);
+    }
+    __device__ __forceinline__ static std::uint32_t add_opt_relu(std::uint32_t a, std::uint32_t b, std::uint32_t c) {
+        return __viaddmax_s16x2_relu(a, b, c);
+    }
+};
+
+constexpr int chunk_columns_k = 64; // lane 0's boundary values and column codes are staged 64 columns at a time
+
+/** Per-warp staging area for lane 0: top-boundary H and F̂, and packed column codes, of the next 64 columns. */
+struct column_chunk_t {
+    std::uint32_t top_h[chunk_columns_k];
+    std::uint32_t top_f[chunk_columns_k];
+    std::uint32_t code[chunk_columns_k];
+};
+
+/**
+ *  Scores tasks @p a and @p b (b may be absent: `b_present == false`) with one warp. All lanes call it together.
+ *
+ *  Per step t, lane L updates column j = t + 1 - L for both pairs. The dependency chain a step waits on is the
+ *  shuffle of the upper lane's bottom values plus two DPX operations per row: with X = max(Ê + open, diag + s)
+ *  computed off the chain, H = max(X, F̂_up + (extend + open), H_up + open). Column codes travel one step ahead of
+ *  the values (a lane forwards its current code, which is the code of the next lane's next column), so every
+ *  profile load is issued a step before it is used.
+ *
+ *  @param scratch  this warp's scratch row, (longest column + 1) x 2 packed words
+ *  @param profile  this warp's shared profile area, dp16_profile_bytes_per_warp bytes
+ *  @param chunk    this warp's staging area
+ */
+template <typename policy_>
+__device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_task_t const &b, bool b_present,
+                                                  score_costs_t const &costs, std::uint32_t *scratch,
+                                                  std::int8_t *profile, column_chunk_t &chunk, std::int64_t &score_a,
+                                                  std::int64_t &score_b) {
+    using ops = packed_ops_t<policy_::maximize_k>;
+    constexpr int R = policy_::rows_per_lane_k;
+    constexpr int S = policy_::strip_rows_k;
+    constexpr bool affine = policy_::affine_k;
+    constexpr bool local = policy_::local_k;
+    static_assert(R == 8, "the packed kernel unpacks one 8-byte profile word per pair and step");
+
+    int const lane = threadIdx.x & 31;
+    std::uint32_t const n_a = a.rows_length, m_a = a.cols_length;
+    std::uint32_t const n_b = b_present ? b.rows_length : 0u, m_b = b_present ? b.cols_length : 0u;
+    std::uint32_t const n_max = max(n_a, n_b), m_max = max(m_a, m_b), m_min = min(m_a, m_b);
+    std::int32_t const open = costs.open, extend = costs.extend;
+    std::uint32_t const open2 = pack16(open, open), extend2 = pack16(extend, extend);
+    std::uint32_t const extend_open2 = pack16(extend + open, extend + open);
+    boundary_t<std::int32_t> const edge {open, extend, affine, local};
+    int const classes = costs.classes;
+    std::int8_t const *table_a = a.transposed ? costs.profile_table_t : costs.profile_table;
+    std::int8_t const *table_b = b.transposed ? costs.profile_table_t : costs.profile_table;
+    std::int8_t *profile_a = profile;
+    std::int8_t *profile_b = profile + classes * S;
+    std::uint8_t const *cols_b = b_present ? b.cols : a.cols;
+
+    // Gap-track seeds, shifted by `open`: global `extend + M[i][0]`, local `extend`.
+    auto gap_seed = [&](std::int64_t i) -> std::int32_t { return local ? extend : extend + edge.score(i); };
+    auto column_code = [&](std::uint32_t j) -> std::uint32_t { // packed codes of column j (1-based) of both pairs
+        std::uint32_t const ca = j <= m_a ? costs.byte_to_compact[a.cols[j - 1]] : 0u;
+        std::uint32_t const cb = j <= m_b ? costs.byte_to_compact[cols_b[j - 1]] : 0u;
+        return ca | (cb << 8);
+    };
+
+    std::int32_t result_a = 0, result_b = 0;
+    std::uint32_t lane_best = 0; // packed running maxima of valid cells (local scores), starts at 0 like the reference
+
+    for (std::uint32_t strip_base = 0; strip_base < n_max; strip_base += S) {
+        std::uint32_t const rows_here = min((std::uint32_t)S, n_max - strip_base);
+        bool const last_strip = strip_base + S >= n_max;
+        int const last_lane = int((rows_here - 1) / R);
+        std::int64_t const row0 = (std::int64_t)strip_base + lane * R + 1;
+
+        // Profiles of both pairs for this strip: profile[cc * S + row] = cost(row class, column class cc).
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            std::int64_t const i = row0 + r;
+            int const class_a = costs.byte_to_class[i <= (std::int64_t)n_a ? a.rows[i - 1] : 0u];
+            int const class_b = costs.byte_to_class[i <= (std::int64_t)n_b ? b.rows[i - 1] : 0u];
+            for (int cc = 0; cc < classes; ++cc) {
+                profile_a[cc * S + lane * R + r] = table_a[cc * 32 + class_a];
+                profile_b[cc * S + lane * R + r] = table_b[cc * 32 + class_b];
+            }
+        }
+
+        std::uint32_t h_col[R], e_col[R], best_row[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            std::int32_t const h = edge.score(row0 + r);
+            h_col[r] = pack16(h, h);
+            std::int32_t const e = gap_seed(row0 + r);
+            e_col[r] = pack16(e, e);
+            best_row[r] = 0;
+        }
+        std::int32_t const diag_seed = edge.score(row0 - 1);
+        std::uint32_t diag_up = pack16(diag_seed, diag_seed);
+
+        // Lanes holding each pair's last row in this strip, and the row inside the lane.
+        bool const a_ends_here = strip_base < n_a && strip_base + S >= n_a;
+        bool const b_ends_here = b_present && strip_base < n_b && strip_base + S >= n_b;
+        int const a_lane = a_ends_here ? int((n_a - 1 - strip_base) / R) : -1;
+        int const b_lane = b_ends_here ? int((n_b - 1 - strip_base) / R) : -1;
+        int const a_row = int((n_a - 1 - strip_base) % R), b_row = int((n_b - 1 - strip_base) % R);
+
+        std::uint32_t const steps = m_max + (std::uint32_t)last_lane;
+        bool const write_bottom = !last_strip;
+        std::uint32_t out_h = 0, out_f = 0;
+        std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
+        __syncwarp();
+        uint2 pa_now = *reinterpret_cast<uint2 const *>(profile_a + (code_now & 0xFF) * S + lane * R);
+        uint2 pb_now = *reinterpret_cast<uint2 const *>(profile_b + (code_now >> 8) * S + lane * R);
+
+        for (std::uint32_t t = 0; t < steps; ++t) {
+            std::uint32_t const e = t & (chunk_columns_k - 1);
+            if (e == 0) {
+                // Stage lane 0's next 64 top-boundary values (columns t+1..) and codes (columns t+2..).
+                __syncwarp();
+#pragma unroll
+                for (int k = lane; k < chunk_columns_k; k += 32) {
+                    std::uint32_t const j = t + 1 + k;
+                    std::uint32_t h = 0, f = 0;
+                    if (j <= m_max) {
+                        if (strip_base == 0) {
+                            std::int32_t const v = edge.score(j), g = gap_seed(j);
+                            h = pack16(v, v), f = pack16(g, g);
+                        }
+                        else {
+                            uint2 const stored = *reinterpret_cast<uint2 const *>(scratch + 2 * j);
+                            h = stored.x, f = stored.y;
+                        }
+                    }
+                    chunk.top_h[k] = h;
+                    chunk.top_f[k] = f;
+                    chunk.code[k] = j + 1 <= m_max ? column_code(j + 1) : 0u;
+                }
+                __syncwarp();
+            }
+            std::uint32_t const staged_h = chunk.top_h[e], staged_f = chunk.top_f[e], staged_code = chunk.code[e];
+            std::uint32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
+            std::uint32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0u;
+            std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
+            if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
+            uint2 const pa_next = *reinterpret_cast<uint2 const *>(profile_a + (code_next & 0xFF) * S + lane * R);
+            uint2 const pb_next = *reinterpret_cast<uint2 const *>(profile_b + (code_next >> 8) * S + lane * R);
+
+            std::int64_t const j = (std::int64_t)t + 1 - lane;
+            if (j >= 1 && j <= (std::int64_t)m_max && lane <= last_lane) {
+                std::uint32_t diag = diag_up;
+                diag_up = up_h;
+                std::uint32_t h_up = up_h, f_up = up_f;
+                std::uint32_t subs[R];
+                subs[0] = interleave_signed_bytes<0>(pa_now.x, pb_now.x);
+                subs[1] = interleave_signed_bytes<1>(pa_now.x, pb_now.x);
+                subs[2] = interleave_signed_bytes<2>(pa_now.x, pb_now.x);
+                subs[3] = interleave_signed_bytes<3>(pa_now.x, pb_now.x);
+                subs[4] = interleave_signed_bytes<0>(pa_now.y, pb_now.y);
+                subs[5] = interleave_signed_bytes<1>(pa_now.y, pb_now.y);
+                subs[6] = interleave_signed_bytes<2>(pa_now.y, pb_now.y);
+                subs[7] = interleave_signed_bytes<3>(pa_now.y, pb_now.y);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    std::uint32_t const substitution = ops::add(diag, subs[r]);
+                    std::uint32_t h;
+                    if constexpr (affine) {
+                        // Off the chain: the horizontal track and X = max(E, diag + s) with E = Ê + open.
+                        std::uint32_t const e_new = ops::add_opt(e_col[r], extend2, h_col[r]);
+                        std::uint32_t const x = ops::add_opt(e_new, open2, substitution);
+                        // On the chain: H = max(X, F̂_up + extend + open, H_up + open); F̂ = max(F̂_up + extend, H_up).
+                        std::uint32_t const via_f = ops::add_opt(f_up, extend_open2, x);
+                        if constexpr (local) h = ops::add_opt_relu(h_up, open2, via_f);
+                        else h = ops::add_opt(h_up, open2, via_f);
+                        f_up = ops::add_opt(f_up, extend2, h_up);
+                        e_col[r] = e_new;
+                    }
+                    else {
+                        std::uint32_t const x = ops::add_opt(h_col[r], open2, substitution);
+                        if constexpr (local) h = ops::add_opt_relu(h_up, open2, x);
+                        else h = ops::add_opt(h_up, open2, x);
+                    }
+                    diag = h_col[r];
+                    h_col[r] = h;
+                    h_up = h;
+                }
+                if constexpr (local) {
+                    // Columns past one pair's end carry filler in that half: mask it out of the maxima (H >= 0).
+                    std::uint32_t const mask = j <= (std::int64_t)m_min
+                                                   ? 0xFFFFFFFFu
+                                                   : ((j <= (std::int64_t)m_a ? 0x0000FFFFu : 0u) |
+                                                      (j <= (std::int64_t)m_b ? 0xFFFF0000u : 0u));
+#pragma unroll
+                    for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], h_col[r] & mask, 0u);
+                }
+                else {
+                    if (lane == a_lane && j == (std::int64_t)m_a) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == a_row) result_a = low16(h_col[r]);
+                    }
+                    if (lane == b_lane && j == (std::int64_t)m_b) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == b_row) result_b = high16(h_col[r]);
+                    }
+                }
+                out_h = h_up, out_f = f_up;
+                if (write_bottom && lane == 31) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
+            }
+            code_now = code_next, pa_now = pa_next, pb_now = pb_next;
+        }
+        if constexpr (local) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                std::uint32_t const keep = ((row0 + r <= (std::int64_t)n_a) ? 0x0000FFFFu : 0u) |
+                                           ((row0 + r <= (std::int64_t)n_b) ? 0xFFFF0000u : 0u);
+                lane_best = __vimax3_s16x2(lane_best, best_row[r] & keep, 0u);
+            }
+        }
+        __syncwarp();
+    }
+    if constexpr (local) {
+#pragma unroll
+        for (int offset = 16; offset > 0; offset >>= 1)
+            lane_best = __vimax3_s16x2(lane_best, __shfl_xor_sync(0xFFFFFFFFu, lane_best, offset), 0u);
+        result_a = low16(lane_best), result_b = high16(lane_best);
+    }
+    else {
+        // The capturing lanes hold the results; broadcast them.
+        int const a_owner = (int)((n_a - 1) % S) / R;
+        int const b_owner = b_present ? (int)((n_b - 1) % S) / R : 0;
+        result_a = __shfl_sync(0xFFFFFFFFu, result_a, a_owner);
+        result_b = __shfl_sync(0xFFFFFFFFu, result_b, b_owner);
+    }
+    score_a = result_a;
+    score_b = result_b;
+}
+
+/** Persistent kernel over the 16x2 bins: warps take two consecutive scheduled pairs at a time. */
+template <typename policy_>
+__global__ void __launch_bounds__(256) dp16_wavefront_kernel(pair_task_t const *__restrict__ tasks,
+                                                             plan_bins_t *__restrict__ bins, int key_begin,
+                                                             int key_end, score_costs_t const costs,
+                                                             std::int64_t *__restrict__ results,
+                                                             std::uint32_t *__restrict__ scratch,
+                                                             std::size_t scratch_cells_per_warp) {
+    extern __shared__ __align__(16) unsigned char shared_bytes[];
+    score_costs_t &costs_s = *reinterpret_cast<score_costs_t *>(shared_bytes);
+    std::int8_t *profiles = reinterpret_cast<std::int8_t *>(shared_bytes + ((sizeof(score_costs_t) + 15) / 16) * 16);
+    {
+        auto const *src = reinterpret_cast<std::uint32_t const *>(&costs);
+        auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
+        for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    int const lane = threadIdx.x & 31;
+    int const warp_in_cta = threadIdx.x >> 5;
+    std::size_t const global_warp = (std::size_t)blockIdx.x * (blockDim.x >> 5) + warp_in_cta;
+    std::uint32_t *warp_scratch = scratch + global_warp * scratch_cells_per_warp;
+    std::size_t const profile_bytes = (std::size_t)dp16_profile_bytes_per_warp<policy_>(costs.classes);
+    auto *chunks = reinterpret_cast<column_chunk_t *>(profiles + (blockDim.x >> 5) * profile_bytes);
+    std::int8_t *warp_profile = profiles + warp_in_cta * profile_bytes;
+    column_chunk_t &warp_chunk = chunks[warp_in_cta];
+    std::uint32_t const begin = bins->begin[key_begin];
+    std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
+    while (true) {
+        std::uint32_t index = 0;
+        if (lane == 0) index = atomicAdd(&bins->cursor[key_begin], 2u);
+        index = __shfl_sync(0xFFFFFFFFu, index, 0);
+        if (index >= count) break;
+        pair_task_t const first = tasks[begin + index];
+        bool const has_second = index + 1 < count;
+        pair_task_t const second = has_second ? tasks[begin + index + 1] : first;
+        std::int64_t score_a = 0, score_b = 0;
+        dp16_score_couple<policy_>(first, second, has_second, costs_s, warp_scratch, warp_profile, warp_chunk, score_a,
+                                   score_b);
+        if (lane == 0) {
+            results[first.slot] = score_a;
+            if (has_second) results[second.slot] = score_b;
+        }
+    }
+}
+
+} // namespace szs_gb300

@@ -174,6 +174,9 @@ struct device_context_t {
         SZS_TRY_CUDA(cudaEventCreate(&compute_stop));
         status_t status = control.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256, own_stream);
         if (!status.ok()) return status;
+        // The alphabet's mark words must start at zero (each alphabet pass clears them again).
+        SZS_TRY_CUDA(cudaMemsetAsync(control.data, 0, control.bytes, own_stream));
+        SZS_TRY_CUDA(cudaStreamSynchronize(own_stream));
         status = readback.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256);
         if (!status.ok()) return status;
         ready = true;
@@ -498,16 +501,35 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     args.steps_beyond_span = costs.affine ? 3 : 1;
     args.force_route = engine.schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
+    args.packed_allowed = 1;
+    bool const levenshtein = engine.kind == kind_levenshtein_k;
+
     SZS_TRY_CUDA(cudaEventRecord(context->start, stream));
     std::uint64_t launches = 0;
     plan_bins_t *bins = context->bins_device();
+    batch_alphabet_t *alphabet = context->alphabet_device();
+    // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code planes by
+    // it, and the 16x2 route builds its substitution profile over it (when it has at most 32 symbols).
+    if (levenshtein) {
+        SZS_TRY_CUDA(launch_alphabet(args.queries, args.candidates, call.has_candidates, alphabet, context->sm_count,
+                                     stream));
+        launches += 2 + (call.has_candidates ? 1 : 0);
+        args.alphabet = alphabet;
+    }
     SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, stream));
     launches += 3;
-    // Read the plan back: which bins are non-empty and how long the columns get.
-    SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t), cudaMemcpyDeviceToHost, stream));
+    // Read the plan (and the alphabet, stored right after it) back: which bins are non-empty, how long columns get.
+    SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t) + sizeof(batch_alphabet_t),
+                                 cudaMemcpyDeviceToHost, stream));
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
+    batch_alphabet_t const &alphabet_host = *context->alphabet_host();
     engine.stats.last_cells = plan.cells;
+    auto pairs_in = [&](int key_begin, int key_end) {
+        std::uint64_t total = 0;
+        for (int key = key_begin; key < key_end; ++key) total += plan.count[key];
+        return total;
+    };
 
     // Scoring kernels are bracketed by their own events so the stats isolate them from planning and copies.
     bool compute_recorded = false;
@@ -517,73 +539,72 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
         return cudaEventRecord(context->compute_start, stream);
     };
 
-    // Bit-parallel routes.
-    if (engine.unit_levenshtein) {
-        bool any_myers = false;
-        for (int key = bin_myers_begin_k; key < bin_dp32_begin_k; ++key) any_myers |= plan.count[key] != 0;
-        if (any_myers) {
-            // Alphabet of the batch, marked over every pair's bytes.
-            SZS_TRY_CUDA(cudaMemsetAsync(bins->symbol_mask, 0, sizeof(plan.symbol_mask), stream));
-            auto mark_range = [&](tape_t const &tape, staging_plan_t const &plan_of) -> cudaError_t {
-                std::uint64_t first = plan_of.first, last = plan_of.last;
-                if (plan_of.offsets_on_device && plan_of.data_on_device) {
-                    // Device-resident tape: read its range.
-                    std::uint64_t ends[2] = {0, 0};
-                    if (tape.offset_bits == 32) {
-                        std::uint32_t e32[2];
-                        cudaMemcpyAsync(&e32[0], tape.offsets, 4, cudaMemcpyDeviceToHost, stream);
-                        cudaMemcpyAsync(&e32[1], static_cast<std::uint32_t const *>(tape.offsets) + tape.count, 4,
-                                        cudaMemcpyDeviceToHost, stream);
-                        cudaStreamSynchronize(stream);
-                        ends[0] = e32[0], ends[1] = e32[1];
-                    }
-                    else {
-                        cudaMemcpyAsync(&ends[0], tape.offsets, 8, cudaMemcpyDeviceToHost, stream);
-                        cudaMemcpyAsync(&ends[1], static_cast<std::uint64_t const *>(tape.offsets) + tape.count, 8,
-                                        cudaMemcpyDeviceToHost, stream);
-                        cudaStreamSynchronize(stream);
-                    }
-                    first = ends[0], last = ends[1];
+    // 16x2 packed wavefront: Levenshtein engines score over the batch alphabet's codes.
+    score_costs_t packed_costs;
+    if (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k)) {
+        packed_costs = costs;
+        if (levenshtein) {
+            int const symbols = (int)alphabet_host.symbols;
+            packed_costs.classes = symbols;
+            for (int b = 0; b < 256; ++b)
+                packed_costs.byte_to_class[b] = packed_costs.byte_to_compact[b] = alphabet_host.code[b];
+            for (int cc = 0; cc < 32; ++cc)
+                for (int rc = 0; rc < 32; ++rc) {
+                    std::int8_t const cost = (std::int8_t)(cc == rc ? costs.match : costs.mismatch);
+                    packed_costs.profile_table[cc * 32 + rc] = packed_costs.profile_table_t[cc * 32 + rc] = cost;
                 }
-                return launch_alphabet(tape.base + first, last - first, bins->symbol_mask, context->sm_count, stream);
-            };
-            SZS_TRY_CUDA(mark_range(args.queries, query_plan));
-            if (call.has_candidates) SZS_TRY_CUDA(mark_range(args.candidates, candidate_plan));
-            SZS_TRY_CUDA(launch_alphabet_codes(bins->symbol_mask, context->alphabet_device(), stream));
-            SZS_TRY_CUDA(cudaMemcpyAsync(context->alphabet_host(), context->alphabet_device(),
-                                         sizeof(batch_alphabet_t), cudaMemcpyDeviceToHost, stream));
-            SZS_TRY_CUDA(cudaStreamSynchronize(stream));
-            launches += 2;
-            int const planes = myers_planes_for((int)context->alphabet_host()->bits);
-            for (int words = 1; words <= myers_max_words_k; ++words) {
-                std::uint64_t pairs_here = 0;
-                for (int k = 0; k < 16; ++k) pairs_here += plan.count[bin_myers_begin_k + words * 16 + k];
-                if (!pairs_here) continue;
-                int const threads = myers_threads_per_cta();
-                std::uint64_t const needed = (pairs_here + threads - 1) / threads;
-                int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
-                bool const exact = engine.schedule != szs_gb300_schedule_plain_k;
-                SZS_TRY_CUDA(mark_compute_start());
-                SZS_TRY_CUDA(launch_myers(words, planes, exact, tasks, bins, context->alphabet_device(), results,
-                                          ctas, stream));
-                ++launches;
-            }
         }
     }
 
-    // Wavefront routes.
+    // Bit-parallel routes.
+    if (engine.unit_levenshtein && pairs_in(bin_myers_begin_k, bin_dp32_begin_k)) {
+        int const planes = myers_planes_for((int)alphabet_host.bits);
+        for (int words = 1; words <= myers_max_words_k; ++words) {
+            std::uint64_t const pairs_here = pairs_in(bin_myers_begin_k + words * 16, bin_myers_begin_k + words * 16 + 16);
+            if (!pairs_here) continue;
+            int const threads = myers_threads_per_cta();
+            std::uint64_t const needed = (pairs_here + threads - 1) / threads;
+            int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
+            bool const exact = engine.schedule != szs_gb300_schedule_plain_k;
+            SZS_TRY_CUDA(mark_compute_start());
+            SZS_TRY_CUDA(launch_myers(words, planes, exact, tasks, bins, alphabet, results, ctas, stream));
+            ++launches;
+        }
+    }
+
+    std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
+    {
+        std::uint64_t const pairs_here = pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k);
+        if (pairs_here) {
+            dp_launch_shape_t const shape = dp16_shape(engine.kind, costs.affine != 0, packed_costs.classes);
+            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
+            std::uint64_t const warps_needed = (pairs_here + 1) / 2;
+            std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
+            int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+            std::size_t const scratch_bytes = cells_per_warp * 4 * (std::size_t)ctas * shape.warps_per_cta;
+            status = context->scratch.reserve(scratch_bytes, stream);
+            if (!status.ok()) return status;
+            SZS_TRY_CUDA(mark_compute_start());
+            SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, bin_dp16_begin_k,
+                                     bin_dp16_begin_k + bin_dp16_classes_k, tasks, bins, packed_costs, results,
+                                     context->scratch.data, cells_per_warp, ctas, stream));
+            ++launches;
+        }
+    }
+
+    // 32- and 64-bit wavefront routes.
     for (int cell_bits : {32, 64}) {
         int const key_begin = cell_bits == 32 ? bin_dp32_begin_k : bin_dp64_begin_k;
         int const key_end = key_begin + bin_dp_classes_k;
-        std::uint64_t pairs_here = 0;
-        for (int key = key_begin; key < key_end; ++key) pairs_here += plan.count[key];
+        std::uint64_t const pairs_here = pairs_in(key_begin, key_end);
         if (!pairs_here) continue;
         dp_launch_shape_t const shape = dp_shape(engine.kind, costs.affine != 0, cell_bits, costs.classes);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Wavefront kernel cannot be resident"};
         std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
-        std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
         std::size_t const scratch_bytes = cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta;
+        // The scratch buffer may be shared with a packed launch queued earlier on this stream: stream order keeps
+        // the two kernels from overlapping.
         status = context->scratch.reserve(scratch_bytes, stream);
         if (!status.ok()) return status;
         SZS_TRY_CUDA(mark_compute_start());

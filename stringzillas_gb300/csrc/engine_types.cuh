@@ -55,6 +55,7 @@ struct batch_alphabet_t {
     std::uint8_t code[256];
     std::uint32_t symbols;
     std::uint32_t bits;
+    std::uint32_t mask_scratch[8]; // bytes seen, accumulated by the mark pass and cleared by the code pass
 };
 
 } // namespace szs_gb300

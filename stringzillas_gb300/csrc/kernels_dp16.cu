@@ -1,0 +1,76 @@
+/**
+ *  @file kernels_dp16.cu
+ *  @brief Instantiations and launcher of the 16x2 packed wavefront kernel (dp_packed.cuh).
+ */
+#include "dp_packed.cuh"
+#include "launchers.h"
+
+namespace szs_gb300 {
+
+namespace {
+
+constexpr int dp16_rows_per_lane_k = 8;
+constexpr int dp16_threads_k = 128;
+
+template <int kind_, bool affine_>
+using dp16_instance_t = dp16_policy_t<kind_, affine_, dp16_rows_per_lane_k>;
+
+template <int kind_, bool affine_>
+dp_launch_shape_t dp16_shape_of(int classes) {
+    using policy_t = dp16_instance_t<kind_, affine_>;
+    dp_launch_shape_t shape;
+    shape.threads_per_cta = dp16_threads_k;
+    shape.warps_per_cta = dp16_threads_k / 32;
+    shape.rows_per_lane = dp16_rows_per_lane_k;
+    shape.shared_bytes = dp16_shared_bytes<policy_t>(shape.warps_per_cta, classes);
+    auto kernel = dp16_wavefront_kernel<policy_t>;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shape.shared_bytes);
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, shape.threads_per_cta, shape.shared_bytes) !=
+        cudaSuccess)
+        blocks = 0;
+    shape.ctas_per_sm = blocks;
+    return shape;
+}
+
+template <int kind_, bool affine_>
+cudaError_t dp16_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                           score_costs_t const &costs, std::int64_t *results, void *scratch,
+                           std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+    using policy_t = dp16_instance_t<kind_, affine_>;
+    int const shared = dp16_shared_bytes<policy_t>(dp16_threads_k / 32, costs.classes);
+    auto kernel = dp16_wavefront_kernel<policy_t>;
+    cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
+    if (status != cudaSuccess) return status;
+    kernel<<<ctas, dp16_threads_k, shared, stream>>>(tasks, bins, key_begin, key_end, costs, results,
+                                                     static_cast<std::uint32_t *>(scratch), scratch_cells_per_warp);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+#define SZS_DP16_DISPATCH(call_, ...)                                                                                \
+    switch (kind * 2 + (affine ? 1 : 0)) {                                                                           \
+    case 0: return call_<kind_levenshtein_k, false>(__VA_ARGS__);                                                    \
+    case 1: return call_<kind_levenshtein_k, true>(__VA_ARGS__);                                                     \
+    case 2: return call_<kind_needleman_wunsch_k, false>(__VA_ARGS__);                                               \
+    case 3: return call_<kind_needleman_wunsch_k, true>(__VA_ARGS__);                                                \
+    case 4: return call_<kind_smith_waterman_k, false>(__VA_ARGS__);                                                 \
+    case 5: return call_<kind_smith_waterman_k, true>(__VA_ARGS__);                                                  \
+    default: break;                                                                                                  \
+    }
+
+dp_launch_shape_t dp16_shape(int kind, bool affine, int classes) {
+    SZS_DP16_DISPATCH(dp16_shape_of, classes)
+    return dp_launch_shape_t {0, 0, 0, 0, 0};
+}
+
+cudaError_t launch_dp16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                        score_costs_t const &costs, std::int64_t *results, void *scratch,
+                        std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+    SZS_DP16_DISPATCH(dp16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
+                      ctas, stream)
+    return cudaErrorInvalidValue;
+}
+
+} // namespace szs_gb300

@@ -16,9 +16,10 @@ namespace szs_gb300 {
 
 cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t *tasks, std::int64_t *results,
                         int sm_count, cudaStream_t stream);
-cudaError_t launch_alphabet(std::uint8_t const *data, std::uint64_t length, std::uint32_t *symbol_mask, int sm_count,
-                            cudaStream_t stream);
-cudaError_t launch_alphabet_codes(std::uint32_t const *symbol_mask, batch_alphabet_t *alphabet, cudaStream_t stream);
+/** Marks the bytes of both tapes and assigns dense codes (`alphabet->code`, `symbols`, `bits`), on the device.
+ *  The alphabet's mark words must be zero on entry (they start zeroed and the code pass clears them again). */
+cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
+                            batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream);
 cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
                                   std::uint64_t stride, int sm_count, cudaStream_t stream);
 
@@ -39,6 +40,15 @@ dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes);
 cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int key_end, pair_task_t const *tasks,
                       plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                       std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
+
+/** Launch shape of the 16x2 packed wavefront kernel; ctas_per_sm = 0 if unsupported. */
+dp_launch_shape_t dp16_shape(int kind, bool affine, int classes);
+
+/** Runs the 16x2 packed wavefront kernel over bins [key_begin, key_end): two scheduled pairs per warp. `scratch`
+ *  holds `ctas * warps_per_cta` rows of `scratch_cells_per_warp` 32-bit words. */
+cudaError_t launch_dp16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                        score_costs_t const &costs, std::int64_t *results, void *scratch,
+                        std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
 
 /** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
  *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be

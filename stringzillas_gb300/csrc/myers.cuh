@@ -10,7 +10,9 @@
  *
  *  Match masks: instead of a 256-entry table per pattern, the pattern is stored as B bit-planes of its characters'
  *  codes in a batch-wide alphabet of at most 2^B symbols (DNA: B = 2). The mask for a text character of code c is
- *  `AND_b (bit_b(c) ? plane_b : ~plane_b)`, one LOP3 per plane and word.
+ *  `AND_b (bit_b(c) ? plane_b : ~plane_b)`, one LOP3 per plane and word, with the per-character selectors read from
+ *  a shared table. The multi-word add chains through the carry flag (one add per word), and the text is consumed in
+ *  aligned 8-byte chunks whose 8 characters are unrolled, so a warp's threads do not diverge per character.
  *
  *  Replaces the reference's Myers tiers (include/stringzillas/similarities/cuda.cuh:2072-2634), which read a
  *  256 x words mask table from shared memory. The serial oracle answers unit-cost Levenshtein the same way
@@ -23,12 +25,73 @@
 
 namespace szs_gb300 {
 
+/**
+ *  Per-byte match-mask selectors for B planes: `select[byte][b]` is all-ones where bit b of the byte's code is 0, so
+ *  the match mask of a word is `AND_b (plane_b ^ select_b)`. Kept in shared memory: one table lookup per text
+ *  character replaces the per-plane bit extraction.
+ */
+template <int bits_>
+struct plane_selectors_t {
+    std::uint32_t select[256][bits_];
+};
+
+/** Bit-parallel state of one pattern (all rows) and the step over one text character. */
+template <int words_, int bits_, bool exact_>
+struct myers_state_t {
+    static constexpr int W = words_, B = bits_;
+    std::uint32_t planes[B][W];
+    std::uint32_t pv[W], mv[W];
+    std::int32_t score;
+    std::uint32_t last_bit;
+    int last_word;
+
+    __device__ __forceinline__ void step(std::uint32_t const (&select)[B]) {
+        std::uint32_t eq[W], xv[W], sum[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            std::uint32_t e = 0xFFFFFFFFu;
+#pragma unroll
+            for (int b = 0; b < B; ++b) e &= planes[b][w] ^ select[b];
+            eq[w] = e;
+            xv[w] = e | mv[w];
+            sum[w] = e & pv[w];
+        }
+        // Multi-word (Eq & Pv) + Pv: one add per word, the carry rippling upwards through the carry flag.
+        asm volatile("add.cc.u32 %0, %0, %1;" : "+r"(sum[0]) : "r"(pv[0]));
+#pragma unroll
+        for (int w = 1; w < W; ++w) asm volatile("addc.cc.u32 %0, %0, %1;" : "+r"(sum[w]) : "r"(pv[w]));
+        std::uint32_t ph_prev = 1u << 31, mh_prev = 0u; // shifting these in brings +1 into row 0, 0 into mh
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            std::uint32_t const xh = (sum[w] ^ pv[w]) | eq[w];
+            std::uint32_t const ph = mv[w] | ~(xh | pv[w]);
+            std::uint32_t const mh = pv[w] & xh;
+            if (exact_ ? w == W - 1 : w == last_word)
+                score += (std::int32_t)((ph >> last_bit) & 1u) - (std::int32_t)((mh >> last_bit) & 1u);
+            std::uint32_t const ph_shifted = __funnelshift_l(ph_prev, ph, 1);
+            std::uint32_t const mh_shifted = __funnelshift_l(mh_prev, mh, 1);
+            pv[w] = mh_shifted | ~(xv[w] | ph_shifted);
+            mv[w] = ph_shifted & xv[w];
+            ph_prev = ph, mh_prev = mh;
+        }
+    }
+
+    template <typename selectors_type_>
+    __device__ __forceinline__ void step_byte(selectors_type_ const &table, std::uint32_t byte) {
+        std::uint32_t select[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) select[b] = table.select[byte][b];
+        step(select);
+    }
+};
+
 template <int words_, int bits_, bool exact_>
 __device__ __forceinline__ std::uint32_t myers_distance(std::uint8_t const *pattern, std::uint32_t n,
                                                         std::uint8_t const *text, std::uint32_t m,
-                                                        std::uint8_t const *code) {
+                                                        std::uint8_t const *code,
+                                                        plane_selectors_t<bits_> const &selectors) {
     constexpr int W = words_, B = bits_;
-    std::uint32_t planes[B][W];
+    myers_state_t<W, B, exact_> state;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         std::uint32_t acc[B];
@@ -42,52 +105,32 @@ __device__ __forceinline__ std::uint32_t myers_distance(std::uint8_t const *patt
             for (int b = 0; b < B; ++b) acc[b] |= ((c >> b) & 1u) << k;
         }
 #pragma unroll
-        for (int b = 0; b < B; ++b) planes[b][w] = acc[b];
+        for (int b = 0; b < B; ++b) state.planes[b][w] = acc[b];
     }
+#pragma unroll
+    for (int w = 0; w < W; ++w) state.pv[w] = 0xFFFFFFFFu, state.mv[w] = 0u;
+    state.last_bit = (n - 1) & 31u;
+    state.last_word = exact_ ? W - 1 : int((n - 1) / 32u); // the word holding row n
+    state.score = (std::int32_t)n;
 
-    std::uint32_t pv[W], mv[W];
+    // Text: a ragged head up to 8-byte alignment, whole aligned 8-byte chunks with the 8 columns unrolled (no
+    // per-character branches, so the lanes of a warp stay converged), and a ragged tail.
+    std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(text);
+    std::uint32_t head = (std::uint32_t)((8 - (address & 7)) & 7);
+    if (head > m) head = m;
+    for (std::uint32_t j = 0; j < head; ++j) state.step_byte(selectors, text[j]);
+    std::uint64_t const *chunks = reinterpret_cast<std::uint64_t const *>(text + head);
+    std::uint32_t const full = (m - head) / 8;
+    for (std::uint32_t c = 0; c < full; ++c) {
+        std::uint64_t const word = __ldg(chunks + c);
+        std::uint32_t const lo = (std::uint32_t)word, hi = (std::uint32_t)(word >> 32);
 #pragma unroll
-    for (int w = 0; w < W; ++w) pv[w] = 0xFFFFFFFFu, mv[w] = 0u;
-    std::uint32_t const last_bit = (n - 1) & 31u;
-    int const last_word = exact_ ? W - 1 : int((n - 1) / 32u); // the word holding row n
-    std::int32_t score = (std::int32_t)n;
-
-    byte_stream_t stream;
-    stream.open_at(text);
-    for (std::uint32_t j = 0; j < m; ++j) {
-        std::uint32_t const c = code[stream.next()];
-        std::uint32_t flip[B];
+        for (int k = 0; k < 4; ++k) state.step_byte(selectors, (lo >> (8 * k)) & 0xFFu);
 #pragma unroll
-        for (int b = 0; b < B; ++b) flip[b] = ((c >> b) & 1u) ? 0u : 0xFFFFFFFFu;
-        std::uint32_t eq[W], xv[W], xh[W];
-        std::uint32_t carry = 0;
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-            std::uint32_t e = 0xFFFFFFFFu;
-#pragma unroll
-            for (int b = 0; b < B; ++b) e &= planes[b][w] ^ flip[b];
-            eq[w] = e;
-            xv[w] = e | mv[w];
-            // Multi-word (Eq & Pv) + Pv with the carry rippling upwards.
-            std::uint64_t const sum = (std::uint64_t)(e & pv[w]) + pv[w] + carry;
-            carry = (std::uint32_t)(sum >> 32);
-            xh[w] = ((std::uint32_t)sum ^ pv[w]) | e;
-        }
-        std::uint32_t ph_prev = 1u << 31, mh_prev = 0u; // shifting these in brings +1 into row 0, 0 into mh
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-            std::uint32_t const ph = mv[w] | ~(xh[w] | pv[w]);
-            std::uint32_t const mh = pv[w] & xh[w];
-            if (w == last_word)
-                score += (std::int32_t)((ph >> last_bit) & 1u) - (std::int32_t)((mh >> last_bit) & 1u);
-            std::uint32_t const ph_shifted = __funnelshift_l(ph_prev, ph, 1);
-            std::uint32_t const mh_shifted = __funnelshift_l(mh_prev, mh, 1);
-            pv[w] = mh_shifted | ~(xv[w] | ph_shifted);
-            mv[w] = ph_shifted & xv[w];
-            ph_prev = ph, mh_prev = mh;
-        }
+        for (int k = 0; k < 4; ++k) state.step_byte(selectors, (hi >> (8 * k)) & 0xFFu);
     }
-    return (std::uint32_t)score;
+    for (std::uint32_t j = head + full * 8; j < m; ++j) state.step_byte(selectors, text[j]);
+    return (std::uint32_t)state.score;
 }
 
 /** Thread-per-pair kernel over the Myers bin of one word count. */
@@ -97,7 +140,13 @@ __global__ void __launch_bounds__(128) myers_kernel(pair_task_t const *__restric
                                                     batch_alphabet_t const *__restrict__ alphabet,
                                                     std::int64_t *__restrict__ results) {
     __shared__ std::uint8_t code_s[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) code_s[i] = alphabet->code[i];
+    __shared__ plane_selectors_t<bits_> selectors_s;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        std::uint32_t const c = alphabet->code[i];
+        code_s[i] = (std::uint8_t)c;
+#pragma unroll
+        for (int b = 0; b < bits_; ++b) selectors_s.select[i][b] = ((c >> b) & 1u) ? 0u : 0xFFFFFFFFu;
+    }
     __syncthreads();
     int const key_begin = bin_myers_begin_k + words_ * 16, key_end = key_begin + 16;
     std::uint32_t const begin = bins->begin[key_begin];
@@ -106,7 +155,8 @@ __global__ void __launch_bounds__(128) myers_kernel(pair_task_t const *__restric
          index += gridDim.x * blockDim.x) {
         pair_task_t const task = tasks[begin + index];
         results[task.slot] =
-            myers_distance<words_, bits_, exact_>(task.rows, task.rows_length, task.cols, task.cols_length, code_s);
+            myers_distance<words_, bits_, exact_>(task.rows, task.rows_length, task.cols, task.cols_length, code_s,
+                                                  selectors_s);
     }
 }
 

@@ -86,6 +86,18 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     bool const maximize = args.kind != kind_levenshtein_k;
     std::uint64_t const span = maximize ? n + m : (n > m ? n : m);
     std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;
+    bool const packed = args.packed_allowed && reach < 32767 &&
+                        (args.kind != kind_levenshtein_k || (args.alphabet && args.alphabet->symbols <= 32));
+    if (packed) {
+        if (args.force_route >= 0) {
+            info.key = bin_dp16_begin_k; // plain form: one bin in input order
+            return info;
+        }
+        int size_class = (int)(4.0f * __log2f((float)(n * m))) - 40;
+        size_class = size_class < 0 ? 0 : (size_class > bin_dp16_classes_k - 1 ? bin_dp16_classes_k - 1 : size_class);
+        info.key = bin_dp16_begin_k + (bin_dp16_classes_k - 1 - size_class);
+        return info;
+    }
     bool const fits32 = reach < (1ull << 31) - 1;
     int const base = fits32 ? bin_dp32_begin_k : bin_dp64_begin_k;
     if (args.force_route >= 0) {
@@ -189,14 +201,24 @@ __global__ void plan_scatter_kernel(plan_args_t const args, plan_bins_t *__restr
     }
 }
 
-/** Marks every byte value present in a tape's data range, 16 bytes per load where aligned. */
-__global__ void alphabet_mark_kernel(std::uint8_t const *__restrict__ data, std::uint64_t length,
-                                     std::uint32_t *__restrict__ symbol_mask) {
+/** Marks every byte value present in a tape's data range [offsets[0], offsets[count]), read on the device; 16 bytes
+ *  per load where aligned. Grid-stride, so the grid does not depend on the data size. */
+__global__ void alphabet_mark_kernel(tape_t const tape, std::uint32_t *__restrict__ symbol_mask) {
     __shared__ std::uint32_t mask[8];
     if (threadIdx.x < 8) mask[threadIdx.x] = 0;
     __syncthreads();
+    std::uint64_t first, last;
+    if (tape.offset_bits == 32) {
+        auto const *offsets = static_cast<std::uint32_t const *>(tape.offsets);
+        first = offsets[0], last = offsets[tape.count];
+    }
+    else {
+        auto const *offsets = static_cast<std::uint64_t const *>(tape.offsets);
+        first = offsets[0], last = offsets[tape.count];
+    }
+    std::uint8_t const *data = tape.base + first;
+    std::uint64_t const length = last - first;
     std::uint32_t local[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    // Head bytes up to 16-byte alignment, then aligned 16-byte loads, then the tail.
     std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(data);
     std::uint64_t head = (16 - (address & 15)) & 15;
     if (head > length) head = length;
@@ -231,8 +253,9 @@ __global__ void alphabet_mark_kernel(std::uint8_t const *__restrict__ data, std:
     if (threadIdx.x < 8 && mask[threadIdx.x]) atomicOr(&symbol_mask[threadIdx.x], mask[threadIdx.x]);
 }
 
-/** Dense codes for the marked bytes; `bits` = planes the Myers kernel needs (1..8). */
-__global__ void alphabet_codes_kernel(std::uint32_t const *__restrict__ symbol_mask,
+/** Dense codes for the marked bytes; `bits` = planes the Myers kernel needs (1..8). Clears the mask afterwards so
+ *  the next call starts from zero. */
+__global__ void alphabet_codes_kernel(std::uint32_t *__restrict__ symbol_mask,
                                       batch_alphabet_t *__restrict__ alphabet) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     std::uint32_t next = 0;
@@ -245,6 +268,7 @@ __global__ void alphabet_codes_kernel(std::uint32_t const *__restrict__ symbol_m
     while ((1u << bits) < next) ++bits;
     alphabet->symbols = next;
     alphabet->bits = bits;
+    for (int k = 0; k < 8; ++k) symbol_mask[k] = 0;
 }
 
 /** Dense per-pair results into the caller's matrix (device-resident output). */
@@ -281,15 +305,13 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_alphabet(std::uint8_t const *data, std::uint64_t length, std::uint32_t *symbol_mask, int sm_count,
-                            cudaStream_t stream) {
-    if (length == 0) return cudaSuccess;
-    alphabet_mark_kernel<<<grid_for(length / 16 + 1, 256, sm_count, 4), 256, 0, stream>>>(data, length, symbol_mask);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_alphabet_codes(std::uint32_t const *symbol_mask, batch_alphabet_t *alphabet, cudaStream_t stream) {
-    alphabet_codes_kernel<<<1, 32, 0, stream>>>(symbol_mask, alphabet);
+cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
+                            batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream) {
+    std::uint32_t *mask = alphabet->mask_scratch;
+    int const grid = sm_count * 2;
+    alphabet_mark_kernel<<<grid, 256, 0, stream>>>(queries, mask);
+    if (has_candidates) alphabet_mark_kernel<<<grid, 256, 0, stream>>>(candidates, mask);
+    alphabet_codes_kernel<<<1, 32, 0, stream>>>(mask, alphabet);
     return cudaGetLastError();
 }
 

@@ -12,6 +12,7 @@
  *    [0, 272)    Myers: key = words * 16 + text-length class (words 1..16)
  *    [272, 304)  32-bit wavefront DP: key = 272 + (31 - size class), size class ~ log2(n * m)
  *    [304, 336)  64-bit wavefront DP: same layout
+ *    [336, 400)  16x2 packed wavefront DP: key = 336 + (63 - size class), size class ~ 4 * log2(n * m)
  */
 #pragma once
 #include "engine_types.cuh"
@@ -22,7 +23,9 @@ constexpr int bin_keys_k = 512;
 constexpr int bin_myers_begin_k = 0;
 constexpr int bin_dp32_begin_k = 272;
 constexpr int bin_dp64_begin_k = 304;
+constexpr int bin_dp16_begin_k = 336;
 constexpr int bin_dp_classes_k = 32;
+constexpr int bin_dp16_classes_k = 64;
 constexpr int myers_max_words_k = 16;
 
 /** Which pairs a call scores. */
@@ -51,7 +54,9 @@ struct plan_args_t {
     int unit_levenshtein;   // 0/1/1/1 Levenshtein: bit-parallel route
     int magnitude;          // max |cost| over substitution and gap costs, at least 1
     int steps_beyond_span;  // 1 linear, 3 affine (serial.hpp:126-140)
-    int force_route;        // -1: normal planning; otherwise every non-trivial pair takes this DP route
+    int force_route;        // -1: normal planning; otherwise one bin per route, input order (the plain form)
+    int packed_allowed;     // 1 if the 16x2 route may be used (class-table engines, or <= 32 distinct bytes)
+    batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)
 };
 
 /** Per-bin counters the planner fills. */
@@ -62,7 +67,6 @@ struct plan_bins_t {
     std::uint32_t cursor[bin_keys_k];
     std::uint32_t max_cols;
     std::uint32_t error_flags;
-    std::uint32_t symbol_mask[8]; // bytes seen in Myers pairs
     std::uint64_t cells;
     std::uint64_t scheduled;
 };

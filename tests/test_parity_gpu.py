@@ -219,3 +219,37 @@ def test_needleman_wunsch_is_negative_levenshtein(szs, port):
     lev = szs.LevenshteinDistances()
     np.testing.assert_array_equal(nw.pairwise(szs.Strs(first), szs.Strs(second)),
                                   -lev.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64))
+
+
+@pytest.mark.parametrize("symbols", [4, 32, 33, 256])
+def test_levenshtein_dp_over_alphabets(szs, port, symbols):
+    """Non-unit Levenshtein takes the 16x2 route over the batch alphabet when it has at most 32 symbols, the 32-bit
+    byte-comparing route otherwise."""
+    rng = np.random.default_rng(symbols)
+    alphabet = np.arange(256, dtype=np.uint8)[:symbols] if symbols < 256 else np.arange(256, dtype=np.uint8)
+    first = random_strings(rng, 101, 0, 700, alphabet)
+    second = random_strings(rng, 101, 0, 700, alphabet)
+    for costs in ((0, 2, 3, 1), (1, 3, 2, 2)):
+        engine = szs.LevenshteinDistances(*costs)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("family,costs", [("nw", (-11, -1)), ("sw", (-5, -2)), ("nw", (-4, -4)), ("sw", (-3, -3))])
+def test_packed_couples_with_uneven_partners(szs, port, family, costs):
+    """Two pairs share a warp on the 16x2 route: odd counts, and partners of very different shapes."""
+    rng = np.random.default_rng(77)
+    b2c, table = protein_tables(rng)
+    first, second = [], []
+    for _ in range(37):  # odd
+        n = int(rng.integers(1, 900))
+        m = int(rng.integers(1, 900))
+        first.append(bytes(rng.choice(PROTEIN, size=n)))
+        second.append(bytes(rng.choice(PROTEIN, size=m)))
+    first += [bytes(rng.choice(PROTEIN, size=1))] * 3 + [bytes(rng.choice(PROTEIN, size=800))]
+    second += [bytes(rng.choice(PROTEIN, size=800))] * 3 + [bytes(rng.choice(PROTEIN, size=2))]
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
