@@ -91,6 +91,29 @@ struct packed_ops_t {
 
 constexpr int chunk_columns_k = 64; // lane 0's boundary values and column codes are staged 64 columns at a time
 
+/** Reads a lane's R profile bytes (R a multiple of 4) with the widest loads their alignment allows. */
+template <int rows_>
+__device__ __forceinline__ void load_profile_words(std::int8_t const *source, std::uint32_t (&out)[rows_ / 4]) {
+    if constexpr (rows_ % 16 == 0) {
+#pragma unroll
+        for (int v = 0; v < rows_ / 16; ++v) {
+            uint4 const x = reinterpret_cast<uint4 const *>(source)[v];
+            out[4 * v + 0] = x.x, out[4 * v + 1] = x.y, out[4 * v + 2] = x.z, out[4 * v + 3] = x.w;
+        }
+    }
+    else if constexpr (rows_ % 8 == 0) {
+#pragma unroll
+        for (int v = 0; v < rows_ / 8; ++v) {
+            uint2 const x = reinterpret_cast<uint2 const *>(source)[v];
+            out[2 * v + 0] = x.x, out[2 * v + 1] = x.y;
+        }
+    }
+    else {
+#pragma unroll
+        for (int v = 0; v < rows_ / 4; ++v) out[v] = reinterpret_cast<std::uint32_t const *>(source)[v];
+    }
+}
+
 /** Per-warp staging area for lane 0: top-boundary H and F̂, and packed column codes, of the next 64 columns. */
 struct column_chunk_t {
     std::uint32_t top_h[chunk_columns_k];
@@ -121,7 +144,8 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
     constexpr int S = policy_::strip_rows_k;
     constexpr bool affine = policy_::affine_k;
     constexpr bool local = policy_::local_k;
-    static_assert(R == 8, "the packed kernel unpacks one 8-byte profile word per pair and step");
+    static_assert(R % 4 == 0, "profile rows are read in 4-byte words");
+    constexpr int words = R / 4;
 
     int const lane = threadIdx.x & 31;
     std::uint32_t const n_a = a.rows_length, m_a = a.cols_length;
@@ -192,8 +216,9 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
         std::uint32_t out_h = 0, out_f = 0;
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
-        uint2 pa_now = *reinterpret_cast<uint2 const *>(profile_a + (code_now & 0xFF) * S + lane * R);
-        uint2 pb_now = *reinterpret_cast<uint2 const *>(profile_b + (code_now >> 8) * S + lane * R);
+        std::uint32_t pa_now[words], pb_now[words];
+        load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
+        load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
 
         for (std::uint32_t t = 0; t < steps; ++t) {
             std::uint32_t const e = t & (chunk_columns_k - 1);
@@ -225,8 +250,9 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
             std::uint32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0u;
             std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
             if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
-            uint2 const pa_next = *reinterpret_cast<uint2 const *>(profile_a + (code_next & 0xFF) * S + lane * R);
-            uint2 const pb_next = *reinterpret_cast<uint2 const *>(profile_b + (code_next >> 8) * S + lane * R);
+            std::uint32_t pa_next[words], pb_next[words];
+            load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane * R, pa_next);
+            load_profile_words<R>(profile_b + (code_next >> 8) * S + lane * R, pb_next);
 
             std::int64_t const j = (std::int64_t)t + 1 - lane;
             if (j >= 1 && j <= (std::int64_t)m_max && lane <= last_lane) {
@@ -234,14 +260,13 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                 diag_up = up_h;
                 std::uint32_t h_up = up_h, f_up = up_f;
                 std::uint32_t subs[R];
-                subs[0] = interleave_signed_bytes<0>(pa_now.x, pb_now.x);
-                subs[1] = interleave_signed_bytes<1>(pa_now.x, pb_now.x);
-                subs[2] = interleave_signed_bytes<2>(pa_now.x, pb_now.x);
-                subs[3] = interleave_signed_bytes<3>(pa_now.x, pb_now.x);
-                subs[4] = interleave_signed_bytes<0>(pa_now.y, pb_now.y);
-                subs[5] = interleave_signed_bytes<1>(pa_now.y, pb_now.y);
-                subs[6] = interleave_signed_bytes<2>(pa_now.y, pb_now.y);
-                subs[7] = interleave_signed_bytes<3>(pa_now.y, pb_now.y);
+#pragma unroll
+                for (int w = 0; w < words; ++w) {
+                    subs[4 * w + 0] = interleave_signed_bytes<0>(pa_now[w], pb_now[w]);
+                    subs[4 * w + 1] = interleave_signed_bytes<1>(pa_now[w], pb_now[w]);
+                    subs[4 * w + 2] = interleave_signed_bytes<2>(pa_now[w], pb_now[w]);
+                    subs[4 * w + 3] = interleave_signed_bytes<3>(pa_now[w], pb_now[w]);
+                }
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     std::uint32_t const substitution = ops::add(diag, subs[r]);
@@ -290,7 +315,9 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                 out_h = h_up, out_f = f_up;
                 if (write_bottom && lane == 31) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
             }
-            code_now = code_next, pa_now = pa_next, pb_now = pb_next;
+            code_now = code_next;
+#pragma unroll
+            for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
         }
         if constexpr (local) {
 #pragma unroll

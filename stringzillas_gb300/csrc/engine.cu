@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -161,6 +162,11 @@ struct device_context_t {
     pinned_buffer_t results_host;
     cudaEvent_t start = nullptr, stop = nullptr;
     cudaEvent_t compute_start = nullptr, compute_stop = nullptr;
+    static constexpr int lanes_k = 4; // auxiliary streams the routes of one call run on concurrently
+    cudaStream_t lanes[lanes_k] = {nullptr};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t joins[lanes_k] = {nullptr};
+    cudaEvent_t trace_events[64] = {nullptr};
 
     status_t prepare(int device_index) noexcept {
         if (ready) return {};
@@ -172,6 +178,12 @@ struct device_context_t {
         SZS_TRY_CUDA(cudaEventCreate(&stop));
         SZS_TRY_CUDA(cudaEventCreate(&compute_start));
         SZS_TRY_CUDA(cudaEventCreate(&compute_stop));
+        for (auto &event : trace_events) SZS_TRY_CUDA(cudaEventCreate(&event));
+        SZS_TRY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        for (int i = 0; i < lanes_k; ++i) {
+            SZS_TRY_CUDA(cudaStreamCreateWithFlags(&lanes[i], cudaStreamNonBlocking));
+            SZS_TRY_CUDA(cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming));
+        }
         status_t status = control.reserve(sizeof(plan_bins_t) + sizeof(batch_alphabet_t) + 256, own_stream);
         if (!status.ok()) return status;
         // The alphabet's mark words must start at zero (each alphabet pass clears them again).
@@ -198,6 +210,13 @@ struct device_context_t {
         readback.release(), results_host.release();
         if (start) cudaEventDestroy(start);
         if (stop) cudaEventDestroy(stop);
+        for (auto &event : trace_events)
+            if (event) cudaEventDestroy(event);
+        for (int i = 0; i < lanes_k; ++i) {
+            if (lanes[i]) cudaStreamSynchronize(lanes[i]), cudaStreamDestroy(lanes[i]);
+            if (joins[i]) cudaEventDestroy(joins[i]);
+        }
+        if (fork) cudaEventDestroy(fork);
         if (compute_start) cudaEventDestroy(compute_start);
         if (compute_stop) cudaEventDestroy(compute_stop);
         if (own_stream) cudaStreamDestroy(own_stream);
@@ -531,86 +550,113 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
         return total;
     };
 
-    // Scoring kernels are bracketed by their own events so the stats isolate them from planning and copies.
-    bool compute_recorded = false;
-    auto mark_compute_start = [&]() -> cudaError_t {
-        if (compute_recorded) return cudaSuccess;
-        compute_recorded = true;
-        return cudaEventRecord(context->compute_start, stream);
-    };
-
     // 16x2 packed wavefront: Levenshtein engines score over the batch alphabet's codes.
-    score_costs_t packed_costs;
-    if (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k)) {
-        packed_costs = costs;
-        if (levenshtein) {
-            int const symbols = (int)alphabet_host.symbols;
-            packed_costs.classes = symbols;
-            for (int b = 0; b < 256; ++b)
-                packed_costs.byte_to_class[b] = packed_costs.byte_to_compact[b] = alphabet_host.code[b];
-            for (int cc = 0; cc < 32; ++cc)
-                for (int rc = 0; rc < 32; ++rc) {
-                    std::int8_t const cost = (std::int8_t)(cc == rc ? costs.match : costs.mismatch);
-                    packed_costs.profile_table[cc * 32 + rc] = packed_costs.profile_table_t[cc * 32 + rc] = cost;
-                }
-        }
+    score_costs_t packed_costs = costs;
+    if (levenshtein && pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k)) {
+        int const symbols = (int)alphabet_host.symbols;
+        packed_costs.classes = symbols;
+        for (int b = 0; b < 256; ++b)
+            packed_costs.byte_to_class[b] = packed_costs.byte_to_compact[b] = alphabet_host.code[b];
+        for (int cc = 0; cc < 32; ++cc)
+            for (int rc = 0; rc < 32; ++rc) {
+                std::int8_t const cost = (std::int8_t)(cc == rc ? costs.match : costs.mismatch);
+                packed_costs.profile_table[cc * 32 + rc] = packed_costs.profile_table_t[cc * 32 + rc] = cost;
+            }
     }
 
-    // Bit-parallel routes.
-    if (engine.unit_levenshtein && pairs_in(bin_myers_begin_k, bin_dp32_begin_k)) {
-        int const planes = myers_planes_for((int)alphabet_host.bits);
-        for (int words = 1; words <= myers_max_words_k; ++words) {
-            std::uint64_t const pairs_here = pairs_in(bin_myers_begin_k + words * 16, bin_myers_begin_k + words * 16 + 16);
-            if (!pairs_here) continue;
-            int const threads = myers_threads_per_cta();
-            std::uint64_t const needed = (pairs_here + threads - 1) / threads;
-            int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
-            bool const exact = engine.schedule != szs_gb300_schedule_plain_k;
-            SZS_TRY_CUDA(mark_compute_start());
-            SZS_TRY_CUDA(launch_myers(words, planes, exact, tasks, bins, alphabet, results, ctas, stream));
-            ++launches;
-        }
-    }
-
+    // The launch list, longest pairs first (64- and 32-bit wavefront, packed with the most rows per lane, then the
+    // bit-parallel kernels by word count), so the routes' tails overlap each other instead of adding up.
+    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k };
+    struct job_t {
+        job_kind_t kind;
+        int variant; // cell bits, rows per lane, or words
+        int key_begin, key_end;
+        std::uint64_t pairs;
+        int ctas;
+        std::size_t scratch_offset, scratch_bytes;
+    };
+    job_t jobs[40];
+    int job_count = 0;
     std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
-    {
-        std::uint64_t const pairs_here = pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k);
-        if (pairs_here) {
-            dp_launch_shape_t const shape = dp16_shape(engine.kind, costs.affine != 0, packed_costs.classes);
-            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
-            std::uint64_t const warps_needed = (pairs_here + 1) / 2;
-            std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
-            int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
-            std::size_t const scratch_bytes = cells_per_warp * 4 * (std::size_t)ctas * shape.warps_per_cta;
-            status = context->scratch.reserve(scratch_bytes, stream);
-            if (!status.ok()) return status;
-            SZS_TRY_CUDA(mark_compute_start());
-            SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, bin_dp16_begin_k,
-                                     bin_dp16_begin_k + bin_dp16_classes_k, tasks, bins, packed_costs, results,
-                                     context->scratch.data, cells_per_warp, ctas, stream));
-            ++launches;
-        }
-    }
-
-    // 32- and 64-bit wavefront routes.
-    for (int cell_bits : {32, 64}) {
+    std::size_t scratch_total = 0;
+    for (int cell_bits : {64, 32}) {
         int const key_begin = cell_bits == 32 ? bin_dp32_begin_k : bin_dp64_begin_k;
-        int const key_end = key_begin + bin_dp_classes_k;
-        std::uint64_t const pairs_here = pairs_in(key_begin, key_end);
+        std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + bin_dp_classes_k);
         if (!pairs_here) continue;
         dp_launch_shape_t const shape = dp_shape(engine.kind, costs.affine != 0, cell_bits, costs.classes);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Wavefront kernel cannot be resident"};
         std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
-        std::size_t const scratch_bytes = cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta;
-        // The scratch buffer may be shared with a packed launch queued earlier on this stream: stream order keeps
-        // the two kernels from overlapping.
-        status = context->scratch.reserve(scratch_bytes, stream);
+        std::size_t const bytes = align_up(cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta, 256);
+        jobs[job_count++] = {job_dp_k, cell_bits, key_begin, key_begin + bin_dp_classes_k, pairs_here, ctas,
+                             scratch_total, bytes};
+        scratch_total += bytes;
+    }
+    for (int choice = dp16_row_choices_k - 1; choice >= 0; --choice) {
+        int const key_begin = bin_dp16_begin_k + choice * dp16_classes_per_rows_k;
+        int const key_end = key_begin + dp16_classes_per_rows_k;
+        std::uint64_t const pairs_here = pairs_in(key_begin, key_end);
+        if (!pairs_here) continue;
+        int const rows = 4 * (choice + 1);
+        dp_launch_shape_t const shape = dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes);
+        if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
+        std::uint64_t const warps_needed = (pairs_here + 1) / 2;
+        std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
+        int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+        std::size_t const bytes = align_up(cells_per_warp * 4 * (std::size_t)ctas * shape.warps_per_cta, 256);
+        jobs[job_count++] = {job_dp16_k, rows, key_begin, key_end, pairs_here, ctas, scratch_total, bytes};
+        scratch_total += bytes;
+    }
+    int myers_planes = 0;
+    if (engine.unit_levenshtein) {
+        myers_planes = myers_planes_for((int)alphabet_host.bits);
+        for (int words = myers_max_words_k; words >= 1; --words) {
+            int const key_begin = bin_myers_begin_k + words * 16;
+            std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + 16);
+            if (!pairs_here) continue;
+            int const threads = myers_threads_per_cta();
+            std::uint64_t const needed = (pairs_here + threads - 1) / threads;
+            int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
+            jobs[job_count++] = {job_myers_k, words, key_begin, key_begin + 16, pairs_here, ctas, 0, 0};
+        }
+    }
+    if (scratch_total) {
+        status = context->scratch.reserve(scratch_total, stream);
         if (!status.ok()) return status;
-        SZS_TRY_CUDA(mark_compute_start());
-        SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, cell_bits, key_begin, key_end, tasks, bins, costs,
-                               results, context->scratch.data, cells_per_warp, ctas, stream));
+    }
+
+    // Fork the launches over the auxiliary streams, join them back into the call's stream.
+    static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
+    int const lanes_used = std::min(job_count, (int)device_context_t::lanes_k);
+    // Scoring kernels are bracketed by their own events so the stats isolate them from planning and copies.
+    bool compute_recorded = false;
+    if (job_count) {
+        SZS_TRY_CUDA(cudaEventRecord(context->compute_start, stream));
+        compute_recorded = true;
+        SZS_TRY_CUDA(cudaEventRecord(context->fork, stream));
+        for (int lane = 0; lane < lanes_used; ++lane) SZS_TRY_CUDA(cudaStreamWaitEvent(context->lanes[lane], context->fork, 0));
+    }
+    for (int i = 0; i < job_count; ++i) {
+        job_t const &job = jobs[i];
+        cudaStream_t const lane_stream = context->lanes[i % lanes_used];
+        bool const traced = tracing && 2 * i + 1 < 64;
+        if (traced) cudaEventRecord(context->trace_events[2 * i], lane_stream);
+        void *scratch = static_cast<unsigned char *>(context->scratch.data) + job.scratch_offset;
+        if (job.kind == job_dp_k)
+            SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
+                                   bins, costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
+        else if (job.kind == job_dp16_k)
+            SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
+                                     bins, packed_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
+        else
+            SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, engine.schedule != szs_gb300_schedule_plain_k, tasks,
+                                      bins, alphabet, results, job.ctas, lane_stream));
+        if (traced) cudaEventRecord(context->trace_events[2 * i + 1], lane_stream);
         ++launches;
+    }
+    for (int lane = 0; lane < lanes_used; ++lane) {
+        SZS_TRY_CUDA(cudaEventRecord(context->joins[lane], context->lanes[lane]));
+        SZS_TRY_CUDA(cudaStreamWaitEvent(stream, context->joins[lane], 0));
     }
 
     if (compute_recorded) SZS_TRY_CUDA(cudaEventRecord(context->compute_stop, stream));
@@ -660,6 +706,16 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     float compute = 0;
     if (compute_recorded) cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
     engine.stats.last_compute_ms = compute;
+    if (tracing) {
+        static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words"};
+        for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
+            float ms = 0, offset = 0;
+            cudaEventElapsedTime(&ms, context->trace_events[2 * i], context->trace_events[2 * i + 1]);
+            cudaEventElapsedTime(&offset, context->compute_start, context->trace_events[2 * i]);
+            std::fprintf(stderr, "[szs_gb300] %-20s %3d  pairs %10llu  start %8.3f ms  took %9.3f ms\n",
+                         names[jobs[i].kind], jobs[i].variant, (unsigned long long)jobs[i].pairs, offset, ms);
+        }
+    }
     engine.stats.last_launches = launches;
     engine.stats.kernel_launches += launches;
     return {};

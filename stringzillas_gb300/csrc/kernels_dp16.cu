@@ -9,19 +9,15 @@ namespace szs_gb300 {
 
 namespace {
 
-constexpr int dp16_rows_per_lane_k = 8;
 constexpr int dp16_threads_k = 128;
 
-template <int kind_, bool affine_>
-using dp16_instance_t = dp16_policy_t<kind_, affine_, dp16_rows_per_lane_k>;
-
-template <int kind_, bool affine_>
-dp_launch_shape_t dp16_shape_of(int classes) {
-    using policy_t = dp16_instance_t<kind_, affine_>;
+template <int kind_, bool affine_, int rows_>
+dp_launch_shape_t dp16_shape_rows(int classes) {
+    using policy_t = dp16_policy_t<kind_, affine_, rows_>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = dp16_threads_k;
     shape.warps_per_cta = dp16_threads_k / 32;
-    shape.rows_per_lane = dp16_rows_per_lane_k;
+    shape.rows_per_lane = rows_;
     shape.shared_bytes = dp16_shared_bytes<policy_t>(shape.warps_per_cta, classes);
     auto kernel = dp16_wavefront_kernel<policy_t>;
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shape.shared_bytes);
@@ -34,10 +30,21 @@ dp_launch_shape_t dp16_shape_of(int classes) {
 }
 
 template <int kind_, bool affine_>
-cudaError_t dp16_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
-                           score_costs_t const &costs, std::int64_t *results, void *scratch,
-                           std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
-    using policy_t = dp16_instance_t<kind_, affine_>;
+dp_launch_shape_t dp16_shape_of(int rows, int classes) {
+    switch (rows) {
+    case 4: return dp16_shape_rows<kind_, affine_, 4>(classes);
+    case 8: return dp16_shape_rows<kind_, affine_, 8>(classes);
+    case 12: return dp16_shape_rows<kind_, affine_, 12>(classes);
+    case 16: return dp16_shape_rows<kind_, affine_, 16>(classes);
+    default: return dp_launch_shape_t {0, 0, 0, 0, 0};
+    }
+}
+
+template <int kind_, bool affine_, int rows_>
+cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                             score_costs_t const &costs, std::int64_t *results, void *scratch,
+                             std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+    using policy_t = dp16_policy_t<kind_, affine_, rows_>;
     int const shared = dp16_shared_bytes<policy_t>(dp16_threads_k / 32, costs.classes);
     auto kernel = dp16_wavefront_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
@@ -45,6 +52,19 @@ cudaError_t dp16_launch_of(int key_begin, int key_end, pair_task_t const *tasks,
     kernel<<<ctas, dp16_threads_k, shared, stream>>>(tasks, bins, key_begin, key_end, costs, results,
                                                      static_cast<std::uint32_t *>(scratch), scratch_cells_per_warp);
     return cudaGetLastError();
+}
+
+template <int kind_, bool affine_>
+cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                           score_costs_t const &costs, std::int64_t *results, void *scratch,
+                           std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+    switch (rows) {
+    case 4: return dp16_launch_rows<kind_, affine_, 4>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
+    case 8: return dp16_launch_rows<kind_, affine_, 8>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
+    case 12: return dp16_launch_rows<kind_, affine_, 12>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
+    case 16: return dp16_launch_rows<kind_, affine_, 16>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 } // namespace
@@ -60,15 +80,15 @@ cudaError_t dp16_launch_of(int key_begin, int key_end, pair_task_t const *tasks,
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t dp16_shape(int kind, bool affine, int classes) {
-    SZS_DP16_DISPATCH(dp16_shape_of, classes)
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes) {
+    SZS_DP16_DISPATCH(dp16_shape_of, rows, classes)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
-cudaError_t launch_dp16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
-                        score_costs_t const &costs, std::int64_t *results, void *scratch,
+cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
+                        plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
-    SZS_DP16_DISPATCH(dp16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
+    SZS_DP16_DISPATCH(dp16_launch_of, rows, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
                       ctas, stream)
     return cudaErrorInvalidValue;
 }

@@ -41,13 +41,14 @@ cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int k
                       plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                       std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
 
-/** Launch shape of the 16x2 packed wavefront kernel; ctas_per_sm = 0 if unsupported. */
-dp_launch_shape_t dp16_shape(int kind, bool affine, int classes);
+/** Launch shape of the 16x2 packed wavefront kernel with `rows` (4, 8, 12, 16) rows per lane; ctas_per_sm = 0 if
+ *  unsupported. */
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes);
 
 /** Runs the 16x2 packed wavefront kernel over bins [key_begin, key_end): two scheduled pairs per warp. `scratch`
  *  holds `ctas * warps_per_cta` rows of `scratch_cells_per_warp` 32-bit words. */
-cudaError_t launch_dp16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
-                        score_costs_t const &costs, std::int64_t *results, void *scratch,
+cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
+                        plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
 
 /** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).

@@ -90,12 +90,22 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
                         (args.kind != kind_levenshtein_k || (args.alphabet && args.alphabet->symbols <= 32));
     if (packed) {
         if (args.force_route >= 0) {
-            info.key = bin_dp16_begin_k; // plain form: one bin in input order
+            info.key = bin_dp16_begin_k + 16; // plain form: one bin (8 rows per lane), input order
             return info;
         }
-        int size_class = (int)(4.0f * __log2f((float)(n * m))) - 40;
-        size_class = size_class < 0 ? 0 : (size_class > bin_dp16_classes_k - 1 ? bin_dp16_classes_k - 1 : size_class);
-        info.key = bin_dp16_begin_k + (bin_dp16_classes_k - 1 - size_class);
+        // Rows per lane: the fewest instructions for strips(R) x (m + 31) steps x (7 R + 40) per step.
+        int best_choice = 0;
+        float best_cost = 3.4e38f;
+        for (int choice = 0; choice < dp16_row_choices_k; ++choice) {
+            std::uint64_t const rows = 4u * (choice + 1);
+            std::uint64_t const strips = (n + 32 * rows - 1) / (32 * rows);
+            float const cost = (float)strips * (float)(m + 31) * (7.0f * rows + 40.0f);
+            if (cost < best_cost) best_cost = cost, best_choice = choice;
+        }
+        int size_class = (int)(2.0f * __log2f((float)(n * m))) - 20;
+        size_class = size_class < 0 ? 0 : (size_class > dp16_classes_per_rows_k - 1 ? dp16_classes_per_rows_k - 1
+                                                                                     : size_class);
+        info.key = bin_dp16_begin_k + best_choice * dp16_classes_per_rows_k + (dp16_classes_per_rows_k - 1 - size_class);
         return info;
     }
     bool const fits32 = reach < (1ull << 31) - 1;

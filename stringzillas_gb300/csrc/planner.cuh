@@ -12,7 +12,8 @@
  *    [0, 272)    Myers: key = words * 16 + text-length class (words 1..16)
  *    [272, 304)  32-bit wavefront DP: key = 272 + (31 - size class), size class ~ log2(n * m)
  *    [304, 336)  64-bit wavefront DP: same layout
- *    [336, 400)  16x2 packed wavefront DP: key = 336 + (63 - size class), size class ~ 4 * log2(n * m)
+ *    [336, 400)  16x2 packed wavefront DP: key = 336 + 16 * rows-per-lane index + (15 - size class),
+ *                size class ~ 2 * log2(n * m); rows per lane R in {4, 8, 12, 16}, chosen per pair
  */
 #pragma once
 #include "engine_types.cuh"
@@ -26,6 +27,8 @@ constexpr int bin_dp64_begin_k = 304;
 constexpr int bin_dp16_begin_k = 336;
 constexpr int bin_dp_classes_k = 32;
 constexpr int bin_dp16_classes_k = 64;
+constexpr int dp16_row_choices_k = 4;       // rows per lane 4, 8, 12, 16
+constexpr int dp16_classes_per_rows_k = 16; // size classes within one rows-per-lane choice
 constexpr int myers_max_words_k = 16;
 
 /** Which pairs a call scores. */
