@@ -30,6 +30,7 @@ UNITS = [
     ("planner", "planner.cu", []),
     ("kernels_dp", "kernels_dp.cu", []),
     ("kernels_dp16", "kernels_dp16.cu", []),
+    ("kernels_band", "kernels_band.cu", []),
     ("probe", "probe.cu", []),
     ("static_scratch", "static_scratch.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),

@@ -1,0 +1,351 @@
+/**
+ *  @file dp_band.cuh
+ *  @brief Long pairs: one CTA per pair, its warps working on consecutive row strips at once.
+ *
+ *  A single warp sweeps a pair strip by strip, so one pair of 30,000 x 30,000 cells keeps one warp busy for
+ *  seconds while the rest of the GPU idles. Here the W warps of a CTA form a ring: warp w scores strips
+ *  w, w + W, w + 2W, ... of the same pair. Strip k's bottom row (H and F̂ per column) goes to ring slot k mod W of the
+ *  CTA's scratch rows; strip k + 1 reads it as its top boundary while strip k is still advancing, so all W strips
+ *  run at the same time, each a few chunks of columns behind the one above. Replaces the reference's tiled device
+ *  tier (include/stringzillas/similarities/cuda.cuh:616-1096), which spins without a bound on per-tile progress
+ *  flags in global memory.
+ *
+ *  Progress: ring slot s holds one 64-bit word in shared memory, `(strip + 1) << 32 | columns written`. Slots are
+ *  reused every W strips, so the word only grows; a consumer of strip k - 1's row waits until the word reaches
+ *  `k << 32 | columns needed`. Only warps of the same CTA wait on each other (co-resident by construction), and every
+ *  wait is bounded: after `band_wait_limit_k` polls the warp raises the CTA's error flag, which also releases the
+ *  other warps' waits, the pair is abandoned and the host reports an error for the call.
+ *
+ *  Inside a strip, lanes, steps, chunk staging and the shortened dependency chain are those of dp_packed.cuh, on
+ *  32-bit cells with DPX `__viaddmax_s32` / `__viaddmin_s32`.
+ */
+#pragma once
+#include "dp_cells.cuh"
+#include "dp_packed.cuh"
+#include "dp_wavefront.cuh"
+#include "engine_types.cuh"
+#include "planner.cuh"
+
+namespace szs_gb300 {
+
+constexpr int band_warps_k = 8;
+constexpr std::uint32_t band_wait_limit_k = 1u << 22; // polls of ~100 ns each, about 0.4 s
+constexpr int band_chunk_k = 32;                      // columns staged and published at a time
+
+template <int kind_, bool affine_, int rows_per_lane_>
+struct band_policy_t {
+    static constexpr int kind_k = kind_;
+    static constexpr bool affine_k = affine_;
+    static constexpr bool maximize_k = kind_ != kind_levenshtein_k;
+    static constexpr bool local_k = kind_ == kind_smith_waterman_k;
+    static constexpr bool uniform_k = kind_ == kind_levenshtein_k;
+    static constexpr int rows_per_lane_k = rows_per_lane_;
+    static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
+    using ops_t = cell_ops_t<std::int32_t, maximize_k>;
+};
+
+/** Per-warp staging of lane 0's inputs for the next `band_chunk_k` columns. */
+struct band_chunk_t {
+    std::int32_t top_h[band_chunk_k];
+    std::int32_t top_f[band_chunk_k];
+    std::uint32_t code[band_chunk_k];
+};
+
+/** Shared state of one CTA. */
+struct band_shared_t {
+    unsigned long long progress[band_warps_k];
+    std::int32_t warp_result[band_warps_k];
+    std::uint32_t pair_index;
+    std::uint32_t failed;
+};
+
+template <typename policy_>
+__host__ __device__ constexpr int band_profile_bytes_per_warp(int classes) {
+    return policy_::uniform_k ? 0 : classes * policy_::strip_rows_k;
+}
+
+template <typename policy_>
+__host__ __device__ constexpr int band_shared_bytes(int classes) {
+    return int((sizeof(score_costs_t) + 15) / 16 * 16) + int((sizeof(band_shared_t) + 15) / 16 * 16) +
+           band_warps_k * (band_profile_bytes_per_warp<policy_>(classes) + int(sizeof(band_chunk_t)));
+}
+
+/** Lane 0 of a warp waits (bounded) until ring slot `slot` has reached `target`; the warp then proceeds together. */
+__device__ __forceinline__ bool band_wait(band_shared_t &shared, int slot, unsigned long long target) {
+    int const lane = threadIdx.x & 31;
+    int ok = 1;
+    if (lane == 0) {
+        std::uint32_t polls = 0;
+        while (true) {
+            unsigned long long const seen = *reinterpret_cast<volatile unsigned long long *>(&shared.progress[slot]);
+            if (seen >= target) break;
+            if (*reinterpret_cast<volatile std::uint32_t *>(&shared.failed)) {
+                ok = 0;
+                break;
+            }
+            if (++polls > band_wait_limit_k) {
+                atomicExch(&shared.failed, 1u);
+                ok = 0;
+                break;
+            }
+            __nanosleep(100);
+        }
+        __threadfence_block();
+    }
+    ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+    return ok != 0;
+}
+
+__device__ __forceinline__ void band_publish(band_shared_t &shared, int slot, unsigned long long value) {
+    __threadfence_block();
+    *reinterpret_cast<volatile unsigned long long *>(&shared.progress[slot]) = value;
+}
+
+/**
+ *  Scores strips w, w + W, ... of one pair with warp w. Returns this warp's contribution: the running maximum of its
+ *  valid cells for local scores, the corner cell for the warp owning the last row of global scores (else 0).
+ */
+template <typename policy_>
+__device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task, score_costs_t const &costs,
+                                                        band_shared_t &shared, std::int32_t *ring,
+                                                        std::size_t ring_cells_per_slot, std::int8_t *profile,
+                                                        band_chunk_t &chunk, int warp) {
+    using ops = typename policy_::ops_t;
+    constexpr int R = policy_::rows_per_lane_k;
+    constexpr int S = policy_::strip_rows_k;
+    constexpr bool affine = policy_::affine_k;
+    constexpr bool local = policy_::local_k;
+    constexpr int W = band_warps_k;
+    static_assert(R % 4 == 0, "profile rows are read in 4-byte words");
+    constexpr int words = R / 4;
+
+    int const lane = threadIdx.x & 31;
+    std::uint32_t const n = task.rows_length, m = task.cols_length;
+    std::int32_t const open = costs.open, extend = costs.extend, extend_open = costs.open + costs.extend;
+    boundary_t<std::int32_t> const edge {open, extend, affine, local};
+    int const classes = costs.classes;
+    std::int8_t const *table = task.transposed ? costs.profile_table_t : costs.profile_table;
+    auto gap_seed = [&](std::int64_t i) -> std::int32_t { return local ? extend : extend + edge.score(i); };
+    auto column_code = [&](std::uint32_t j) -> std::uint32_t {
+        std::uint32_t const byte = task.cols[j - 1];
+        if constexpr (policy_::uniform_k) return byte;
+        else return costs.byte_to_compact[byte];
+    };
+
+    std::uint32_t const strips = (n + S - 1) / S;
+    std::int32_t result = 0;
+    std::int32_t lane_best = 0;
+
+    for (std::uint32_t k = (std::uint32_t)warp; k < strips; k += W) {
+        std::uint32_t const strip_base = k * S;
+        std::uint32_t const rows_here = min((std::uint32_t)S, n - strip_base);
+        bool const last_strip = k + 1 == strips;
+        int const last_lane = int((rows_here - 1) / R);
+        std::int64_t const row0 = (std::int64_t)strip_base + lane * R + 1;
+        int const slot_in = int((k + W - 1) % W), slot_out = int(k % W);
+        std::int32_t const *top = ring + (std::size_t)slot_in * ring_cells_per_slot;
+        std::int32_t *bottom = ring + (std::size_t)slot_out * ring_cells_per_slot;
+
+        // Row characters / profile for this strip.
+        std::uint32_t row_bytes[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            std::int64_t const i = row0 + r;
+            row_bytes[r] = i <= (std::int64_t)n ? task.rows[i - 1] : 0u;
+        }
+        __syncwarp();
+        if constexpr (!policy_::uniform_k) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                int const row_class = costs.byte_to_class[row_bytes[r]];
+                for (int cc = 0; cc < classes; ++cc) profile[cc * S + lane * R + r] = table[cc * 32 + row_class];
+            }
+        }
+        std::int32_t h_col[R], e_col[R], best_row[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            h_col[r] = edge.score(row0 + r);
+            e_col[r] = affine ? gap_seed(row0 + r) : 0;
+            best_row[r] = 0;
+        }
+        std::int32_t diag_up = edge.score(row0 - 1);
+        int const result_lane = int((n - 1 - strip_base) / R), result_row = int((n - 1 - strip_base) % R);
+
+        std::uint32_t const steps = m + (std::uint32_t)last_lane;
+        bool const write_bottom = !last_strip;
+        std::int32_t out_h = 0, out_f = 0;
+        std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
+        __syncwarp();
+        std::uint32_t p_now[words];
+        if constexpr (!policy_::uniform_k)
+            load_profile_words<R>(profile + (int)code_now * S + lane * R, p_now);
+        bool healthy = true;
+
+        for (std::uint32_t t = 0; t < steps && healthy; ++t) {
+            std::uint32_t const e = t & (band_chunk_k - 1);
+            if (e == 0) {
+                // Stage lane 0's next columns; strips below the first wait for the strip above to write them.
+                std::uint32_t const need = min(m, t + band_chunk_k);
+                if (k > 0 && t + 1 <= m) healthy = band_wait(shared, slot_in, ((unsigned long long)k << 32) | need);
+                __syncwarp();
+                for (int c = lane; c < band_chunk_k; c += 32) {
+                    std::uint32_t const j = t + 1 + c;
+                    std::int32_t h = 0, f = 0;
+                    if (j <= m) {
+                        if (k == 0) h = edge.score(j), f = gap_seed(j);
+                        else h = __ldcg(top + 2 * j), f = __ldcg(top + 2 * j + 1);
+                    }
+                    chunk.top_h[c] = h;
+                    chunk.top_f[c] = f;
+                    chunk.code[c] = j + 1 <= m ? column_code(j + 1) : 0u;
+                }
+                __syncwarp();
+                // The writer of the bottom row publishes its finished columns (it wrote column j at step j + 30).
+                if (write_bottom && lane == 31 && t > 31) {
+                    std::uint32_t const done = min(m, t - 31);
+                    band_publish(shared, slot_out, ((unsigned long long)(k + 1) << 32) | done);
+                }
+            }
+            std::int32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
+            std::int32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0;
+            std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
+            if (lane == 0) up_h = chunk.top_h[e], up_f = chunk.top_f[e], code_next = chunk.code[e];
+            std::uint32_t p_next[words];
+            if constexpr (!policy_::uniform_k)
+                load_profile_words<R>(profile + (int)code_next * S + lane * R, p_next);
+
+            std::int64_t const j = (std::int64_t)t + 1 - lane;
+            if (j >= 1 && j <= (std::int64_t)m && lane <= last_lane) {
+                std::int32_t diag = diag_up;
+                diag_up = up_h;
+                std::int32_t h_up = up_h, f_up = up_f;
+                std::int32_t subs[R];
+                if constexpr (policy_::uniform_k) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) subs[r] = row_bytes[r] == code_now ? costs.match : costs.mismatch;
+                }
+                else {
+#pragma unroll
+                    for (int w = 0; w < words; ++w)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) subs[4 * w + b] = (std::int32_t)(std::int8_t)(p_now[w] >> (8 * b));
+                }
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    std::int32_t const substitution = diag + subs[r];
+                    std::int32_t h;
+                    if constexpr (affine) {
+                        std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
+                        std::int32_t const x = ops::add_opt(e_new, open, substitution);
+                        std::int32_t const via_f = ops::add_opt(f_up, extend_open, x);
+                        if constexpr (local) h = ops::add_opt_relu(h_up, open, via_f);
+                        else h = ops::add_opt(h_up, open, via_f);
+                        f_up = ops::add_opt(f_up, extend, h_up);
+                        e_col[r] = e_new;
+                    }
+                    else {
+                        std::int32_t const x = ops::add_opt(h_col[r], open, substitution);
+                        if constexpr (local) h = ops::add_opt_relu(h_up, open, x);
+                        else h = ops::add_opt(h_up, open, x);
+                    }
+                    diag = h_col[r];
+                    h_col[r] = h;
+                    h_up = h;
+                    if constexpr (local) best_row[r] = max(best_row[r], h);
+                }
+                out_h = h_up, out_f = f_up;
+                if (write_bottom && lane == 31) {
+                    __stcg(bottom + 2 * j, out_h);
+                    __stcg(bottom + 2 * j + 1, out_f);
+                }
+                if constexpr (!local)
+                    if (last_strip && lane == result_lane && j == (std::int64_t)m) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == result_row) result = h_col[r];
+                    }
+            }
+            code_now = code_next;
+            if constexpr (!policy_::uniform_k) {
+#pragma unroll
+                for (int w = 0; w < words; ++w) p_now[w] = p_next[w];
+            }
+        }
+        __syncwarp();
+        if (write_bottom && lane == 31) band_publish(shared, slot_out, ((unsigned long long)(k + 1) << 32) | m);
+        if constexpr (local) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (row0 + r <= (std::int64_t)n) lane_best = max(lane_best, best_row[r]);
+        }
+        if (!healthy) break;
+    }
+    if constexpr (local) {
+#pragma unroll
+        for (int offset = 16; offset > 0; offset >>= 1)
+            lane_best = max(lane_best, __shfl_xor_sync(0xFFFFFFFFu, lane_best, offset));
+        return lane_best;
+    }
+    else {
+        // Only the lane holding row n of the last strip captured the corner; it is the warp's only non-zero value
+        // for global scores when this warp owns the last strip.
+        std::uint32_t const last_strip_index = strips - 1;
+        int const owner_lane = int((n - 1 - last_strip_index * S) / R);
+        return __shfl_sync(0xFFFFFFFFu, result, owner_lane);
+    }
+}
+
+/** Persistent band kernel: one pair per CTA at a time, pulled from a cursor over bins [key_begin, key_end). */
+template <typename policy_>
+__global__ void __launch_bounds__(band_warps_k * 32)
+    band_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t *__restrict__ bins, int key_begin, int key_end,
+                score_costs_t const costs, std::int64_t *__restrict__ results, std::int32_t *__restrict__ scratch,
+                std::size_t ring_cells_per_slot) {
+    extern __shared__ __align__(16) unsigned char shared_bytes[];
+    score_costs_t &costs_s = *reinterpret_cast<score_costs_t *>(shared_bytes);
+    std::size_t const costs_bytes = (sizeof(score_costs_t) + 15) / 16 * 16;
+    band_shared_t &shared = *reinterpret_cast<band_shared_t *>(shared_bytes + costs_bytes);
+    std::size_t const shared_state_bytes = (sizeof(band_shared_t) + 15) / 16 * 16;
+    std::size_t const profile_bytes = (std::size_t)band_profile_bytes_per_warp<policy_>(costs.classes);
+    std::int8_t *profiles = reinterpret_cast<std::int8_t *>(shared_bytes + costs_bytes + shared_state_bytes);
+    auto *chunks = reinterpret_cast<band_chunk_t *>(profiles + band_warps_k * profile_bytes);
+    {
+        auto const *src = reinterpret_cast<std::uint32_t const *>(&costs);
+        auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
+        for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    std::int32_t *ring = scratch + (std::size_t)blockIdx.x * band_warps_k * ring_cells_per_slot;
+    std::uint32_t const begin = bins->begin[key_begin];
+    std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
+    while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) shared.pair_index = atomicAdd(&bins->cursor[key_begin], 1u);
+        if (threadIdx.x < band_warps_k) shared.progress[threadIdx.x] = 0ull;
+        if (threadIdx.x == 0) shared.failed = 0u;
+        __syncthreads();
+        std::uint32_t const index = shared.pair_index;
+        if (index >= count) break;
+        pair_task_t const task = tasks[begin + index];
+        std::int32_t const value = band_score_warp<policy_>(task, costs_s, shared, ring, ring_cells_per_slot,
+                                                            profiles + warp * profile_bytes, chunks[warp], warp);
+        if (lane == 0) shared.warp_result[warp] = value;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            std::int64_t score;
+            if (policy_::local_k) {
+                std::int32_t best = 0;
+                for (int w = 0; w < band_warps_k; ++w) best = max(best, shared.warp_result[w]);
+                score = best;
+            }
+            else {
+                std::uint32_t const strips = (task.rows_length + policy_::strip_rows_k - 1) / policy_::strip_rows_k;
+                score = shared.warp_result[(strips - 1) % band_warps_k];
+            }
+            if (shared.failed) atomicOr(&bins->error_flags, 1u);
+            results[task.slot] = score;
+        }
+    }
+}
+
+} // namespace szs_gb300

@@ -566,7 +566,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
 
     // The launch list, longest pairs first (64- and 32-bit wavefront, packed with the most rows per lane, then the
     // bit-parallel kernels by word count), so the routes' tails overlap each other instead of adding up.
-    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k };
+    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k };
     struct job_t {
         job_kind_t kind;
         int variant; // cell bits, rows per lane, or words
@@ -579,6 +579,19 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     int job_count = 0;
     std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
     std::size_t scratch_total = 0;
+    {
+        std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
+        if (pairs_here) {
+            dp_launch_shape_t const shape = band_shape(engine.kind, costs.affine != 0, costs.classes);
+            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
+            int const ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+            std::size_t const bytes =
+                align_up(cells_per_warp * 4 * (std::size_t)ctas * (std::size_t)band_warps_per_cta(), 256);
+            jobs[job_count++] = {job_band_k, 32, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here,
+                                 ctas, scratch_total, bytes};
+            scratch_total += bytes;
+        }
+    }
     for (int cell_bits : {64, 32}) {
         int const key_begin = cell_bits == 32 ? bin_dp32_begin_k : bin_dp64_begin_k;
         std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + bin_dp_classes_k);
@@ -642,7 +655,10 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
         bool const traced = tracing && 2 * i + 1 < 64;
         if (traced) cudaEventRecord(context->trace_events[2 * i], lane_stream);
         void *scratch = static_cast<unsigned char *>(context->scratch.data) + job.scratch_offset;
-        if (job.kind == job_dp_k)
+        if (job.kind == job_band_k)
+            SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins, costs,
+                                     results, scratch, cells_per_warp, job.ctas, lane_stream));
+        else if (job.kind == job_dp_k)
             SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                    bins, costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
         else if (job.kind == job_dp16_k)
@@ -660,6 +676,10 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     }
 
     if (compute_recorded) SZS_TRY_CUDA(cudaEventRecord(context->compute_stop, stream));
+
+    // The band kernel's bounded waits report through the plan's error word; read it back with the results.
+    SZS_TRY_CUDA(cudaMemcpyAsync(&context->bins_host()->error_flags, &bins->error_flags, sizeof(std::uint32_t),
+                                 cudaMemcpyDeviceToHost, stream));
 
     // Results into the caller's matrix.
     bool const out_on_device = device_accessible(call.out);
@@ -700,6 +720,9 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
         }
     }
     SZS_TRY_CUDA(cudaGetLastError());
+    if (context->bins_host()->error_flags)
+        return {sz_status_unknown_k, "A long pair's band of warps stopped waiting for its neighbour (bounded wait "
+                                     "expired); its score was not computed"};
     float elapsed = 0;
     cudaEventElapsedTime(&elapsed, context->start, context->stop);
     engine.stats.last_call_ms = elapsed;
@@ -707,7 +730,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     if (compute_recorded) cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
     engine.stats.last_compute_ms = compute;
     if (tracing) {
-        static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words"};
+        static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits"};
         for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
             float ms = 0, offset = 0;
             cudaEventElapsedTime(&ms, context->trace_events[2 * i], context->trace_events[2 * i + 1]);

@@ -51,6 +51,17 @@ cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
 
+/** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells). */
+dp_launch_shape_t band_shape(int kind, bool affine, int classes);
+/** Warps per band CTA (ring slots per CTA). */
+int band_warps_per_cta();
+
+/** Runs the band kernel over bins [key_begin, key_end). `scratch` holds `ctas * band_warps_per_cta()` ring slots of
+ *  `ring_cells_per_slot` 32-bit cells. Bounded waits that give up set bit 0 of `bins->error_flags`. */
+cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                        score_costs_t const &costs, std::int64_t *results, void *scratch,
+                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream);
+
 /** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
  *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be
  *  shorter (the plain schedule puts every bit-parallel pair in the 16-word bin). */

@@ -14,6 +14,7 @@
  *    [304, 336)  64-bit wavefront DP: same layout
  *    [336, 400)  16x2 packed wavefront DP: key = 336 + 16 * rows-per-lane index + (15 - size class),
  *                size class ~ 2 * log2(n * m); rows per lane R in {4, 8, 12, 16}, chosen per pair
+ *    [400, 432)  band (one CTA per pair, 32-bit cells): key = 400 + (31 - size class), size class ~ log2(n * m)
  */
 #pragma once
 #include "engine_types.cuh"
@@ -29,6 +30,8 @@ constexpr int bin_dp_classes_k = 32;
 constexpr int bin_dp16_classes_k = 64;
 constexpr int dp16_row_choices_k = 4;       // rows per lane 4, 8, 12, 16
 constexpr int dp16_classes_per_rows_k = 16; // size classes within one rows-per-lane choice
+constexpr int bin_band_begin_k = 400;
+constexpr int band_min_rows_k = 1024; // pairs whose shorter side exceeds this are scored by a whole CTA
 constexpr int myers_max_words_k = 16;
 
 /** Which pairs a call scores. */

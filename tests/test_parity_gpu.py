@@ -253,3 +253,20 @@ def test_packed_couples_with_uneven_partners(szs, port, family, costs):
         engine.set_schedule(schedule)
         got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
         np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 1, 1, 1)), ("lev", (0, 3, 2, 2)),
+                                          ("sw", (-4, -4)), ("nw", (-3, -3))])
+def test_band_route_long_pairs(szs, port, family, costs):
+    """Shorter sides above 1,024 go to the band kernel (one CTA of warps per pair, strips in a ring)."""
+    rng = np.random.default_rng(123)
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
+    lengths = [(1025, 1025), (1100, 9000), (2600, 3100), (4100, 2050), (1500, 1500), (5000, 5003)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    # A related pair, so local scores are large.
+    second[2] = first[2][100:2900] + bytes(rng.choice(alphabet, size=300))
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
