@@ -9,21 +9,26 @@
  *  never interact (16x2 instructions have no carries between halves), so such filler cannot change a result even
  *  when it wraps.
  *
- *  Gap tracks are kept shifted by the gap-open cost, `Ê = E - open` and `F̂ = F - open`, which turns the affine
- *  recurrence into fused DPX operations without separate additions:
+ *  Affine tracks keep `Ĥ = H + open` instead of H (both gap tracks extend from H + open) and take the substitution
+ *  profile as `s - open`, so that every cell is five fused DPX operations:
  *
- *      Ê = max(Ê_left + extend, H_left)        (was max(E_left + extend, H_left + open))
- *      F̂ = max(F̂_up + extend, H_up)
- *      H = max(max(Ê, F̂) + open, diag + s)      (local: also max(., 0))
+ *      E = max(E_left + extend, Ĥ_left)
+ *      X = max(Ĥ_diag + (s - open), E)            (= max(H_diag + s, E))
+ *      F = max(F_up + extend, Ĥ_up)
+ *      H = max(X, F)                              (local: also max(., 0))
+ *      Ĥ = H + open
  *
- *  (min for Levenshtein). Substitution costs come from two per-warp int8 profiles, one per pair, and one byte-permute
- *  with sign replication builds the packed cost of both pairs for a row.
+ *  (min for Levenshtein). The planner routes an affine pair here only when every `s - open` of its table fits a
+ *  byte. Substitution costs come from two per-warp int8 profiles, one per pair, and one byte-permute with sign
+ *  replication builds the packed cost of both pairs for a row.
  *
  *  The layout of a pair inside the warp is the one of dp_wavefront.cuh: strips of 32 x R rows, lane L owns rows
  *  L*R..L*R+R-1, column j = t + 1 - L at step t, bottom values passed down with `__shfl_up_sync`, lane 0 fed by the
  *  closed-form row 0 or by the previous strip's bottom row in the warp's scratch row.
  */
 #pragma once
+#include <type_traits>
+
 #include "dp_cells.cuh"
 #include "dp_wavefront.cuh"
 #include "engine_types.cuh"
@@ -87,6 +92,9 @@ struct packed_ops_t {
     __device__ __forceinline__ static std::uint32_t add_opt_relu(std::uint32_t a, std::uint32_t b, std::uint32_t c) {
         return __viaddmax_s16x2_relu(a, b, c);
     }
+    __device__ __forceinline__ static std::uint32_t opt2_relu(std::uint32_t a, std::uint32_t b) {
+        return __vimax_s16x2_relu(a, b);
+    }
 };
 
 constexpr int chunk_columns_k = 64; // lane 0's boundary values and column codes are staged 64 columns at a time
@@ -114,7 +122,8 @@ __device__ __forceinline__ void load_profile_words(std::int8_t const *source, st
     }
 }
 
-/** Per-warp staging area for lane 0: top-boundary H and F̂, and packed column codes, of the next 64 columns. */
+/** Per-warp staging area for lane 0: top-boundary H (Ĥ for affine tracks) and F, and packed column codes, of the
+ *  next 64 columns. */
 struct column_chunk_t {
     std::uint32_t top_h[chunk_columns_k];
     std::uint32_t top_f[chunk_columns_k];
@@ -125,8 +134,8 @@ struct column_chunk_t {
  *  Scores tasks @p a and @p b (b may be absent: `b_present == false`) with one warp. All lanes call it together.
  *
  *  Per step t, lane L updates column j = t + 1 - L for both pairs. The dependency chain a step waits on is the
- *  shuffle of the upper lane's bottom values plus two DPX operations per row: with X = max(Ê + open, diag + s)
- *  computed off the chain, H = max(X, F̂_up + (extend + open), H_up + open). Column codes travel one step ahead of
+ *  shuffle of the upper lane's bottom values plus, per row, F, H and Ĥ (affine) or H alone (linear, with
+ *  X = max(H_left + gap, diag + s) computed off the chain). Column codes travel one step ahead of
  *  the values (a lane forwards its current code, which is the code of the next lane's next column), so every
  *  profile load is issued a step before it is used.
  *
@@ -162,8 +171,14 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
     std::int8_t *profile_b = profile + classes * S;
     std::uint8_t const *cols_b = b_present ? b.cols : a.cols;
 
-    // Gap-track seeds, shifted by `open`: global `extend + M[i][0]`, local `extend`.
-    auto gap_seed = [&](std::int64_t i) -> std::int32_t { return local ? extend : extend + edge.score(i); };
+    // Affine tracks: Ĥ = H + open (the one value both gap tracks extend from), E and F as they are; the profile holds
+    // s - open so that Ĥ_diag + (s - open) = H_diag + s. The host routes a pair here only when s - open fits a byte.
+    // Linear tracks: H as it is.
+    std::int32_t const h_shift = affine ? open : 0;
+    // Gap-track seeds: global `open + extend + M[i][0]`, local `open + extend` (unused by linear tracks).
+    auto gap_seed = [&](std::int64_t i) -> std::int32_t {
+        return local ? open + extend : open + extend + edge.score(i);
+    };
     auto column_code = [&](std::uint32_t j) -> std::uint32_t { // packed codes of column j (1-based) of both pairs
         std::uint32_t const ca = j <= m_a ? costs.byte_to_compact[a.cols[j - 1]] : 0u;
         std::uint32_t const cb = j <= m_b ? costs.byte_to_compact[cols_b[j - 1]] : 0u;
@@ -187,21 +202,21 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
             int const class_a = costs.byte_to_class[i <= (std::int64_t)n_a ? a.rows[i - 1] : 0u];
             int const class_b = costs.byte_to_class[i <= (std::int64_t)n_b ? b.rows[i - 1] : 0u];
             for (int cc = 0; cc < classes; ++cc) {
-                profile_a[cc * S + lane * R + r] = table_a[cc * 32 + class_a];
-                profile_b[cc * S + lane * R + r] = table_b[cc * 32 + class_b];
+                profile_a[cc * S + lane * R + r] = std::int8_t(table_a[cc * 32 + class_a] - h_shift);
+                profile_b[cc * S + lane * R + r] = std::int8_t(table_b[cc * 32 + class_b] - h_shift);
             }
         }
 
         std::uint32_t h_col[R], e_col[R], best_row[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            std::int32_t const h = edge.score(row0 + r);
+            std::int32_t const h = edge.score(row0 + r) + h_shift;
             h_col[r] = pack16(h, h);
             std::int32_t const e = gap_seed(row0 + r);
             e_col[r] = pack16(e, e);
             best_row[r] = 0;
         }
-        std::int32_t const diag_seed = edge.score(row0 - 1);
+        std::int32_t const diag_seed = edge.score(row0 - 1) + h_shift;
         std::uint32_t diag_up = pack16(diag_seed, diag_seed);
 
         // Lanes holding each pair's last row in this strip, and the row inside the lane.
@@ -213,14 +228,19 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
 
         std::uint32_t const steps = m_max + (std::uint32_t)last_lane;
         bool const write_bottom = !last_strip;
+        bool const bottom_writer = write_bottom && lane == 31;
         std::uint32_t out_h = 0, out_f = 0;
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
         std::uint32_t pa_now[words], pb_now[words];
         load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
         load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
+        int const lane_rows = lane * R;
 
-        for (std::uint32_t t = 0; t < steps; ++t) {
+        // One step of the sweep. `steady` steps are those where every lane is on a real column below both pairs'
+        // ends (31 <= t < m_min - 1): no range predicates, no masks, no result capture.
+        auto step = [&](std::uint32_t t, auto steady_tag) {
+            constexpr bool steady = decltype(steady_tag)::value;
             std::uint32_t const e = t & (chunk_columns_k - 1);
             if (e == 0) {
                 // Stage lane 0's next 64 top-boundary values (columns t+1..) and codes (columns t+2..).
@@ -231,7 +251,7 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                     std::uint32_t h = 0, f = 0;
                     if (j <= m_max) {
                         if (strip_base == 0) {
-                            std::int32_t const v = edge.score(j), g = gap_seed(j);
+                            std::int32_t const v = edge.score(j) + h_shift, g = gap_seed(j);
                             h = pack16(v, v), f = pack16(g, g);
                         }
                         else {
@@ -251,15 +271,16 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
             std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
             if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
             std::uint32_t pa_next[words], pb_next[words];
-            load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane * R, pa_next);
-            load_profile_words<R>(profile_b + (code_next >> 8) * S + lane * R, pb_next);
+            load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane_rows, pa_next);
+            load_profile_words<R>(profile_b + (code_next >> 8) * S + lane_rows, pb_next);
 
-            std::int64_t const j = (std::int64_t)t + 1 - lane;
-            if (j >= 1 && j <= (std::int64_t)m_max && lane <= last_lane) {
+            int const j = (int)t + 1 - lane;
+            bool const active = steady || (j >= 1 && j <= (int)m_max && lane <= last_lane);
+            if (active) {
                 std::uint32_t diag = diag_up;
                 diag_up = up_h;
                 std::uint32_t h_up = up_h, f_up = up_f;
-                std::uint32_t subs[R];
+                std::uint32_t subs[R], cell_h[R];
 #pragma unroll
                 for (int w = 0; w < words; ++w) {
                     subs[4 * w + 0] = interleave_signed_bytes<0>(pa_now[w], pb_now[w]);
@@ -269,56 +290,69 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                 }
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    std::uint32_t const substitution = ops::add(diag, subs[r]);
-                    std::uint32_t h;
+                    std::uint32_t h, kept;
                     if constexpr (affine) {
-                        // Off the chain: the horizontal track and X = max(E, diag + s) with E = Ê + open.
-                        std::uint32_t const e_new = ops::add_opt(e_col[r], extend2, h_col[r]);
-                        std::uint32_t const x = ops::add_opt(e_new, open2, substitution);
-                        // On the chain: H = max(X, F̂_up + extend + open, H_up + open); F̂ = max(F̂_up + extend, H_up).
-                        std::uint32_t const via_f = ops::add_opt(f_up, extend_open2, x);
-                        if constexpr (local) h = ops::add_opt_relu(h_up, open2, via_f);
-                        else h = ops::add_opt(h_up, open2, via_f);
-                        f_up = ops::add_opt(f_up, extend2, h_up);
+                        // h_col, h_up and diag hold Ĥ = H + open; e_col and f_up hold E and F.
+                        std::uint32_t const e_new = ops::add_opt(e_col[r], extend2, h_col[r]); // max(E + ext, H + open)
+                        std::uint32_t const x = ops::add_opt(diag, subs[r], e_new);            // max(H_diag + s, E)
+                        f_up = ops::add_opt(f_up, extend2, h_up);                              // max(F + ext, H + open)
+                        h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
+                        kept = ops::add(h, open2);
                         e_col[r] = e_new;
                     }
                     else {
+                        std::uint32_t const substitution = ops::add(diag, subs[r]);
                         std::uint32_t const x = ops::add_opt(h_col[r], open2, substitution);
                         if constexpr (local) h = ops::add_opt_relu(h_up, open2, x);
                         else h = ops::add_opt(h_up, open2, x);
+                        kept = h;
                     }
+                    cell_h[r] = h;
                     diag = h_col[r];
-                    h_col[r] = h;
-                    h_up = h;
+                    h_col[r] = kept;
+                    h_up = kept;
                 }
                 if constexpr (local) {
-                    // Columns past one pair's end carry filler in that half: mask it out of the maxima (H >= 0).
-                    std::uint32_t const mask = j <= (std::int64_t)m_min
-                                                   ? 0xFFFFFFFFu
-                                                   : ((j <= (std::int64_t)m_a ? 0x0000FFFFu : 0u) |
-                                                      (j <= (std::int64_t)m_b ? 0xFFFF0000u : 0u));
+                    if constexpr (steady) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], h_col[r] & mask, 0u);
-                }
-                else {
-                    if (lane == a_lane && j == (std::int64_t)m_a) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if (r == a_row) result_a = low16(h_col[r]);
+                        for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r], 0u);
                     }
-                    if (lane == b_lane && j == (std::int64_t)m_b) {
+                    else {
+                        // Columns past one pair's end carry filler in that half: mask it out of the maxima (H >= 0).
+                        std::uint32_t const mask = j <= (int)m_min ? 0xFFFFFFFFu
+                                                                   : ((j <= (int)m_a ? 0x0000FFFFu : 0u) |
+                                                                      (j <= (int)m_b ? 0xFFFF0000u : 0u));
+#pragma unroll
+                        for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r] & mask, 0u);
+                    }
+                }
+                else if constexpr (!steady) {
+                    if (lane == a_lane && j == (int)m_a) {
 #pragma unroll
                         for (int r = 0; r < R; ++r)
-                            if (r == b_row) result_b = high16(h_col[r]);
+                            if (r == a_row) result_a = low16(cell_h[r]);
+                    }
+                    if (lane == b_lane && j == (int)m_b) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == b_row) result_b = high16(cell_h[r]);
                     }
                 }
                 out_h = h_up, out_f = f_up;
-                if (write_bottom && lane == 31) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
+                if (bottom_writer) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
             }
             code_now = code_next;
 #pragma unroll
             for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
-        }
+        };
+
+        std::uint32_t const fill_end = min(steps, 31u);
+        std::uint32_t const steady_end = m_min >= 1u + 31u ? max(fill_end, m_min - 1u) : fill_end;
+        std::uint32_t t = 0;
+        for (; t < fill_end; ++t) step(t, std::false_type {});
+#pragma unroll 2
+        for (; t < steady_end; ++t) step(t, std::true_type {});
+        for (; t < steps; ++t) step(t, std::false_type {});
         if constexpr (local) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {

@@ -244,6 +244,7 @@ struct engine_t {
     score_costs_t costs {};
     int magnitude = 1;
     bool unit_levenshtein = false;
+    bool packed_profile_fits = false; // every substitution cost (minus `open` for affine gaps) fits a signed byte
     device_context_t devices[max_devices_k];
     szs_gb300_stats_t stats {};
     ~engine_t() {
@@ -312,6 +313,25 @@ static void prepare_class_costs(score_costs_t &costs, std::uint8_t const *byte_t
             // rows = second string: cost(first = column, second = row)
             costs.profile_table_t[cc * 32 + row_class] = table[column_class * 32 + row_class];
         }
+}
+
+/**
+ *  Whether the 16x2 packed route can hold this engine's substitution costs in its int8 profiles: the costs as they
+ *  are for linear gaps, `cost - open` for affine gaps (the packed affine tracks carry H + open). Only classes that
+ *  some byte maps to are checked; Levenshtein engines check their match and mismatch costs.
+ */
+static bool packed_profile_fits(score_costs_t const &costs) {
+    int const shift = costs.affine ? costs.open : 0;
+    auto fits = [&](int cost) { return cost - shift >= -128 && cost - shift <= 127; };
+    if (costs.kind == kind_levenshtein_k) return fits(costs.match) && fits(costs.mismatch);
+    bool used[32] = {};
+    for (int b = 0; b < 256; ++b) used[costs.byte_to_class[b] & 31] = true;
+    for (int cc = 0; cc < costs.classes; ++cc)
+        for (int row_class = 0; row_class < 32; ++row_class)
+            if (used[row_class] &&
+                (!fits(costs.profile_table[cc * 32 + row_class]) || !fits(costs.profile_table_t[cc * 32 + row_class])))
+                return false;
+    return true;
 }
 
 /* ---- inputs ----------------------------------------------------------------------------------------------------- */
@@ -520,7 +540,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     args.steps_beyond_span = costs.affine ? 3 : 1;
     args.force_route = engine.schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
-    args.packed_allowed = 1;
+    args.packed_allowed = engine.packed_profile_fits ? 1 : 0;
     bool const levenshtein = engine.kind == kind_levenshtein_k;
 
     SZS_TRY_CUDA(cudaEventRecord(context->start, stream));
@@ -856,6 +876,7 @@ sz_status_t create_engine(int kind, int match, int mismatch, int open, int exten
         for (int i = 0; i < 1024; ++i) magnitude = std::max(magnitude, cost_abs(table[i]));
     }
     engine->magnitude = std::max(magnitude, 1);
+    engine->packed_profile_fits = packed_profile_fits(costs);
     *engine_out = engine;
     return report({}, error_message);
 }

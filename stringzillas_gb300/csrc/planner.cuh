@@ -61,7 +61,7 @@ struct plan_args_t {
     int magnitude;          // max |cost| over substitution and gap costs, at least 1
     int steps_beyond_span;  // 1 linear, 3 affine (serial.hpp:126-140)
     int force_route;        // -1: normal planning; otherwise one bin per route, input order (the plain form)
-    int packed_allowed;     // 1 if the 16x2 route may be used (class-table engines, or <= 32 distinct bytes)
+    int packed_allowed;     // 1 if the 16x2 route may hold the substitution costs in int8 profiles
     batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)
 };
 

@@ -270,3 +270,36 @@ def test_band_route_long_pairs(szs, port, family, costs):
     engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
     got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("family,costs,extreme", [
+    ("nw", (-30, -2), 120),    # 120 - (-30) leaves a signed byte: the affine pairs leave the 16x2 route
+    ("sw", (-30, -2), 110),
+    ("nw", (-30, -2), 90),     # 90 + 30 still fits: the 16x2 route keeps them
+    ("sw", (-40, -40), 127),   # linear gaps take costs as they are
+    ("nw", (20, 1), -110),     # positive open: -110 - 20 leaves a signed byte
+])
+def test_profile_byte_range(szs, port, family, costs, extreme):
+    """The 16x2 route stores `cost - open` (affine) or `cost` (linear) in int8 profiles; tables outside that range
+    are scored by the 32-bit route. Either way the scores equal the oracle's."""
+    rng = np.random.default_rng(abs(extreme) + (0 if family == "nw" else 1000))
+    b2c, table = protein_tables(rng)
+    table[3, 3] = extreme
+    table[5, 7] = -extreme // 2
+    first = random_strings(rng, 96, 1, 400, PROTEIN)
+    second = random_strings(rng, 96, 1, 400, PROTEIN)
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("costs", [(0, 127, 100, 100), (0, 120, 127, 1), (5, 100, 120, 127), (0, 127, 0, 127)])
+def test_levenshtein_large_costs(szs, port, costs):
+    """Levenshtein costs near the top of their signed-byte range on short strings, where the length bound alone
+    allows 16-bit cells: profile entries `cost - open` stay inside a signed byte for non-negative costs."""
+    rng = np.random.default_rng(sum(costs))
+    first = random_strings(rng, 64, 0, 60, DNA)
+    second = random_strings(rng, 64, 0, 60, DNA)
+    engine = szs.LevenshteinDistances(*costs)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second)))
