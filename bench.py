@@ -271,6 +271,81 @@ def cpu_baseline(first, second, kind_and_tables, seconds_budget):
             "sample": f"first {k} of {count} pairs ({cells:.3e} cells, {elapsed:.2f} s), oracle C restatement"}
 
 
+SERVING_RATE = 120.0      # offered load, requests per second (Poisson arrivals)
+SERVING_REQUESTS = 240    # requests per run, drawn from a pool of 48 distinct ones
+
+
+def serving_engines(szs):
+    from stringzillas_gb300 import workloads as w
+    protein = w.protein_table(seed=42)
+    return {"lev": szs.LevenshteinDistances(),
+            "nw": szs.NeedlemanWunschScores(*protein, open=-11, extend=-1),
+            "sw": szs.SmithWatermanScores(*protein, open=-11, extend=-1)}
+
+
+def serve_stream(szs, server, engines, pool, order, arrivals):
+    """Submits pool[order[i]] at host time arrivals[i] (seconds from start); returns per-request infos and the
+    wall time from the first submission to the last result."""
+    import threading
+    strs = [(szs.Strs.from_buffers(*r["first"]), szs.Strs.from_buffers(*r["second"])) for r in pool]
+    tickets = [None] * len(order)
+    ready = threading.Semaphore(0)
+
+    def submitter(start):
+        for i, (k, at) in enumerate(zip(order, arrivals)):
+            delay = start + at - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets[i] = server.submit(engines[pool[k]["kind"]], *strs[k])
+            ready.release()
+
+    start = time.perf_counter()
+    thread = threading.Thread(target=submitter, args=(start,))
+    thread.start()
+    infos = []
+    for i in range(len(order)):
+        ready.acquire()
+        tickets[i].result()
+        infos.append(tickets[i].info)
+    wall = time.perf_counter() - start
+    thread.join()
+    return infos, wall
+
+
+def serving_leg(szs):
+    """C5: Poisson arrivals at a fixed offered load, and a saturating burst, against the serving loop (merged
+    batches, 4 lanes) and the per-request plain form (one lane, one request per batch, plain schedule)."""
+    from stringzillas_gb300 import workloads as w
+    pool = w.serving_requests(48, seed=42)
+    engines = serving_engines(szs)
+    rng = np.random.Generator(np.random.PCG64(7))
+    order = rng.integers(0, len(pool), size=SERVING_REQUESTS)
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVING_RATE, size=SERVING_REQUESTS))
+    cells = int(sum(pool[k]["cells"] for k in order))
+    forms = {"serving": dict(lanes=4, arena_bytes=4 << 30),
+             "per_request_plain": dict(lanes=1, max_batch_requests=1, schedule="plain", arena_bytes=4 << 30)}
+    out = {"offered_requests_per_s": SERVING_RATE, "requests": SERVING_REQUESTS,
+           "offered_gcups": cells / arrivals[-1] / 1e9, "cells": cells,
+           "mix": "Levenshtein:NW:SW 2:1:1, 1-4,096 pairs per request, pair lengths log-uniform [16, 16,384]"}
+    for name, config in forms.items():
+        with szs.Server(**config) as server:
+            serve_stream(szs, server, engines, pool, order[:8], np.zeros(8))  # warm-up: builds lane buffers
+            infos, wall = serve_stream(szs, server, engines, pool, order, arrivals)
+            latencies = np.array([i["done_ms"] for i in infos])
+            burst_infos, burst_wall = serve_stream(szs, server, engines, pool, order, np.zeros(len(order)))
+            stats = server.stats()
+        out[name] = {
+            "p50_ms": float(np.percentile(latencies, 50)), "p99_ms": float(np.percentile(latencies, 99)),
+            "mean_ms": float(latencies.mean()), "achieved_gcups_at_offered_load": cells / wall / 1e9,
+            "saturated_gcups": cells / burst_wall / 1e9,
+            "saturated_p99_ms": float(np.percentile([i["done_ms"] for i in burst_infos], 99)),
+            "batches": stats["batches"], "peak_inflight_batches": stats["peak_inflight"],
+            "arena_peak_bytes": stats["arena_peak_bytes"], "kernel_launches": stats["kernel_launches"]}
+    out["saturated_serving_over_plain"] = (out["serving"]["saturated_gcups"] /
+                                           out["per_request_plain"]["saturated_gcups"])
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -405,6 +480,7 @@ def run_ours(args):
             extra[name] = row
             del batch
         line["extra"] = extra
+        line["serving"] = serving_leg(szs)
     elif rank == 0:
         line["cpu_baseline"] = None
     if rank == 0:

@@ -372,9 +372,11 @@ SZS_GB300_API sz_status_t szs_smith_waterman_scores_pairwise_u64tape(szs_smith_w
 
 /** Scheduling forms an engine can run a batch in. */
 typedef enum szs_gb300_schedule_t {
-    /** Length-binned plan, persistent kernels per bin, cached CUDA graph when inputs are device-resident. */
+    /** Length-binned plan: pairs sorted into bins by route and size, longest first, tile shape chosen per pair,
+        the routes' persistent kernels running concurrently on forked streams. */
     szs_gb300_schedule_batched_k = 0,
-    /** One launch of one kernel shape over all pairs in input order: the "plain one-launch-per-batch" form. */
+    /** The "plain one-launch-per-batch" form of the same kernels: one launch per route (one kernel shape, pairs in
+        input order; pairs longer than one warp's strip still take the band kernel), launches one after another. */
     szs_gb300_schedule_plain_k = 1,
 } szs_gb300_schedule_t;
 
@@ -436,6 +438,81 @@ SZS_GB300_API sz_status_t szs_gb300_score_pairwise_noalloc_u64tape(void *engine,
  */
 SZS_GB300_API sz_status_t szs_gb300_measure_integer_peaks(sz_size_t gpu_device, double *ops_per_second,
                                                           sz_size_t count, char const **error_message);
+
+/* ---- serving loop (no counterpart in the reference) ----------------------------------------------------------- */
+
+/** A serving loop on one GPU: requests in, merged batches on the device, results out. */
+typedef void *szs_gb300_server_t;
+
+/** How a serving loop admits and batches requests. Zero fields take the defaults given. */
+typedef struct szs_gb300_server_config_t {
+    sz_size_t gpu_device;         /**< device index */
+    sz_size_t arena_bytes;        /**< HBM budget of the device arena that holds admitted batches' sequences,
+                                       offsets and results (default 1 GiB) */
+    sz_size_t lanes;              /**< batches in flight at once, each on its own stream (default 4) */
+    sz_size_t max_batch_pairs;    /**< pairs merged into one batch at most (default 2^22) */
+    sz_size_t max_batch_requests; /**< requests merged into one batch at most (default unlimited; 1 = per-request) */
+    int schedule;                 /**< `szs_gb300_schedule_t` of the batches (default batched) */
+} szs_gb300_server_config_t;
+
+/** What happened to one request. Times are host wall-clock milliseconds from its submission. */
+typedef struct szs_gb300_request_info_t {
+    sz_status_t status;     /**< the request's outcome (the batch's status) */
+    double admitted_ms;     /**< submission -> its batch was admitted into the arena */
+    double done_ms;         /**< submission -> its results were in the caller's buffer */
+    sz_u64_t batch;         /**< sequence number of the batch it ran in */
+    sz_u64_t batch_requests; /**< requests merged into that batch */
+    sz_u64_t batch_pairs;   /**< pairs in that batch */
+    sz_u64_t cells;         /**< sum of len(a)*len(b) over this request's pairs */
+} szs_gb300_request_info_t;
+
+/** Counters of a serving loop since it started. */
+typedef struct szs_gb300_server_stats_t {
+    sz_u64_t requests;            /**< requests submitted */
+    sz_u64_t completed;           /**< requests whose results are delivered */
+    sz_u64_t batches;             /**< batches run */
+    sz_u64_t pairs;               /**< pairs scored */
+    sz_u64_t cells;               /**< cells scored */
+    sz_u64_t arena_bytes;         /**< the arena's size */
+    sz_u64_t arena_peak_bytes;    /**< most arena bytes held by admitted batches at once */
+    sz_u64_t peak_inflight;       /**< most batches on the device at once */
+    sz_u64_t kernel_launches;     /**< kernels launched by all lanes */
+    double device_ms;             /**< sum over batches of their CUDA-event time */
+} szs_gb300_server_stats_t;
+
+/**
+ *  Starts a serving loop: one admission thread and `lanes` lane threads, each lane with its own stream and
+ *  scoring buffers, all sharing one device arena of `arena_bytes`. Requests wait in arrival order; whenever a lane
+ *  is free, every waiting request of the first waiter's engine that fits the arena and the batch caps is merged
+ *  into one batch (continuous batching), copied into the arena and scored with one planned call while other lanes'
+ *  batches are still on the device.
+ */
+SZS_GB300_API sz_status_t szs_gb300_server_init(szs_gb300_server_config_t const *config, szs_gb300_server_t *server,
+                                                char const **error_message);
+
+/**
+ *  Queues `results[i] = score(first[i], second[i])` on @p engine (any engine of the `*_init` functions; 8-byte
+ *  results). Tapes and results may be host or device memory and must stay valid until the request is waited for.
+ *  Returns at once with a ticket; the engine must not be freed while requests on it are pending.
+ */
+SZS_GB300_API sz_status_t szs_gb300_server_submit(szs_gb300_server_t server, void *engine,
+                                                  sz_sequence_u64tape_t const *first,
+                                                  sz_sequence_u64tape_t const *second, void *results,
+                                                  sz_u64_t *ticket, char const **error_message);
+
+/**
+ *  Blocks until request @p ticket is done, fills @p info (may be NULL) and forgets the ticket. Returns the request's
+ *  status; an unknown or already-waited ticket gives `sz_unexpected_dimensions_k`.
+ */
+SZS_GB300_API sz_status_t szs_gb300_server_wait(szs_gb300_server_t server, sz_u64_t ticket,
+                                                szs_gb300_request_info_t *info, char const **error_message);
+
+/** Copies the loop's counters into @p stats. */
+SZS_GB300_API sz_status_t szs_gb300_server_get_stats(szs_gb300_server_t server, szs_gb300_server_stats_t *stats,
+                                                     char const **error_message);
+
+/** Finishes every queued request, stops the threads and frees the arena. */
+SZS_GB300_API void szs_gb300_server_free(szs_gb300_server_t server);
 
 #ifdef __cplusplus
 }

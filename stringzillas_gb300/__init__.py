@@ -24,7 +24,7 @@ from ._native import lib
 
 __all__ = [
     "Strs", "DeviceScope", "LevenshteinDistances", "NeedlemanWunschScores", "SmithWatermanScores", "to_device",
-    "__version__", "__capabilities__",
+    "Server", "Ticket", "__version__", "__capabilities__",
 ]
 
 __version__ = f"{lib.szs_version_major()}.{lib.szs_version_minor()}.{lib.szs_version_patch()}"
@@ -439,3 +439,5 @@ class SmithWatermanScores(_Alignment):
 
     _algo = "smith_waterman_scores"
     _name = "Smith-Waterman scores"
+
+from .serving import Server, Ticket  # noqa: E402  (needs the engine classes above)

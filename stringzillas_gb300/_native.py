@@ -113,6 +113,60 @@ lib.szs_gb300_measure_integer_peaks.argtypes = [c_size_t, ctypes.POINTER(ctypes.
 lib.szs_gb300_engine_get_stats.restype = c_status
 lib.szs_gb300_engine_get_stats.argtypes = [c_void_p, ctypes.POINTER(Stats), _err]
 
+
+class ServerConfig(ctypes.Structure):
+    """``szs_gb300_server_config_t``"""
+    _fields_ = [
+        ("gpu_device", c_size_t),
+        ("arena_bytes", c_size_t),
+        ("lanes", c_size_t),
+        ("max_batch_pairs", c_size_t),
+        ("max_batch_requests", c_size_t),
+        ("schedule", c_int),
+    ]
+
+
+class RequestInfo(ctypes.Structure):
+    """``szs_gb300_request_info_t``"""
+    _fields_ = [
+        ("status", c_status),
+        ("admitted_ms", ctypes.c_double),
+        ("done_ms", ctypes.c_double),
+        ("batch", ctypes.c_uint64),
+        ("batch_requests", ctypes.c_uint64),
+        ("batch_pairs", ctypes.c_uint64),
+        ("cells", ctypes.c_uint64),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    """``szs_gb300_server_stats_t``"""
+    _fields_ = [
+        ("requests", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("batches", ctypes.c_uint64),
+        ("pairs", ctypes.c_uint64),
+        ("cells", ctypes.c_uint64),
+        ("arena_bytes", ctypes.c_uint64),
+        ("arena_peak_bytes", ctypes.c_uint64),
+        ("peak_inflight", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("device_ms", ctypes.c_double),
+    ]
+
+
+lib.szs_gb300_server_init.restype = c_status
+lib.szs_gb300_server_init.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(c_void_p), _err]
+lib.szs_gb300_server_submit.restype = c_status
+lib.szs_gb300_server_submit.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        ctypes.POINTER(ctypes.c_uint64), _err]
+lib.szs_gb300_server_wait.restype = c_status
+lib.szs_gb300_server_wait.argtypes = [c_void_p, ctypes.c_uint64, ctypes.POINTER(RequestInfo), _err]
+lib.szs_gb300_server_get_stats.restype = c_status
+lib.szs_gb300_server_get_stats.argtypes = [c_void_p, ctypes.POINTER(ServerStats), _err]
+lib.szs_gb300_server_free.restype = None
+lib.szs_gb300_server_free.argtypes = [c_void_p]
+
 # Status codes (include/stringzillas_gb300.h; values of the reference's types.h:699-721).
 SUCCESS = 0
 BAD_ALLOC = -10

@@ -33,6 +33,7 @@ UNITS = [
     ("kernels_band", "kernels_band.cu", []),
     ("probe", "probe.cu", []),
     ("static_scratch", "static_scratch.cu", []),
+    ("server", "server.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),
     ("myers_p3", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=3"]),
     ("myers_p5", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=5"]),

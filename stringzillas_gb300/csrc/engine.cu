@@ -473,13 +473,13 @@ static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &str
     return {};
 }
 
-static status_t run_call(engine_t &engine, void *scope_handle, call_t const &call) noexcept {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    device_context_t *context = nullptr;
-    status_t status = resolve_scope(scope_handle, device, stream, engine, context);
-    if (!status.ok()) return status;
-
+/**
+ *  One call on an explicit device context and stream. The engine is only read (costs, kind, schedule), so several
+ *  contexts may run calls of the same engine at once; @p stats receives the call's timings and counters.
+ */
+static status_t run_on(engine_t const &engine, device_context_t *context, cudaStream_t stream, call_t const &call,
+                       int schedule, szs_gb300_stats_t &stats) noexcept {
+    status_t status;
     std::uint64_t const queries_count = call.queries.count;
     std::uint64_t const candidates_count = call.has_candidates ? call.candidates.count : queries_count;
     plan_args_t args {};
@@ -491,11 +491,11 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     else if (call.mode == mode_cross_k) args.pairs = queries_count * candidates_count;
     else args.pairs = queries_count * (queries_count + 1) / 2;
     args.candidates_count = candidates_count;
-    engine.stats.last_pairs = args.pairs;
-    engine.stats.last_cells = 0;
-    engine.stats.last_launches = 0;
-    engine.stats.last_call_ms = 0;
-    engine.stats.last_compute_ms = 0;
+    stats.last_pairs = args.pairs;
+    stats.last_cells = 0;
+    stats.last_launches = 0;
+    stats.last_call_ms = 0;
+    stats.last_compute_ms = 0;
     if (args.pairs == 0) return {};
     if (args.pairs > 0xFFFFFFFFull) return {sz_overflow_risk_k, "More than 2^32 pairs in one call"};
 
@@ -538,7 +538,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     args.unit_levenshtein = engine.unit_levenshtein ? 1 : 0;
     args.magnitude = engine.magnitude;
     args.steps_beyond_span = costs.affine ? 3 : 1;
-    args.force_route = engine.schedule == szs_gb300_schedule_plain_k ? 1 : -1;
+    args.force_route = schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
     args.packed_allowed = engine.packed_profile_fits ? 1 : 0;
     bool const levenshtein = engine.kind == kind_levenshtein_k;
@@ -563,7 +563,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
     batch_alphabet_t const &alphabet_host = *context->alphabet_host();
-    engine.stats.last_cells = plan.cells;
+    stats.last_cells = plan.cells;
     auto pairs_in = [&](int key_begin, int key_end) {
         std::uint64_t total = 0;
         for (int key = key_begin; key < key_end; ++key) total += plan.count[key];
@@ -660,7 +660,9 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
 
     // Fork the launches over the auxiliary streams, join them back into the call's stream.
     static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
-    int const lanes_used = std::min(job_count, (int)device_context_t::lanes_k);
+    // The plain form runs its launches one after another on one stream; the batched form spreads them.
+    int const lanes_used = schedule == szs_gb300_schedule_plain_k ? std::min(job_count, 1)
+                                                                   : std::min(job_count, (int)device_context_t::lanes_k);
     // Scoring kernels are bracketed by their own events so the stats isolate them from planning and copies.
     bool compute_recorded = false;
     if (job_count) {
@@ -685,7 +687,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
             SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                      bins, packed_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
         else
-            SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, engine.schedule != szs_gb300_schedule_plain_k, tasks,
+            SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, schedule != szs_gb300_schedule_plain_k, tasks,
                                       bins, alphabet, results, job.ctas, lane_stream));
         if (traced) cudaEventRecord(context->trace_events[2 * i + 1], lane_stream);
         ++launches;
@@ -745,10 +747,10 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
                                      "expired); its score was not computed"};
     float elapsed = 0;
     cudaEventElapsedTime(&elapsed, context->start, context->stop);
-    engine.stats.last_call_ms = elapsed;
+    stats.last_call_ms = elapsed;
     float compute = 0;
     if (compute_recorded) cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
-    engine.stats.last_compute_ms = compute;
+    stats.last_compute_ms = compute;
     if (tracing) {
         static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits"};
         for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
@@ -759,10 +761,79 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
                          names[jobs[i].kind], jobs[i].variant, (unsigned long long)jobs[i].pairs, offset, ms);
         }
     }
-    engine.stats.last_launches = launches;
-    engine.stats.kernel_launches += launches;
+    stats.last_launches = launches;
+    stats.kernel_launches += launches;
     return {};
 }
+
+static status_t run_call(engine_t &engine, void *scope_handle, call_t const &call) noexcept {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    device_context_t *context = nullptr;
+    status_t status = resolve_scope(scope_handle, device, stream, engine, context);
+    if (!status.ok()) return status;
+    return run_on(engine, context, stream, call, engine.schedule, engine.stats);
+}
+
+/* ---- execution contexts for callers that run one engine from several threads (the serving loop) ---------------- */
+
+struct exec_context_t {
+    device_context_t context;
+    szs_gb300_stats_t stats {};
+};
+
+sz_status_t exec_context_create(int device, void **out, char const **error_message) noexcept {
+    if (device < 0 || device >= visible_devices()) return report({sz_missing_gpu_k, nullptr}, error_message);
+    auto *exec = new (std::nothrow) exec_context_t();
+    if (!exec) return report({sz_bad_alloc_k, nullptr}, error_message);
+    status_t const status = exec->context.prepare(device);
+    if (!status.ok()) {
+        exec->context.release();
+        delete exec;
+        return report(status, error_message);
+    }
+    *out = exec;
+    return report({}, error_message);
+}
+
+void exec_context_free(void *handle) noexcept {
+    auto *exec = static_cast<exec_context_t *>(handle);
+    if (!exec) return;
+    exec->context.release();
+    delete exec;
+}
+
+cudaStream_t exec_context_stream(void *handle) noexcept { return static_cast<exec_context_t *>(handle)->context.own_stream; }
+
+szs_gb300_stats_t const &exec_context_stats(void *handle) noexcept { return static_cast<exec_context_t *>(handle)->stats; }
+
+/** Pairwise scores of device-resident u64 tapes into device-resident `results`, on the context's stream. */
+sz_status_t exec_pairwise(void *engine_handle, void *handle, sz_sequence_u64tape_t const *first,
+                          sz_sequence_u64tape_t const *second, std::int64_t *results, int schedule,
+                          char const **error_message) noexcept {
+    auto *exec = static_cast<exec_context_t *>(handle);
+    engine_t *engine = as_engine(engine_handle, -1);
+    if (!engine || !exec) return report({sz_status_unknown_k, "Invalid engine or execution context"}, error_message);
+    if (!first || !second) return report({sz_unexpected_dimensions_k, nullptr}, error_message);
+    cudaError_t const selected = cudaSetDevice(exec->context.device);
+    if (selected != cudaSuccess) return report(from_cuda(selected), error_message);
+    auto view = [](sz_sequence_u64tape_t const *tape) {
+        tape_view_t v;
+        v.data = tape->data, v.offsets = tape->offsets, v.count = tape->count, v.offset_bits = 64;
+        return v;
+    };
+    call_t call;
+    call.queries = view(first);
+    call.candidates = view(second);
+    call.has_candidates = true;
+    call.mode = mode_pairwise_k;
+    call.out = results;
+    call.stride = 1;
+    return report(run_on(*engine, &exec->context, exec->context.own_stream, call, schedule, exec->stats),
+                  error_message);
+}
+
+bool engine_handle_valid(void *engine_handle) noexcept { return as_engine(engine_handle, -1) != nullptr; }
 
 } // namespace szs_gb300
 

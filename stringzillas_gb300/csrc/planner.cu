@@ -87,7 +87,12 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     std::uint64_t const span = maximize ? n + m : (n > m ? n : m);
     std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;
     bool const fits32_early = reach < (1ull << 31) - 1;
-    if (args.force_route < 0 && n > (std::uint64_t)band_min_rows_k && fits32_early) {
+    if (n > (std::uint64_t)band_min_rows_k && fits32_early) {
+        // Long pairs take the band in both forms; the plain form keeps them in one bin, in input order.
+        if (args.force_route >= 0) {
+            info.key = bin_band_begin_k;
+            return info;
+        }
         int size_class = floor_log2_u64(n * m) - 10;
         size_class = size_class < 0 ? 0 : (size_class > bin_dp_classes_k - 1 ? bin_dp_classes_k - 1 : size_class);
         info.key = bin_band_begin_k + (bin_dp_classes_k - 1 - size_class);

@@ -13,6 +13,9 @@ Each generator returns tapes as ``(data: uint8[], offsets: int64[count + 1])`` p
 * ``local_dna_pairs``: DNA strings with log-uniform lengths in [1,000, 30,000], each pair sharing one planted
   segment of U{500..5000} bp at random offsets with 10% divergence, random flanks.
 * ``dna_table``: match +2 / mismatch -3 over A, C, G, T (classes 1..4), class 0 for other bytes.
+* ``serving_requests``: the serving stream's requests: 1-4,096 pairs each (log-uniform), kinds Levenshtein /
+  Needleman-Wunsch / Smith-Waterman in ratio 2:1:1, pair lengths log-uniform in [16, 16,384]; Levenshtein pairs are
+  DNA reads with 5% substitutions + 2% indels, alignment pairs are proteins with a 70%-identity partner.
 """
 from __future__ import annotations
 
@@ -134,3 +137,28 @@ def local_dna_pairs(count, low=1000, high=30000, segment_low=500, segment_high=5
 def cells(first, second) -> int:
     """Sum over pairs of len(first_i) * len(second_i): the cell count GCUPS divides by."""
     return int(np.dot(np.diff(first[1]).astype(np.int64), np.diff(second[1]).astype(np.int64)))
+
+
+def serving_requests(count, min_pairs=1, max_pairs=4096, min_length=16, max_length=16384, seed=42):
+    """`count` requests of the serving stream: dicts with ``kind`` ("lev", "nw" or "sw"), ``first`` and ``second``
+    tapes, ``pairs`` and ``cells``. Kinds are drawn 2:1:1; each pair's first length is log-uniform and its partner
+    is a mutant of it."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    kinds = rng.choice(np.array(["lev", "lev", "nw", "sw"]), size=count)
+    pair_counts = np.exp(rng.uniform(np.log(min_pairs), np.log(max_pairs + 1), size=count)).astype(np.int64)
+    pair_counts = np.clip(pair_counts, min_pairs, max_pairs)
+    requests = []
+    p = AMINO_FREQUENCIES / AMINO_FREQUENCIES.sum()
+    for kind, pairs in zip(kinds, pair_counts):
+        lengths = np.exp(rng.uniform(np.log(min_length), np.log(max_length + 1), size=int(pairs))).astype(np.int64)
+        lengths = np.clip(lengths, min_length, max_length)
+        offsets = _offsets(lengths)
+        if kind == "lev":
+            first = _letters(rng, DNA, int(offsets[-1]))
+            second, second_offsets = _mutate(rng, first, offsets, DNA, 0.05, 0.02)
+        else:
+            first = _letters(rng, AMINO_ACIDS, int(offsets[-1]), p)
+            second, second_offsets = _mutate(rng, first, offsets, AMINO_ACIDS, 0.30, 0.02, probabilities=p)
+        requests.append({"kind": str(kind), "first": (first, offsets), "second": (second, second_offsets),
+                         "pairs": int(pairs), "cells": cells((first, offsets), (second, second_offsets))})
+    return requests

@@ -92,3 +92,37 @@ def test_calls_validate_before_running():
     # Empty inputs return empty matrices without touching a device.
     assert engine(szs.Strs([]), szs.Strs([])).shape == (0, 0)
     assert engine(szs.Strs(["a"]), szs.Strs([])).shape == (1, 0)
+
+
+def test_server_validation_without_a_gpu():
+    """The serving loop needs a GPU; the ABI structs match the header's layout."""
+    from stringzillas_gb300 import _native
+    import ctypes
+    assert ctypes.sizeof(_native.ServerConfig) == 6 * 8
+    assert ctypes.sizeof(_native.RequestInfo) == 7 * 8
+    assert ctypes.sizeof(_native.ServerStats) == 10 * 8
+    if "cuda" in szs.__capabilities__:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(RuntimeError):
+        szs.Server()
+    # Submissions to an invalid handle fail cleanly instead of crashing.
+    handle = ctypes.c_void_p()
+    err = ctypes.c_char_p()
+    ticket = ctypes.c_uint64()
+    status = _native.lib.szs_gb300_server_submit(handle, None, None, None, None, ctypes.byref(ticket),
+                                                 ctypes.byref(err))
+    assert status != 0 and err.value
+    assert _native.lib.szs_gb300_server_wait(handle, 1, None, ctypes.byref(err)) != 0
+
+
+def test_serving_workload_shape():
+    from stringzillas_gb300 import workloads as w
+    requests = w.serving_requests(40, seed=3, max_pairs=64, max_length=300)
+    kinds = [r["kind"] for r in requests]
+    assert set(kinds) <= {"lev", "nw", "sw"} and kinds.count("lev") > 5
+    for r in requests:
+        assert 1 <= r["pairs"] <= 64
+        assert len(r["first"][1]) == r["pairs"] + 1 == len(r["second"][1])
+        lengths = np.diff(r["first"][1])
+        assert lengths.min() >= 16 and lengths.max() <= 300
+        assert r["cells"] == int(np.dot(lengths, np.diff(r["second"][1])))
