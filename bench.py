@@ -86,13 +86,23 @@ def make_workload(name, seed):
 
 
 def make_engine(kind_and_tables):
+    """The workload's engine with the committed autotuned table installed (if the package has one)."""
     import stringzillas_gb300 as szs
+    from stringzillas_gb300 import autotune
     kind, tables = kind_and_tables
     if kind == "lev":
-        return szs.LevenshteinDistances()
-    if kind == "nw":
-        return szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
-    return szs.SmithWatermanScores(*tables, open=-5, extend=-2)
+        engine = szs.LevenshteinDistances()
+    elif kind == "nw":
+        engine = szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
+    else:
+        engine = szs.SmithWatermanScores(*tables, open=-5, extend=-2)
+    autotune.apply(engine)
+    return engine
+
+
+def tuning_source():
+    from stringzillas_gb300 import autotune
+    return "autotuned table " + os.path.relpath(autotune.DEFAULT_TABLE, HERE) if autotune.load() else "built-in"
 
 
 def oracle_costs(kind_and_tables):
@@ -278,9 +288,13 @@ SERVING_REQUESTS = 240    # requests per run, drawn from a pool of 48 distinct o
 def serving_engines(szs):
     from stringzillas_gb300 import workloads as w
     protein = w.protein_table(seed=42)
-    return {"lev": szs.LevenshteinDistances(),
-            "nw": szs.NeedlemanWunschScores(*protein, open=-11, extend=-1),
-            "sw": szs.SmithWatermanScores(*protein, open=-11, extend=-1)}
+    from stringzillas_gb300 import autotune
+    engines = {"lev": szs.LevenshteinDistances(),
+               "nw": szs.NeedlemanWunschScores(*protein, open=-11, extend=-1),
+               "sw": szs.SmithWatermanScores(*protein, open=-11, extend=-1)}
+    for engine in engines.values():
+        autotune.apply(engine)
+    return engines
 
 
 def serve_stream(szs, server, engines, pool, order, arrivals):
@@ -440,7 +454,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32" if kind_and_tables[0] == "lev" else "int32",
             "data": "synthetic (seeded numpy PCG64)",
             "config": {"workload": WORKLOADS[args.workload], "pairs": pairs, "cells_per_step": cells_per_step,
-                       "input_bytes_per_step": input_bytes,
+                       "input_bytes_per_step": input_bytes, "tuning": tuning_source(),
                        "l2": "inputs larger than L2 (129 MB), no flush between steps",
                        "parallelism": f"pairs: each of {world} ranks scores its own batch, no collective"},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",

@@ -406,6 +406,27 @@ typedef struct szs_gb300_stats_t {
 SZS_GB300_API sz_status_t szs_gb300_device_scope_init_stream(sz_size_t gpu_device, void *cuda_stream,
                                                              szs_device_scope_t *scope, char const **error_message);
 
+/**
+ *  Per-length-bin choices of the planner and of the launch shapes. Length class k holds the pairs whose shorter
+ *  side n has floor(log2(n)) == k (class 15 also holds everything longer). Zero fields keep the built-in choice.
+ *  No counterpart in the reference, whose tier thresholds are compile-time constants.
+ */
+typedef struct szs_gb300_tuning_t {
+    sz_u8_t packed_rows[16]; /**< rows per lane of the 16x2 route (4, 8, 12 or 16); 0 = instruction-count model */
+    sz_u8_t cell_bits[16];   /**< 0 = the narrowest cells the length bound proves safe; 32 = never 16-bit cells */
+    sz_u32_t band_min_rows;  /**< shorter sides above this take the band kernel (0 = 1,024) */
+    sz_u32_t packed_warps[4]; /**< warps per CTA (1..8) of the 16x2 launches with 4, 8, 12, 16 rows (0 = 4) */
+} szs_gb300_tuning_t;
+
+/** Installs @p tuning on @p engine (NULL restores the built-in choices); out-of-range values are rejected with
+ *  `sz_unexpected_dimensions_k`. No counterpart in the reference. */
+SZS_GB300_API sz_status_t szs_gb300_engine_set_tuning(void *engine, szs_gb300_tuning_t const *tuning,
+                                                      char const **error_message);
+
+/** Copies the engine's current tuning into @p tuning. No counterpart in the reference. */
+SZS_GB300_API sz_status_t szs_gb300_engine_get_tuning(void *engine, szs_gb300_tuning_t *tuning,
+                                                      char const **error_message);
+
 /** Copies the engine's counters into @p stats. No counterpart in the reference. */
 SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine, szs_gb300_stats_t *stats,
                                                      char const **error_message);

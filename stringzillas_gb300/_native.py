@@ -114,6 +114,22 @@ lib.szs_gb300_engine_get_stats.restype = c_status
 lib.szs_gb300_engine_get_stats.argtypes = [c_void_p, ctypes.POINTER(Stats), _err]
 
 
+class Tuning(ctypes.Structure):
+    """``szs_gb300_tuning_t``"""
+    _fields_ = [
+        ("packed_rows", ctypes.c_uint8 * 16),
+        ("cell_bits", ctypes.c_uint8 * 16),
+        ("band_min_rows", ctypes.c_uint32),
+        ("packed_warps", ctypes.c_uint32 * 4),
+    ]
+
+
+lib.szs_gb300_engine_set_tuning.restype = c_status
+lib.szs_gb300_engine_set_tuning.argtypes = [c_void_p, ctypes.POINTER(Tuning), _err]
+lib.szs_gb300_engine_get_tuning.restype = c_status
+lib.szs_gb300_engine_get_tuning.argtypes = [c_void_p, ctypes.POINTER(Tuning), _err]
+
+
 class ServerConfig(ctypes.Structure):
     """``szs_gb300_server_config_t``"""
     _fields_ = [

@@ -148,6 +148,53 @@ static bool device_accessible(void const *pointer) noexcept {
     return attributes.type == cudaMemoryTypeDevice || attributes.type == cudaMemoryTypeManaged;
 }
 
+/**
+ *  Instantiated CUDA graphs of earlier calls, keyed by every byte their launches depend on (kernel arguments,
+ *  buffer addresses, grid sizes). A call whose key matches replays the graph instead of issuing its launches.
+ */
+struct graph_cache_t {
+    static constexpr int capacity_k = 8;
+    struct entry_t {
+        std::vector<unsigned char> key;
+        cudaGraphExec_t exec = nullptr;
+        std::uint64_t used = 0;
+    };
+    entry_t entries[capacity_k];
+    std::uint64_t clock = 0;
+
+    cudaGraphExec_t find(std::vector<unsigned char> const &key) noexcept {
+        for (auto &entry : entries)
+            if (entry.exec && entry.key == key) {
+                entry.used = ++clock;
+                return entry.exec;
+            }
+        return nullptr;
+    }
+    void insert(std::vector<unsigned char> key, cudaGraphExec_t exec) noexcept {
+        entry_t *victim = &entries[0];
+        for (auto &entry : entries)
+            if (!entry.exec || entry.used < victim->used) victim = &entry;
+        if (victim->exec) cudaGraphExecDestroy(victim->exec);
+        victim->key = std::move(key);
+        victim->exec = exec;
+        victim->used = ++clock;
+    }
+    void release() noexcept {
+        for (auto &entry : entries) {
+            if (entry.exec) cudaGraphExecDestroy(entry.exec);
+            entry.exec = nullptr;
+            entry.key.clear();
+        }
+    }
+};
+
+/** Appends the object representation of @p value to a graph key. */
+template <typename value_type_>
+static void key_append(std::vector<unsigned char> &key, value_type_ const &value) {
+    auto const *bytes = reinterpret_cast<unsigned char const *>(&value);
+    key.insert(key.end(), bytes, bytes + sizeof(value_type_));
+}
+
 /** Per-device state of an engine: its stream for the default scope, buffers, plan readback, timers. */
 struct device_context_t {
     bool ready = false;
@@ -167,6 +214,8 @@ struct device_context_t {
     cudaEvent_t fork = nullptr;
     cudaEvent_t joins[lanes_k] = {nullptr};
     cudaEvent_t trace_events[64] = {nullptr};
+    graph_cache_t prologue_graphs; // alphabet + plan + plan readback
+    graph_cache_t launch_graphs;   // the scoring kernels of a plan
 
     status_t prepare(int device_index) noexcept {
         if (ready) return {};
@@ -206,6 +255,7 @@ struct device_context_t {
         if (!ready) return;
         cudaSetDevice(device);
         cudaStreamSynchronize(own_stream);
+        prologue_graphs.release(), launch_graphs.release();
         control.release(), inputs.release(), work.release(), scratch.release();
         readback.release(), results_host.release();
         if (start) cudaEventDestroy(start);
@@ -245,6 +295,7 @@ struct engine_t {
     int magnitude = 1;
     bool unit_levenshtein = false;
     bool packed_profile_fits = false; // every substitution cost (minus `open` for affine gaps) fits a signed byte
+    szs_gb300_tuning_t tuning {};     // zeros: built-in choices
     device_context_t devices[max_devices_k];
     szs_gb300_stats_t stats {};
     ~engine_t() {
@@ -482,7 +533,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     status_t status;
     std::uint64_t const queries_count = call.queries.count;
     std::uint64_t const candidates_count = call.has_candidates ? call.candidates.count : queries_count;
-    plan_args_t args {};
+    plan_args_t args;
+    std::memset(&args, 0, sizeof(args)); // graph keys compare its bytes, padding included
     args.mode = call.mode;
     if (call.mode == mode_pairwise_k) {
         if (call.candidates.count != call.queries.count) return {sz_unexpected_dimensions_k, nullptr};
@@ -541,25 +593,70 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.force_route = schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
     args.packed_allowed = engine.packed_profile_fits ? 1 : 0;
+    std::memcpy(args.packed_rows, engine.tuning.packed_rows, 16);
+    std::memcpy(args.cell_bits, engine.tuning.cell_bits, 16);
+    args.band_min_rows = engine.tuning.band_min_rows ? engine.tuning.band_min_rows : (std::uint32_t)band_min_rows_k;
     bool const levenshtein = engine.kind == kind_levenshtein_k;
+
+    static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
+    // Device-resident inputs make every launch of the call a function of bytes the call can key on, so both phases
+    // (planning, then scoring) are captured once as CUDA graphs and replayed by later calls with the same key.
+    bool const graphs = !tracing && query_plan.offsets_bytes == 0 && query_plan.data_bytes == 0 &&
+                        candidate_plan.offsets_bytes == 0 && candidate_plan.data_bytes == 0;
+    bool prologue_replayed = false, launches_replayed = false;
+    // Runs `issue(capture_stream)` directly on the call's stream, or captures it on the context's own stream into a
+    // graph (once per key) and launches that graph on the call's stream.
+    auto issue_or_replay = [&](graph_cache_t &cache, std::vector<unsigned char> const &key, bool &replayed,
+                               auto &&issue) -> status_t {
+        if (!graphs) return issue(stream);
+        cudaGraphExec_t exec = cache.find(key);
+        replayed = exec != nullptr;
+        if (!exec) {
+            cudaStream_t const capture = context->own_stream;
+            SZS_TRY_CUDA(cudaStreamBeginCapture(capture, cudaStreamCaptureModeRelaxed));
+            status_t const issued = issue(capture);
+            cudaGraph_t graph = nullptr;
+            cudaError_t const ended = cudaStreamEndCapture(capture, &graph);
+            if (!issued.ok() || ended != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                cudaGetLastError();
+                return issued.ok() ? from_cuda(ended) : issued;
+            }
+            cudaError_t const made = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            SZS_TRY_CUDA(made);
+            cache.insert(key, exec);
+        }
+        SZS_TRY_CUDA(cudaGraphLaunch(exec, stream));
+        return {};
+    };
 
     SZS_TRY_CUDA(cudaEventRecord(context->start, stream));
     std::uint64_t launches = 0;
     plan_bins_t *bins = context->bins_device();
     batch_alphabet_t *alphabet = context->alphabet_device();
-    // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code planes by
-    // it, and the 16x2 route builds its substitution profile over it (when it has at most 32 symbols).
-    if (levenshtein) {
-        SZS_TRY_CUDA(launch_alphabet(args.queries, args.candidates, call.has_candidates, alphabet, context->sm_count,
-                                     stream));
-        launches += 2 + (call.has_candidates ? 1 : 0);
-        args.alphabet = alphabet;
+    if (levenshtein) args.alphabet = alphabet;
+    std::vector<unsigned char> prologue_key;
+    if (graphs) {
+        key_append(prologue_key, args);
+        key_append(prologue_key, bins), key_append(prologue_key, tasks), key_append(prologue_key, results);
+        key_append(prologue_key, context->readback.data), key_append(prologue_key, context->sm_count);
+        key_append(prologue_key, call.has_candidates);
     }
-    SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, stream));
-    launches += 3;
-    // Read the plan (and the alphabet, stored right after it) back: which bins are non-empty, how long columns get.
-    SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t) + sizeof(batch_alphabet_t),
-                                 cudaMemcpyDeviceToHost, stream));
+    status = issue_or_replay(context->prologue_graphs, prologue_key, prologue_replayed, [&](cudaStream_t s) -> status_t {
+        // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code planes
+        // by it, and the 16x2 route builds its substitution profile over it (when it has at most 32 symbols).
+        if (levenshtein)
+            SZS_TRY_CUDA(launch_alphabet(args.queries, args.candidates, call.has_candidates, alphabet,
+                                         context->sm_count, s));
+        SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, s));
+        // Read the plan (and the alphabet, stored right after it) back: which bins are non-empty, column lengths.
+        SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t) + sizeof(batch_alphabet_t),
+                                     cudaMemcpyDeviceToHost, s));
+        return {};
+    });
+    if (!status.ok()) return status;
+    launches += 3 + (levenshtein ? 2 + (call.has_candidates ? 1 : 0) : 0);
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
     batch_alphabet_t const &alphabet_host = *context->alphabet_host();
@@ -590,6 +687,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     struct job_t {
         job_kind_t kind;
         int variant; // cell bits, rows per lane, or words
+        int warps;   // warps per CTA of the 16x2 launches
         int key_begin, key_end;
         std::uint64_t pairs;
         int ctas;
@@ -607,7 +705,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             int const ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
             std::size_t const bytes =
                 align_up(cells_per_warp * 4 * (std::size_t)ctas * (std::size_t)band_warps_per_cta(), 256);
-            jobs[job_count++] = {job_band_k, 32, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here,
+            jobs[job_count++] = {job_band_k, 32, 0, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here,
                                  ctas, scratch_total, bytes};
             scratch_total += bytes;
         }
@@ -621,7 +719,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
         std::size_t const bytes = align_up(cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta, 256);
-        jobs[job_count++] = {job_dp_k, cell_bits, key_begin, key_begin + bin_dp_classes_k, pairs_here, ctas,
+        jobs[job_count++] = {job_dp_k, cell_bits, 0, key_begin, key_begin + bin_dp_classes_k, pairs_here, ctas,
                              scratch_total, bytes};
         scratch_total += bytes;
     }
@@ -631,13 +729,14 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t const pairs_here = pairs_in(key_begin, key_end);
         if (!pairs_here) continue;
         int const rows = 4 * (choice + 1);
-        dp_launch_shape_t const shape = dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes);
+        int const warps = engine.tuning.packed_warps[choice] ? (int)engine.tuning.packed_warps[choice] : 4;
+        dp_launch_shape_t const shape = dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
         std::uint64_t const warps_needed = (pairs_here + 1) / 2;
         std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
         std::size_t const bytes = align_up(cells_per_warp * 4 * (std::size_t)ctas * shape.warps_per_cta, 256);
-        jobs[job_count++] = {job_dp16_k, rows, key_begin, key_end, pairs_here, ctas, scratch_total, bytes};
+        jobs[job_count++] = {job_dp16_k, rows, warps, key_begin, key_end, pairs_here, ctas, scratch_total, bytes};
         scratch_total += bytes;
     }
     int myers_planes = 0;
@@ -650,7 +749,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             int const threads = myers_threads_per_cta();
             std::uint64_t const needed = (pairs_here + threads - 1) / threads;
             int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
-            jobs[job_count++] = {job_myers_k, words, key_begin, key_begin + 16, pairs_here, ctas, 0, 0};
+            jobs[job_count++] = {job_myers_k, words, 0, key_begin, key_begin + 16, pairs_here, ctas, 0, 0};
         }
     }
     if (scratch_total) {
@@ -659,7 +758,6 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     }
 
     // Fork the launches over the auxiliary streams, join them back into the call's stream.
-    static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
     // The plain form runs its launches one after another on one stream; the batched form spreads them.
     int const lanes_used = schedule == szs_gb300_schedule_plain_k ? std::min(job_count, 1)
                                                                    : std::min(job_count, (int)device_context_t::lanes_k);
@@ -668,34 +766,58 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     if (job_count) {
         SZS_TRY_CUDA(cudaEventRecord(context->compute_start, stream));
         compute_recorded = true;
-        SZS_TRY_CUDA(cudaEventRecord(context->fork, stream));
+    }
+    std::vector<unsigned char> launch_key;
+    if (graphs && job_count) {
+        for (int i = 0; i < job_count; ++i) { // field by field: the struct's padding bytes are indeterminate
+            key_append(launch_key, (int)jobs[i].kind), key_append(launch_key, jobs[i].variant);
+            key_append(launch_key, jobs[i].warps);
+            key_append(launch_key, jobs[i].key_begin), key_append(launch_key, jobs[i].key_end);
+            key_append(launch_key, jobs[i].ctas), key_append(launch_key, jobs[i].scratch_offset);
+        }
+        key_append(launch_key, packed_costs), key_append(launch_key, costs);
+        key_append(launch_key, tasks), key_append(launch_key, bins), key_append(launch_key, results);
+        key_append(launch_key, context->scratch.data), key_append(launch_key, alphabet);
+        key_append(launch_key, cells_per_warp), key_append(launch_key, myers_planes);
+        key_append(launch_key, schedule), key_append(launch_key, lanes_used);
+        key_append(launch_key, engine.kind);
+    }
+    auto issue_jobs = [&](cudaStream_t s) -> status_t {
+        SZS_TRY_CUDA(cudaEventRecord(context->fork, s));
         for (int lane = 0; lane < lanes_used; ++lane) SZS_TRY_CUDA(cudaStreamWaitEvent(context->lanes[lane], context->fork, 0));
+        for (int i = 0; i < job_count; ++i) {
+            job_t const &job = jobs[i];
+            cudaStream_t const lane_stream = context->lanes[i % lanes_used];
+            bool const traced = tracing && 2 * i + 1 < 64;
+            if (traced) cudaEventRecord(context->trace_events[2 * i], lane_stream);
+            void *scratch = static_cast<unsigned char *>(context->scratch.data) + job.scratch_offset;
+            if (job.kind == job_band_k)
+                SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins, costs,
+                                         results, scratch, cells_per_warp, job.ctas, lane_stream));
+            else if (job.kind == job_dp_k)
+                SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
+                                       bins, costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
+            else if (job.kind == job_dp16_k)
+                SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
+                                         bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
+                                         lane_stream));
+            else
+                SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, schedule != szs_gb300_schedule_plain_k, tasks,
+                                          bins, alphabet, results, job.ctas, lane_stream));
+            if (traced) cudaEventRecord(context->trace_events[2 * i + 1], lane_stream);
+        }
+        for (int lane = 0; lane < lanes_used; ++lane) {
+            SZS_TRY_CUDA(cudaEventRecord(context->joins[lane], context->lanes[lane]));
+            SZS_TRY_CUDA(cudaStreamWaitEvent(s, context->joins[lane], 0));
+        }
+        return {};
+    };
+    if (job_count) {
+        status = issue_or_replay(context->launch_graphs, launch_key, launches_replayed, issue_jobs);
+        if (!status.ok()) return status;
+        launches += job_count;
     }
-    for (int i = 0; i < job_count; ++i) {
-        job_t const &job = jobs[i];
-        cudaStream_t const lane_stream = context->lanes[i % lanes_used];
-        bool const traced = tracing && 2 * i + 1 < 64;
-        if (traced) cudaEventRecord(context->trace_events[2 * i], lane_stream);
-        void *scratch = static_cast<unsigned char *>(context->scratch.data) + job.scratch_offset;
-        if (job.kind == job_band_k)
-            SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins, costs,
-                                     results, scratch, cells_per_warp, job.ctas, lane_stream));
-        else if (job.kind == job_dp_k)
-            SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
-                                   bins, costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
-        else if (job.kind == job_dp16_k)
-            SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
-                                     bins, packed_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
-        else
-            SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, schedule != szs_gb300_schedule_plain_k, tasks,
-                                      bins, alphabet, results, job.ctas, lane_stream));
-        if (traced) cudaEventRecord(context->trace_events[2 * i + 1], lane_stream);
-        ++launches;
-    }
-    for (int lane = 0; lane < lanes_used; ++lane) {
-        SZS_TRY_CUDA(cudaEventRecord(context->joins[lane], context->lanes[lane]));
-        SZS_TRY_CUDA(cudaStreamWaitEvent(stream, context->joins[lane], 0));
-    }
+    if (graphs && prologue_replayed && (launches_replayed || !job_count)) ++stats.graph_replays;
 
     if (compute_recorded) SZS_TRY_CUDA(cudaEventRecord(context->compute_stop, stream));
 
@@ -834,6 +956,34 @@ sz_status_t exec_pairwise(void *engine_handle, void *handle, sz_sequence_u64tape
 }
 
 bool engine_handle_valid(void *engine_handle) noexcept { return as_engine(engine_handle, -1) != nullptr; }
+
+sz_status_t set_tuning(void *engine_handle, szs_gb300_tuning_t const *tuning, char const **error_message) noexcept {
+    engine_t *engine = as_engine(engine_handle, -1);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!tuning) {
+        engine->tuning = szs_gb300_tuning_t {};
+        return report({}, error_message);
+    }
+    for (int k = 0; k < 16; ++k) {
+        int const rows = tuning->packed_rows[k], bits = tuning->cell_bits[k];
+        if (rows != 0 && rows != 4 && rows != 8 && rows != 12 && rows != 16)
+            return report({sz_unexpected_dimensions_k, "Rows per lane must be 0, 4, 8, 12 or 16"}, error_message);
+        if (bits != 0 && bits != 32)
+            return report({sz_unexpected_dimensions_k, "Cell bits must be 0 or 32"}, error_message);
+    }
+    for (int choice = 0; choice < 4; ++choice)
+        if (tuning->packed_warps[choice] > 8)
+            return report({sz_unexpected_dimensions_k, "Warps per CTA must be at most 8"}, error_message);
+    engine->tuning = *tuning;
+    return report({}, error_message);
+}
+
+sz_status_t get_tuning(void *engine_handle, szs_gb300_tuning_t *tuning, char const **error_message) noexcept {
+    engine_t *engine = as_engine(engine_handle, -1);
+    if (!engine || !tuning) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    *tuning = engine->tuning;
+    return report({}, error_message);
+}
 
 } // namespace szs_gb300
 
@@ -1349,6 +1499,16 @@ SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine_handle, szs_gb
     if (!engine || !stats) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
     *stats = engine->stats;
     return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_engine_set_tuning(void *engine, szs_gb300_tuning_t const *tuning,
+                                                      char const **error_message) {
+    return set_tuning(engine, tuning, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_engine_get_tuning(void *engine, szs_gb300_tuning_t *tuning,
+                                                      char const **error_message) {
+    return get_tuning(engine, tuning, error_message);
 }
 
 } // extern "C"

@@ -9,14 +9,12 @@ namespace szs_gb300 {
 
 namespace {
 
-constexpr int dp16_threads_k = 128;
-
 template <int kind_, bool affine_, int rows_>
-dp_launch_shape_t dp16_shape_rows(int classes) {
+dp_launch_shape_t dp16_shape_rows(int classes, int warps) {
     using policy_t = dp16_policy_t<kind_, affine_, rows_>;
     dp_launch_shape_t shape;
-    shape.threads_per_cta = dp16_threads_k;
-    shape.warps_per_cta = dp16_threads_k / 32;
+    shape.threads_per_cta = warps * 32;
+    shape.warps_per_cta = warps;
     shape.rows_per_lane = rows_;
     shape.shared_bytes = dp16_shared_bytes<policy_t>(shape.warps_per_cta, classes);
     auto kernel = dp16_wavefront_kernel<policy_t>;
@@ -30,12 +28,12 @@ dp_launch_shape_t dp16_shape_rows(int classes) {
 }
 
 template <int kind_, bool affine_>
-dp_launch_shape_t dp16_shape_of(int rows, int classes) {
+dp_launch_shape_t dp16_shape_of(int rows, int classes, int warps) {
     switch (rows) {
-    case 4: return dp16_shape_rows<kind_, affine_, 4>(classes);
-    case 8: return dp16_shape_rows<kind_, affine_, 8>(classes);
-    case 12: return dp16_shape_rows<kind_, affine_, 12>(classes);
-    case 16: return dp16_shape_rows<kind_, affine_, 16>(classes);
+    case 4: return dp16_shape_rows<kind_, affine_, 4>(classes, warps);
+    case 8: return dp16_shape_rows<kind_, affine_, 8>(classes, warps);
+    case 12: return dp16_shape_rows<kind_, affine_, 12>(classes, warps);
+    case 16: return dp16_shape_rows<kind_, affine_, 16>(classes, warps);
     default: return dp_launch_shape_t {0, 0, 0, 0, 0};
     }
 }
@@ -43,13 +41,13 @@ dp_launch_shape_t dp16_shape_of(int rows, int classes) {
 template <int kind_, bool affine_, int rows_>
 cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
-                             std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+                             std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
     using policy_t = dp16_policy_t<kind_, affine_, rows_>;
-    int const shared = dp16_shared_bytes<policy_t>(dp16_threads_k / 32, costs.classes);
+    int const shared = dp16_shared_bytes<policy_t>(warps, costs.classes);
     auto kernel = dp16_wavefront_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
     if (status != cudaSuccess) return status;
-    kernel<<<ctas, dp16_threads_k, shared, stream>>>(tasks, bins, key_begin, key_end, costs, results,
+    kernel<<<ctas, warps * 32, shared, stream>>>(tasks, bins, key_begin, key_end, costs, results,
                                                      static_cast<std::uint32_t *>(scratch), scratch_cells_per_warp);
     return cudaGetLastError();
 }
@@ -57,12 +55,12 @@ cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *task
 template <int kind_, bool affine_>
 cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                            score_costs_t const &costs, std::int64_t *results, void *scratch,
-                           std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+                           std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
     switch (rows) {
-    case 4: return dp16_launch_rows<kind_, affine_, 4>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
-    case 8: return dp16_launch_rows<kind_, affine_, 8>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
-    case 12: return dp16_launch_rows<kind_, affine_, 12>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
-    case 16: return dp16_launch_rows<kind_, affine_, 16>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, stream);
+    case 4: return dp16_launch_rows<kind_, affine_, 4>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 8: return dp16_launch_rows<kind_, affine_, 8>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 12: return dp16_launch_rows<kind_, affine_, 12>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 16: return dp16_launch_rows<kind_, affine_, 16>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -80,16 +78,18 @@ cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t con
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes) {
-    SZS_DP16_DISPATCH(dp16_shape_of, rows, classes)
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps) {
+    if (warps < 1 || warps > 8) return dp_launch_shape_t {0, 0, 0, 0, 0};
+    SZS_DP16_DISPATCH(dp16_shape_of, rows, classes, warps)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
 cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
+                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
+    if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
     SZS_DP16_DISPATCH(dp16_launch_of, rows, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
-                      ctas, stream)
+                      ctas, warps, stream)
     return cudaErrorInvalidValue;
 }
 

@@ -87,7 +87,8 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     std::uint64_t const span = maximize ? n + m : (n > m ? n : m);
     std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;
     bool const fits32_early = reach < (1ull << 31) - 1;
-    if (n > (std::uint64_t)band_min_rows_k && fits32_early) {
+    int const length_class = min(15, floor_log2_u64(n));
+    if (n > (std::uint64_t)args.band_min_rows && fits32_early) {
         // Long pairs take the band in both forms; the plain form keeps them in one bin, in input order.
         if (args.force_route >= 0) {
             info.key = bin_band_begin_k;
@@ -98,7 +99,7 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         info.key = bin_band_begin_k + (bin_dp_classes_k - 1 - size_class);
         return info;
     }
-    bool const packed = args.packed_allowed && reach < 32767 &&
+    bool const packed = args.packed_allowed && reach < 32767 && args.cell_bits[length_class] != 32 &&
                         (args.kind != kind_levenshtein_k || (args.alphabet && args.alphabet->symbols <= 32));
     if (packed) {
         if (args.force_route >= 0) {
@@ -107,12 +108,15 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         }
         // Rows per lane: the fewest instructions for strips(R) x (m + 31) steps x (7 R + 40) per step.
         int best_choice = 0;
-        float best_cost = 3.4e38f;
-        for (int choice = 0; choice < dp16_row_choices_k; ++choice) {
-            std::uint64_t const rows = 4u * (choice + 1);
-            std::uint64_t const strips = (n + 32 * rows - 1) / (32 * rows);
-            float const cost = (float)strips * (float)(m + 31) * (7.0f * rows + 40.0f);
-            if (cost < best_cost) best_cost = cost, best_choice = choice;
+        if (args.packed_rows[length_class]) best_choice = args.packed_rows[length_class] / 4 - 1; // tuned
+        else {
+            float best_cost = 3.4e38f;
+            for (int choice = 0; choice < dp16_row_choices_k; ++choice) {
+                std::uint64_t const rows = 4u * (choice + 1);
+                std::uint64_t const strips = (n + 32 * rows - 1) / (32 * rows);
+                float const cost = (float)strips * (float)(m + 31) * (7.0f * rows + 40.0f);
+                if (cost < best_cost) best_cost = cost, best_choice = choice;
+            }
         }
         int size_class = (int)(2.0f * __log2f((float)(n * m))) - 20;
         size_class = size_class < 0 ? 0 : (size_class > dp16_classes_per_rows_k - 1 ? dp16_classes_per_rows_k - 1
@@ -226,8 +230,9 @@ __global__ void plan_scatter_kernel(plan_args_t const args, plan_bins_t *__restr
 /** Marks every byte value present in a tape's data range [offsets[0], offsets[count]), read on the device; 16 bytes
  *  per load where aligned. Grid-stride, so the grid does not depend on the data size. */
 __global__ void alphabet_mark_kernel(tape_t const tape, std::uint32_t *__restrict__ symbol_mask) {
-    __shared__ std::uint32_t mask[8];
-    if (threadIdx.x < 8) mask[threadIdx.x] = 0;
+    // One flag byte per symbol, set with plain stores (every writer stores 1), folded into the mask at the end.
+    __shared__ __align__(16) std::uint8_t seen[256];
+    for (unsigned i = threadIdx.x; i < 256; i += blockDim.x) seen[i] = 0;
     __syncthreads();
     std::uint64_t first, last;
     if (tape.offset_bits == 32) {
@@ -240,39 +245,42 @@ __global__ void alphabet_mark_kernel(tape_t const tape, std::uint32_t *__restric
     }
     std::uint8_t const *data = tape.base + first;
     std::uint64_t const length = last - first;
-    std::uint32_t local[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(data);
     std::uint64_t head = (16 - (address & 15)) & 15;
     if (head > length) head = length;
     std::uint64_t const thread = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     std::uint64_t const threads = (std::uint64_t)gridDim.x * blockDim.x;
-    if (thread < head) {
-        std::uint32_t const b = data[thread];
-        local[b >> 5] |= 1u << (b & 31);
-    }
+    if (thread < head) seen[data[thread]] = 1;
     std::uint64_t const body = (length - head) / 16;
     uint4 const *vectors = reinterpret_cast<uint4 const *>(data + head);
-    for (std::uint64_t v = thread; v < body; v += threads) {
-        uint4 const x = __ldg(vectors + v);
-        std::uint32_t const words[4] = {x.x, x.y, x.z, x.w};
+    // Four 16-byte loads in flight per thread before their flags are stored (the pass is bound by HBM).
+    constexpr int unroll = 4;
+    for (std::uint64_t v0 = thread; v0 < body; v0 += threads * unroll) {
+        uint4 x[unroll];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int u = 0; u < unroll; ++u) {
+            std::uint64_t const v = v0 + u * threads;
+            // Past the end: repeat the first byte, which is in the data (body > 0 implies length >= 16).
+            std::uint32_t const filler = std::uint32_t(data[head]) * 0x01010101u;
+            x[u] = v < body ? __ldcs(vectors + v) : make_uint4(filler, filler, filler, filler);
+        }
 #pragma unroll
-            for (int s = 0; s < 32; s += 8) {
-                std::uint32_t const b = (words[k] >> s) & 0xFF;
-                local[b >> 5] |= 1u << (b & 31);
-            }
+        for (int u = 0; u < unroll; ++u) {
+            std::uint32_t const words[4] = {x[u].x, x[u].y, x[u].z, x[u].w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int s = 0; s < 32; s += 8) seen[(words[k] >> s) & 0xFF] = 1;
+        }
     }
     std::uint64_t const tail_begin = head + body * 16;
-    if (thread < length - tail_begin) {
-        std::uint32_t const b = data[tail_begin + thread];
-        local[b >> 5] |= 1u << (b & 31);
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (local[k]) atomicOr(&mask[k], local[k]);
+    if (thread < length - tail_begin) seen[data[tail_begin + thread]] = 1;
     __syncthreads();
-    if (threadIdx.x < 8 && mask[threadIdx.x]) atomicOr(&symbol_mask[threadIdx.x], mask[threadIdx.x]);
+    if (threadIdx.x < 8) {
+        std::uint32_t word = 0;
+        for (int b = 0; b < 32; ++b) word |= std::uint32_t(seen[threadIdx.x * 32 + b] != 0) << b;
+        if (word) atomicOr(&symbol_mask[threadIdx.x], word);
+    }
 }
 
 /** Dense codes for the marked bytes; `bits` = planes the Myers kernel needs (1..8). Clears the mask afterwards so
@@ -330,7 +338,7 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
 cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
                             batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream) {
     std::uint32_t *mask = alphabet->mask_scratch;
-    int const grid = sm_count * 2;
+    int const grid = sm_count * 8;
     alphabet_mark_kernel<<<grid, 256, 0, stream>>>(queries, mask);
     if (has_candidates) alphabet_mark_kernel<<<grid, 256, 0, stream>>>(candidates, mask);
     alphabet_codes_kernel<<<1, 32, 0, stream>>>(mask, alphabet);

@@ -31,7 +31,7 @@ constexpr int bin_dp16_classes_k = 64;
 constexpr int dp16_row_choices_k = 4;       // rows per lane 4, 8, 12, 16
 constexpr int dp16_classes_per_rows_k = 16; // size classes within one rows-per-lane choice
 constexpr int bin_band_begin_k = 400;
-constexpr int band_min_rows_k = 1024; // pairs whose shorter side exceeds this are scored by a whole CTA
+constexpr int band_min_rows_k = 1024; // default: pairs whose shorter side exceeds this are scored by a whole CTA
 constexpr int myers_max_words_k = 16;
 
 /** Which pairs a call scores. */
@@ -63,6 +63,10 @@ struct plan_args_t {
     int force_route;        // -1: normal planning; otherwise one bin per route, input order (the plain form)
     int packed_allowed;     // 1 if the 16x2 route may hold the substitution costs in int8 profiles
     batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)
+    // Tuning by length class k = floor(log2(shorter side)), 15 for everything longer.
+    std::uint8_t packed_rows[16];     // 0: instruction-count model; else rows per lane 4, 8, 12, 16
+    std::uint8_t cell_bits[16];       // 0: narrowest safe; 32: never 16-bit cells
+    std::uint32_t band_min_rows;      // shorter sides above this take the band
 };
 
 /** Per-bin counters the planner fills. */

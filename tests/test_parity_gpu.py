@@ -303,3 +303,59 @@ def test_levenshtein_large_costs(szs, port, costs):
     engine = szs.LevenshteinDistances(*costs)
     got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
     np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("family,costs", [("lev", (0, 1, 1, 1)), ("lev", (0, 2, 3, 1)), ("nw", (-11, -1)), ("sw", (-5, -2))])
+def test_graph_replay_reads_fresh_inputs(szs, port, family, costs):
+    """Device-resident calls are captured as CUDA graphs and replayed; a replay must score the bytes currently in
+    the buffers, and a new alphabet or a new shape must not replay a stale graph."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(31)
+    b2c, table = dna_tables()
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    lengths_a = rng.integers(0, 700, size=300)
+    lengths_b = rng.integers(0, 700, size=300)
+    lengths_a[:3] = [1500, 2100, 40]  # a band pair and a 32-bit pair among the packed ones
+    lengths_b[:3] = [1400, 2200, 3000]
+    offsets_a = np.concatenate([[0], np.cumsum(lengths_a)]).astype(np.int64)
+    offsets_b = np.concatenate([[0], np.cumsum(lengths_b)]).astype(np.int64)
+    data_a = torch.empty(int(offsets_a[-1]), dtype=torch.uint8, device="cuda")
+    data_b = torch.empty(int(offsets_b[-1]), dtype=torch.uint8, device="cuda")
+    first = szs.Strs.from_buffers(data_a, torch.from_numpy(offsets_a).cuda())
+    second = szs.Strs.from_buffers(data_b, torch.from_numpy(offsets_b).cuda())
+    out = torch.empty(300, dtype=torch.int64, device="cuda")
+    before = engine.stats()["graph_replays"]
+    for round_, alphabet in enumerate([b"ACGT", b"ACGT", b"ACGT", b"AC", b"ACGT"]):
+        letters = np.frombuffer(alphabet, dtype=np.uint8)
+        host_a = rng.choice(letters, size=int(offsets_a[-1])).astype(np.uint8)
+        host_b = rng.choice(letters, size=int(offsets_b[-1])).astype(np.uint8)
+        shared = min(len(host_a), len(host_b)) // 3
+        host_b[:shared] = host_a[:shared]  # related stretches: larger local scores
+        data_a.copy_(torch.from_numpy(host_a))
+        data_b.copy_(torch.from_numpy(host_b))
+        engine.pairwise(first, second, out=out)
+        want = port.pairs(oracle_costs, (host_a, offsets_a), (host_b, offsets_b))
+        np.testing.assert_array_equal(out.cpu().numpy(), want, err_msg=f"round {round_}")
+    assert engine.stats()["graph_replays"] - before >= 2
+
+
+@pytest.mark.parametrize("tuning", [
+    {"packed_rows": [4] * 16, "packed_warps": [1, 2, 8, 3]},
+    {"packed_rows": [16] * 16, "band_min_rows": 300, "packed_warps": [8, 8, 8, 8]},
+    {"cell_bits": [32] * 16, "band_min_rows": 4096},
+    {"packed_rows": [12] * 8 + [8] * 8, "cell_bits": [0, 0, 0, 0, 0, 32, 0, 32] + [0] * 8},
+], ids=["rows4", "rows16-lowband", "wide-only", "mixed"])
+@pytest.mark.parametrize("family,costs", [("nw", (-11, -1)), ("sw", (-5, -5)), ("lev", (0, 2, 3, 1))])
+def test_any_tuning_keeps_scores(szs, port, tuning, family, costs):
+    """Tunings only move pairs between routes and launch shapes: every tuning gives the oracle's scores."""
+    rng = np.random.default_rng(17)
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = protein_tables(rng) if family == "nw" else dna_tables()
+    lengths = [(int(rng.integers(0, 1500)), int(rng.integers(0, 1500))) for _ in range(120)]
+    lengths += [(3000, 2500), (600, 4000), (5, 5000)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    engine.set_tuning(tuning)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))

@@ -126,3 +126,29 @@ def test_serving_workload_shape():
         lengths = np.diff(r["first"][1])
         assert lengths.min() >= 16 and lengths.max() <= 300
         assert r["cells"] == int(np.dot(lengths, np.diff(r["second"][1])))
+
+
+def test_tuning_round_trip_and_validation():
+    from stringzillas_gb300 import autotune, workloads as w
+    engine = szs.NeedlemanWunschScores(*w.protein_table(), open=-11, extend=-1)
+    assert engine.get_tuning() == {"packed_rows": [0] * 16, "cell_bits": [0] * 16, "band_min_rows": 0,
+                                   "packed_warps": [0] * 4}
+    tuning = {"packed_rows": [0, 0, 0, 4, 4, 8, 8, 12, 16, 16, 16, 0, 0, 0, 0, 0], "cell_bits": [32] + [0] * 15,
+              "band_min_rows": 2048, "packed_warps": [2, 4, 8, 4]}
+    engine.set_tuning(tuning)
+    assert engine.get_tuning() == tuning
+    for bad in ({"packed_rows": [3] * 16}, {"cell_bits": [16] * 16}, {"packed_warps": [9, 0, 0, 0]},
+                {"packed_rows": [4] * 15}, {"bogus": 1}):
+        with pytest.raises(ValueError):
+            engine.set_tuning(bad)
+    assert engine.get_tuning() == tuning  # rejected tunings leave the installed one
+    engine.set_tuning(None)
+    assert engine.get_tuning()["band_min_rows"] == 0
+    # Families and applying a table.
+    assert autotune.family_of(engine) == "nw-affine"
+    assert autotune.family_of(szs.LevenshteinDistances()) == "lev-unit"
+    assert autotune.family_of(szs.LevenshteinDistances(0, 2, 3, 3)) == "lev-linear"
+    assert autotune.family_of(szs.SmithWatermanScores(*w.dna_table(), open=-5, extend=-5)) == "sw-linear"
+    table = {"families": {"nw-affine": {"tuning": tuning}}}
+    assert autotune.apply(engine, table) and engine.get_tuning() == tuning
+    assert not autotune.apply(szs.LevenshteinDistances(), table)
