@@ -121,6 +121,8 @@ class Tuning(ctypes.Structure):
         ("cell_bits", ctypes.c_uint8 * 16),
         ("band_min_rows", ctypes.c_uint32),
         ("packed_warps", ctypes.c_uint32 * 4),
+        ("band_min_rows_packed", ctypes.c_uint32),
+        ("pipeline_chunk_kb", ctypes.c_uint32),
     ]
 
 

@@ -29,6 +29,7 @@ CLASSES = range(3, 11)        # shorter sides 8 .. 2047 (longer pairs take the b
 ROWS = (4, 8, 12, 16)
 WARPS = (2, 4, 8)
 BAND_THRESHOLDS = (512, 1024, 2048, 4096)
+PACKED_BAND_THRESHOLDS = (1024, 2048, 4096, 8192)
 
 
 def family_of(engine) -> str:
@@ -90,7 +91,7 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
     engine = make_engine()
     # While the warp routes are measured, keep every measured class off the band.
     table = {"packed_rows": [0] * 16, "cell_bits": [0] * 16, "band_min_rows": 1 << (max(CLASSES) + 1),
-             "packed_warps": [0] * 4}
+             "packed_warps": [0] * 4, "band_min_rows_packed": 1 << (max(CLASSES) + 1)}
     measurements = {}
     rows_votes = {}
     for k in CLASSES:
@@ -133,7 +134,8 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
         measurements[f"warps per CTA, R={rows}"] = {str(w_): cells / (ms * 1e6) for w_, ms in timings.items()}
         log(f"  {family:10s} R={rows:2d}: warps per CTA {best} "
             + " ".join(f"{w_}={cells / (ms * 1e6):7.0f}" for w_, ms in timings.items()))
-    # Band threshold on a batch of long pairs (shorter sides log-uniform in [256, 8192]).
+    # Band thresholds on batches of long pairs (shorter sides log-uniform in [256, 8192]): first for pairs on
+    # 32-bit cells (16-bit cells switched off while measuring), then for pairs that fit 16-bit cells.
     count = 512
     lengths = [np.exp(rng.uniform(np.log(256), np.log(8192), size=count)).astype(np.int64) for _ in range(2)]
     tapes = []
@@ -144,14 +146,17 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
             rng.choice(alphabet, size=int(offsets[-1])).astype(np.uint8), offsets)))
     cells = int(np.dot(lengths[0], lengths[1]))
     out = np.empty(count, dtype=engine._dtype)
-    timings = {}
-    for threshold in BAND_THRESHOLDS:
-        engine.set_tuning(dict(table, band_min_rows=threshold))
-        timings[threshold] = _time(engine, tapes[0], tapes[1], out, repeats=2)
-    best = min(timings, key=timings.get)
-    table["band_min_rows"] = best
-    measurements["band threshold"] = {str(t): cells / (ms * 1e6) for t, ms in timings.items()}
-    log(f"  {family:10s} band threshold {best} " + " ".join(f"{t}={cells / (ms * 1e6):7.0f}"
+    for field, thresholds, trial_base in (
+            ("band_min_rows", BAND_THRESHOLDS, dict(table, cell_bits=[32] * 16)),
+            ("band_min_rows_packed", PACKED_BAND_THRESHOLDS, dict(table))):
+        timings = {}
+        for threshold in thresholds:
+            engine.set_tuning(dict(trial_base, **{field: threshold}))
+            timings[threshold] = _time(engine, tapes[0], tapes[1], out, repeats=2)
+        best = min(timings, key=timings.get)
+        table[field] = best
+        measurements[field] = {str(t): cells / (ms * 1e6) for t, ms in timings.items()}
+        log(f"  {family:10s} {field} {best} " + " ".join(f"{t}={cells / (ms * 1e6):7.0f}"
                                                         for t, ms in timings.items()))
     return table, measurements
 

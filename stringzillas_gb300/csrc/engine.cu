@@ -153,7 +153,7 @@ static bool device_accessible(void const *pointer) noexcept {
  *  buffer addresses, grid sizes). A call whose key matches replays the graph instead of issuing its launches.
  */
 struct graph_cache_t {
-    static constexpr int capacity_k = 8;
+    static constexpr int capacity_k = 32;
     struct entry_t {
         std::vector<unsigned char> key;
         cudaGraphExec_t exec = nullptr;
@@ -216,6 +216,16 @@ struct device_context_t {
     cudaEvent_t trace_events[64] = {nullptr};
     graph_cache_t prologue_graphs; // alphabet + plan + plan readback
     graph_cache_t launch_graphs;   // the scoring kernels of a plan
+    // Pipelined host-input calls: every chunk's copy is queued on `copy_stream` up front, into its own slot of
+    // `chunk_inputs`; chunk c is scored as soon as its copy has landed, while the later copies continue.
+    static constexpr int max_chunks_k = 64;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copied[max_chunks_k] = {nullptr};
+    cudaEvent_t pipe_start = nullptr, pipe_stop = nullptr;
+    device_buffer_t chunk_inputs;
+    device_context_t *partner = nullptr; // second context of pipelined calls: its chunks alternate with this one's
+    bool deferred = false, deferred_compute = false;
+    std::uint64_t deferred_launches = 0;
 
     status_t prepare(int device_index) noexcept {
         if (ready) return {};
@@ -229,6 +239,10 @@ struct device_context_t {
         SZS_TRY_CUDA(cudaEventCreate(&compute_stop));
         for (auto &event : trace_events) SZS_TRY_CUDA(cudaEventCreate(&event));
         SZS_TRY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        SZS_TRY_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+        for (auto &event : copied) SZS_TRY_CUDA(cudaEventCreateWithFlags(&event, cudaEventDisableTiming));
+        SZS_TRY_CUDA(cudaEventCreate(&pipe_start));
+        SZS_TRY_CUDA(cudaEventCreate(&pipe_stop));
         for (int i = 0; i < lanes_k; ++i) {
             SZS_TRY_CUDA(cudaStreamCreateWithFlags(&lanes[i], cudaStreamNonBlocking));
             SZS_TRY_CUDA(cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming));
@@ -256,6 +270,17 @@ struct device_context_t {
         cudaSetDevice(device);
         cudaStreamSynchronize(own_stream);
         prologue_graphs.release(), launch_graphs.release();
+        if (copy_stream) cudaStreamSynchronize(copy_stream), cudaStreamDestroy(copy_stream);
+        for (auto &event : copied)
+            if (event) cudaEventDestroy(event);
+        if (pipe_start) cudaEventDestroy(pipe_start);
+        if (pipe_stop) cudaEventDestroy(pipe_stop);
+        chunk_inputs.release();
+        if (partner) {
+            partner->release();
+            delete partner;
+            partner = nullptr;
+        }
         control.release(), inputs.release(), work.release(), scratch.release();
         readback.release(), results_host.release();
         if (start) cudaEventDestroy(start);
@@ -507,6 +532,8 @@ struct call_t {
     int mode = mode_cross_k;
     std::int64_t *out = nullptr;
     std::size_t stride = 0;
+    bool pre_staged = false;           // the tapes below are already on the device (a chunk of a pipelined call)
+    tape_t staged_queries {}, staged_candidates {};
 };
 
 static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &stream, engine_t &engine,
@@ -528,8 +555,14 @@ static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &str
  *  One call on an explicit device context and stream. The engine is only read (costs, kind, schedule), so several
  *  contexts may run calls of the same engine at once; @p stats receives the call's timings and counters.
  */
+static status_t finish_deferred(device_context_t *context, szs_gb300_stats_t &stats) noexcept;
+
+/**
+ *  @param defer  pairwise calls with host results only: return once the work is queued, without waiting for it;
+ *                `finish_deferred` later waits and fills @p stats (the pipelined driver keeps two chunks in flight).
+ */
 static status_t run_on(engine_t const &engine, device_context_t *context, cudaStream_t stream, call_t const &call,
-                       int schedule, szs_gb300_stats_t &stats) noexcept {
+                       int schedule, szs_gb300_stats_t &stats, bool defer = false) noexcept {
     status_t status;
     std::uint64_t const queries_count = call.queries.count;
     std::uint64_t const candidates_count = call.has_candidates ? call.candidates.count : queries_count;
@@ -553,26 +586,38 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
 
     // Stage inputs.
     staging_plan_t query_plan, candidate_plan;
-    status = plan_staging(call.queries, query_plan, stream);
-    if (!status.ok()) return status;
-    if (call.has_candidates) {
-        status = plan_staging(call.candidates, candidate_plan, stream);
+    if (call.pre_staged) {
+        query_plan.offsets_on_device = query_plan.data_on_device = true;
+        candidate_plan.offsets_on_device = candidate_plan.data_on_device = true;
+    }
+    else {
+        status = plan_staging(call.queries, query_plan, stream);
         if (!status.ok()) return status;
+        if (call.has_candidates) {
+            status = plan_staging(call.candidates, candidate_plan, stream);
+            if (!status.ok()) return status;
+        }
     }
     std::size_t const query_area = align_up(query_plan.offsets_bytes, 256) + align_up(query_plan.data_bytes, 256);
     std::size_t const candidate_area =
         call.has_candidates ? align_up(candidate_plan.offsets_bytes, 256) + align_up(candidate_plan.data_bytes, 256)
                             : 0;
-    status = context->inputs.reserve(query_area + candidate_area + 512, stream);
-    if (!status.ok()) return status;
-    unsigned char *inputs_area = static_cast<unsigned char *>(context->inputs.data);
-    status = stage_tape(call.queries, query_plan, inputs_area, args.queries, stream);
-    if (!status.ok()) return status;
-    if (call.has_candidates) {
-        status = stage_tape(call.candidates, candidate_plan, inputs_area + query_area, args.candidates, stream);
-        if (!status.ok()) return status;
+    if (call.pre_staged) {
+        args.queries = call.staged_queries;
+        args.candidates = call.has_candidates ? call.staged_candidates : call.staged_queries;
     }
-    else args.candidates = args.queries;
+    else {
+        status = context->inputs.reserve(query_area + candidate_area + 512, stream);
+        if (!status.ok()) return status;
+        unsigned char *inputs_area = static_cast<unsigned char *>(context->inputs.data);
+        status = stage_tape(call.queries, query_plan, inputs_area, args.queries, stream);
+        if (!status.ok()) return status;
+        if (call.has_candidates) {
+            status = stage_tape(call.candidates, candidate_plan, inputs_area + query_area, args.candidates, stream);
+            if (!status.ok()) return status;
+        }
+        else args.candidates = args.queries;
+    }
 
     // Work buffers: tasks, then dense results.
     std::size_t const tasks_bytes = align_up(args.pairs * sizeof(pair_task_t), 256);
@@ -596,6 +641,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     std::memcpy(args.packed_rows, engine.tuning.packed_rows, 16);
     std::memcpy(args.cell_bits, engine.tuning.cell_bits, 16);
     args.band_min_rows = engine.tuning.band_min_rows ? engine.tuning.band_min_rows : (std::uint32_t)band_min_rows_k;
+    args.band_min_rows_packed = engine.tuning.band_min_rows_packed ? engine.tuning.band_min_rows_packed
+                                                                   : (std::uint32_t)band_min_rows_packed_k;
     bool const levenshtein = engine.kind == kind_levenshtein_k;
 
     static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
@@ -838,6 +885,12 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             SZS_TRY_CUDA(cudaMemcpyAsync(call.out, results, args.pairs * sizeof(std::int64_t), cudaMemcpyDeviceToHost,
                                          stream));
             SZS_TRY_CUDA(cudaEventRecord(context->stop, stream));
+            if (defer) {
+                context->deferred = true;
+                context->deferred_compute = compute_recorded;
+                context->deferred_launches = launches;
+                return {};
+            }
             SZS_TRY_CUDA(cudaStreamSynchronize(stream));
         }
         else {
@@ -888,12 +941,193 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     return {};
 }
 
+/** Waits for a deferred call on @p context and reports it like `run_on` would have. */
+static status_t finish_deferred(device_context_t *context, szs_gb300_stats_t &stats) noexcept {
+    if (!context->deferred) return {};
+    context->deferred = false;
+    SZS_TRY_CUDA(cudaEventSynchronize(context->stop));
+    SZS_TRY_CUDA(cudaGetLastError());
+    if (context->bins_host()->error_flags)
+        return {sz_status_unknown_k, "A long pair's band of warps stopped waiting for its neighbour (bounded wait "
+                                     "expired); its score was not computed"};
+    float elapsed = 0, compute = 0;
+    cudaEventElapsedTime(&elapsed, context->start, context->stop);
+    if (context->deferred_compute) cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
+    stats.last_call_ms = elapsed;
+    stats.last_compute_ms = compute;
+    stats.last_launches = context->deferred_launches;
+    stats.kernel_launches += context->deferred_launches;
+    return {};
+}
+
+static bool pinned_host(void const *pointer) noexcept {
+    if (!pointer) return false;
+    cudaPointerAttributes attributes;
+    if (cudaPointerGetAttributes(&attributes, pointer) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attributes.type == cudaMemoryTypeHost;
+}
+
+constexpr std::size_t pipeline_chunk_bytes_k = std::size_t(64) << 20; // default input bytes per pipelined chunk
+
+/**
+ *  Pairwise calls on large pinned-host tapes: the pairs are cut into chunks of about equal input bytes and every
+ *  chunk's host-to-device copy is queued at once on the context's copy stream, each into its own slot; chunk c is
+ *  planned and scored on the call's stream as soon as its own copy has landed, while the later copies continue, so
+ *  the link stays busy and scoring hides behind it. Each chunk is one ordinary call on device-resident tapes
+ *  (`pre_staged`), so results equal the unchunked call's.
+ */
+static status_t run_pipelined(engine_t const &engine, device_context_t *context, cudaStream_t stream,
+                              call_t const &call, int schedule, szs_gb300_stats_t &stats, int chunks) noexcept {
+    tape_view_t const tapes[2] = {call.queries, call.candidates};
+    std::uint64_t const pairs = call.queries.count;
+    auto bytes_before = [&](std::uint64_t p) { // input bytes of pairs [0, p) of both tapes
+        return (host_offset(tapes[0], p) - host_offset(tapes[0], 0)) + (host_offset(tapes[1], p) - host_offset(tapes[1], 0));
+    };
+    std::uint64_t const total = bytes_before(pairs);
+    std::vector<std::uint64_t> cuts(chunks + 1, pairs);
+    cuts[0] = 0;
+    for (int c = 1; c < chunks; ++c) { // first pair whose prefix reaches c / chunks of the bytes
+        std::uint64_t const target = total / chunks * c;
+        std::uint64_t low = cuts[c - 1], high = pairs;
+        while (low < high) {
+            std::uint64_t const mid = low + (high - low) / 2;
+            if (bytes_before(mid) < target) low = mid + 1;
+            else high = mid;
+        }
+        cuts[c] = low;
+    }
+    std::size_t const offset_size = call.queries.offset_bits == 32 ? 4 : 8;
+    std::vector<std::size_t> slot(chunks + 1, 0); // byte offset of each chunk's slot
+    for (int c = 0; c < chunks; ++c) {
+        std::uint64_t const count = cuts[c + 1] - cuts[c];
+        std::size_t area = 0;
+        for (auto const &tape : tapes)
+            area += align_up((count + 1) * offset_size, 256) +
+                    align_up(host_offset(tape, cuts[c + 1]) - host_offset(tape, cuts[c]), 256);
+        slot[c + 1] = slot[c] + area;
+    }
+    status_t status = context->chunk_inputs.reserve(slot[chunks], stream);
+    if (!status.ok()) return status;
+    auto *area = static_cast<unsigned char *>(context->chunk_inputs.data);
+
+    std::vector<tape_t> staged(2 * chunks);
+    SZS_TRY_CUDA(cudaEventRecord(context->pipe_start, stream));
+    // Earlier work on the call's stream may still read the slots: the copies wait for it.
+    SZS_TRY_CUDA(cudaStreamWaitEvent(context->copy_stream, context->pipe_start, 0));
+    for (int c = 0; c < chunks; ++c) {
+        unsigned char *cursor = area + slot[c];
+        std::uint64_t const first = cuts[c], count = cuts[c + 1] - cuts[c];
+        for (int t = 0; t < 2; ++t) {
+            tape_view_t const &tape = tapes[t];
+            std::size_t const offsets_bytes = (count + 1) * offset_size;
+            SZS_TRY_CUDA(cudaMemcpyAsync(cursor, static_cast<unsigned char const *>(tape.offsets) + first * offset_size,
+                                         offsets_bytes, cudaMemcpyHostToDevice, context->copy_stream));
+            tape_t &out = staged[2 * c + t];
+            out.offsets = cursor;
+            out.count = count;
+            out.offset_bits = tape.offset_bits;
+            cursor += align_up(offsets_bytes, 256);
+            std::uint64_t const begin = host_offset(tape, first), end = host_offset(tape, first + count);
+            if (end > begin)
+                SZS_TRY_CUDA(cudaMemcpyAsync(cursor, tape.data + begin, end - begin, cudaMemcpyHostToDevice,
+                                             context->copy_stream));
+            out.base = reinterpret_cast<std::uint8_t const *>(cursor) - begin; // offsets stay absolute
+            cursor += align_up(end - begin, 256);
+        }
+        SZS_TRY_CUDA(cudaEventRecord(context->copied[c], context->copy_stream));
+    }
+    // Chunks alternate between this context (on the call's stream) and its partner (on the partner's stream), so
+    // chunk c + 1 is planned and launched while chunk c's kernels still drain.
+    if (!context->partner) {
+        context->partner = new (std::nothrow) device_context_t();
+        if (!context->partner) return {sz_bad_alloc_k, nullptr};
+        status = context->partner->prepare(context->device);
+        if (!status.ok()) {
+            context->partner->release();
+            delete context->partner;
+            context->partner = nullptr;
+            return status;
+        }
+    }
+    device_context_t *const contexts[2] = {context, context->partner};
+    cudaStream_t const streams[2] = {stream, context->partner->own_stream};
+    SZS_TRY_CUDA(cudaStreamWaitEvent(streams[1], context->pipe_start, 0));
+    szs_gb300_stats_t chunk_stats[2] {};
+    std::uint64_t cells = 0, launches = 0, graph_replays = 0;
+    double compute_ms = 0;
+    auto settle = [&](int which) -> status_t { // waits for the chunk in flight on contexts[which], if any
+        if (!contexts[which]->deferred) return {};
+        std::uint64_t const before = chunk_stats[which].kernel_launches;
+        status_t const finished = finish_deferred(contexts[which], chunk_stats[which]);
+        if (!finished.ok()) return finished;
+        launches += chunk_stats[which].kernel_launches - before;
+        compute_ms += chunk_stats[which].last_compute_ms;
+        return {};
+    };
+    for (int c = 0; c < chunks && status.ok(); ++c) {
+        int const which = c & 1;
+        status = settle(which); // the chunk this context ran two chunks ago
+        if (!status.ok()) break;
+        call_t chunk = call;
+        chunk.pre_staged = true;
+        chunk.staged_queries = staged[2 * c];
+        chunk.staged_candidates = staged[2 * c + 1];
+        chunk.queries.count = chunk.candidates.count = cuts[c + 1] - cuts[c];
+        chunk.out = call.out + cuts[c];
+        if (!chunk.queries.count) continue;
+        cudaError_t const waited = cudaStreamWaitEvent(streams[which], context->copied[c], 0);
+        if (waited != cudaSuccess) {
+            status = from_cuda(waited);
+            break;
+        }
+        chunk_stats[which].graph_replays = 0;
+        status = run_on(engine, contexts[which], streams[which], chunk, schedule, chunk_stats[which], true);
+        if (!status.ok()) break;
+        cells += chunk_stats[which].last_cells, graph_replays += chunk_stats[which].graph_replays;
+    }
+    for (int which = 0; which < 2; ++which) {
+        status_t const settled = settle(which);
+        if (status.ok()) status = settled;
+    }
+    if (!status.ok()) {
+        cudaStreamSynchronize(context->copy_stream);
+        cudaStreamSynchronize(streams[1]);
+        cudaStreamSynchronize(stream);
+        return status;
+    }
+    SZS_TRY_CUDA(cudaEventRecord(context->partner->stop, streams[1]));
+    SZS_TRY_CUDA(cudaStreamWaitEvent(stream, context->partner->stop, 0));
+    SZS_TRY_CUDA(cudaEventRecord(context->pipe_stop, stream));
+    SZS_TRY_CUDA(cudaEventSynchronize(context->pipe_stop));
+    float elapsed = 0;
+    cudaEventElapsedTime(&elapsed, context->pipe_start, context->pipe_stop);
+    stats.last_pairs = pairs, stats.last_cells = cells, stats.last_launches = launches;
+    stats.last_call_ms = elapsed, stats.last_compute_ms = compute_ms;
+    stats.kernel_launches += launches, stats.graph_replays += graph_replays;
+    return {};
+}
+
 static status_t run_call(engine_t &engine, void *scope_handle, call_t const &call) noexcept {
     int device = 0;
     cudaStream_t stream = nullptr;
     device_context_t *context = nullptr;
     status_t status = resolve_scope(scope_handle, device, stream, engine, context);
     if (!status.ok()) return status;
+    if (call.mode == mode_pairwise_k && call.queries.count == call.candidates.count && call.queries.count > 1 &&
+        !call.pre_staged && pinned_host(call.queries.offsets) && pinned_host(call.candidates.offsets) &&
+        pinned_host(call.queries.data) && pinned_host(call.candidates.data) && pinned_host(call.out)) {
+        std::uint64_t const bytes = (host_offset(call.queries, call.queries.count) - host_offset(call.queries, 0)) +
+                                    (host_offset(call.candidates, call.candidates.count) - host_offset(call.candidates, 0));
+        std::size_t const chunk_bytes = engine.tuning.pipeline_chunk_kb
+                                            ? std::size_t(engine.tuning.pipeline_chunk_kb) << 10
+                                            : pipeline_chunk_bytes_k;
+        int const chunks = (int)std::min<std::uint64_t>(device_context_t::max_chunks_k,
+                                                        std::min<std::uint64_t>(call.queries.count, bytes / chunk_bytes));
+        if (chunks >= 2) return run_pipelined(engine, context, stream, call, engine.schedule, engine.stats, chunks);
+    }
     return run_on(engine, context, stream, call, engine.schedule, engine.stats);
 }
 

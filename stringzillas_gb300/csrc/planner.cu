@@ -88,7 +88,10 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;
     bool const fits32_early = reach < (1ull << 31) - 1;
     int const length_class = min(15, floor_log2_u64(n));
-    if (n > (std::uint64_t)args.band_min_rows && fits32_early) {
+    bool const packed = args.packed_allowed && reach < 32767 && args.cell_bits[length_class] != 32 &&
+                        (args.kind != kind_levenshtein_k || (args.alphabet && args.alphabet->symbols <= 32));
+    std::uint64_t const band_rows = packed ? args.band_min_rows_packed : args.band_min_rows;
+    if (n > band_rows && fits32_early) {
         // Long pairs take the band in both forms; the plain form keeps them in one bin, in input order.
         if (args.force_route >= 0) {
             info.key = bin_band_begin_k;
@@ -99,8 +102,6 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         info.key = bin_band_begin_k + (bin_dp_classes_k - 1 - size_class);
         return info;
     }
-    bool const packed = args.packed_allowed && reach < 32767 && args.cell_bits[length_class] != 32 &&
-                        (args.kind != kind_levenshtein_k || (args.alphabet && args.alphabet->symbols <= 32));
     if (packed) {
         if (args.force_route >= 0) {
             info.key = bin_dp16_begin_k + 16; // plain form: one bin (8 rows per lane), input order

@@ -31,7 +31,8 @@ constexpr int bin_dp16_classes_k = 64;
 constexpr int dp16_row_choices_k = 4;       // rows per lane 4, 8, 12, 16
 constexpr int dp16_classes_per_rows_k = 16; // size classes within one rows-per-lane choice
 constexpr int bin_band_begin_k = 400;
-constexpr int band_min_rows_k = 1024; // default: pairs whose shorter side exceeds this are scored by a whole CTA
+constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shorter side exceeds this take a whole CTA
+constexpr int band_min_rows_packed_k = 4096; // default for pairs that fit 16-bit cells (their warp route is 2x denser)
 constexpr int myers_max_words_k = 16;
 
 /** Which pairs a call scores. */
@@ -66,7 +67,8 @@ struct plan_args_t {
     // Tuning by length class k = floor(log2(shorter side)), 15 for everything longer.
     std::uint8_t packed_rows[16];     // 0: instruction-count model; else rows per lane 4, 8, 12, 16
     std::uint8_t cell_bits[16];       // 0: narrowest safe; 32: never 16-bit cells
-    std::uint32_t band_min_rows;      // shorter sides above this take the band
+    std::uint32_t band_min_rows;      // shorter sides above this take the band (pairs on 32-bit cells)
+    std::uint32_t band_min_rows_packed; // the same for pairs that fit 16-bit cells
 };
 
 /** Per-bin counters the planner fills. */

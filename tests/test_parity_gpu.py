@@ -341,7 +341,7 @@ def test_graph_replay_reads_fresh_inputs(szs, port, family, costs):
 
 @pytest.mark.parametrize("tuning", [
     {"packed_rows": [4] * 16, "packed_warps": [1, 2, 8, 3]},
-    {"packed_rows": [16] * 16, "band_min_rows": 300, "packed_warps": [8, 8, 8, 8]},
+    {"packed_rows": [16] * 16, "band_min_rows": 300, "packed_warps": [8, 8, 8, 8], "band_min_rows_packed": 300},
     {"cell_bits": [32] * 16, "band_min_rows": 4096},
     {"packed_rows": [12] * 8 + [8] * 8, "cell_bits": [0, 0, 0, 0, 0, 32, 0, 32] + [0] * 8},
 ], ids=["rows4", "rows16-lowband", "wide-only", "mixed"])
@@ -359,3 +359,32 @@ def test_any_tuning_keeps_scores(szs, port, tuning, family, costs):
     engine.set_tuning(tuning)
     got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("family", ["lev", "sw"])
+def test_pipelined_pinned_host_call(szs, port, family):
+    """Pairwise calls on large pinned host tapes are cut into chunks whose copies overlap the previous chunk's
+    scoring; the chunked call must equal the oracle and the device-resident call."""
+    torch = pytest.importorskip("torch")
+    from stringzillas_gb300 import workloads as w
+    count = 420_000 if family == "lev" else 700_000
+    (fd, fo), (sd, so) = w.levenshtein_reads(count, 100, 300, 0.05, 0.02, seed=3) if family == "lev" else \
+        w.levenshtein_reads(count, 60, 100, 0.10, 0.02, seed=4)
+    assert fd.nbytes + sd.nbytes > 2 * (48 << 20), "the call must span several chunks"
+    b2c, table = dna_tables()
+    engine, oracle_costs = make_engine(szs, family, (0, 1, 1, 1) if family == "lev" else (-5, -2), b2c, table)
+    pinned = [torch.from_numpy(x).pin_memory() for x in (fd, fo.astype(np.uint64).view(np.int64),
+                                                          sd, so.astype(np.uint64).view(np.int64))]
+    first = szs.Strs.from_buffers(pinned[0], pinned[1])
+    second = szs.Strs.from_buffers(pinned[2], pinned[3])
+    want = port.pairs(oracle_costs, (fd, fo), (sd, so))
+    for chunk_kb in (0, 4096):  # the default chunks, then about forty smaller ones
+        engine.set_tuning({"pipeline_chunk_kb": chunk_kb})
+        out = torch.full((count,), -7, dtype=torch.int64).pin_memory()
+        engine.pairwise(first, second, out=out)
+        stats = engine.stats()
+        assert stats["last_pairs"] == count and stats["last_cells"] == w.cells((fd, fo), (sd, so))
+        np.testing.assert_array_equal(out.numpy(), want)
+    device = szs.to_device(szs.Strs.from_buffers(fd, fo.astype(np.uint64)))
+    device_b = szs.to_device(szs.Strs.from_buffers(sd, so.astype(np.uint64)))
+    np.testing.assert_array_equal(engine.pairwise(device, device_b).astype(np.int64), want)
