@@ -58,6 +58,11 @@ WORKLOADS = {
 }
 
 
+# DRAM bytes per step of the dominant kernels, from one ncu capture of the same command
+# (profiles/myers_c2_dram_traffic.txt: dram__bytes_read.sum + dram__bytes_write.sum over one step's launches).
+DRAM_TRAFFIC_PER_STEP = {"c2": 681.1e6 + 0.51e6}
+
+
 def parse_args():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -458,7 +463,8 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (129 MB), no flush between steps",
                        "parallelism": f"pairs: each of {world} ranks scores its own batch, no collective"},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm_peak, "traffic": None,
+                         "frac": achieved_gbs / hbm_peak, "traffic": DRAM_TRAFFIC_PER_STEP.get(args.workload),
+                         "traffic_unit": "bytes per step (all scoring launches of one step)",
                          "note": f"peak of {peak_source}; the path is integer-issue bound, see roofline_int"},
             "roofline_int": {"bound": "int_pipe", "achieved": int_ops / step_compute_s / 1e12,
                              "peak": None if int_peak is None else int_peak / 1e12, "unit": "Tops/s",
