@@ -31,6 +31,7 @@ UNITS = [
     ("kernels_dp", "kernels_dp.cu", []),
     ("kernels_dp16", "kernels_dp16.cu", []),
     ("kernels_band", "kernels_band.cu", []),
+    ("kernels_band16", "kernels_band16.cu", []),
     ("probe", "probe.cu", []),
     ("static_scratch", "static_scratch.cu", []),
     ("server", "server.cu", []),

@@ -57,6 +57,7 @@ struct band_shared_t {
     std::int32_t warp_result[band_warps_k];
     std::uint32_t pair_index;
     std::uint32_t failed;
+    std::uint32_t redo; // 16-bit band: the pair reached the 16-bit limit and is scored again on 32-bit cells
 };
 
 template <typename policy_>

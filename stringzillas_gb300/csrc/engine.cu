@@ -321,6 +321,7 @@ struct engine_t {
     bool unit_levenshtein = false;
     bool packed_profile_fits = false; // every substitution cost (minus `open` for affine gaps) fits a signed byte
     szs_gb300_tuning_t tuning {};     // zeros: built-in choices
+    int local_gain = -1;              // local scores with non-positive gaps: largest substitution gain (>= 0)
     device_context_t devices[max_devices_k];
     szs_gb300_stats_t stats {};
     ~engine_t() {
@@ -634,6 +635,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.match = costs.match, args.mismatch = costs.mismatch;
     args.unit_levenshtein = engine.unit_levenshtein ? 1 : 0;
     args.magnitude = engine.magnitude;
+    args.local_gain = engine.local_gain;
     args.steps_beyond_span = costs.affine ? 3 : 1;
     args.force_route = schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
@@ -714,9 +716,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         return total;
     };
 
-    // 16x2 packed wavefront: Levenshtein engines score over the batch alphabet's codes.
+    // 16x2 routes (packed wavefront, 16-bit band): Levenshtein engines score over the batch alphabet's codes.
     score_costs_t packed_costs = costs;
-    if (levenshtein && pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k)) {
+    if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
+                        pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k))) {
         int const symbols = (int)alphabet_host.symbols;
         packed_costs.classes = symbols;
         for (int b = 0; b < 256; ++b)
@@ -730,7 +733,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
 
     // The launch list, longest pairs first (64- and 32-bit wavefront, packed with the most rows per lane, then the
     // bit-parallel kernels by word count), so the routes' tails overlap each other instead of adding up.
-    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k };
+    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k };
     struct job_t {
         job_kind_t kind;
         int variant; // cell bits, rows per lane, or words
@@ -743,7 +746,23 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     job_t jobs[40];
     int job_count = 0;
     std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
+    std::size_t const band16_words_per_slot = align_up((std::size_t)plan.max_cols + 1, 64);
     std::size_t scratch_total = 0;
+    {
+        std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
+        if (pairs_here) {
+            dp_launch_shape_t const shape = band16_shape(engine.kind, costs.affine != 0, packed_costs.classes);
+            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
+            int const ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+            // Local scores keep room for a 32-bit ring: a pair that reaches the 16-bit limit is scored again.
+            std::size_t const ring_scale = engine.kind == kind_smith_waterman_k ? 2 : 1;
+            std::size_t const bytes = align_up(band16_words_per_slot * 4 * ring_scale * (std::size_t)ctas *
+                                                   (std::size_t)band_warps_per_cta(), 256);
+            jobs[job_count++] = {job_band16_k, 16, 0, bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k,
+                                 pairs_here, ctas, scratch_total, bytes};
+            scratch_total += bytes;
+        }
+    }
     {
         std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
         if (pairs_here) {
@@ -841,6 +860,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             if (job.kind == job_band_k)
                 SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins, costs,
                                          results, scratch, cells_per_warp, job.ctas, lane_stream));
+            else if (job.kind == job_band16_k)
+                SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
+                                           packed_costs, results, scratch, band16_words_per_slot, job.ctas,
+                                           lane_stream));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                        bins, costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
@@ -927,7 +950,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     if (compute_recorded) cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
     stats.last_compute_ms = compute;
     if (tracing) {
-        static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits"};
+        static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits",
+                                            "band16 bits"};
         for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
             float ms = 0, offset = 0;
             cudaEventElapsedTime(&ms, context->trace_events[2 * i], context->trace_events[2 * i + 1]);
@@ -1332,6 +1356,17 @@ sz_status_t create_engine(int kind, int match, int mismatch, int open, int exten
     }
     engine->magnitude = std::max(magnitude, 1);
     engine->packed_profile_fits = packed_profile_fits(costs);
+    if (kind == kind_smith_waterman_k && open <= 0 && extend <= 0) {
+        // The bound of a local score: every used substitution cost, at most, per diagonal step.
+        bool used[32] = {};
+        for (int b = 0; b < 256; ++b) used[byte_to_class[b] & 31] = true;
+        int gain = 0;
+        for (int row = 0; row < 32; ++row)
+            for (int column = 0; column < 32; ++column)
+                if (used[row] && used[column]) gain = std::max(gain, (int)table[row * 32 + column]);
+        engine->local_gain = gain;
+        costs.local_limit16 = 32767 - gain;
+    }
     *engine_out = engine;
     return report({}, error_message);
 }

@@ -1,0 +1,75 @@
+/**
+ *  @file kernels_band16.cu
+ *  @brief Instantiations and launcher of the 16-bit band kernel (dp_band16.cuh).
+ */
+#include "dp_band16.cuh"
+#include "launchers.h"
+
+namespace szs_gb300 {
+
+namespace {
+
+constexpr int band16_rows_per_lane_k = 8;
+
+template <int kind_, bool affine_>
+using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k>;
+
+template <int kind_, bool affine_>
+dp_launch_shape_t band16_shape_of(int classes) {
+    using policy_t = band16_instance_t<kind_, affine_>;
+    dp_launch_shape_t shape;
+    shape.threads_per_cta = band_warps_k * 32;
+    shape.warps_per_cta = band_warps_k;
+    shape.rows_per_lane = band16_rows_per_lane_k;
+    shape.shared_bytes = band16_shared_bytes<policy_t>(classes);
+    auto kernel = band16_kernel<policy_t>;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shape.shared_bytes);
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, shape.threads_per_cta, shape.shared_bytes) !=
+        cudaSuccess)
+        blocks = 0;
+    shape.ctas_per_sm = blocks;
+    return shape;
+}
+
+template <int kind_, bool affine_>
+cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                             score_costs_t const &costs, std::int64_t *results, void *scratch,
+                             std::size_t ring_words_per_slot, int ctas, cudaStream_t stream) {
+    using policy_t = band16_instance_t<kind_, affine_>;
+    int const shared = band16_shared_bytes<policy_t>(costs.classes);
+    auto kernel = band16_kernel<policy_t>;
+    cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
+    if (status != cudaSuccess) return status;
+    kernel<<<ctas, band_warps_k * 32, shared, stream>>>(tasks, bins, key_begin, key_end, costs, results,
+                                                         static_cast<std::uint32_t *>(scratch), ring_words_per_slot);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+#define SZS_BAND16_DISPATCH(call_, ...)                                                                              \
+    switch (kind * 2 + (affine ? 1 : 0)) {                                                                           \
+    case 0: return call_<kind_levenshtein_k, false>(__VA_ARGS__);                                                    \
+    case 1: return call_<kind_levenshtein_k, true>(__VA_ARGS__);                                                     \
+    case 2: return call_<kind_needleman_wunsch_k, false>(__VA_ARGS__);                                               \
+    case 3: return call_<kind_needleman_wunsch_k, true>(__VA_ARGS__);                                                \
+    case 4: return call_<kind_smith_waterman_k, false>(__VA_ARGS__);                                                 \
+    case 5: return call_<kind_smith_waterman_k, true>(__VA_ARGS__);                                                  \
+    default: break;                                                                                                  \
+    }
+
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes) {
+    SZS_BAND16_DISPATCH(band16_shape_of, classes)
+    return dp_launch_shape_t {0, 0, 0, 0, 0};
+}
+
+cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
+                          plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                          std::size_t ring_words_per_slot, int ctas, cudaStream_t stream) {
+    SZS_BAND16_DISPATCH(band16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                        ring_words_per_slot, ctas, stream)
+    return cudaErrorInvalidValue;
+}
+
+} // namespace szs_gb300

@@ -62,6 +62,16 @@ cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream);
 
+/** Launch shape of the 16-bit band kernel (one CTA per long pair, two row strips per warp in 16x2 cells). */
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes);
+
+/** Runs the 16-bit band kernel over bins [key_begin, key_end). `scratch` holds `ctas * band_warps_per_cta()` ring
+ *  slots of `ring_words_per_slot` 32-bit words (twice that for local scores, which may rescore a pair on 32-bit
+ *  cells). Bounded waits that give up set bit 0 of `bins->error_flags`. */
+cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
+                          plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                          std::size_t ring_words_per_slot, int ctas, cudaStream_t stream);
+
 /** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
  *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be
  *  shorter (the plain schedule puts every bit-parallel pair in the 16-word bin). */

@@ -88,18 +88,27 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;
     bool const fits32_early = reach < (1ull << 31) - 1;
     int const length_class = min(15, floor_log2_u64(n));
-    bool const packed = args.packed_allowed && reach < 32767 && args.cell_bits[length_class] != 32 &&
+    // Local scores with non-positive gaps stay in [0, gain * min(n, m)] (a local path gains at most one substitution
+    // per diagonal step) and their gap tracks never fall below open + 2 extend: a tighter bound than the reach.
+    std::uint64_t const reach16 =
+        args.local_gain >= 0 ? (std::uint64_t)args.local_gain * (n < m ? n : m) + 1 : reach;
+    bool const packed = args.packed_allowed && reach16 < 32767 && args.cell_bits[length_class] != 32 &&
                         (args.kind != kind_levenshtein_k || (args.alphabet && args.alphabet->symbols <= 32));
     std::uint64_t const band_rows = packed ? args.band_min_rows_packed : args.band_min_rows;
+    // Local scores with non-positive gaps take the 16-bit band even beyond their proven bound: the kernel checks the
+    // running maximum against the 16-bit limit and scores a pair that reached it again on 32-bit cells.
+    bool const local_band16 = args.local_gain >= 0 && args.packed_allowed && args.cell_bits[length_class] != 32;
     if (n > band_rows && fits32_early) {
-        // Long pairs take the band in both forms; the plain form keeps them in one bin, in input order.
+        // Long pairs take a band in both forms (16-bit cells when they fit); the plain form keeps them in one bin,
+        // in input order.
+        int const band_begin = (packed || local_band16) ? bin_band16_begin_k : bin_band_begin_k;
         if (args.force_route >= 0) {
-            info.key = bin_band_begin_k;
+            info.key = band_begin;
             return info;
         }
         int size_class = floor_log2_u64(n * m) - 10;
         size_class = size_class < 0 ? 0 : (size_class > bin_dp_classes_k - 1 ? bin_dp_classes_k - 1 : size_class);
-        info.key = bin_band_begin_k + (bin_dp_classes_k - 1 - size_class);
+        info.key = band_begin + (bin_dp_classes_k - 1 - size_class);
         return info;
     }
     if (packed) {

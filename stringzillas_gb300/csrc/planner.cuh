@@ -15,6 +15,7 @@
  *    [336, 400)  16x2 packed wavefront DP: key = 336 + 16 * rows-per-lane index + (15 - size class),
  *                size class ~ 2 * log2(n * m); rows per lane R in {4, 8, 12, 16}, chosen per pair
  *    [400, 432)  band (one CTA per pair, 32-bit cells): key = 400 + (31 - size class), size class ~ log2(n * m)
+ *    [432, 464)  16-bit band (one CTA per pair, 16x2 cells): same layout from 432
  */
 #pragma once
 #include "engine_types.cuh"
@@ -31,6 +32,7 @@ constexpr int bin_dp16_classes_k = 64;
 constexpr int dp16_row_choices_k = 4;       // rows per lane 4, 8, 12, 16
 constexpr int dp16_classes_per_rows_k = 16; // size classes within one rows-per-lane choice
 constexpr int bin_band_begin_k = 400;
+constexpr int bin_band16_begin_k = 432;
 constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shorter side exceeds this take a whole CTA
 constexpr int band_min_rows_packed_k = 4096; // default for pairs that fit 16-bit cells (their warp route is 2x denser)
 constexpr int myers_max_words_k = 16;
@@ -60,6 +62,7 @@ struct plan_args_t {
     int open, extend, match, mismatch;
     int unit_levenshtein;   // 0/1/1/1 Levenshtein: bit-parallel route
     int magnitude;          // max |cost| over substitution and gap costs, at least 1
+    int local_gain;         // local scores with non-positive gaps: max(0, largest substitution cost); else -1
     int steps_beyond_span;  // 1 linear, 3 affine (serial.hpp:126-140)
     int force_route;        // -1: normal planning; otherwise one bin per route, input order (the plain form)
     int packed_allowed;     // 1 if the 16x2 route may hold the substitution costs in int8 profiles

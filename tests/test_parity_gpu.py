@@ -388,3 +388,53 @@ def test_pipelined_pinned_host_call(szs, port, family):
     device = szs.to_device(szs.Strs.from_buffers(fd, fo.astype(np.uint64)))
     device_b = szs.to_device(szs.Strs.from_buffers(sd, so.astype(np.uint64)))
     np.testing.assert_array_equal(engine.pairwise(device, device_b).astype(np.int64), want)
+
+
+@pytest.mark.parametrize("family,costs", [("lev", (0, 1, 1, 1)), ("lev", (0, 2, 3, 1)), ("lev", (0, 3, 2, 2)),
+                                          ("nw", (-11, -1)), ("nw", (-4, -4)), ("sw", (-5, -2)), ("sw", (-3, -3))])
+def test_band16_route(szs, port, family, costs):
+    """Long pairs that fit 16-bit cells take the 16-bit band (two row strips per warp, 512-row super-strips):
+    shapes around the super-strip size, a high half that is all filler, and local scores near their bound."""
+    rng = np.random.default_rng(91)
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
+    if family == "nw":  # the reach bound (n + m + 4) * 11 < 32767 keeps these on 16-bit cells
+        lengths = [(601, 601), (700, 1400), (1023, 1024), (1025, 1300), (1400, 1500), (512 * 2 + 3, 1200)]
+    else:
+        lengths = [(601, 601), (700, 2400), (1024, 1024), (1025, 3000), (1536, 1600), (2049, 2100), (3000, 9000),
+                   (520, 6000)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    second[1] = first[1][:600] + second[1][600:]         # a long related stretch: large local scores
+    second[4] = first[4][100:1500] + second[4][1400:]
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    engine.set_tuning({"band_min_rows_packed": 600})
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+    # The plain form keeps the same route, in input order.
+    engine.set_schedule("plain")
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+def test_band16_local_scores_past_the_16bit_limit(szs, port):
+    """Local scores run on 16-bit cells beyond their proven bound; a pair whose maximum reaches 32767 minus the
+    largest gain is scored again on 32-bit cells inside the same CTA. Identical long strings score 2 per base."""
+    rng = np.random.default_rng(5)
+    b2c, table = dna_tables()  # match +2, mismatch -3
+    engine, oracle_costs = make_engine(szs, "sw", (-5, -2), b2c, table)
+    base = rng.choice(DNA, size=17_500)
+    first, second = [], []
+    for n, m, related in ((17_000, 17_000, True),    # 34,000: past the limit, rescored
+                          (16_383, 16_383, True),    # 32,766: at the limit (32,765), rescored
+                          (16_382, 16_382, True),    # 32,764: just below, exact on 16-bit cells
+                          (17_000, 17_400, False),   # unrelated: small score, never rescored
+                          (2_000, 3_000, True)):     # short: provably within the bound
+        a = bytes(base[:n])
+        b = bytes(base[:m]) if related else bytes(rng.choice(DNA, size=m))
+        first.append(a)
+        second.append(b)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    np.testing.assert_array_equal(got, want)
+    assert want[0] == 34_000 and want[1] == 32_766 and want[2] == 32_764
