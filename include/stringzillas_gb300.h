@@ -462,6 +462,30 @@ SZS_GB300_API sz_status_t szs_gb300_score_pairwise_noalloc_u64tape(void *engine,
 SZS_GB300_API sz_status_t szs_gb300_measure_integer_peaks(sz_size_t gpu_device, double *ops_per_second,
                                                           sz_size_t count, char const **error_message);
 
+/* ---- dense substitution tables (no counterpart in the reference) ------------------------------------------------ */
+
+/**
+ *  Needleman-Wunsch / Smith-Waterman engines over a dense 256 x 256 table, `costs[a * 256 + b]` = cost of aligning
+ *  byte a of the first string with byte b of the second, instead of the reference's 32-class fold. Every scoring
+ *  entry point accepts these engines. Each call maps the bytes its batch actually uses onto dense codes on the
+ *  device and scores over that sub-table, so a call may use at most 32 distinct byte values (more give
+ *  `sz_unexpected_dimensions_k`); the allocation-free entry point does not accept them. No counterpart in the
+ *  reference, whose engines take `byte_to_class` + a 32 x 32 table.
+ */
+SZS_GB300_API sz_status_t szs_gb300_needleman_wunsch_scores_init_dense(sz_error_cost_t const *costs,
+                                                                       sz_error_cost_t open, sz_error_cost_t extend,
+                                                                       sz_memory_allocator_t const *alloc,
+                                                                       sz_capability_t capabilities,
+                                                                       szs_needleman_wunsch_scores_t *engine,
+                                                                       char const **error_message);
+/** The Smith-Waterman counterpart of `szs_gb300_needleman_wunsch_scores_init_dense`. */
+SZS_GB300_API sz_status_t szs_gb300_smith_waterman_scores_init_dense(sz_error_cost_t const *costs,
+                                                                     sz_error_cost_t open, sz_error_cost_t extend,
+                                                                     sz_memory_allocator_t const *alloc,
+                                                                     sz_capability_t capabilities,
+                                                                     szs_smith_waterman_scores_t *engine,
+                                                                     char const **error_message);
+
 /* ---- serving loop (no counterpart in the reference) ----------------------------------------------------------- */
 
 /** A serving loop on one GPU: requests in, merged batches on the device, results out. */

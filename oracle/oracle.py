@@ -37,6 +37,7 @@ class Costs(ctypes.Structure):
         ("extend", ctypes.c_int8),
         ("byte_to_class", ctypes.c_uint8 * 256),
         ("class_costs", ctypes.c_int8 * 1024),
+        ("dense_costs", ctypes.c_void_p),
     ]
 
 
@@ -53,6 +54,16 @@ def alignment_costs(kind, byte_to_class, class_costs, open, extend) -> Costs:
     table = np.ascontiguousarray(class_costs, dtype=np.int8).reshape(1024)
     ctypes.memmove(c.byte_to_class, b2c.ctypes.data, 256)
     ctypes.memmove(c.class_costs, table.ctypes.data, 1024)
+    return c
+
+
+def dense_costs(kind, table, open, extend) -> Costs:
+    """Costs over a dense 256 x 256 table [first byte][second byte] (the engine's dense-table extension). The
+    returned object keeps the table alive."""
+    c = Costs()
+    c.kind, c.open, c.extend = kind, open, extend
+    c._dense = np.ascontiguousarray(table, dtype=np.int8).reshape(65536)
+    c.dense_costs = c._dense.ctypes.data
     return c
 
 

@@ -75,6 +75,7 @@ static inline int64_t oracle_opt_(int maximize, int64_t a, int64_t b) {
 
 static inline int64_t oracle_cost_(oracle_costs_t const *k, uint8_t a, uint8_t b) {
     if (k->kind == oracle_levenshtein_k) return a == b ? k->match : k->mismatch;
+    if (k->dense_costs) return k->dense_costs[a * 256 + b];
     return k->class_costs[k->byte_to_class[a] * 32 + k->byte_to_class[b]];
 }
 

@@ -34,6 +34,9 @@ typedef struct oracle_costs_t {
     int8_t open, extend;            /**< gap costs; `open == extend` means linear gaps */
     uint8_t byte_to_class[256];     /**< NW / SW only */
     int8_t class_costs[32 * 32];    /**< NW / SW only, row-major [first class][second class] */
+    int8_t const *dense_costs;      /**< NW / SW, optional: [first byte][second byte] 256 x 256, replaces the
+                                         class fold when set (the engine's dense-table extension; no reference
+                                         counterpart) */
 } oracle_costs_t;
 
 /** Scores one pair. Levenshtein results are non-negative for non-negative costs. */

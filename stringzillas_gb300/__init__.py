@@ -460,6 +460,29 @@ class _Alignment(_Engine):
         _native.raise_for(status, err.value, f"{self._name} initialization")
         self.description = f"open={open},extend={extend}"
 
+    @classmethod
+    def dense(cls, substitution_matrix, open=-1, extend=-1, capabilities=None):
+        """Extension: an engine over a dense 256 x 256 int8 table, ``substitution_matrix[a, b]`` = cost of aligning
+        byte a of the first string with byte b of the second (no counterpart in the reference, which folds bytes
+        into 32 classes). Each call may use at most 32 distinct byte values."""
+        if not isinstance(substitution_matrix, np.ndarray):
+            raise TypeError("substitution_matrix must be a NumPy array")
+        if substitution_matrix.shape != (256, 256):
+            raise ValueError("substitution_matrix must be a 256x256 array")
+        if substitution_matrix.dtype != np.int8:
+            raise TypeError("substitution_matrix must have int8 dtype")
+        table = np.ascontiguousarray(substitution_matrix)
+        self = cls.__new__(cls)
+        _Engine.__init__(self)
+        self._check_capabilities(capabilities)
+        open, extend = _int8("open", open), _int8("extend", extend)
+        err = ctypes.c_char_p()
+        status = getattr(lib, f"szs_gb300_{self._algo}_init_dense")(
+            table.ctypes.data, open, extend, None, 0x7FFFFFFF, ctypes.byref(self.handle), ctypes.byref(err))
+        _native.raise_for(status, err.value, f"{self._name} initialization")
+        self.description = f"open={open},extend={extend}"
+        return self
+
 
 class NeedlemanWunschScores(_Alignment):
     """Global alignment scores (maximised); pass negative gap costs."""

@@ -104,6 +104,11 @@ for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterma
     fn.restype = None
     fn.argtypes = [c_void_p]
 
+for _algo in ("needleman_wunsch_scores", "smith_waterman_scores"):
+    fn = getattr(lib, f"szs_gb300_{_algo}_init_dense")
+    fn.restype = c_status
+    fn.argtypes = [c_void_p, c_int8, c_int8, c_void_p, ctypes.c_uint32, ctypes.POINTER(c_void_p), _err]
+
 lib.szs_gb300_score_pairwise_noalloc_u64tape.restype = c_status
 lib.szs_gb300_score_pairwise_noalloc_u64tape.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, _err]
 lib.szs_gb300_engine_set_schedule.restype = c_status

@@ -322,6 +322,7 @@ struct engine_t {
     bool packed_profile_fits = false; // every substitution cost (minus `open` for affine gaps) fits a signed byte
     szs_gb300_tuning_t tuning {};     // zeros: built-in choices
     int local_gain = -1;              // local scores with non-positive gaps: largest substitution gain (>= 0)
+    std::vector<std::int8_t> dense;   // 256 x 256 [first byte][second byte] table of a dense engine, else empty
     device_context_t devices[max_devices_k];
     szs_gb300_stats_t stats {};
     ~engine_t() {
@@ -646,6 +647,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.band_min_rows_packed = engine.tuning.band_min_rows_packed ? engine.tuning.band_min_rows_packed
                                                                    : (std::uint32_t)band_min_rows_packed_k;
     bool const levenshtein = engine.kind == kind_levenshtein_k;
+    bool const dense = !engine.dense.empty();
+    bool const alphabet_pass = levenshtein || dense; // both score over the batch's own byte codes
 
     static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
     // Device-resident inputs make every launch of the call a function of bytes the call can key on, so both phases
@@ -684,7 +687,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     std::uint64_t launches = 0;
     plan_bins_t *bins = context->bins_device();
     batch_alphabet_t *alphabet = context->alphabet_device();
-    if (levenshtein) args.alphabet = alphabet;
+    if (alphabet_pass) args.alphabet = alphabet;
     std::vector<unsigned char> prologue_key;
     if (graphs) {
         key_append(prologue_key, args);
@@ -695,7 +698,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     status = issue_or_replay(context->prologue_graphs, prologue_key, prologue_replayed, [&](cudaStream_t s) -> status_t {
         // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code planes
         // by it, and the 16x2 route builds its substitution profile over it (when it has at most 32 symbols).
-        if (levenshtein)
+        if (alphabet_pass)
             SZS_TRY_CUDA(launch_alphabet(args.queries, args.candidates, call.has_candidates, alphabet,
                                          context->sm_count, s));
         SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, s));
@@ -705,7 +708,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         return {};
     });
     if (!status.ok()) return status;
-    launches += 3 + (levenshtein ? 2 + (call.has_candidates ? 1 : 0) : 0);
+    launches += 3 + (alphabet_pass ? 2 + (call.has_candidates ? 1 : 0) : 0);
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
     batch_alphabet_t const &alphabet_host = *context->alphabet_host();
@@ -716,8 +719,32 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         return total;
     };
 
+    // Dense-table engines score every route over the sub-table of the bytes this batch uses (dense codes from the
+    // alphabet pass), which must fit the kernels' 32 compact classes.
+    score_costs_t dense_costs;
+    if (dense) {
+        int const symbols = (int)alphabet_host.symbols;
+        if (symbols > 32)
+            return {sz_unexpected_dimensions_k, "A dense-table call may use at most 32 distinct byte values"};
+        dense_costs = engine.costs;
+        int byte_of_code[32] = {0};
+        for (int b = 0; b < 256; ++b)
+            if ((alphabet_host.present[b >> 5] >> (b & 31)) & 1u) byte_of_code[alphabet_host.code[b]] = b;
+        for (int b = 0; b < 256; ++b) dense_costs.byte_to_class[b] = dense_costs.byte_to_compact[b] = alphabet_host.code[b];
+        dense_costs.classes = symbols < 1 ? 1 : symbols;
+        std::memset(dense_costs.profile_table, 0, sizeof(dense_costs.profile_table));
+        std::memset(dense_costs.profile_table_t, 0, sizeof(dense_costs.profile_table_t));
+        for (int cc = 0; cc < symbols; ++cc)
+            for (int rc = 0; rc < symbols; ++rc) {
+                int const row_byte = byte_of_code[rc], column_byte = byte_of_code[cc];
+                dense_costs.profile_table[cc * 32 + rc] = engine.dense[row_byte * 256 + column_byte];
+                dense_costs.profile_table_t[cc * 32 + rc] = engine.dense[column_byte * 256 + row_byte];
+            }
+    }
+    score_costs_t const &call_costs = dense ? dense_costs : costs;
+
     // 16x2 routes (packed wavefront, 16-bit band): Levenshtein engines score over the batch alphabet's codes.
-    score_costs_t packed_costs = costs;
+    score_costs_t packed_costs = call_costs;
     if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
                         pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k))) {
         int const symbols = (int)alphabet_host.symbols;
@@ -766,7 +793,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            dp_launch_shape_t const shape = band_shape(engine.kind, costs.affine != 0, costs.classes);
+            dp_launch_shape_t const shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
             int const ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
             std::size_t const bytes =
@@ -780,7 +807,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int const key_begin = cell_bits == 32 ? bin_dp32_begin_k : bin_dp64_begin_k;
         std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + bin_dp_classes_k);
         if (!pairs_here) continue;
-        dp_launch_shape_t const shape = dp_shape(engine.kind, costs.affine != 0, cell_bits, costs.classes);
+        dp_launch_shape_t const shape = dp_shape(engine.kind, call_costs.affine != 0, cell_bits, call_costs.classes);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Wavefront kernel cannot be resident"};
         std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
@@ -841,7 +868,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             key_append(launch_key, jobs[i].key_begin), key_append(launch_key, jobs[i].key_end);
             key_append(launch_key, jobs[i].ctas), key_append(launch_key, jobs[i].scratch_offset);
         }
-        key_append(launch_key, packed_costs), key_append(launch_key, costs);
+        key_append(launch_key, packed_costs), key_append(launch_key, call_costs);
         key_append(launch_key, tasks), key_append(launch_key, bins), key_append(launch_key, results);
         key_append(launch_key, context->scratch.data), key_append(launch_key, alphabet);
         key_append(launch_key, cells_per_warp), key_append(launch_key, myers_planes);
@@ -858,15 +885,15 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             if (traced) cudaEventRecord(context->trace_events[2 * i], lane_stream);
             void *scratch = static_cast<unsigned char *>(context->scratch.data) + job.scratch_offset;
             if (job.kind == job_band_k)
-                SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins, costs,
-                                         results, scratch, cells_per_warp, job.ctas, lane_stream));
+                SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
+                                         call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
                                            lane_stream));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
-                                       bins, costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
+                                       bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
             else if (job.kind == job_dp16_k)
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
@@ -1371,6 +1398,41 @@ sz_status_t create_engine(int kind, int match, int mismatch, int open, int exten
     return report({}, error_message);
 }
 
+/** A Needleman-Wunsch or Smith-Waterman engine over a dense 256 x 256 table (see the header's extension). */
+sz_status_t create_dense_engine(int kind, int open, int extend, std::int8_t const *table, void **engine_out,
+                                char const **error_message) {
+    if (!engine_out) return report({sz_status_unknown_k, "Engine output pointer must not be NULL"}, error_message);
+    if (*engine_out) return report({sz_status_unknown_k, "Engine must be uninitialized (NULL) on entry"}, error_message);
+    if (!table) return report({sz_unexpected_dimensions_k, "The dense table must not be NULL"}, error_message);
+    engine_t *engine = new (std::nothrow) engine_t();
+    if (!engine) return report({sz_bad_alloc_k, "Failed to allocate the engine"}, error_message);
+    engine->kind = kind;
+    engine->dense.assign(table, table + 256 * 256);
+    score_costs_t &costs = engine->costs;
+    std::memset(&costs, 0, sizeof(costs));
+    costs.kind = kind;
+    costs.open = open, costs.extend = extend;
+    costs.affine = open != extend;
+    costs.classes = 1; // replaced per call by the batch's own codes
+    int magnitude = std::max(cost_abs(open), cost_abs(extend));
+    int shift = costs.affine ? open : 0, gain = 0;
+    bool fits = true;
+    for (int i = 0; i < 256 * 256; ++i) {
+        int const cost = table[i];
+        magnitude = std::max(magnitude, cost_abs(cost));
+        gain = std::max(gain, cost);
+        fits = fits && cost - shift >= -128 && cost - shift <= 127;
+    }
+    engine->magnitude = std::max(magnitude, 1);
+    engine->packed_profile_fits = fits;
+    if (kind == kind_smith_waterman_k && open <= 0 && extend <= 0) {
+        engine->local_gain = gain;
+        costs.local_limit16 = 32767 - gain;
+    }
+    *engine_out = engine;
+    return report({}, error_message);
+}
+
 void free_engine(void *handle) {
     engine_t *engine = as_engine(handle, -1);
     if (!engine) return;
@@ -1742,6 +1804,8 @@ SZS_GB300_API sz_status_t szs_gb300_score_pairwise_noalloc_u64tape(void *engine_
     scope_t *scope = as_scope(device);
     if (device && !scope) return report({sz_status_unknown_k, "Invalid device scope handle"}, error_message);
     if (scope && scope->kind == scope_cpu_k) return report({sz_device_code_mismatch_k, nullptr}, error_message);
+    if (!engine->dense.empty())
+        return report({sz_unexpected_dimensions_k, "Dense-table engines need the planned entry points"}, error_message);
     static_call_t call;
     call.costs = &engine->costs;
     call.kind = engine->kind;
@@ -1768,6 +1832,22 @@ SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine_handle, szs_gb
     if (!engine || !stats) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
     *stats = engine->stats;
     return report({}, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_needleman_wunsch_scores_init_dense(sz_error_cost_t const *costs,
+                                                                       sz_error_cost_t open, sz_error_cost_t extend,
+                                                                       sz_memory_allocator_t const *, sz_capability_t,
+                                                                       szs_needleman_wunsch_scores_t *engine,
+                                                                       char const **error_message) {
+    return create_dense_engine(kind_needleman_wunsch_k, open, extend, costs, engine, error_message);
+}
+
+SZS_GB300_API sz_status_t szs_gb300_smith_waterman_scores_init_dense(sz_error_cost_t const *costs,
+                                                                     sz_error_cost_t open, sz_error_cost_t extend,
+                                                                     sz_memory_allocator_t const *, sz_capability_t,
+                                                                     szs_smith_waterman_scores_t *engine,
+                                                                     char const **error_message) {
+    return create_dense_engine(kind_smith_waterman_k, open, extend, costs, engine, error_message);
 }
 
 SZS_GB300_API sz_status_t szs_gb300_engine_set_tuning(void *engine, szs_gb300_tuning_t const *tuning,

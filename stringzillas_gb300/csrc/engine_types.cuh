@@ -58,6 +58,7 @@ struct batch_alphabet_t {
     std::uint32_t symbols;
     std::uint32_t bits;
     std::uint32_t mask_scratch[8]; // bytes seen, accumulated by the mark pass and cleared by the code pass
+    std::uint32_t present[8];      // the bytes of the batch (bit b of word b / 32); absent bytes also have code 0
 };
 
 } // namespace szs_gb300

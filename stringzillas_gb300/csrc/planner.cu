@@ -308,7 +308,7 @@ __global__ void alphabet_codes_kernel(std::uint32_t *__restrict__ symbol_mask,
     while ((1u << bits) < next) ++bits;
     alphabet->symbols = next;
     alphabet->bits = bits;
-    for (int k = 0; k < 8; ++k) symbol_mask[k] = 0;
+    for (int k = 0; k < 8; ++k) alphabet->present[k] = symbol_mask[k], symbol_mask[k] = 0;
 }
 
 /** Dense per-pair results into the caller's matrix (device-resident output). */

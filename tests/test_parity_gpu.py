@@ -438,3 +438,41 @@ def test_band16_local_scores_past_the_16bit_limit(szs, port):
     want = port.pairs(oracle_costs, tape(first), tape(second))
     np.testing.assert_array_equal(got, want)
     assert want[0] == 34_000 and want[1] == 32_766 and want[2] == 32_764
+
+
+@pytest.mark.parametrize("family,costs", [("nw", (-11, -1)), ("nw", (-4, -4)), ("sw", (-5, -2)), ("sw", (-3, -3))])
+def test_dense_tables(szs, port, family, costs):
+    """Dense 256 x 256 tables: a dense expansion of a class fold scores like the class engine (which the reference
+    pins), and an arbitrary asymmetric dense table matches the oracle's dense restatement on every route."""
+    rng = np.random.default_rng(23)
+    b2c, table = protein_tables(rng, symmetric=False)
+    expanded = table[b2c[:, None], b2c[None, :]]  # [first byte][second byte]
+    cls = szs.NeedlemanWunschScores if family == "nw" else szs.SmithWatermanScores
+    kind = oracle.NEEDLEMAN_WUNSCH if family == "nw" else oracle.SMITH_WATERMAN
+    lengths = [(int(rng.integers(0, 900)), int(rng.integers(0, 900))) for _ in range(150)]
+    lengths += [(1100, 1350), (1400, 1200), (3000, 200)]  # band routes and long single strips
+    first = [bytes(rng.choice(PROTEIN, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(PROTEIN, size=m)) for _, m in lengths]
+    dense_engine = cls.dense(np.ascontiguousarray(expanded), open=costs[0], extend=costs[1])
+    class_engine = cls(b2c, table, open=costs[0], extend=costs[1])
+    got = dense_engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, class_engine.pairwise(szs.Strs(first), szs.Strs(second)))
+    # An arbitrary table over 24 bytes (not expressible as a 32-class fold of these letters' classes).
+    letters = np.frombuffer(b"ARNDCQEGHILKMFPSTWYVBZX*", dtype=np.uint8)
+    arbitrary = np.zeros((256, 256), dtype=np.int8)
+    arbitrary[np.ix_(letters, letters)] = rng.integers(-6, 9, size=(24, 24))
+    first = [bytes(rng.choice(letters, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(letters, size=m)) for _, m in lengths]
+    engine = cls.dense(arbitrary, open=costs[0], extend=costs[1])
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle.dense_costs(kind, arbitrary, *costs), tape(first), tape(second))
+    np.testing.assert_array_equal(got, want)
+    # A cross product and the symmetric form go through the same per-call table.
+    cross = engine(szs.Strs(first[:20]), szs.Strs(second[:15]))
+    for q in range(20):
+        np.testing.assert_array_equal(cross[q], port.pairs(oracle.dense_costs(kind, arbitrary, *costs),
+                                                           tape([first[q]] * 15), tape(second[:15])))
+    # More than 32 distinct bytes in one call is refused.
+    wide = [bytes(range(40))]
+    with pytest.raises(ValueError):
+        engine.pairwise(szs.Strs(wide), szs.Strs(wide))

@@ -153,3 +153,16 @@ def test_tuning_round_trip_and_validation():
     table = {"families": {"nw-affine": {"tuning": tuning}}}
     assert autotune.apply(engine, table) and engine.get_tuning() == tuning
     assert not autotune.apply(szs.LevenshteinDistances(), table)
+
+
+def test_dense_table_constructor_validation():
+    table = np.zeros((256, 256), dtype=np.int8)
+    engine = szs.NeedlemanWunschScores.dense(table, open=-4, extend=-1)
+    assert isinstance(engine, szs.NeedlemanWunschScores)
+    assert isinstance(szs.SmithWatermanScores.dense(table), szs.SmithWatermanScores)
+    with pytest.raises(ValueError):
+        szs.NeedlemanWunschScores.dense(np.zeros((32, 32), dtype=np.int8))
+    with pytest.raises(TypeError):
+        szs.NeedlemanWunschScores.dense(np.zeros((256, 256), dtype=np.int16))
+    with pytest.raises(TypeError):
+        szs.NeedlemanWunschScores.dense([[0] * 256] * 256)
