@@ -416,7 +416,7 @@ typedef struct szs_gb300_tuning_t {
     sz_u8_t cell_bits[16];   /**< 0 = the narrowest cells the length bound proves safe; 32 = never 16-bit cells */
     sz_u32_t band_min_rows;  /**< pairs on 32-bit cells whose shorter side exceeds this take the band (0 = 1,024) */
     sz_u32_t packed_warps[4]; /**< warps per CTA (1..8) of the 16x2 launches with 4, 8, 12, 16 rows (0 = 4) */
-    sz_u32_t band_min_rows_packed; /**< the same threshold for pairs that fit 16-bit cells (0 = 4,096) */
+    sz_u32_t band_min_rows_packed; /**< the same threshold for pairs that fit 16-bit cells (0 = 2,048) */
     sz_u32_t pipeline_chunk_kb;   /**< input KiB per chunk of a pipelined pinned-host pairwise call (0 = 64 MiB) */
 } szs_gb300_tuning_t;
 

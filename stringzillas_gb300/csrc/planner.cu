@@ -113,7 +113,7 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     }
     if (packed) {
         if (args.force_route >= 0) {
-            info.key = bin_dp16_begin_k + 16; // plain form: one bin (8 rows per lane), input order
+            info.key = bin_dp16_begin_k + dp16_classes_per_rows_k; // plain form: one bin (8 rows per lane), input order
             return info;
         }
         // Rows per lane: the fewest instructions for strips(R) x (m + 31) steps x (7 R + 40) per step.
@@ -128,10 +128,13 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
                 if (cost < best_cost) best_cost = cost, best_choice = choice;
             }
         }
-        int size_class = (int)(2.0f * __log2f((float)(n * m))) - 20;
-        size_class = size_class < 0 ? 0 : (size_class > dp16_classes_per_rows_k - 1 ? dp16_classes_per_rows_k - 1
-                                                                                     : size_class);
-        info.key = bin_dp16_begin_k + best_choice * dp16_classes_per_rows_k + (dp16_classes_per_rows_k - 1 - size_class);
+        // Quarter octaves of the shorter side, half octaves of the aspect ratio: the two pairs a warp scores at
+        // once come from one bin, so they have nearly the same strips and the same number of steps.
+        int n_class = (int)(4.0f * __log2f((float)n)) - 12;
+        n_class = n_class < 0 ? 0 : (n_class > 31 ? 31 : n_class);
+        int ratio_class = (int)(2.0f * __log2f((float)m / (float)n));
+        ratio_class = ratio_class < 0 ? 0 : (ratio_class > 7 ? 7 : ratio_class);
+        info.key = bin_dp16_begin_k + best_choice * dp16_classes_per_rows_k + 8 * (31 - n_class) + (7 - ratio_class);
         return info;
     }
     bool const fits32 = reach < (1ull << 31) - 1;
@@ -189,23 +192,27 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
     }
 }
 
-/** Pass 2: exclusive scan of bin counts (one CTA of `bin_keys_k` threads). */
+/** Pass 2: exclusive scan of bin counts (one CTA of `bin_keys_k / 2` threads, two adjacent keys each). */
 __global__ void plan_scan_kernel(plan_bins_t *__restrict__ bins) {
-    __shared__ std::uint32_t scan[bin_keys_k];
+    constexpr int threads = bin_keys_k / 2;
+    __shared__ std::uint32_t scan[threads];
     int const i = threadIdx.x;
-    std::uint32_t const own = bins->count[i];
+    std::uint32_t const first = bins->count[2 * i], second = bins->count[2 * i + 1];
+    std::uint32_t const own = first + second;
     scan[i] = own;
     __syncthreads();
-    for (int offset = 1; offset < bin_keys_k; offset <<= 1) {
+    for (int offset = 1; offset < threads; offset <<= 1) {
         std::uint32_t const add = i >= offset ? scan[i - offset] : 0u;
         __syncthreads();
         scan[i] += add;
         __syncthreads();
     }
-    bins->begin[i] = scan[i] - own;
-    bins->fill[i] = 0;
-    bins->cursor[i] = 0;
-    if (i == bin_keys_k - 1) bins->scheduled = scan[i];
+    std::uint32_t const before = scan[i] - own;
+    bins->begin[2 * i] = before;
+    bins->begin[2 * i + 1] = before + first;
+    bins->fill[2 * i] = bins->fill[2 * i + 1] = 0;
+    bins->cursor[2 * i] = bins->cursor[2 * i + 1] = 0;
+    if (i == threads - 1) bins->scheduled = scan[i];
 }
 
 /** Pass 3: write each routed pair into its bin; lanes sharing a bin reserve their slots with one atomic. */
@@ -340,7 +347,7 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
     if (status != cudaSuccess) return status;
     if (args.pairs == 0) return cudaSuccess;
     plan_count_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, bins, results);
-    plan_scan_kernel<<<1, bin_keys_k, 0, stream>>>(bins);
+    plan_scan_kernel<<<1, bin_keys_k / 2, 0, stream>>>(bins);
     plan_scatter_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, bins, tasks);
     return cudaGetLastError();
 }

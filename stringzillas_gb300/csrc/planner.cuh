@@ -12,29 +12,33 @@
  *    [0, 272)    Myers: key = words * 16 + text-length class (words 1..16)
  *    [272, 304)  32-bit wavefront DP: key = 272 + (31 - size class), size class ~ log2(n * m)
  *    [304, 336)  64-bit wavefront DP: same layout
- *    [336, 400)  16x2 packed wavefront DP: key = 336 + 16 * rows-per-lane index + (15 - size class),
- *                size class ~ 2 * log2(n * m); rows per lane R in {4, 8, 12, 16}, chosen per pair
- *    [400, 432)  band (one CTA per pair, 32-bit cells): key = 400 + (31 - size class), size class ~ log2(n * m)
- *    [432, 464)  16-bit band (one CTA per pair, 16x2 cells): same layout from 432
+ *    [336, 1360) 16x2 packed wavefront DP: key = 336 + 256 * rows-per-lane index + 8 * (31 - n class)
+ *                + (7 - ratio class), n class = 4 log2(n) - 12 (quarter octaves of the shorter side), ratio class
+ *                = 2 log2(m / n); rows per lane R in {4, 8, 12, 16}, chosen per pair. A warp scores two consecutive
+ *                pairs of a bin at once and pays for the larger of each dimension, so bins are narrow in both.
+ *    [1360, 1392) band (one CTA per pair, 32-bit cells): key = 1360 + (31 - size class), size class ~ log2(n * m)
+ *    [1392, 1424) 16-bit band (one CTA per pair, 16x2 cells): same layout from 1392
  */
 #pragma once
 #include "engine_types.cuh"
 
 namespace szs_gb300 {
 
-constexpr int bin_keys_k = 512;
+constexpr int bin_keys_k = 2048;
 constexpr int bin_myers_begin_k = 0;
 constexpr int bin_dp32_begin_k = 272;
 constexpr int bin_dp64_begin_k = 304;
 constexpr int bin_dp16_begin_k = 336;
 constexpr int bin_dp_classes_k = 32;
-constexpr int bin_dp16_classes_k = 64;
+constexpr int bin_dp16_classes_k = 1024;
 constexpr int dp16_row_choices_k = 4;       // rows per lane 4, 8, 12, 16
-constexpr int dp16_classes_per_rows_k = 16; // size classes within one rows-per-lane choice
-constexpr int bin_band_begin_k = 400;
-constexpr int bin_band16_begin_k = 432;
+constexpr int dp16_classes_per_rows_k = 256; // shape classes within one rows-per-lane choice (32 n x 8 ratio)
+constexpr int bin_band_begin_k = bin_dp16_begin_k + bin_dp16_classes_k; // 1360
+constexpr int bin_band16_begin_k = bin_band_begin_k + bin_dp_classes_k;  // 1392
+static_assert(bin_band16_begin_k + bin_dp_classes_k <= bin_keys_k, "bin layout exceeds the key space");
+static_assert(bin_keys_k % 2 == 0 && bin_keys_k / 2 <= 1024, "the scan kernel uses one CTA of bin_keys_k / 2 threads");
 constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shorter side exceeds this take a whole CTA
-constexpr int band_min_rows_packed_k = 4096; // default for pairs that fit 16-bit cells (their warp route is 2x denser)
+constexpr int band_min_rows_packed_k = 2048; // default for pairs that fit 16-bit cells (the 16-bit band above it)
 constexpr int myers_max_words_k = 16;
 
 /** Which pairs a call scores. */
