@@ -198,9 +198,13 @@ SZS_GB300_API sz_status_t szs_levenshtein_distances_u64tape(szs_levenshtein_dist
 /** Replaces stringzillas.h:223. */
 SZS_GB300_API void szs_levenshtein_distances_free(szs_levenshtein_distances_t engine);
 
-/* ---- UTF-8 Levenshtein: out of this engine's scope; present so bindings load (stringzillas.h:224-292) ---------- */
+/* ---- UTF-8 Levenshtein (replaces stringzillas.h:224-292) ------------------------------------------------------- */
 
-/** Always fails with `sz_status_unknown_k` ("not implemented by the GB300 engine"). Replaces stringzillas.h:239. */
+/**
+ *  Distances over UTF-8 code points. Each call decodes both tapes on the device the way the reference does
+ *  (lead-byte lengths, continuation bytes not checked) and numbers the batch's distinct code points; a call may
+ *  use at most 256 distinct code points (more give `sz_unexpected_dimensions_k`). Replaces stringzillas.h:239.
+ */
 SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_init(sz_error_cost_t match, sz_error_cost_t mismatch,
                                                               sz_error_cost_t open, sz_error_cost_t extend,
                                                               sz_memory_allocator_t const *alloc,

@@ -38,12 +38,20 @@ class Costs(ctypes.Structure):
         ("byte_to_class", ctypes.c_uint8 * 256),
         ("class_costs", ctypes.c_int8 * 1024),
         ("dense_costs", ctypes.c_void_p),
+        ("utf8", ctypes.c_int),
     ]
 
 
 def levenshtein_costs(match=0, mismatch=1, open=1, extend=1) -> Costs:
     c = Costs()
     c.kind, c.match, c.mismatch, c.open, c.extend = LEVENSHTEIN, match, mismatch, open, extend
+    return c
+
+
+def levenshtein_utf8_costs(match=0, mismatch=1, open=1, extend=1) -> Costs:
+    """Levenshtein over UTF-8 code points (the batch drivers decode both strings first)."""
+    c = levenshtein_costs(match, mismatch, open, extend)
+    c.utf8 = 1
     return c
 
 
@@ -150,6 +158,11 @@ class Reference:
 
     def _engine(self, costs: Costs):
         engine, err = ctypes.c_void_p(), ctypes.c_char_p()
+        if costs.kind == LEVENSHTEIN and costs.utf8:
+            rc = self.lib.szs_levenshtein_distances_utf8_init(
+                ctypes.c_int8(costs.match), ctypes.c_int8(costs.mismatch), ctypes.c_int8(costs.open),
+                ctypes.c_int8(costs.extend), None, ctypes.c_int(CAP_SERIAL), ctypes.byref(engine), ctypes.byref(err))
+            return engine, rc, "levenshtein_distances_utf8"
         if costs.kind == LEVENSHTEIN:
             rc = self.lib.szs_levenshtein_distances_init(
                 ctypes.c_int8(costs.match), ctypes.c_int8(costs.mismatch), ctypes.c_int8(costs.open),

@@ -39,6 +39,8 @@
 typedef struct oracle_scratch_t {
     int64_t *rows;      /* 2 rows of (longest second + 1) cells: M and the vertical-gap track */
     size_t rows_cells;
+    uint32_t *runes;    /* decoded code points of both strings (UTF-8 Levenshtein) */
+    size_t runes_capacity;
     uint64_t *peq;      /* 256 x words match masks for the bit-parallel method, kept all-zero between calls */
     size_t peq_words;
     uint64_t *vectors;  /* 2 x words: Pv, Mv */
@@ -46,6 +48,7 @@ typedef struct oracle_scratch_t {
 
 static void oracle_scratch_free_(oracle_scratch_t *s) {
     free(s->rows);
+    free(s->runes);
     free(s->peq);
     free(s->vectors);
     memset(s, 0, sizeof(*s));
@@ -171,6 +174,82 @@ static int64_t oracle_dp_(oracle_costs_t const *k, uint8_t const *a, size_t n, u
     return local ? best : m_row[m];
 }
 
+/**
+ *  Decodes like the reference's `sz_rune_decode_unchecked` (include/stringzilla/utf8_runes/serial.h:101-115), which
+ *  the UTF-8 distance calls rune by rune (include/stringzillas/similarities/serial.hpp:2288-2299): the length comes
+ *  from the lead byte alone (1 + [lead >= 0xC0] + [lead >= 0xE0] + [lead >= 0xF0]) and continuation bytes are not
+ *  checked, so a sequence cut off by the end of a string reads on into the bytes that follow it. Those bytes are the
+ *  next strings of the tape; past the tape's end (`limit`) they are read as 0 here.
+ */
+static size_t oracle_utf8_decode_(uint8_t const *s, size_t n, uint8_t const *limit, uint32_t *out) {
+    size_t runes = 0;
+    for (size_t i = 0; i < n; ++runes) {
+        uint8_t const lead = s[i];
+        unsigned const length = 1u + (lead >= 0xC0u) + (lead >= 0xE0u) + (lead >= 0xF0u);
+#define ORACLE_NEXT_(k) ((s + i + (k) < limit) ? (uint32_t)(s[i + (k)] & 0x3Fu) : 0u)
+        uint32_t rune;
+        switch (length) {
+        case 1: rune = lead; break;
+        case 2: rune = (uint32_t)(lead & 0x1Fu) << 6 | ORACLE_NEXT_(1); break;
+        case 3: rune = (uint32_t)(lead & 0x0Fu) << 12 | ORACLE_NEXT_(1) << 6 | ORACLE_NEXT_(2); break;
+        default: rune = (uint32_t)(lead & 0x07u) << 18 | ORACLE_NEXT_(1) << 12 | ORACLE_NEXT_(2) << 6 | ORACLE_NEXT_(3); break;
+        }
+#undef ORACLE_NEXT_
+        out[runes] = rune;
+        i += length;
+    }
+    return runes;
+}
+
+/** The Levenshtein recurrences of `oracle_dp_` over code points (uniform costs, global, minimised). */
+static int64_t oracle_rune_dp_(oracle_costs_t const *k, uint32_t const *a, size_t n, uint32_t const *b, size_t m,
+                               int64_t *rows) {
+    int const linear = k->open == k->extend;
+    int64_t const open = k->open, extend = k->extend;
+    int64_t *m_row = rows, *v_row = rows + (m + 1);
+    for (size_t j = 0; j <= m; ++j) {
+        int64_t const boundary = linear ? open * (int64_t)j : (j ? open + extend * (int64_t)(j - 1) : 0);
+        m_row[j] = boundary;
+        v_row[j] = open + extend + boundary;
+    }
+    for (size_t i = 1; i <= n; ++i) {
+        int64_t const left_boundary = linear ? open * (int64_t)i : open + extend * (int64_t)(i - 1);
+        int64_t diag = m_row[0], m_left = left_boundary, h_left = open + extend + left_boundary;
+        m_row[0] = left_boundary;
+        for (size_t j = 1; j <= m; ++j) {
+            int64_t const up = m_row[j];
+            int64_t const substitution = diag + (a[i - 1] == b[j - 1] ? k->match : k->mismatch);
+            int64_t cell;
+            if (linear) cell = oracle_opt_(0, oracle_opt_(0, up, m_left) + open, substitution);
+            else {
+                int64_t const vertical = oracle_opt_(0, up + open, v_row[j] + extend);
+                int64_t const horizontal = oracle_opt_(0, m_left + open, h_left + extend);
+                cell = oracle_opt_(0, oracle_opt_(0, vertical, horizontal), substitution);
+                v_row[j] = vertical;
+                h_left = horizontal;
+            }
+            diag = up;
+            m_row[j] = cell;
+            m_left = cell;
+        }
+    }
+    return m_row[m];
+}
+
+static int64_t oracle_score_utf8_(oracle_costs_t const *k, char const *first, size_t n, char const *first_limit,
+                                  char const *second, size_t m, char const *second_limit, oracle_scratch_t *s,
+                                  int *status) {
+    if (n + m + 8 > s->runes_capacity) {
+        uint32_t *runes = (uint32_t *)realloc(s->runes, (n + m + 8) * sizeof(uint32_t));
+        if (!runes) return *status = -1, 0;
+        s->runes = runes, s->runes_capacity = n + m + 8;
+    }
+    size_t const rn = oracle_utf8_decode_((uint8_t const *)first, n, (uint8_t const *)first_limit, s->runes);
+    size_t const rm = oracle_utf8_decode_((uint8_t const *)second, m, (uint8_t const *)second_limit, s->runes + rn);
+    if (oracle_scratch_reserve_(s, rm, 0) != 0) return *status = -1, 0;
+    return oracle_rune_dp_(k, s->runes, rn, s->runes + rn, rm, s->rows);
+}
+
 static int oracle_is_unit_levenshtein_(oracle_costs_t const *k) {
     return k->kind == oracle_levenshtein_k && k->match == 0 && k->mismatch == 1 && k->open == 1 && k->extend == 1;
 }
@@ -238,7 +317,10 @@ static void *oracle_worker_(void *arg) {
         char const *cs = job->c_data + job->c_offsets[c];
         size_t const cn = (size_t)(job->c_offsets[c + 1] - job->c_offsets[c]);
         int status = 0;
-        int64_t const score = oracle_score_with_(job->costs, qs, qn, cs, cn, &scratch, &status);
+        int64_t const score =
+            job->costs->utf8 ? oracle_score_utf8_(job->costs, qs, qn, job->q_data + job->q_offsets[job->q_count], cs,
+                                                  cn, job->c_data + job->c_offsets[job->c_count], &scratch, &status)
+                             : oracle_score_with_(job->costs, qs, qn, cs, cn, &scratch, &status);
         if (status) {
             atomic_store(&job->status, status);
             break;

@@ -37,6 +37,7 @@ typedef struct oracle_costs_t {
     int8_t const *dense_costs;      /**< NW / SW, optional: [first byte][second byte] 256 x 256, replaces the
                                          class fold when set (the engine's dense-table extension; no reference
                                          counterpart) */
+    int utf8;                       /**< Levenshtein over UTF-8 code points instead of bytes (the batch drivers) */
 } oracle_costs_t;
 
 /** Scores one pair. Levenshtein results are non-negative for non-negative costs. */

@@ -23,7 +23,8 @@ from . import _native
 from ._native import lib
 
 __all__ = [
-    "Strs", "DeviceScope", "LevenshteinDistances", "NeedlemanWunschScores", "SmithWatermanScores", "to_device",
+    "Strs", "DeviceScope", "LevenshteinDistances", "LevenshteinDistancesUTF8", "NeedlemanWunschScores",
+    "SmithWatermanScores", "to_device",
     "Server", "Ticket", "__version__", "__capabilities__",
 ]
 
@@ -427,6 +428,37 @@ class LevenshteinDistances(_Engine):
 
     def __repr__(self):
         return f"LevenshteinDistances(match,mismatch,open,extend={self.description})"
+
+
+class LevenshteinDistancesUTF8(LevenshteinDistances):
+    """Edit distances over UTF-8 code points (``LevenshteinDistancesUTF8`` of the reference). Each call numbers the
+    distinct code points of its batch on the device; a call may use at most 256 of them."""
+
+    _algo = "levenshtein_distances_utf8"
+    _name = "UTF-8 Levenshtein distances"
+
+    def __init__(self, match=0, mismatch=1, open=1, extend=1, capabilities=None):
+        _Engine.__init__(self)
+        self._check_capabilities(capabilities)
+        match, mismatch = _int8("match", match), _int8("mismatch", mismatch)
+        open, extend = _int8("open", open), _int8("extend", extend)
+        err = ctypes.c_char_p()
+        status = lib.szs_levenshtein_distances_utf8_init(match, mismatch, open, extend, None, 0x7FFFFFFF,
+                                                         ctypes.byref(self.handle), ctypes.byref(err))
+        _native.raise_for(status, err.value, "UTF-8 Levenshtein distances initialization")
+        self.description = f"{match},{mismatch},{open},{extend}"
+
+    def pairwise(self, first, second, device=None, out=None):
+        """Extension: ``out[i] = distance(first[i], second[i])`` over code points."""
+        algo = self._algo
+        try:
+            self._algo = "levenshtein_distances"  # the pairwise entry points serve every Levenshtein engine
+            return super().pairwise(first, second, device=device, out=out)
+        finally:
+            self._algo = algo
+
+    def __repr__(self):
+        return f"LevenshteinDistancesUTF8(match,mismatch,open,extend={self.description})"
 
 
 class _Alignment(_Engine):

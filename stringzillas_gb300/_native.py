@@ -87,15 +87,23 @@ lib.szs_unified_free.argtypes = [c_void_p, c_size_t]
 lib.szs_levenshtein_distances_init.restype = c_status
 lib.szs_levenshtein_distances_init.argtypes = [c_int8, c_int8, c_int8, c_int8, c_void_p, ctypes.c_uint32,
                                                ctypes.POINTER(c_void_p), _err]
+lib.szs_levenshtein_distances_utf8_init.restype = c_status
+lib.szs_levenshtein_distances_utf8_init.argtypes = [c_int8, c_int8, c_int8, c_int8, c_void_p, ctypes.c_uint32,
+                                                    ctypes.POINTER(c_void_p), _err]
 for _algo in ("needleman_wunsch_scores", "smith_waterman_scores"):
     fn = getattr(lib, f"szs_{_algo}_init")
     fn.restype = c_status
     fn.argtypes = [c_void_p, c_void_p, c_int8, c_int8, c_void_p, ctypes.c_uint32, ctypes.POINTER(c_void_p), _err]
-for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterman_scores"):
+for _algo in ("levenshtein_distances", "levenshtein_distances_utf8", "needleman_wunsch_scores",
+              "smith_waterman_scores"):
     for _suffix in ("_u32tape", "_u64tape", ""):
         fn = getattr(lib, f"szs_{_algo}{_suffix}")
         fn.restype = c_status
         fn.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, _err]
+    fn = getattr(lib, f"szs_{_algo}_free")
+    fn.restype = None
+    fn.argtypes = [c_void_p]
+for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterman_scores"):
     for _suffix in ("_pairwise_u32tape", "_pairwise_u64tape"):
         fn = getattr(lib, f"szs_{_algo}{_suffix}")
         fn.restype = c_status

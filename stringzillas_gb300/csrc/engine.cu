@@ -224,6 +224,7 @@ struct device_context_t {
     cudaEvent_t pipe_start = nullptr, pipe_stop = nullptr;
     device_buffer_t chunk_inputs;
     device_context_t *partner = nullptr; // second context of pipelined calls: its chunks alternate with this one's
+    device_buffer_t utf8;                // UTF-8 calls: code-point set, counts, offsets and transcoded tapes
     bool deferred = false, deferred_compute = false;
     std::uint64_t deferred_launches = 0;
 
@@ -276,6 +277,7 @@ struct device_context_t {
         if (pipe_start) cudaEventDestroy(pipe_start);
         if (pipe_stop) cudaEventDestroy(pipe_stop);
         chunk_inputs.release();
+        utf8.release();
         if (partner) {
             partner->release();
             delete partner;
@@ -323,6 +325,7 @@ struct engine_t {
     szs_gb300_tuning_t tuning {};     // zeros: built-in choices
     int local_gain = -1;              // local scores with non-positive gaps: largest substitution gain (>= 0)
     std::vector<std::int8_t> dense;   // 256 x 256 [first byte][second byte] table of a dense engine, else empty
+    bool utf8 = false;                // Levenshtein over UTF-8 code points (transcoded to one-byte codes per call)
     device_context_t devices[max_devices_k];
     szs_gb300_stats_t stats {};
     ~engine_t() {
@@ -560,6 +563,67 @@ static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &str
 static status_t finish_deferred(device_context_t *context, szs_gb300_stats_t &stats) noexcept;
 
 /**
+ *  UTF-8 Levenshtein: rewrites both device-resident tapes as one-byte codes of their code points (see utf8.cu), in
+ *  place of @p queries and @p candidates. A call may use at most 256 distinct code points.
+ */
+static status_t transcode_utf8(device_context_t *context, cudaStream_t stream, tape_t &queries, tape_t &candidates,
+                               bool has_candidates) noexcept {
+    tape_t *tapes[2] = {&queries, has_candidates ? &candidates : nullptr};
+    std::uint64_t first[2] = {0, 0}, end[2] = {0, 0};
+    // The tapes' extents: the transcoded data can hold no more runes than bytes.
+    for (int t = 0; t < 2; ++t) {
+        if (!tapes[t]) continue;
+        std::size_t const size = tapes[t]->offset_bits == 32 ? 4 : 8;
+        auto const *offsets = static_cast<unsigned char const *>(tapes[t]->offsets);
+        SZS_TRY_CUDA(cudaMemcpyAsync(&first[t], offsets, size, cudaMemcpyDeviceToHost, stream));
+        SZS_TRY_CUDA(cudaMemcpyAsync(&end[t], offsets + tapes[t]->count * size, size, cudaMemcpyDeviceToHost, stream));
+    }
+    SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+    std::size_t layout[2][3] = {}; // counts, offsets, data
+    std::size_t cursor = align_up(sizeof(rune_set_t), 256);
+    std::size_t scan_bytes = 0;
+    for (int t = 0; t < 2; ++t) {
+        if (!tapes[t]) continue;
+        std::uint64_t const count = tapes[t]->count;
+        layout[t][0] = cursor, cursor += align_up((count + 1) * 8, 256);
+        layout[t][1] = cursor, cursor += align_up((count + 1) * 8, 256);
+        layout[t][2] = cursor, cursor += align_up(end[t] - first[t] + 1, 256);
+        scan_bytes = std::max(scan_bytes, utf8_scan_scratch_bytes(count));
+    }
+    std::size_t const scan_at = cursor;
+    status_t status = context->utf8.reserve(cursor + align_up(scan_bytes, 256), stream);
+    if (!status.ok()) return status;
+    auto *area = static_cast<unsigned char *>(context->utf8.data);
+    auto *set = reinterpret_cast<rune_set_t *>(area);
+    SZS_TRY_CUDA(cudaMemsetAsync(set, 0, sizeof(rune_set_t), stream));
+    for (int t = 0; t < 2; ++t) {
+        if (!tapes[t]) continue;
+        auto *counts = reinterpret_cast<std::uint64_t *>(area + layout[t][0]);
+        SZS_TRY_CUDA(cudaMemsetAsync(counts, 0, (tapes[t]->count + 1) * 8, stream));
+        SZS_TRY_CUDA(launch_utf8_count(*tapes[t], end[t], counts, set, context->sm_count, stream));
+    }
+    SZS_TRY_CUDA(launch_utf8_codes(set, stream));
+    std::uint32_t seen[2] = {0, 0}; // symbols, overflow
+    SZS_TRY_CUDA(cudaMemcpyAsync(seen, &set->symbols, sizeof(seen), cudaMemcpyDeviceToHost, stream));
+    SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (seen[1] || seen[0] > 256)
+        return {sz_unexpected_dimensions_k, "A UTF-8 call may use at most 256 distinct code points"};
+    for (int t = 0; t < 2; ++t) {
+        if (!tapes[t]) continue;
+        auto const *counts = reinterpret_cast<std::uint64_t const *>(area + layout[t][0]);
+        auto *offsets = reinterpret_cast<std::uint64_t *>(area + layout[t][1]);
+        auto *data = reinterpret_cast<std::uint8_t *>(area + layout[t][2]);
+        SZS_TRY_CUDA(launch_utf8_scan(counts, offsets, tapes[t]->count, area + scan_at, scan_bytes, stream));
+        SZS_TRY_CUDA(launch_utf8_write(*tapes[t], end[t], offsets, set, data, context->sm_count, stream));
+        tapes[t]->base = data;
+        tapes[t]->offsets = offsets;
+        tapes[t]->offset_bits = 64;
+    }
+    if (!has_candidates) candidates = queries;
+    return {};
+}
+
+/**
  *  @param defer  pairwise calls with host results only: return once the work is queued, without waiting for it;
  *                `finish_deferred` later waits and fills @p stats (the pipelined driver keeps two chunks in flight).
  */
@@ -619,6 +683,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             if (!status.ok()) return status;
         }
         else args.candidates = args.queries;
+    }
+    if (engine.utf8) {
+        status = transcode_utf8(context, stream, args.queries, args.candidates, call.has_candidates);
+        if (!status.ok()) return status;
     }
 
     // Work buffers: tasks, then dense results.
@@ -1168,7 +1236,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     status_t status = resolve_scope(scope_handle, device, stream, engine, context);
     if (!status.ok()) return status;
     if (call.mode == mode_pairwise_k && call.queries.count == call.candidates.count && call.queries.count > 1 &&
-        !call.pre_staged && pinned_host(call.queries.offsets) && pinned_host(call.candidates.offsets) &&
+        !call.pre_staged && !engine.utf8 && pinned_host(call.queries.offsets) && pinned_host(call.candidates.offsets) &&
         pinned_host(call.queries.data) && pinned_host(call.candidates.data) && pinned_host(call.out)) {
         std::uint64_t const bytes = (host_offset(call.queries, call.queries.count) - host_offset(call.queries, 0)) +
                                     (host_offset(call.candidates, call.candidates.count) - host_offset(call.candidates, 0));
@@ -1291,9 +1359,10 @@ tape_view_t view_of(sz_sequence_u64tape_t const *tape) {
 
 template <typename tape_type_>
 sz_status_t score_cross(int kind, void *engine_handle, void *scope, tape_type_ const *queries,
-                        tape_type_ const *candidates, void *results, sz_size_t stride, char const **error_message) {
+                        tape_type_ const *candidates, void *results, sz_size_t stride, char const **error_message,
+                        bool utf8 = false) {
     engine_t *engine = as_engine(engine_handle, kind);
-    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!engine || engine->utf8 != utf8) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
     if (!queries || !results) return report({sz_unexpected_dimensions_k, "Queries and results must not be NULL"},
                                             error_message);
     call_t call;
@@ -1312,9 +1381,9 @@ sz_status_t score_cross(int kind, void *engine_handle, void *scope, tape_type_ c
 
 sz_status_t score_cross_sequence(int kind, void *engine_handle, void *scope, sz_sequence_t const *queries,
                                  sz_sequence_t const *candidates, void *results, sz_size_t stride,
-                                 char const **error_message) {
+                                 char const **error_message, bool utf8 = false) {
     engine_t *engine = as_engine(engine_handle, kind);
-    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    if (!engine || engine->utf8 != utf8) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
     if (!queries || !results) return report({sz_unexpected_dimensions_k, "Queries and results must not be NULL"},
                                             error_message);
     gathered_tape_t q, c;
@@ -1618,32 +1687,46 @@ SZS_GB300_API sz_status_t szs_levenshtein_distances_u64tape(szs_levenshtein_dist
 }
 SZS_GB300_API void szs_levenshtein_distances_free(szs_levenshtein_distances_t engine) { free_engine(engine); }
 
-/* UTF-8 Levenshtein: outside the engine's scope */
+/* UTF-8 Levenshtein: code points instead of bytes (transcoded to one-byte codes on the device, see utf8.cu) */
 
-SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_init(sz_error_cost_t, sz_error_cost_t, sz_error_cost_t,
-                                                              sz_error_cost_t, sz_memory_allocator_t const *,
-                                                              sz_capability_t, szs_levenshtein_distances_utf8_t *,
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_init(sz_error_cost_t match, sz_error_cost_t mismatch,
+                                                              sz_error_cost_t open, sz_error_cost_t extend,
+                                                              sz_memory_allocator_t const *, sz_capability_t,
+                                                              szs_levenshtein_distances_utf8_t *engine,
                                                               char const **error_message) {
-    return not_in_scope(error_message);
+    sz_status_t const status =
+        create_engine(kind_levenshtein_k, match, mismatch, open, extend, nullptr, nullptr, engine, error_message);
+    if (status == sz_success_k) static_cast<engine_t *>(*engine)->utf8 = true;
+    return status;
 }
-SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8(szs_levenshtein_distances_utf8_t, szs_device_scope_t,
-                                                         sz_sequence_t const *, sz_sequence_t const *, sz_size_t *,
-                                                         sz_size_t, char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8(szs_levenshtein_distances_utf8_t engine,
+                                                         szs_device_scope_t device, sz_sequence_t const *queries,
+                                                         sz_sequence_t const *candidates, sz_size_t *results,
+                                                         sz_size_t results_row_stride, char const **error_message) {
+    return score_cross_sequence(kind_levenshtein_k, engine, device, queries, candidates, results, results_row_stride,
+                                error_message, true);
 }
-SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u32tape(szs_levenshtein_distances_utf8_t,
-                                                                 szs_device_scope_t, sz_sequence_u32tape_t const *,
-                                                                 sz_sequence_u32tape_t const *, sz_size_t *,
-                                                                 sz_size_t, char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u32tape(szs_levenshtein_distances_utf8_t engine,
+                                                                 szs_device_scope_t device,
+                                                                 sz_sequence_u32tape_t const *queries,
+                                                                 sz_sequence_u32tape_t const *candidates,
+                                                                 sz_size_t *results, sz_size_t results_row_stride,
+                                                                 char const **error_message) {
+    return score_cross(kind_levenshtein_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message, true);
 }
-SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u64tape(szs_levenshtein_distances_utf8_t,
-                                                                 szs_device_scope_t, sz_sequence_u64tape_t const *,
-                                                                 sz_sequence_u64tape_t const *, sz_size_t *,
-                                                                 sz_size_t, char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_u64tape(szs_levenshtein_distances_utf8_t engine,
+                                                                 szs_device_scope_t device,
+                                                                 sz_sequence_u64tape_t const *queries,
+                                                                 sz_sequence_u64tape_t const *candidates,
+                                                                 sz_size_t *results, sz_size_t results_row_stride,
+                                                                 char const **error_message) {
+    return score_cross(kind_levenshtein_k, engine, device, queries, candidates, results, results_row_stride,
+                       error_message, true);
 }
-SZS_GB300_API void szs_levenshtein_distances_utf8_free(szs_levenshtein_distances_utf8_t) {}
+SZS_GB300_API void szs_levenshtein_distances_utf8_free(szs_levenshtein_distances_utf8_t engine) {
+    free_engine(engine);
+}
 
 /* Needleman-Wunsch */
 

@@ -23,6 +23,31 @@ cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, boo
 cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
                                   std::uint64_t stride, int sm_count, cudaStream_t stream);
 
+/** The set of a batch's code points (UTF-8 Levenshtein): open addressing over `code point + 1` (0 = empty), then
+ *  dense codes in slot order. */
+constexpr int rune_set_bits_k = 15;
+constexpr std::uint32_t rune_set_slots_k = 1u << rune_set_bits_k;
+struct rune_set_t {
+    std::uint32_t keys[rune_set_slots_k];
+    std::uint32_t codes[rune_set_slots_k];
+    std::uint32_t symbols;  // distinct code points
+    std::uint32_t overflow; // set if an insertion found no free slot
+};
+/** Counts each string's code points into `counts[i]` and inserts them into `set` (both zeroed by the caller);
+ *  `end` is the tape's last offset: a sequence cut off there reads zeros beyond it. */
+cudaError_t launch_utf8_count(tape_t const &tape, std::uint64_t end, std::uint64_t *counts, rune_set_t *set,
+                              int sm_count, cudaStream_t stream);
+/** Numbers the set's occupied slots 0..symbols-1. */
+cudaError_t launch_utf8_codes(rune_set_t *set, cudaStream_t stream);
+/** Device scratch the exclusive scan of `count + 1` counts needs. */
+std::size_t utf8_scan_scratch_bytes(std::uint64_t count);
+/** `offsets[0..count]` = exclusive scan of `counts[0..count]` (counts[count] must be 0). */
+cudaError_t launch_utf8_scan(std::uint64_t const *counts, std::uint64_t *offsets, std::uint64_t count, void *scratch,
+                             std::size_t scratch_bytes, cudaStream_t stream);
+/** Writes each string's one-byte codes at `out + offsets[i]`. */
+cudaError_t launch_utf8_write(tape_t const &tape, std::uint64_t end, std::uint64_t const *offsets,
+                              rune_set_t const *set, std::uint8_t *out, int sm_count, cudaStream_t stream);
+
 /** Shape of a wavefront-DP launch for one engine configuration. */
 struct dp_launch_shape_t {
     int threads_per_cta;

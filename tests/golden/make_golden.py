@@ -14,7 +14,8 @@ Cases:
 * ``asym_*``: an asymmetric class table, to pin which string indexes the rows of the table;
 * ``blosum62_*`` / ``nuc44_*``: the reference's built-in tables (serial.hpp:191-256);
 * ``config1``: the whole CPU-runnable benchmark configuration (1,024 DNA pairs);
-* ``c3_sample`` / ``c4_sample``: seeded samples of the NW protein and SW long-DNA configurations.
+* ``c3_sample`` / ``c4_sample``: seeded samples of the NW protein and SW long-DNA configurations;
+* ``utf8_*``: UTF-8 Levenshtein (code points), known answers, degenerate corpus and random multi-script pairs.
 """
 from __future__ import annotations
 
@@ -98,6 +99,7 @@ class Fixture:
         prefix = f"{name}__"
         self.arrays[prefix + "kind"] = np.array([costs.kind])
         self.arrays[prefix + "costs"] = np.array([costs.match, costs.mismatch, costs.open, costs.extend], np.int8)
+        self.arrays[prefix + "utf8"] = np.array([costs.utf8])
         self.arrays[prefix + "b2c"] = np.frombuffer(bytes(costs.byte_to_class), np.uint8).copy()
         self.arrays[prefix + "table"] = np.frombuffer(bytes(costs.class_costs), np.int8).reshape(32, 32).copy()
         self.arrays[prefix + "mode"] = np.array([MODES[mode]])
@@ -195,6 +197,36 @@ def main():
     d_b2c, d_table = workloads.dna_table(2, -3)
     fx.add("c4_sample", oracle.alignment_costs(oracle.SMITH_WATERMAN, d_b2c, d_table, -5, -2), "pairwise",
            tape_strings(first), tape_strings(second))
+
+    # UTF-8 Levenshtein: the reference tests' known answers (test/similarities.py:151-166), its degenerate UTF-8
+    # corpus (:473, :484-493) under the three cost modes, and random multi-script pairs, some of whose strings end
+    # in the middle of a sequence (the decoder then reads on into the next string of the tape).
+    utf8 = oracle.levenshtein_utf8_costs
+    kat_a = ["hello", "\U0002070e \U00020731 \U00020779 \U00020c53", "\U0001f496", "αβγδ",
+             "école", "façade", "Schön", "München", "こんにちは世界"]
+    kat_b = ["hell", "\U0002070e\U00020731\U00020779\U00020c53", "\U0001f497", "αγδ",
+             "école", "facade", "Schön", "Muenchen", "こんばんは世界"]
+    fx.add("utf8_kat_unit", utf8(), "pairwise", kat_a, kat_b)
+    fx.add("utf8_kat_custom_gaps", utf8(0, 4, 3, 3), "pairwise", kat_a, kat_b)
+    degenerate_utf8 = ["", "x", "é", "\U0001f680", "あ" * 10, "abcXYZ123",
+                       "こんにちは世界" * 5, "あ" * 600 + "い" * 20]
+    for mode_name, costs in (("unit", utf8()), ("linear", utf8(0, 3, 2, 2)), ("affine", utf8(0, 4, 5, 2))):
+        fx.add(f"utf8_degenerate_{mode_name}", costs, "cross", degenerate_utf8, degenerate_utf8)
+        fx.add(f"utf8_degenerate_{mode_name}_self", costs, "symmetric", degenerate_utf8)
+    letters = list("abcdefghéüñαβжאあい世界\U0001f680\U0001f496")
+
+    def utf8_strings(count, low, high):
+        return ["".join(rng.choice(letters, size=int(rng.integers(low, high + 1)))).encode() for _ in range(count)]
+
+    first, second = utf8_strings(80, 0, 120), utf8_strings(80, 0, 120)
+    for i in range(0, 79, 9):  # cut inside a multi-byte sequence (never the tape's last string)
+        if len(first[i]) > 1 and first[i][-1] >= 0x80:
+            first[i] = first[i][:-1]
+        if len(second[i]) > 1 and second[i][-1] >= 0x80:
+            second[i] = second[i][:-1]
+    fx.add("utf8_random_unit", utf8(), "pairwise", first, second)
+    fx.add("utf8_random_affine", utf8(0, 2, 3, 1), "pairwise", first, second)
+    fx.add("utf8_random_cross", utf8(0, 3, 2, 2), "cross", first[:25], second[:30])
 
     path = os.path.join(HERE, "golden.npz")
     fx.save(path)

@@ -126,6 +126,28 @@ def test_pairwise_count_mismatch_and_small_stride(native):
 def test_out_of_scope_entry_points_fail_cleanly(native):
     err = ctypes.c_char_p()
     handle = ctypes.c_void_p()
-    assert native.lib.szs_levenshtein_distances_utf8_init(0, 1, 1, 1, None, 0, ctypes.byref(handle),
-                                                          ctypes.byref(err)) == native.UNKNOWN
+    widths = (ctypes.c_size_t * 1)(5)
+    assert native.lib.szs_fingerprints_init(ctypes.c_size_t(64), ctypes.c_size_t(256), widths, ctypes.c_size_t(1),
+                                            ctypes.c_uint64(42), None, 0, ctypes.byref(handle),
+                                            ctypes.byref(err)) == native.UNKNOWN
     assert b"GB300" in err.value
+
+
+def test_utf8_and_byte_engines_do_not_mix(native):
+    """UTF-8 engines are their own handle type, as in the reference: byte entry points refuse them and back."""
+    err = ctypes.c_char_p()
+    utf8, byte = ctypes.c_void_p(), ctypes.c_void_p()
+    assert native.lib.szs_levenshtein_distances_utf8_init(0, 1, 1, 1, None, 0, ctypes.byref(utf8),
+                                                          ctypes.byref(err)) == native.SUCCESS
+    assert native.lib.szs_levenshtein_distances_init(0, 1, 1, 1, None, 0, ctypes.byref(byte),
+                                                     ctypes.byref(err)) == native.SUCCESS
+    data = np.frombuffer("αβγ".encode(), dtype=np.uint8).copy()
+    offsets = np.array([0, len(data)], dtype=np.uint64)
+    tape = native.U64Tape(data.ctypes.data, offsets.ctypes.data, 1)
+    out = np.zeros(1, dtype=np.uint64)
+    assert native.lib.szs_levenshtein_distances_u64tape(utf8, None, ctypes.byref(tape), ctypes.byref(tape),
+                                                        out.ctypes.data, 1, ctypes.byref(err)) == native.UNKNOWN
+    assert native.lib.szs_levenshtein_distances_utf8_u64tape(byte, None, ctypes.byref(tape), ctypes.byref(tape),
+                                                             out.ctypes.data, 1, ctypes.byref(err)) == native.UNKNOWN
+    native.lib.szs_levenshtein_distances_utf8_free(utf8)
+    native.lib.szs_levenshtein_distances_free(byte)

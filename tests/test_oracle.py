@@ -17,7 +17,7 @@ def golden_cases():
         for name in names:
             cases[name] = {field: data[f"{name}__{field}"] for field in
                            ("kind", "costs", "b2c", "table", "mode", "q_data", "q_offsets", "c_data", "c_offsets",
-                            "expected")}
+                            "expected", "utf8")}
     return cases
 
 
@@ -28,6 +28,8 @@ def costs_of(case):
     kind = int(case["kind"][0])
     match, mismatch, open_, extend = (int(x) for x in case["costs"])
     if kind == oracle.LEVENSHTEIN:
+        if int(case["utf8"][0]):
+            return oracle.levenshtein_utf8_costs(match, mismatch, open_, extend)
         return oracle.levenshtein_costs(match, mismatch, open_, extend)
     return oracle.alignment_costs(kind, case["b2c"], case["table"], open_, extend)
 
@@ -56,6 +58,11 @@ def test_golden_covers_the_reference_known_answers():
     mismatch, opening, extension = 4, 3, 2
     assert list(custom) == [0, opening, 0, opening + 2 * extension, opening + 2 * extension, opening, opening,
                             mismatch, opening, min(14 * mismatch, 2 * opening + 12 * extension)]
+
+
+def test_golden_covers_the_reference_utf8_known_answers():
+    """The UTF-8 pairs the reference's tests assert by hand (test/similarities.py:159-166): code points, not bytes."""
+    assert list(CASES["utf8_kat_unit"]["expected"]) == [1, 3, 1, 1, 2, 1, 2, 2, 2]
 
 
 def test_bit_parallel_equals_dynamic_programming(port):

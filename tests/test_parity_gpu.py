@@ -476,3 +476,63 @@ def test_dense_tables(szs, port, family, costs):
     wide = [bytes(range(40))]
     with pytest.raises(ValueError):
         engine.pairwise(szs.Strs(wide), szs.Strs(wide))
+
+
+def _golden_cases():
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.npz")
+    with np.load(path) as data:
+        return {str(name): {k.split("__", 1)[1]: data[k] for k in data.files if k.startswith(f"{name}__")}
+                for name in data["__names__"]}
+
+
+GOLDEN = _golden_cases()
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN))
+def test_engine_matches_reference_outputs(szs, name):
+    """Every golden case (outputs of the reference library compiled from its sources) through the engine."""
+    case = GOLDEN[name]
+    kind = int(case["kind"][0])
+    match, mismatch, open_, extend = (int(x) for x in case["costs"])
+    if kind == oracle.LEVENSHTEIN:
+        cls = szs.LevenshteinDistancesUTF8 if int(case["utf8"][0]) else szs.LevenshteinDistances
+        engine = cls(match, mismatch, open_, extend)
+    else:
+        cls = szs.NeedlemanWunschScores if kind == oracle.NEEDLEMAN_WUNSCH else szs.SmithWatermanScores
+        engine = cls(case["b2c"], np.ascontiguousarray(case["table"]), open=open_, extend=extend)
+    q = szs.Strs.from_buffers(case["q_data"], case["q_offsets"])
+    c = szs.Strs.from_buffers(case["c_data"], case["c_offsets"])
+    mode = int(case["mode"][0])
+    if mode == 0:
+        got = engine.pairwise(q, c)
+    elif mode == 1:
+        got = engine(q, c)
+    else:
+        got = engine(q)
+    np.testing.assert_array_equal(np.asarray(got).astype(np.int64), case["expected"])
+
+
+@pytest.mark.parametrize("costs", [(0, 1, 1, 1), (0, 3, 2, 2), (0, 4, 5, 2), (1, 3, 4, 1)])
+def test_utf8_levenshtein_routes(szs, port, costs):
+    """Code-point distances across the routes: short and long pairs, up to 256 distinct code points, and more
+    refused."""
+    rng = np.random.default_rng(sum(costs) + 1)
+    letters = [chr(c) for c in range(0x3041, 0x3041 + 80)] + [chr(c) for c in range(0x1F600, 0x1F600 + 60)] + \
+        list("abcdefghij") + [chr(c) for c in range(0x400, 0x400 + 100)]
+    assert len(letters) == 250
+    lengths = [(int(rng.integers(0, 300)), int(rng.integers(0, 300))) for _ in range(200)]
+    lengths += [(700, 900), (1500, 1600), (3000, 2600)]
+    first = ["".join(rng.choice(letters, size=n)) for n, _ in lengths]
+    second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
+    second[-1] = first[-1][:2000] + second[-1][2000:]  # related: small distance on a band pair
+    engine = szs.LevenshteinDistancesUTF8(*costs)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
+    np.testing.assert_array_equal(got, want)
+    cross = engine(szs.Strs(first[:12]), szs.Strs(second[:9]))
+    np.testing.assert_array_equal(cross.astype(np.int64), port.cross(oracle.levenshtein_utf8_costs(*costs),
+                                                                     tape(first[:12]), tape(second[:9])))
+    too_many = ["".join(chr(0x4E00 + i) for i in range(300))]
+    with pytest.raises(ValueError):
+        engine(szs.Strs(too_many), szs.Strs(too_many))
