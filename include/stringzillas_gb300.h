@@ -301,15 +301,27 @@ SZS_GB300_API sz_status_t szs_smith_waterman_scores_u64tape(szs_smith_waterman_s
 /** Replaces stringzillas.h:434. */
 SZS_GB300_API void szs_smith_waterman_scores_free(szs_smith_waterman_scores_t engine);
 
-/* ---- Fingerprints: out of this engine's scope; present so bindings load (stringzillas.h:435-536) --------------- */
+/* ---- Fingerprints (replaces stringzillas.h:435-536) ------------------------------------------------------------ */
 
-/** Always fails with `sz_status_unknown_k`. Replaces stringzillas.h:476-480. */
+/**
+ *  Min-Hash engine of @p dimensions rolling hashers. Dimension `d` rolls a hash over windows of
+ *  `window_widths[(d / 64) % count]` bytes when `dimensions` is a multiple of `64 * count` (the reference's sliced
+ *  layout), else of `window_widths[d % count]`; NULL / zero widths select {3, 4, 5, 7, 9, 11, 15, 31}. Modulus and
+ *  multiplier come from `seed + d` as in the reference's `floating_rolling_hasher<f64_t>`. @p alphabet_size,
+ *  @p alloc and @p capabilities are accepted and unused, as in the reference. `*engine` must be NULL on entry.
+ *  Replaces stringzillas.h:476-480 (c/stringzillas/fingerprints.cuh:27-141).
+ */
 SZS_GB300_API sz_status_t szs_fingerprints_init(sz_size_t dimensions, sz_size_t alphabet_size,
                                                 sz_size_t const *window_widths, sz_size_t window_widths_count,
                                                 sz_u64_t seed, sz_memory_allocator_t const *alloc,
                                                 sz_capability_t capabilities, szs_fingerprints_t *engine,
                                                 char const **error_message);
-/** Replaces stringzillas.h:495. */
+/**
+ *  Writes, for text `i` and dimension `d`, the low 32 bits of the minimum window hash to
+ *  `(char *)min_hashes + i * min_hashes_stride` [d] and its number of occurrences to the same place in
+ *  @p min_counts; strides are in BYTES and at least `dimensions * 4`. Texts shorter than a dimension's window get
+ *  0xFFFFFFFF and 0. Outputs may be host or device memory. Replaces stringzillas.h:495.
+ */
 SZS_GB300_API sz_status_t szs_fingerprints_sequence(szs_fingerprints_t engine, szs_device_scope_t device,
                                                     sz_sequence_t const *texts, sz_u32_t *min_hashes,
                                                     sz_size_t min_hashes_stride, sz_u32_t *min_counts,
@@ -326,6 +338,31 @@ SZS_GB300_API sz_status_t szs_fingerprints_u32tape(szs_fingerprints_t engine, sz
                                                    sz_size_t min_counts_stride, char const **error_message);
 /** Replaces stringzillas.h:536. */
 SZS_GB300_API void szs_fingerprints_free(szs_fingerprints_t engine);
+
+/** The UTF-8 entry points hash the same bytes as the byte ones; the reference's library exports them as forwards
+ *  (c/stringzillas/fingerprints.cuh:181-222). */
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_init(sz_size_t dimensions, sz_size_t alphabet_size,
+                                                     sz_size_t const *window_widths, sz_size_t window_widths_count,
+                                                     sz_u64_t seed, sz_memory_allocator_t const *alloc,
+                                                     sz_capability_t capabilities, szs_fingerprints_utf8_t *engine,
+                                                     char const **error_message);
+/** Forwards to `szs_fingerprints_sequence` (c/stringzillas/fingerprints.cuh:192-200). */
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_sequence(szs_fingerprints_utf8_t engine, szs_device_scope_t device,
+                                                         sz_sequence_t const *texts, sz_u32_t *min_hashes,
+                                                         sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                         sz_size_t min_counts_stride, char const **error_message);
+/** Forwards to `szs_fingerprints_u32tape` (c/stringzillas/fingerprints.cuh:201-209). */
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_u32tape(szs_fingerprints_utf8_t engine, szs_device_scope_t device,
+                                                        sz_sequence_u32tape_t const *texts, sz_u32_t *min_hashes,
+                                                        sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                        sz_size_t min_counts_stride, char const **error_message);
+/** Forwards to `szs_fingerprints_u64tape` (c/stringzillas/fingerprints.cuh:210-218). */
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_u64tape(szs_fingerprints_utf8_t engine, szs_device_scope_t device,
+                                                        sz_sequence_u64tape_t const *texts, sz_u32_t *min_hashes,
+                                                        sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                        sz_size_t min_counts_stride, char const **error_message);
+/** Forwards to `szs_fingerprints_free` (c/stringzillas/fingerprints.cuh:219-221). */
+SZS_GB300_API void szs_fingerprints_utf8_free(szs_fingerprints_utf8_t engine);
 
 /* ---- Unified memory (replaces stringzillas.h:545-551) ---------------------------------------------------------- */
 

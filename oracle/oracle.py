@@ -146,6 +146,23 @@ def reference_available() -> bool:
     return os.path.exists(REF_PATH)
 
 
+def fingerprints(dimensions, texts, window_widths=None, seed=0):
+    """(hashes, counts), uint32 [count, dimensions], from the oracle's restatement of the reference's Min-Hash."""
+    data, offsets = texts
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    data = np.ascontiguousarray(data, dtype=np.uint8) if len(data) else np.zeros(1, dtype=np.uint8)
+    count = len(offsets) - 1
+    hashes = np.zeros((count, dimensions), dtype=np.uint32)
+    counts = np.zeros((count, dimensions), dtype=np.uint32)
+    widths = None if window_widths is None else np.ascontiguousarray(window_widths, dtype=np.uint64)
+    lib = Port().lib
+    lib.oracle_fingerprints_u64tape(ctypes.c_size_t(dimensions), None if widths is None else _ptr(widths),
+                                    ctypes.c_size_t(0 if widths is None else len(widths)), ctypes.c_uint64(seed),
+                                    _ptr(data), _ptr(offsets), ctypes.c_size_t(count), _ptr(hashes),
+                                    ctypes.c_size_t(dimensions * 4), _ptr(counts), ctypes.c_size_t(dimensions * 4))
+    return hashes, counts
+
+
 class Reference:
     """The reference's own ``szs_*`` C-ABI, compiled from its sources (serial engines)."""
 
@@ -203,6 +220,33 @@ class Reference:
             return out.astype(np.int64)
         finally:
             getattr(self.lib, f"szs_{name}_free")(engine)
+
+    def fingerprints(self, dimensions, texts, window_widths=None, seed=0):
+        """(hashes, counts) from the reference's `szs_fingerprints_u64tape` (rows `dimensions * 4` bytes apart)."""
+        engine, err = ctypes.c_void_p(), ctypes.c_char_p()
+        widths = None if window_widths is None else (ctypes.c_size_t * len(window_widths))(*window_widths)
+        rc = self.lib.szs_fingerprints_init(ctypes.c_size_t(dimensions), ctypes.c_size_t(256), widths,
+                                            ctypes.c_size_t(0 if window_widths is None else len(window_widths)),
+                                            ctypes.c_uint64(seed), None, ctypes.c_int(CAP_SERIAL),
+                                            ctypes.byref(engine), ctypes.byref(err))
+        if rc != 0:
+            raise RuntimeError(f"reference fingerprint init failed: {rc} {err.value}")
+        try:
+            data, offsets = texts
+            offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+            data = np.ascontiguousarray(data, dtype=np.uint8) if len(data) else np.zeros(1, dtype=np.uint8)
+            tape = _U64Tape(data.ctypes.data, offsets.ctypes.data, len(offsets) - 1)
+            hashes = np.zeros((len(offsets) - 1, dimensions), dtype=np.uint32)
+            counts = np.zeros_like(hashes)
+            rc = self.lib.szs_fingerprints_u64tape(engine, self._scope, ctypes.byref(tape),
+                                                   ctypes.c_void_p(hashes.ctypes.data), ctypes.c_size_t(dimensions * 4),
+                                                   ctypes.c_void_p(counts.ctypes.data), ctypes.c_size_t(dimensions * 4),
+                                                   ctypes.byref(err))
+            if rc != 0:
+                raise RuntimeError(f"reference fingerprints failed: {rc} {err.value}")
+            return hashes, counts
+        finally:
+            self.lib.szs_fingerprints_free(engine)
 
     def pairs(self, costs: Costs, first, second) -> np.ndarray:
         """One 1x1 call per pair, the way a pairwise caller drives the cross-product ABI."""

@@ -380,3 +380,58 @@ int oracle_score_cross_u64tape(oracle_costs_t const *costs, char const *queries_
     if (job.tasks == 0) return 0;
     return oracle_run_(&job, threads);
 }
+
+/* ---- Min-Hash fingerprints ------------------------------------------------------------------------------------ */
+
+static uint64_t oracle_splitmix64_(uint64_t state) {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int oracle_fingerprints_u64tape(size_t dimensions, size_t const *window_widths, size_t window_widths_count,
+                                uint64_t seed, char const *data, uint64_t const *offsets, size_t count,
+                                uint32_t *min_hashes, size_t hashes_stride, uint32_t *min_counts,
+                                size_t counts_stride) {
+    static size_t const default_widths[] = {3, 4, 5, 7, 9, 11, 15, 31};
+    if (!window_widths || !window_widths_count) window_widths = default_widths, window_widths_count = 8;
+    size_t const per_width = dimensions / window_widths_count;
+    int const sliced = dimensions % window_widths_count == 0 && per_width % 64 == 0;
+    for (size_t dim = 0; dim < dimensions; ++dim) {
+        size_t const width = window_widths[(sliced ? dim / 64 : dim) % window_widths_count];
+        uint64_t const multiplier = 256u + oracle_splitmix64_(seed + dim) % 384u;
+        uint64_t const modulo = 4503599626977ull - oracle_splitmix64_(oracle_splitmix64_(seed + dim)) % (1ull << 20);
+        uint64_t leading = 1; /* multiplier^(width - 1) mod modulo: the weight of a window's oldest byte */
+        for (size_t i = 0; i + 1 < width; ++i) leading = leading * multiplier % modulo;
+        for (size_t t = 0; t < count; ++t) {
+            uint8_t const *text = (uint8_t const *)data + offsets[t];
+            size_t const length = (size_t)(offsets[t + 1] - offsets[t]);
+            uint32_t *hash_out = (uint32_t *)((char *)min_hashes + t * hashes_stride) + dim;
+            uint32_t *count_out = (uint32_t *)((char *)min_counts + t * counts_stride) + dim;
+            if (length < width) {
+                *hash_out = 0xFFFFFFFFu, *count_out = 0;
+                continue;
+            }
+            uint64_t state = 0, minimum = 0;
+            uint32_t occurrences = 0;
+            for (size_t i = 0; i < length; ++i) {
+                uint64_t const incoming = (uint64_t)text[i] + 1u;
+                if (i >= width) { /* drop the oldest byte: state - leading * outgoing, kept non-negative */
+                    uint64_t const outgoing = (uint64_t)text[i - width] + 1u;
+                    state = (state + modulo - leading * outgoing % modulo) % modulo;
+                }
+                state = (state * multiplier + incoming) % modulo;
+                if (i + 1 == width) minimum = state, occurrences = 1;
+                else if (i + 1 > width) {
+                    if (state < minimum) minimum = state, occurrences = 1;
+                    else if (state == minimum) ++occurrences;
+                }
+            }
+            *hash_out = (uint32_t)(minimum & 0xFFFFFFFFu);
+            *count_out = occurrences;
+        }
+    }
+    return 0;
+}

@@ -65,6 +65,20 @@ int oracle_score_cross_u64tape(oracle_costs_t const *costs, char const *queries_
                                size_t queries_count, char const *candidates_data, uint64_t const *candidates_offsets,
                                size_t candidates_count, int64_t *results, size_t results_stride, size_t threads);
 
+/**
+ *  Min-Hash fingerprints (include/stringzillas/fingerprints/serial.hpp): for each of @p dimensions rolling hashes,
+ *  the minimum hash over all windows of the dimension's width and how often it occurs. Dimension d rolls a
+ *  Rabin-Karp hash `(state * multiplier + byte + 1) mod modulo` with parameters from `splitmix64` streams of
+ *  `seed + d` (:33-41, :426-432, :326-333), in exact integer arithmetic (the reference's double-precision Barrett
+ *  steps are exact on these magnitudes). Widths follow the engine's layout (c/stringzillas/fingerprints.cuh:34-140):
+ *  64-dimension slices per width when every width gets a whole number of slices, else widths interleaved per
+ *  dimension. Rows of @p min_hashes / @p min_counts are @p hashes_stride / @p counts_stride bytes apart.
+ */
+int oracle_fingerprints_u64tape(size_t dimensions, size_t const *window_widths, size_t window_widths_count,
+                                uint64_t seed, char const *data, uint64_t const *offsets, size_t count,
+                                uint32_t *min_hashes, size_t hashes_stride, uint32_t *min_counts,
+                                size_t counts_stride);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,7 +24,7 @@ from ._native import lib
 
 __all__ = [
     "Strs", "DeviceScope", "LevenshteinDistances", "LevenshteinDistancesUTF8", "NeedlemanWunschScores",
-    "SmithWatermanScores", "to_device",
+    "SmithWatermanScores", "Fingerprints", "to_device",
     "Server", "Ticket", "__version__", "__capabilities__",
 ]
 
@@ -528,5 +528,85 @@ class SmithWatermanScores(_Alignment):
 
     _algo = "smith_waterman_scores"
     _name = "Smith-Waterman scores"
+
+
+class Fingerprints:
+    """Min-Hash fingerprints: for every text and dimension, the low 32 bits of the minimum rolling hash over the
+    text's windows of that dimension's width, and how many windows reach it (the reference's
+    python/stringzillas/fingerprints.c:35-211). Texts shorter than a window give 0xFFFFFFFF and 0."""
+
+    def __init__(self, ndim, window_widths=None, alphabet_size=256, seed=0, capabilities=None):
+        _Engine._check_capabilities(None, capabilities)
+        ndim = int(ndim)
+        widths = None
+        if window_widths is not None:
+            if not isinstance(window_widths, np.ndarray):
+                raise TypeError("window_widths must be a numpy array of uint64")
+            if window_widths.dtype != np.uint64:
+                raise TypeError("window_widths must have dtype uint64")
+            if window_widths.ndim != 1:
+                raise ValueError("window_widths must be a 1D array")
+            if not window_widths.flags.c_contiguous:
+                raise ValueError("window_widths must be a contiguous C-style array (no strides)")
+            widths = window_widths
+        self.handle = ctypes.c_void_p()
+        err = ctypes.c_char_p()
+        count = 0 if widths is None else len(widths)
+        status = lib.szs_fingerprints_init(ndim, int(alphabet_size),
+                                           None if widths is None else ctypes.c_void_p(widths.ctypes.data), count,
+                                           ctypes.c_uint64(int(seed)), None, 0, ctypes.byref(self.handle),
+                                           ctypes.byref(err))
+        _native.raise_for(status, err.value, "Fingerprints initialization")
+        self.ndim = ndim
+        self._description = f"ndim={ndim},window_widths={count},alphabet_size={int(alphabet_size)},seed={int(seed)}"
+
+    def __del__(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            lib.szs_fingerprints_free(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __repr__(self):
+        return f"Fingerprints({self._description})"
+
+    @property
+    def __capabilities__(self):
+        return __capabilities__
+
+    def _outputs(self, rows, out):
+        if out is None:
+            return [np.empty((rows, self.ndim), dtype=np.uint32) for _ in range(2)]
+        if not isinstance(out, (tuple, list)) or len(out) != 2:
+            raise TypeError("out must be a (hashes, counts) pair")
+        for array in out:
+            if isinstance(array, np.ndarray):
+                if array.ndim != 2 or array.dtype != np.uint32 or array.strides[1] != 4:
+                    raise ValueError("out arrays must be 2-D uint32 with contiguous rows")
+                shape = array.shape
+            else:
+                if array.dim() != 2 or array.element_size() != 4 or array.stride(1) != 1:
+                    raise ValueError("out tensors must be 2-D, 4-byte elements, unit column stride")
+                shape = tuple(array.shape)
+            if shape[0] < rows or shape[1] < self.ndim:
+                raise ValueError("out arrays are too small for results")
+        return list(out)
+
+    @staticmethod
+    def _row_bytes(array):
+        return array.strides[0] if isinstance(array, np.ndarray) else array.stride(0) * 4
+
+    def __call__(self, texts, device=None, out=None):
+        texts = _as_strs(texts, "texts")
+        rows = len(texts)
+        hashes, counts = self._outputs(rows, out)
+        if rows == 0:
+            return hashes, counts
+        tape, bits = texts.tape()
+        err = ctypes.c_char_p()
+        fn = lib.szs_fingerprints_u32tape if bits == 32 else lib.szs_fingerprints_u64tape
+        status = fn(self.handle, _scope_handle(device), ctypes.byref(tape), ctypes.c_void_p(_pointer_of(hashes)),
+                    self._row_bytes(hashes), ctypes.c_void_p(_pointer_of(counts)), self._row_bytes(counts),
+                    ctypes.byref(err))
+        _native.raise_for(status, err.value, "Fingerprints computation")
+        return hashes, counts
 
 from .serving import Server, Ticket  # noqa: E402  (needs the engine classes above)

@@ -112,6 +112,19 @@ for _algo in ("levenshtein_distances", "needleman_wunsch_scores", "smith_waterma
     fn.restype = None
     fn.argtypes = [c_void_p]
 
+for _algo in ("fingerprints", "fingerprints_utf8"):
+    fn = getattr(lib, f"szs_{_algo}_init")
+    fn.restype = c_status
+    fn.argtypes = [c_size_t, c_size_t, c_void_p, c_size_t, ctypes.c_uint64, c_void_p, ctypes.c_uint32,
+                   ctypes.POINTER(c_void_p), _err]
+    for _suffix in ("_sequence", "_u32tape", "_u64tape"):
+        fn = getattr(lib, f"szs_{_algo}{_suffix}")
+        fn.restype = c_status
+        fn.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, _err]
+    fn = getattr(lib, f"szs_{_algo}_free")
+    fn.restype = None
+    fn.argtypes = [c_void_p]
+
 for _algo in ("needleman_wunsch_scores", "smith_waterman_scores"):
     fn = getattr(lib, f"szs_gb300_{_algo}_init_dense")
     fn.restype = c_status

@@ -541,14 +541,14 @@ struct call_t {
     tape_t staged_queries {}, staged_candidates {};
 };
 
-static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &stream, engine_t &engine,
+static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &stream, device_context_t *contexts,
                               device_context_t *&context) noexcept {
     scope_t *scope = as_scope(scope_handle);
     if (scope_handle && !scope) return {sz_status_unknown_k, "Invalid device scope handle"};
     if (scope && scope->kind == scope_cpu_k) return {sz_device_code_mismatch_k, nullptr};
     device = scope ? scope->device : 0;
     if (device < 0 || device >= max_devices_k || device >= visible_devices()) return {sz_missing_gpu_k, nullptr};
-    context = &engine.devices[device];
+    context = &contexts[device];
     status_t status = context->prepare(device);
     if (!status.ok()) return status;
     SZS_TRY_CUDA(cudaSetDevice(device));
@@ -1233,7 +1233,7 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
     int device = 0;
     cudaStream_t stream = nullptr;
     device_context_t *context = nullptr;
-    status_t status = resolve_scope(scope_handle, device, stream, engine, context);
+    status_t status = resolve_scope(scope_handle, device, stream, engine.devices, context);
     if (!status.ok()) return status;
     if (call.mode == mode_pairwise_k && call.queries.count == call.candidates.count && call.queries.count > 1 &&
         !call.pre_staged && !engine.utf8 && pinned_host(call.queries.offsets) && pinned_host(call.candidates.offsets) &&
@@ -1507,6 +1507,132 @@ void free_engine(void *handle) {
     if (!engine) return;
     engine->magic = 0;
     delete engine;
+}
+
+/* ---- fingerprints ----------------------------------------------------------------------------------------------- */
+
+constexpr std::uint32_t fingerprint_magic_k = 0x50524746u;
+
+/** A Min-Hash engine: per-dimension parameters on the host, uploaded once per device. */
+struct fingerprint_engine_t {
+    std::uint32_t magic = fingerprint_magic_k;
+    std::uint32_t dimensions = 0;
+    std::vector<fingerprint_dim_t> params;
+    device_context_t devices[max_devices_k];
+    device_buffer_t params_device[max_devices_k];
+    device_buffer_t outputs[max_devices_k];
+    ~fingerprint_engine_t() {
+        for (int d = 0; d < max_devices_k; ++d) {
+            if (!devices[d].ready) continue;
+            cudaSetDevice(d);
+            params_device[d].release();
+            outputs[d].release();
+            devices[d].release();
+        }
+    }
+};
+
+fingerprint_engine_t *as_fingerprints(void *handle) {
+    auto *engine = static_cast<fingerprint_engine_t *>(handle);
+    return engine && engine->magic == fingerprint_magic_k ? engine : nullptr;
+}
+
+/**
+ *  Dimension d's window width follows the reference's layout (c/stringzillas/fingerprints.cuh:44-139): when every
+ *  width gets a whole number of 64-dimension slices, slice k has width `widths[k % count]`; otherwise dimension d
+ *  has width `widths[d % count]`. Parameters are seeded by the dimension's index either way.
+ */
+sz_status_t create_fingerprints(std::size_t dimensions, std::size_t alphabet_size, std::size_t const *widths,
+                                std::size_t widths_count, std::uint64_t seed, void **engine_out,
+                                char const **error_message) {
+    if (!engine_out) return report({sz_status_unknown_k, "Engine output pointer must not be NULL"}, error_message);
+    if (*engine_out) return report({sz_status_unknown_k, "Engine must be uninitialized (NULL) on entry"}, error_message);
+    static std::size_t const default_widths[] = {3, 4, 5, 7, 9, 11, 15, 31};
+    if (!widths || !widths_count) widths = default_widths, widths_count = 8;
+    if (!dimensions || dimensions > 0xFFFFFFFFull)
+        return report({sz_unexpected_dimensions_k, "Fingerprints need between 1 and 2^32 - 1 dimensions"},
+                      error_message);
+    for (std::size_t i = 0; i < widths_count; ++i)
+        if (!widths[i]) return report({sz_unexpected_dimensions_k, "Window widths must be positive"}, error_message);
+    (void)alphabet_size; // the reference's double-precision hasher does not use it
+    auto *engine = new (std::nothrow) fingerprint_engine_t();
+    if (!engine) return report({sz_bad_alloc_k, "Failed to allocate the engine"}, error_message);
+    engine->dimensions = (std::uint32_t)dimensions;
+    bool const sliced = dimensions % widths_count == 0 && (dimensions / widths_count) % 64 == 0;
+    engine->params.resize(dimensions);
+    for (std::size_t d = 0; d < dimensions; ++d)
+        engine->params[d] = fingerprint_dimension(d, widths[(sliced ? d / 64 : d) % widths_count], seed);
+    *engine_out = engine;
+    return report({}, error_message);
+}
+
+void free_fingerprints(void *handle) {
+    fingerprint_engine_t *engine = as_fingerprints(handle);
+    if (!engine) return;
+    engine->magic = 0;
+    delete engine;
+}
+
+sz_status_t fingerprint_call(void *engine_handle, void *scope_handle, tape_view_t const &texts,
+                             std::uint32_t *hashes, std::size_t hashes_stride, std::uint32_t *counts,
+                             std::size_t counts_stride, char const **error_message) {
+    fingerprint_engine_t *engine = as_fingerprints(engine_handle);
+    if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
+    std::size_t const row_bytes = (std::size_t)engine->dimensions * 4;
+    if (texts.count && (!hashes || !counts))
+        return report({sz_unexpected_dimensions_k, "Outputs must not be NULL"}, error_message);
+    if (texts.count && (hashes_stride < row_bytes || counts_stride < row_bytes))
+        return report({sz_unexpected_dimensions_k, "Output strides (bytes) are smaller than a row"}, error_message);
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    device_context_t *context = nullptr;
+    status_t status = resolve_scope(scope_handle, device, stream, engine->devices, context);
+    if (!status.ok()) return report(status, error_message);
+    if (!texts.count) return report({}, error_message);
+    // Inputs.
+    staging_plan_t plan;
+    status = plan_staging(texts, plan, stream);
+    if (!status.ok()) return report(status, error_message);
+    status = context->inputs.reserve(align_up(plan.offsets_bytes, 256) + align_up(plan.data_bytes, 256) + 512, stream);
+    if (!status.ok()) return report(status, error_message);
+    tape_t staged;
+    status = stage_tape(texts, plan, static_cast<unsigned char *>(context->inputs.data), staged, stream);
+    if (!status.ok()) return report(status, error_message);
+    // Parameters, once per device.
+    device_buffer_t &params = engine->params_device[device];
+    std::size_t const params_bytes = engine->params.size() * sizeof(fingerprint_dim_t);
+    if (params.bytes < params_bytes) {
+        status = params.reserve(params_bytes, stream);
+        if (!status.ok()) return report(status, error_message);
+        cudaError_t const copied = cudaMemcpyAsync(params.data, engine->params.data(), params_bytes,
+                                                   cudaMemcpyHostToDevice, stream);
+        if (copied != cudaSuccess) return report(from_cuda(copied), error_message);
+    }
+    // Outputs: in place when device-reachable, else through a dense device buffer and 2-D copies.
+    bool const hashes_on_device = device_accessible(hashes), counts_on_device = device_accessible(counts);
+    std::uint32_t *hashes_target = hashes, *counts_target = counts;
+    std::size_t hashes_pitch = hashes_stride, counts_pitch = counts_stride;
+    std::size_t const dense_bytes = align_up(texts.count * row_bytes, 256);
+    if (!hashes_on_device || !counts_on_device) {
+        status = engine->outputs[device].reserve(2 * dense_bytes, stream);
+        if (!status.ok()) return report(status, error_message);
+        auto *area = static_cast<unsigned char *>(engine->outputs[device].data);
+        if (!hashes_on_device) hashes_target = reinterpret_cast<std::uint32_t *>(area), hashes_pitch = row_bytes;
+        if (!counts_on_device)
+            counts_target = reinterpret_cast<std::uint32_t *>(area + dense_bytes), counts_pitch = row_bytes;
+    }
+    cudaError_t error = launch_fingerprints(staged, static_cast<fingerprint_dim_t const *>(params.data),
+                                            engine->dimensions, hashes_target, hashes_pitch, counts_target,
+                                            counts_pitch, context->sm_count, stream);
+    if (error == cudaSuccess && !hashes_on_device)
+        error = cudaMemcpy2DAsync(hashes, hashes_stride, hashes_target, row_bytes, row_bytes, texts.count,
+                                  cudaMemcpyDeviceToHost, stream);
+    if (error == cudaSuccess && !counts_on_device)
+        error = cudaMemcpy2DAsync(counts, counts_stride, counts_target, row_bytes, row_bytes, texts.count,
+                                  cudaMemcpyDeviceToHost, stream);
+    if (error == cudaSuccess) error = cudaStreamSynchronize(stream);
+    if (error != cudaSuccess) return report(from_cuda(error), error_message);
+    return report({}, error_message);
 }
 
 sz_status_t not_in_scope(char const **error_message) {
@@ -1804,29 +1930,76 @@ SZS_GB300_API sz_status_t szs_smith_waterman_scores_u64tape(szs_smith_waterman_s
 }
 SZS_GB300_API void szs_smith_waterman_scores_free(szs_smith_waterman_scores_t engine) { free_engine(engine); }
 
-/* Fingerprints: outside the engine's scope */
+/* Fingerprints: Min-Hash over rolling hashes (see fingerprints.cu) */
 
-SZS_GB300_API sz_status_t szs_fingerprints_init(sz_size_t, sz_size_t, sz_size_t const *, sz_size_t, sz_u64_t,
-                                                sz_memory_allocator_t const *, sz_capability_t, szs_fingerprints_t *,
-                                                char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_fingerprints_init(sz_size_t dimensions, sz_size_t alphabet_size,
+                                                sz_size_t const *window_widths, sz_size_t window_widths_count,
+                                                sz_u64_t seed, sz_memory_allocator_t const *, sz_capability_t,
+                                                szs_fingerprints_t *engine, char const **error_message) {
+    return create_fingerprints(dimensions, alphabet_size, window_widths, window_widths_count, seed, engine,
+                               error_message);
 }
-SZS_GB300_API sz_status_t szs_fingerprints_sequence(szs_fingerprints_t, szs_device_scope_t, sz_sequence_t const *,
-                                                    sz_u32_t *, sz_size_t, sz_u32_t *, sz_size_t,
-                                                    char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_fingerprints_sequence(szs_fingerprints_t engine, szs_device_scope_t device,
+                                                    sz_sequence_t const *texts, sz_u32_t *min_hashes,
+                                                    sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                    sz_size_t min_counts_stride, char const **error_message) {
+    if (!texts) return report({sz_unexpected_dimensions_k, "Texts must not be NULL"}, error_message);
+    gathered_tape_t gathered;
+    status_t const status = gather_sequence(texts, gathered);
+    if (!status.ok()) return report(status, error_message);
+    return fingerprint_call(engine, device, gathered.view(), min_hashes, min_hashes_stride, min_counts,
+                            min_counts_stride, error_message);
 }
-SZS_GB300_API sz_status_t szs_fingerprints_u64tape(szs_fingerprints_t, szs_device_scope_t,
-                                                   sz_sequence_u64tape_t const *, sz_u32_t *, sz_size_t, sz_u32_t *,
-                                                   sz_size_t, char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_fingerprints_u64tape(szs_fingerprints_t engine, szs_device_scope_t device,
+                                                   sz_sequence_u64tape_t const *texts, sz_u32_t *min_hashes,
+                                                   sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                   sz_size_t min_counts_stride, char const **error_message) {
+    if (!texts) return report({sz_unexpected_dimensions_k, "Texts must not be NULL"}, error_message);
+    return fingerprint_call(engine, device, view_of(texts), min_hashes, min_hashes_stride, min_counts,
+                            min_counts_stride, error_message);
 }
-SZS_GB300_API sz_status_t szs_fingerprints_u32tape(szs_fingerprints_t, szs_device_scope_t,
-                                                   sz_sequence_u32tape_t const *, sz_u32_t *, sz_size_t, sz_u32_t *,
-                                                   sz_size_t, char const **error_message) {
-    return not_in_scope(error_message);
+SZS_GB300_API sz_status_t szs_fingerprints_u32tape(szs_fingerprints_t engine, szs_device_scope_t device,
+                                                   sz_sequence_u32tape_t const *texts, sz_u32_t *min_hashes,
+                                                   sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                   sz_size_t min_counts_stride, char const **error_message) {
+    if (!texts) return report({sz_unexpected_dimensions_k, "Texts must not be NULL"}, error_message);
+    return fingerprint_call(engine, device, view_of(texts), min_hashes, min_hashes_stride, min_counts,
+                            min_counts_stride, error_message);
 }
-SZS_GB300_API void szs_fingerprints_free(szs_fingerprints_t) {}
+SZS_GB300_API void szs_fingerprints_free(szs_fingerprints_t engine) { free_fingerprints(engine); }
+
+/* UTF-8 fingerprints hash the same bytes (the reference's c/stringzillas/fingerprints.cuh:181-222 forwards them) */
+
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_init(sz_size_t dimensions, sz_size_t alphabet_size,
+                                                     sz_size_t const *window_widths, sz_size_t window_widths_count,
+                                                     sz_u64_t seed, sz_memory_allocator_t const *alloc,
+                                                     sz_capability_t capabilities, szs_fingerprints_utf8_t *engine,
+                                                     char const **error_message) {
+    return szs_fingerprints_init(dimensions, alphabet_size, window_widths, window_widths_count, seed, alloc,
+                                 capabilities, engine, error_message);
+}
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_sequence(szs_fingerprints_utf8_t engine, szs_device_scope_t device,
+                                                         sz_sequence_t const *texts, sz_u32_t *min_hashes,
+                                                         sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                         sz_size_t min_counts_stride, char const **error_message) {
+    return szs_fingerprints_sequence(engine, device, texts, min_hashes, min_hashes_stride, min_counts,
+                                     min_counts_stride, error_message);
+}
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_u32tape(szs_fingerprints_utf8_t engine, szs_device_scope_t device,
+                                                        sz_sequence_u32tape_t const *texts, sz_u32_t *min_hashes,
+                                                        sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                        sz_size_t min_counts_stride, char const **error_message) {
+    return szs_fingerprints_u32tape(engine, device, texts, min_hashes, min_hashes_stride, min_counts,
+                                    min_counts_stride, error_message);
+}
+SZS_GB300_API sz_status_t szs_fingerprints_utf8_u64tape(szs_fingerprints_utf8_t engine, szs_device_scope_t device,
+                                                        sz_sequence_u64tape_t const *texts, sz_u32_t *min_hashes,
+                                                        sz_size_t min_hashes_stride, sz_u32_t *min_counts,
+                                                        sz_size_t min_counts_stride, char const **error_message) {
+    return szs_fingerprints_u64tape(engine, device, texts, min_hashes, min_hashes_stride, min_counts,
+                                    min_counts_stride, error_message);
+}
+SZS_GB300_API void szs_fingerprints_utf8_free(szs_fingerprints_utf8_t engine) { free_fingerprints(engine); }
 
 /* Extensions */
 

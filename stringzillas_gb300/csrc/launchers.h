@@ -23,6 +23,19 @@ cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, boo
 cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
                                   std::uint64_t stride, int sm_count, cudaStream_t stream);
 
+/** One Min-Hash dimension: modulus m (2^42 < m < 2^43), multiplier a (< 640), D = -a^w mod m, the quotient
+ *  estimate's constant mu = floor(2^74 / m) (< 2^32), window width w. */
+struct fingerprint_dim_t {
+    std::uint64_t modulo, discard;
+    std::uint32_t multiplier, mu, width, reserved;
+};
+/** The reference's parameters of dimension @p dim for a window of @p width bytes and a reproducibility @p seed. */
+fingerprint_dim_t fingerprint_dimension(std::uint64_t dim, std::uint64_t width, std::uint64_t seed);
+/** Min-Hash fingerprints of every text: rows `hashes_stride` / `counts_stride` bytes apart, `dimensions` columns. */
+cudaError_t launch_fingerprints(tape_t const &texts, fingerprint_dim_t const *params, std::uint32_t dimensions,
+                                std::uint32_t *hashes, std::uint64_t hashes_stride, std::uint32_t *counts,
+                                std::uint64_t counts_stride, int sm_count, cudaStream_t stream);
+
 /** The set of a batch's code points (UTF-8 Levenshtein): open addressing over `code point + 1` (0 = empty), then
  *  dense codes in slot order. */
 constexpr int rune_set_bits_k = 15;

@@ -15,7 +15,8 @@ Cases:
 * ``blosum62_*`` / ``nuc44_*``: the reference's built-in tables (serial.hpp:191-256);
 * ``config1``: the whole CPU-runnable benchmark configuration (1,024 DNA pairs);
 * ``c3_sample`` / ``c4_sample``: seeded samples of the NW protein and SW long-DNA configurations;
-* ``utf8_*``: UTF-8 Levenshtein (code points), known answers, degenerate corpus and random multi-script pairs.
+* ``utf8_*``: UTF-8 Levenshtein (code points), known answers, degenerate corpus and random multi-script pairs;
+* ``fp_*``: Min-Hash fingerprints in both dimension layouts of the reference's engine.
 """
 from __future__ import annotations
 
@@ -86,6 +87,7 @@ class Fixture:
         self.ref = oracle.Reference()
         self.arrays = {}
         self.names = []
+        self.fingerprint_names = []
 
     def add(self, name, costs, mode, queries, candidates=None):
         q = tape(queries)
@@ -108,8 +110,20 @@ class Fixture:
         self.arrays[prefix + "expected"] = np.asarray(expected, dtype=np.int64)
         self.names.append(name)
 
+    def add_fingerprints(self, name, dimensions, widths, seed, texts):
+        """Min-Hash fingerprints: stored under `fp_<name>__*`, listed in `__fingerprints__`."""
+        t = tape(texts)
+        hashes, counts = self.ref.fingerprints(dimensions, t, widths, seed)
+        prefix = f"fp_{name}__"
+        self.arrays[prefix + "params"] = np.array([dimensions, seed], dtype=np.uint64)
+        self.arrays[prefix + "widths"] = np.array(widths if widths else [], dtype=np.uint64)
+        self.arrays[prefix + "data"], self.arrays[prefix + "offsets"] = t
+        self.arrays[prefix + "hashes"], self.arrays[prefix + "counts"] = hashes, counts
+        self.fingerprint_names.append(name)
+
     def save(self, path):
         self.arrays["__names__"] = np.array(self.names)
+        self.arrays["__fingerprints__"] = np.array(self.fingerprint_names)
         np.savez_compressed(path, **self.arrays)
 
 
@@ -227,6 +241,16 @@ def main():
     fx.add("utf8_random_unit", utf8(), "pairwise", first, second)
     fx.add("utf8_random_affine", utf8(0, 2, 3, 1), "pairwise", first, second)
     fx.add("utf8_random_cross", utf8(0, 3, 2, 2), "cross", first[:25], second[:30])
+
+    # Min-Hash fingerprints (include/stringzillas/fingerprints/serial.hpp) in both dimension layouts: 64-dimension
+    # slices per width (1,024 dims over the default widths; 128 over two) and widths interleaved per dimension.
+    printable = [bytes(rng.integers(32, 127, size=int(rng.integers(0, 400))).astype(np.uint8)) for _ in range(60)]
+    printable += [b"", b"a", b"ab", b"abc", b"x" * 31, b"y" * 32, "こんにちは世界".encode() * 3]
+    dna_texts = random_strings(rng, 30, 0, 2000, b"ACGT")
+    fx.add_fingerprints("default_1024", 1024, None, 0, printable)
+    fx.add_fingerprints("sliced_128", 128, [4, 8], 42, printable)
+    fx.add_fingerprints("interleaved_100", 100, [3, 5, 7], 0, printable)
+    fx.add_fingerprints("interleaved_dna", 96, [2, 3, 31], 123456789, dna_texts)
 
     path = os.path.join(HERE, "golden.npz")
     fx.save(path)

@@ -38,7 +38,9 @@ def test_reference_entry_points_are_all_declared():
                 "szs_device_scope_get_cpu_cores", "szs_device_scope_get_gpu_device",
                 "szs_device_scope_get_capabilities", "szs_device_scope_free", "szs_unified_alloc", "szs_unified_free",
                 "szs_fingerprints_init", "szs_fingerprints_sequence", "szs_fingerprints_u32tape",
-                "szs_fingerprints_u64tape", "szs_fingerprints_free"}
+                "szs_fingerprints_u64tape", "szs_fingerprints_free", "szs_fingerprints_utf8_init",
+                "szs_fingerprints_utf8_sequence", "szs_fingerprints_utf8_u32tape", "szs_fingerprints_utf8_u64tape",
+                "szs_fingerprints_utf8_free"}
     for algo in ("levenshtein_distances", "levenshtein_distances_utf8", "needleman_wunsch_scores",
                  "smith_waterman_scores"):
         expected |= {f"szs_{algo}_init", f"szs_{algo}", f"szs_{algo}_u32tape", f"szs_{algo}_u64tape",
@@ -123,14 +125,37 @@ def test_pairwise_count_mismatch_and_small_stride(native):
     native.lib.szs_levenshtein_distances_free(engine)
 
 
-def test_out_of_scope_entry_points_fail_cleanly(native):
+def test_fingerprints_engine_validates_its_arguments(native):
+    """Creation is host-only; calls need a GPU (c/stringzillas/fingerprints.cuh:27-141)."""
     err = ctypes.c_char_p()
+    widths = (ctypes.c_size_t * 2)(5, 0)
     handle = ctypes.c_void_p()
-    widths = (ctypes.c_size_t * 1)(5)
-    assert native.lib.szs_fingerprints_init(ctypes.c_size_t(64), ctypes.c_size_t(256), widths, ctypes.c_size_t(1),
-                                            ctypes.c_uint64(42), None, 0, ctypes.byref(handle),
-                                            ctypes.byref(err)) == native.UNKNOWN
-    assert b"GB300" in err.value
+    assert native.lib.szs_fingerprints_init(64, 256, widths, 2, 42, None, 0, ctypes.byref(handle),
+                                            ctypes.byref(err)) == native.UNEXPECTED_DIMENSIONS
+    assert not handle.value
+    assert native.lib.szs_fingerprints_init(0, 256, None, 0, 42, None, 0, ctypes.byref(handle),
+                                            ctypes.byref(err)) == native.UNEXPECTED_DIMENSIONS
+    for init in (native.lib.szs_fingerprints_init, native.lib.szs_fingerprints_utf8_init):
+        handle = ctypes.c_void_p()
+        assert init(100, 256, None, 0, 7, None, 0, ctypes.byref(handle), ctypes.byref(err)) == native.SUCCESS
+        assert handle.value
+        # A second init into a live handle is refused.
+        assert init(100, 256, None, 0, 7, None, 0, ctypes.byref(handle), ctypes.byref(err)) == native.UNKNOWN
+        data = np.frombuffer(b"hello world", dtype=np.uint8).copy()
+        offsets = np.array([0, 5, 11], dtype=np.uint64)
+        tape = native.U64Tape(data.ctypes.data, offsets.ctypes.data, 2)
+        hashes = np.zeros((2, 100), np.uint32)
+        counts = np.zeros((2, 100), np.uint32)
+        # Strides are bytes and must cover a row.
+        assert native.lib.szs_fingerprints_u64tape(handle, None, ctypes.byref(tape), hashes.ctypes.data, 100,
+                                                   counts.ctypes.data, 400, ctypes.byref(err)) == \
+            native.UNEXPECTED_DIMENSIONS
+        status = native.lib.szs_fingerprints_u64tape(handle, None, ctypes.byref(tape), hashes.ctypes.data, 400,
+                                                     counts.ctypes.data, 400, ctypes.byref(err))
+        assert status == native.MISSING_GPU  # no GPU in the CPU suite
+        native.lib.szs_fingerprints_free(handle)
+    # Freeing a scoring engine through the fingerprint entry point is ignored (handles are tagged).
+    native.lib.szs_fingerprints_free(None)
 
 
 def test_utf8_and_byte_engines_do_not_mix(native):

@@ -108,3 +108,23 @@ def test_port_matches_reference_library_on_random_inputs(port):
         c = [bytes(rng.choice(np.frombuffer(b"ACGT", np.uint8), size=int(rng.integers(0, 90)))) for _ in range(6)]
         np.testing.assert_array_equal(port.cross(costs, tape(q), tape(c)), ref.cross(costs, tape(q), tape(c)))
         np.testing.assert_array_equal(port.cross(costs, tape(q)), ref.cross(costs, tape(q)))
+
+
+def _fingerprint_cases():
+    with np.load(GOLDEN) as data:
+        return {str(name): {k.split("__", 1)[1]: data[k] for k in data.files if k.startswith(f"fp_{name}__")}
+                for name in data["__fingerprints__"]}
+
+
+FINGERPRINTS = _fingerprint_cases()
+
+
+@pytest.mark.parametrize("name", sorted(FINGERPRINTS))
+def test_fingerprints_match_reference_outputs(name):
+    """The oracle's integer restatement of the Min-Hash engine against the reference library's own outputs."""
+    case = FINGERPRINTS[name]
+    dimensions, seed = (int(x) for x in case["params"])
+    widths = [int(w) for w in case["widths"]] or None
+    hashes, counts = oracle.fingerprints(dimensions, (case["data"], case["offsets"]), widths, seed)
+    np.testing.assert_array_equal(hashes, case["hashes"])
+    np.testing.assert_array_equal(counts, case["counts"])
