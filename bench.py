@@ -72,6 +72,9 @@ def parse_args():
     parser.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     parser.add_argument("--no-extra", action="store_true", help="skip the other workloads' lines")
     parser.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    parser.add_argument("--fingerprints-only", action="store_true",
+                        help="run only the Min-Hash leg and print its JSON object")
+    parser.add_argument("--fp-documents", type=int, default=16384, help="documents of the Min-Hash leg")
     return parser.parse_args()
 
 
@@ -365,6 +368,95 @@ def serving_leg(szs):
     return out
 
 
+FINGERPRINT_WORKLOAD = ("Min-Hash fingerprints: 16,384 documents, len U[1,000, 3,000] printable bytes, 1,024 dimensions, "
+                        "default widths {3,4,5,7,9,11,15,31} (64-dimension slices), seed 0")
+# Integer operations per byte and dimension, counted from the rolling step: x = state*a + D*out + (D + 1 + in) (two
+# 32x64-bit products as multiply-adds and two 64-bit adds: 6), the reduction to [0, 2m) (shift, multiply-high,
+# shift, 32x64-bit product, 64-bit subtract: 7) and the high-word test against the running minimum (3). The
+# executed count (ncu, profiles/fingerprints_minhash_1024d.txt) is 28.8 instructions per byte-dimension.
+FINGERPRINT_OPS_PER_BYTE_DIM = 16.0
+FINGERPRINT_EXECUTED_INST_PER_BYTE_DIM = 28.8
+
+
+def fingerprint_texts(count=16384, low=1000, high=3000, seed=7):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = rng.integers(low, high + 1, size=count)
+    offsets = np.zeros(count + 1, dtype=np.uint64)
+    np.cumsum(lengths, out=offsets[1:])
+    data = rng.integers(32, 127, size=int(offsets[-1]), dtype=np.uint8)
+    return data, offsets
+
+
+def fingerprints_leg(szs, torch, scope, peaks, steps=3, warmup=3, cpu_seconds=10.0, documents=16384):
+    """Min-Hash leg: device-resident texts and outputs timed with CUDA events; e2e from pinned host tapes into
+    pinned host outputs; the oracle's C restatement on one core over a sample of the documents."""
+    dims = 1024
+    data, offsets = fingerprint_texts(documents)
+    count = len(offsets) - 1
+    engine = szs.Fingerprints(dims)
+    stream = torch.cuda.current_stream()
+
+    def timed(texts, out, k):
+        for _ in range(warmup):
+            engine(texts, device=scope, out=out)
+        begin, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        begin.record(stream)
+        for _ in range(k):
+            engine(texts, device=scope, out=out)
+        end.record(stream)
+        torch.cuda.synchronize()
+        return begin.elapsed_time(end) / k
+
+    d_texts = szs.Strs.from_buffers(torch.from_numpy(data).cuda(), torch.from_numpy(offsets.astype(np.int64)).cuda())
+    d_out = (torch.empty((count, dims), dtype=torch.int32, device="cuda"),
+             torch.empty((count, dims), dtype=torch.int32, device="cuda"))
+    device_ms = timed(d_texts, d_out, steps)
+    h_texts = szs.Strs.from_buffers(torch.from_numpy(data).pin_memory(),
+                                    torch.from_numpy(offsets.astype(np.int64)).pin_memory())
+    h_out = (torch.empty((count, dims), dtype=torch.int32).pin_memory(),
+             torch.empty((count, dims), dtype=torch.int32).pin_memory())
+    e2e_ms = timed(h_texts, h_out, steps)
+    # Parity of the timed outputs on a sample of documents.
+    from oracle import oracle
+    picks = np.arange(0, count, 997)
+    sub_offsets = np.concatenate([[0], np.cumsum(offsets[picks + 1] - offsets[picks])]).astype(np.uint64)
+    sub_data = np.concatenate([data[offsets[i]:offsets[i + 1]] for i in picks])
+    want_h, want_c = oracle.fingerprints(dims, (sub_data, sub_offsets))
+    got_h = h_out[0].numpy().view(np.uint32)[picks]
+    got_c = h_out[1].numpy().view(np.uint32)[picks]
+    exact = bool(np.array_equal(got_h, want_h) and np.array_equal(got_c, want_c))
+    # CPU: the oracle on one core, documents until the time budget is spent.
+    done_bytes, begin = 0, time.perf_counter()
+    for i in range(count):
+        a, b = int(offsets[i]), int(offsets[i + 1])
+        oracle.fingerprints(dims, (data[a:b], np.array([0, b - a], dtype=np.uint64)))
+        done_bytes += b - a
+        if time.perf_counter() - begin > cpu_seconds:
+            break
+    cpu_s = time.perf_counter() - begin
+    byte_dims = float(offsets[-1]) * dims
+    int_peak = None if not peaks else peaks["lop3"]
+    ops = byte_dims * FINGERPRINT_OPS_PER_BYTE_DIM
+    return {
+        "workload": FINGERPRINT_WORKLOAD.replace("16,384", f"{count:,}"), "unit": "G byte-dimensions/s",
+        "value": byte_dims / (device_ms * 1e-3) / 1e9, "ms_per_step": device_ms,
+        "documents_per_s": count / (device_ms * 1e-3), "text_gbs": float(offsets[-1]) / (device_ms * 1e-3) / 1e9,
+        "e2e": {"value": byte_dims / (e2e_ms * 1e-3) / 1e9, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(data.nbytes + offsets.nbytes), "d2h_bytes_per_step": 2 * count * dims * 4},
+        "roofline_int": {"bound": "int_pipe", "achieved": ops / (device_ms * 1e-3) / 1e12,
+                         "peak": None if int_peak is None else int_peak / 1e12, "unit": "Tops/s",
+                         "frac": None if int_peak is None else ops / (device_ms * 1e-3) / int_peak,
+                         "ops_per_byte_dimension": FINGERPRINT_OPS_PER_BYTE_DIM,
+                         "executed_instructions_per_byte_dimension": FINGERPRINT_EXECUTED_INST_PER_BYTE_DIM,
+                         "note": "bound by the integer multiply-add pipe (68.9% busy in ncu), not by memory"},
+        "cpu_baseline": {"value": done_bytes * dims / cpu_s / 1e9, "unit": "G byte-dimensions/s", "cores": 1,
+                         "kind": "port", "sample": f"{done_bytes} bytes of the documents, oracle C restatement"},
+        "sample_parity_exact": exact,
+        "gpu_launches_per_step": 1,
+    }
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -501,6 +593,7 @@ def run_ours(args):
             del batch
         line["extra"] = extra
         line["serving"] = serving_leg(szs)
+        line["fingerprints"] = fingerprints_leg(szs, torch, scope, peaks)
     elif rank == 0:
         line["cpu_baseline"] = None
     if rank == 0:
@@ -509,9 +602,21 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_fingerprints_only(args):
+    import torch
+    import stringzillas_gb300 as szs
+    torch.cuda.set_device(0)
+    scope = szs.DeviceScope(gpu_device=0, stream=torch.cuda.current_stream())
+    leg = fingerprints_leg(szs, torch, scope, integer_peaks(0), steps=args.steps, warmup=args.warmup,
+                           cpu_seconds=args.cpu_seconds, documents=args.fp_documents)
+    print(json.dumps(leg), flush=True)
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.fingerprints_only:
+        run_fingerprints_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -10,10 +10,16 @@
  *  (byte_out + 1)` with D = -a^w mod m, the reference's two reductions (drop the outgoing byte, append the incoming
  *  one) folded into one.
  *
- *  Magnitudes: 2^42 < m < 2^43 and a < 640, so state * a < 2^52.4 and the whole sum x < 2^52; every product is a
- *  32 x 64-bit one (two multiply-adds). The quotient q = floor(x / m) < 2^10 is estimated from the top 32 bits of x:
- *  with t = x >> 20 and mu = floor(2^74 / m), floor(t * mu / 2^54) is q or q - 1 (the dropped low bits and mu's
- *  truncation each cost less than 2^-22 of a unit), so one conditional subtraction finishes the reduction.
+ *  Magnitudes: 2^42 < m < 2^43 and a < 640. The rolling state is kept in [0, 2m) rather than [0, m): any
+ *  representative continues the recurrence, and the conditional subtraction that would make it canonical is only
+ *  paid where the running minimum needs it. Then x < 2m * a + 256 * D + 256 < 2^54, every product is a 32 x 64-bit
+ *  one (two multiply-adds), and the quotient is estimated from the top 32 bits of x: with t = x >> 22 and
+ *  mu = floor(2^74 / m), floor(t * mu / 2^52) is q or q - 1 (the dropped low bits and mu's truncation each cost
+ *  less than 2^-20 of a unit), so x - estimate * m lies in [0, 2m) again.
+ *
+ *  The running minimum is over canonical values c = state or state - m. A window can only reach it when the high
+ *  words pass `state_hi <= min_hi || state_hi - m_hi <= min_hi + 1` (a borrow can lower state - m's high word by one),
+ *  a 32-bit test that fails for nearly every window of a long text; the exact comparison runs behind it.
  *
  *  One warp scores 32 consecutive dimensions of one text: the lanes read the same byte stream (the reference's
  *  64-dimension slices share a width, so their outgoing bytes coincide too) and write 32 adjacent outputs.
@@ -24,11 +30,14 @@ namespace szs_gb300 {
 
 namespace {
 
-/** x mod m for x < 2^52 (see the file comment). */
+/** A representative in [0, 2m) of x mod m, for x < 2^54 (see the file comment). */
 __device__ __forceinline__ std::uint64_t reduce(std::uint64_t x, std::uint64_t modulo, std::uint32_t mu) {
-    std::uint32_t const top = (std::uint32_t)(x >> 20);
-    std::uint32_t const quotient = __umulhi(top, mu) >> 22;
-    std::uint64_t const r = x - (std::uint64_t)quotient * modulo;
+    std::uint32_t const top = (std::uint32_t)(x >> 22);
+    std::uint32_t const quotient = __umulhi(top, mu) >> 20;
+    return x - (std::uint64_t)quotient * modulo;
+}
+
+__device__ __forceinline__ std::uint64_t canonical(std::uint64_t r, std::uint64_t modulo) {
     return r >= modulo ? r - modulo : r;
 }
 
@@ -60,15 +69,27 @@ __global__ void fingerprints_kernel(tape_t const texts, fingerprint_dim_t const 
             std::uint64_t state = 0;
             for (std::uint32_t i = 0; i < p.width; ++i)
                 state = reduce(state * p.multiplier + bytes[i] + 1u, p.modulo, p.mu);
-            std::uint64_t minimum = state;
+            std::uint64_t minimum = canonical(state, p.modulo);
             std::uint32_t occurrences = 1;
-            std::uint8_t const *outgoing = bytes;
-            for (std::uint8_t const *incoming = bytes + p.width, *end = bytes + length; incoming != end;
-                 ++incoming, ++outgoing) {
-                std::uint64_t const x = state * p.multiplier + (*incoming + 1u) + p.discard * (*outgoing + 1u);
+            std::uint32_t const modulo_hi = (std::uint32_t)(p.modulo >> 32);
+            std::uint32_t minimum_hi = (std::uint32_t)(minimum >> 32);
+            // in + 1 + D * (out + 1) = in + D * out + (D + 1)
+            std::uint64_t const constant = p.discard + 1u;
+            std::uint64_t const windows = length - p.width;
+#pragma unroll 8
+            for (std::uint64_t i = 0; i < windows; ++i) {
+                std::uint64_t const x =
+                    state * p.multiplier + p.discard * bytes[i] + (constant + bytes[p.width + i]);
                 state = reduce(x, p.modulo, p.mu);
-                occurrences = state < minimum ? 1u : occurrences + (state == minimum);
-                minimum = state < minimum ? state : minimum;
+                std::uint32_t const state_hi = (std::uint32_t)(state >> 32);
+                if (__builtin_expect(state_hi <= minimum_hi || state_hi - modulo_hi <= minimum_hi + 1u, 0)) {
+                    std::uint64_t const value = canonical(state, p.modulo);
+                    if (value <= minimum) {
+                        occurrences = value == minimum ? occurrences + 1u : 1u;
+                        minimum = value;
+                        minimum_hi = (std::uint32_t)(minimum >> 32);
+                    }
+                }
             }
             min_hash = (std::uint32_t)(minimum & 0xFFFFFFFFu), min_count = occurrences;
         }

@@ -159,3 +159,27 @@ def test_large_corpus_sampled_rows(szs):
     np.testing.assert_array_equal(hashes[picks], want_h)
     np.testing.assert_array_equal(counts[picks], want_c)
     assert (counts >= 1).all()
+
+
+@pytest.mark.parametrize("ndim", [1, 7, 64, 1024])
+def test_reference_test_shapes(szs, ndim):
+    """The reference's own checks (test/fingerprints.py): shapes and dtypes, identical texts agree, different texts
+    differ, degenerate texts are deterministic; values from the oracle."""
+    engine = szs.Fingerprints(ndim=ndim)
+    hashes, counts = engine(szs.Strs([]))
+    assert hashes.shape == (0, ndim) and counts.shape == (0, ndim)
+    assert hashes.dtype == np.uint32 and counts.dtype == np.uint32
+    texts = ["hello", "world", "hello", "a", "a" * 40, "b", "", "a" * 5]
+    hashes, counts = engine(szs.Strs(texts))
+    assert hashes.shape == (len(texts), ndim)
+    np.testing.assert_array_equal(hashes[0], hashes[2])
+    np.testing.assert_array_equal(counts[0], counts[2])
+    assert ndim < 7 or not np.array_equal(hashes[0], hashes[1])
+    data = np.frombuffer("".join(texts).encode(), dtype=np.uint8).copy()
+    offsets = np.concatenate([[0], np.cumsum([len(t) for t in texts])]).astype(np.uint64)
+    want_h, want_c = oracle.fingerprints(ndim, (data, offsets))
+    np.testing.assert_array_equal(hashes, want_h)
+    np.testing.assert_array_equal(counts, want_c)
+    again_h, again_c = engine(szs.Strs(texts))
+    np.testing.assert_array_equal(again_h, hashes)
+    np.testing.assert_array_equal(again_c, counts)
