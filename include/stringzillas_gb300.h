@@ -38,6 +38,7 @@ extern "C" {
 #ifndef STRINGZILLA_TYPES_H_
 typedef int8_t sz_i8_t;                /* types.h:530 */
 typedef uint8_t sz_u8_t;               /* types.h:531 */
+typedef uint16_t sz_u16_t;             /* types.h:533 */
 typedef uint32_t sz_u32_t;             /* types.h:535 */
 typedef uint64_t sz_u64_t;             /* types.h:536 */
 typedef size_t sz_size_t;              /* types.h:538 */
@@ -453,12 +454,16 @@ SZS_GB300_API sz_status_t szs_gb300_device_scope_init_stream(sz_size_t gpu_devic
  *  No counterpart in the reference, whose tier thresholds are compile-time constants.
  */
 typedef struct szs_gb300_tuning_t {
-    sz_u8_t packed_rows[16]; /**< rows per lane of the 16x2 route (4, 8, 12 or 16); 0 = instruction-count model */
+    sz_u8_t packed_rows[16]; /**< rows per lane of the 16x2 route (4, 8, 12 or 16); 0 = per-pair step-cost model */
     sz_u8_t cell_bits[16];   /**< 0 = the narrowest cells the length bound proves safe; 32 = never 16-bit cells */
     sz_u32_t band_min_rows;  /**< pairs on 32-bit cells whose shorter side exceeds this take the band (0 = 1,024) */
     sz_u32_t packed_warps[4]; /**< warps per CTA (1..8) of the 16x2 launches with 4, 8, 12, 16 rows (0 = 4) */
     sz_u32_t band_min_rows_packed; /**< the same threshold for pairs that fit 16-bit cells (0 = 2,048) */
     sz_u32_t pipeline_chunk_kb;   /**< input KiB per chunk of a pipelined pinned-host pairwise call (0 = 64 MiB) */
+    /** Relative cost of one lane step of the 16x2 route with 4, 8, 12, 16 rows per lane. Where `packed_rows` is 0
+        the planner gives each pair the rows per lane of least `strips x (m + 31) x cost` (0 = built-in 100, 165,
+        245, 330). */
+    sz_u16_t packed_step_cost[4];
 } szs_gb300_tuning_t;
 
 /** Installs @p tuning on @p engine (NULL restores the built-in choices); out-of-range values are rejected with

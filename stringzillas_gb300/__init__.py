@@ -357,17 +357,18 @@ class _Engine:
     def set_tuning(self, tuning=None):
         """Extension: per-length-bin choices (see ``szs_gb300_tuning_t``): a dict with any of ``packed_rows`` (16
         values), ``cell_bits`` (16 values), ``band_min_rows``, ``packed_warps`` (4 values),
-        ``band_min_rows_packed`` and ``pipeline_chunk_kb``; None restores the built-in choices."""
+        ``band_min_rows_packed``, ``pipeline_chunk_kb`` and ``packed_step_cost`` (4 values); None restores the
+        built-in choices."""
         err = ctypes.c_char_p()
         if tuning is None:
             status = lib.szs_gb300_engine_set_tuning(self.handle, None, ctypes.byref(err))
         else:
             unknown = set(tuning) - {"packed_rows", "cell_bits", "band_min_rows", "packed_warps", "band_min_rows_packed",
-                                     "pipeline_chunk_kb"}
+                                     "pipeline_chunk_kb", "packed_step_cost"}
             if unknown:
                 raise ValueError(f"unknown tuning fields {sorted(unknown)}")
             t = _native.Tuning()
-            for name, size in (("packed_rows", 16), ("cell_bits", 16), ("packed_warps", 4)):
+            for name, size in (("packed_rows", 16), ("cell_bits", 16), ("packed_warps", 4), ("packed_step_cost", 4)):
                 values = list(tuning.get(name, [0] * size))
                 if len(values) != size:
                     raise ValueError(f"{name} needs {size} values")
@@ -386,7 +387,8 @@ class _Engine:
                           "get_tuning")
         return {"packed_rows": list(t.packed_rows), "cell_bits": list(t.cell_bits),
                 "band_min_rows": t.band_min_rows, "packed_warps": list(t.packed_warps),
-                "band_min_rows_packed": t.band_min_rows_packed, "pipeline_chunk_kb": t.pipeline_chunk_kb}
+                "band_min_rows_packed": t.band_min_rows_packed, "pipeline_chunk_kb": t.pipeline_chunk_kb,
+                "packed_step_cost": list(t.packed_step_cost)}
 
     def stats(self) -> dict:
         """Extension: counters of the last call (device time, cells, pairs, launches)."""

@@ -149,6 +149,7 @@ class Tuning(ctypes.Structure):
         ("packed_warps", ctypes.c_uint32 * 4),
         ("band_min_rows_packed", ctypes.c_uint32),
         ("pipeline_chunk_kb", ctypes.c_uint32),
+        ("packed_step_cost", ctypes.c_uint16 * 4),
     ]
 
 

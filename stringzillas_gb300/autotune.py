@@ -4,11 +4,14 @@ For every engine family (kind x linear/affine gaps) and every length class k (pa
 floor(log2 n) == k) it times, on synthetic pairs of that class, each candidate of
 
 * cell width: 16x2 packed cells (where the length bound allows them) or 32-bit cells,
-* tile shape: rows per lane R in {4, 8, 12, 16} of the packed wavefront (a warp's strip is 32 R rows),
+* tile shape: rows per lane R in {4, 8, 12, 16} of the packed wavefront (a warp's strip is 32 R rows), one R for
+  the whole class or R chosen per pair by the planner's step-cost model,
 * pairs per block: warps per CTA in {2, 4, 8} of the packed launches (each warp scores two pairs at once),
 
-and keeps the fastest by the scoring kernels' CUDA-event time (``last_compute_ms``); then it picks the band
-threshold (shorter sides above it go to the one-CTA-per-pair band kernel) on a batch of long pairs. The result is a
+and keeps the fastest by the scoring kernels' CUDA-event time (``last_compute_ms``). The step-cost model's four
+costs (one lane step with R rows per lane) are fitted from the fixed-R timings: each timing divided by the lane
+steps its batch needs with that R (strips x (m + 31) summed over the pairs). Then it picks the band threshold
+(shorter sides above it go to the one-CTA-per-pair band kernel) on a batch of long pairs. The result is a
 JSON file that ``apply`` installs on an engine. The reference fixes its tier thresholds at compile time; this module
 has no counterpart there.
 
@@ -60,8 +63,9 @@ def _engines(szs):
     }
 
 
-def _batch(szs, rng, low, high, target_cells, alphabet):
-    """Device-resident pairs with both lengths uniform in [low, high), about `target_cells` cells."""
+def _batch(szs, rng, low, high, target_cells, alphabet, sides=None):
+    """Device-resident pairs with both lengths uniform in [low, high), about `target_cells` cells; with `sides`
+    (a list) the pairs' (shorter, longer) sides are appended to it."""
     mean = (low + high) / 2
     # Enough pairs for several waves of warps on every SM, so a class is not measured on a half-empty GPU.
     count = int(max(1 << 15, min(1 << 20, target_cells / (mean * mean))))
@@ -73,7 +77,27 @@ def _batch(szs, rng, low, high, target_cells, alphabet):
         np.cumsum(lengths, out=offsets[1:])
         data = rng.choice(alphabet, size=int(offsets[-1])).astype(np.uint8)
         tapes.append(szs.to_device(szs.Strs.from_buffers(data, offsets)))
+    if sides is not None:
+        sides.append((np.minimum(la, lb), np.maximum(la, lb)))
     return tapes[0], tapes[1], int(np.dot(la, lb))
+
+
+def lane_steps(n, m, rows):
+    """Lane steps of the 16x2 route for pairs of shorter sides n and longer sides m with `rows` rows per lane."""
+    strips = (n + 32 * rows - 1) // (32 * rows)
+    return float(np.sum(strips * (m + 31)))
+
+
+def fit_step_costs(classes):
+    """Relative cost of one lane step per rows choice (R = 4 -> 100) from fixed-R timings: for each class, time / lane
+    steps; the median over the classes."""
+    ratios = []
+    for timings, (n, m) in classes:
+        per_step = [timings[f"16x2 R={rows}"] / lane_steps(n, m, rows) for rows in ROWS]
+        ratios.append([p / per_step[0] for p in per_step])
+    if not ratios:
+        return [0, 0, 0, 0]
+    return [int(round(100 * float(np.median([r[i] for r in ratios])))) for i in range(len(ROWS))]
 
 
 def _time(engine, first, second, out, repeats=3):
@@ -94,10 +118,12 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
              "packed_warps": [0] * 4, "band_min_rows_packed": 1 << (max(CLASSES) + 1)}
     measurements = {}
     rows_votes = {}
+    batches, fits = {}, []
     for k in CLASSES:
         if family == "lev-unit" and k < 9:
             continue  # the bit-parallel route takes these
-        first, second, cells = _batch(szs, rng, 1 << k, 1 << (k + 1), target_cells, alphabet)
+        lengths = []
+        first, second, cells = _batch(szs, rng, 1 << k, 1 << (k + 1), target_cells, alphabet, lengths)
         out = np.empty(len(first), dtype=engine._dtype)
         timings = {}
         base = dict(table)
@@ -112,11 +138,34 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
         else:
             rows = int(best.split("=")[1])
             table["packed_rows"][k] = rows
-            rows_votes.setdefault(rows, []).append(k)
+            if 6 <= k <= 9:  # classes with several strips and many waves of warps fit the step costs
+                fits.append((timings, lengths[0]))
+            batches[k] = (first, second, cells, out, timings)
         measurements[f"class {k} (n in [{1 << k}, {1 << (k + 1)}))"] = {
             "cells": cells, "GCUPS": {name: cells / (ms * 1e6) for name, ms in timings.items()}, "best": best}
         log(f"  {family:10s} class {k:2d}: best {best:12s} "
             + " ".join(f"{n}={cells / (ms * 1e6):7.0f}" for n, ms in timings.items()))
+    # Rows per lane chosen per pair by the step-cost model, against the class's best fixed choice.
+    table["packed_step_cost"] = fit_step_costs(fits)
+    measurements["packed_step_cost"] = table["packed_step_cost"]
+    for k, (first, second, cells, out, timings) in sorted(batches.items()):
+        trial = dict(table, packed_rows=[0 if c == k else r for c, r in enumerate(table["packed_rows"])])
+        engine.set_tuning(trial)
+        model_ms = _time(engine, first, second, out)
+        best_ms = min(timings.values())
+        key = f"class {k} (n in [{1 << k}, {1 << (k + 1)}))"
+        measurements[key]["GCUPS"]["16x2 per-pair model"] = cells / (model_ms * 1e6)
+        if model_ms < best_ms:
+            table["packed_rows"][k] = 0
+            measurements[key]["best"] = "16x2 per-pair model"
+        log(f"  {family:10s} class {k:2d}: per-pair model {cells / (model_ms * 1e6):7.0f} "
+            f"(best fixed {cells / (best_ms * 1e6):7.0f})")
+    del batches
+    # The rows choices that classes use, for the warps-per-CTA pass (the model's pairs count for every choice).
+    for k in CLASSES:
+        rows = table["packed_rows"][k]
+        if rows:
+            rows_votes.setdefault(rows, []).append(k)
     # Pairs per block: warps per CTA for each rows choice, on the classes that chose it.
     engine.set_tuning(table)
     for rows, classes in sorted(rows_votes.items()):

@@ -714,6 +714,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.band_min_rows = engine.tuning.band_min_rows ? engine.tuning.band_min_rows : (std::uint32_t)band_min_rows_k;
     args.band_min_rows_packed = engine.tuning.band_min_rows_packed ? engine.tuning.band_min_rows_packed
                                                                    : (std::uint32_t)band_min_rows_packed_k;
+    for (int choice = 0; choice < 4; ++choice)
+        args.packed_step_cost[choice] = engine.tuning.packed_step_cost[choice]
+                                            ? engine.tuning.packed_step_cost[choice]
+                                            : (std::uint16_t)packed_step_cost_k[choice];
     bool const levenshtein = engine.kind == kind_levenshtein_k;
     bool const dense = !engine.dense.empty();
     bool const alphabet_pass = levenshtein || dense; // both score over the batch's own byte codes

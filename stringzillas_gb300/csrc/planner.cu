@@ -116,7 +116,9 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
             info.key = bin_dp16_begin_k + dp16_classes_per_rows_k; // plain form: one bin (8 rows per lane), input order
             return info;
         }
-        // Rows per lane: the fewest instructions for strips(R) x (m + 31) steps x (7 R + 40) per step.
+        // Rows per lane: a tuned choice for the length class, else the least strips(R) x (m + 31) steps x the
+        // measured cost of one step with R rows per lane (a strip holds 32 R rows, so the last strip's padding
+        // rows count as work).
         int best_choice = 0;
         if (args.packed_rows[length_class]) best_choice = args.packed_rows[length_class] / 4 - 1; // tuned
         else {
@@ -124,7 +126,7 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
             for (int choice = 0; choice < dp16_row_choices_k; ++choice) {
                 std::uint64_t const rows = 4u * (choice + 1);
                 std::uint64_t const strips = (n + 32 * rows - 1) / (32 * rows);
-                float const cost = (float)strips * (float)(m + 31) * (7.0f * rows + 40.0f);
+                float const cost = (float)strips * (float)(m + 31) * (float)args.packed_step_cost[choice];
                 if (cost < best_cost) best_cost = cost, best_choice = choice;
             }
         }

@@ -38,6 +38,9 @@ constexpr int bin_band16_begin_k = bin_band_begin_k + bin_dp_classes_k;  // 1392
 static_assert(bin_band16_begin_k + bin_dp_classes_k <= bin_keys_k, "bin layout exceeds the key space");
 static_assert(bin_keys_k % 2 == 0 && bin_keys_k / 2 <= 1024, "the scan kernel uses one CTA of bin_keys_k / 2 threads");
 constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shorter side exceeds this take a whole CTA
+/** Built-in relative costs of one lane step of the 16x2 route with 4, 8, 12, 16 rows per lane, measured on GB300
+ *  (affine protein alignment, shorter sides 128-1,023). */
+constexpr int packed_step_cost_k[4] = {100, 165, 245, 330};
 constexpr int band_min_rows_packed_k = 2048; // default for pairs that fit 16-bit cells (the 16-bit band above it)
 constexpr int myers_max_words_k = 16;
 
@@ -72,10 +75,11 @@ struct plan_args_t {
     int packed_allowed;     // 1 if the 16x2 route may hold the substitution costs in int8 profiles
     batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)
     // Tuning by length class k = floor(log2(shorter side)), 15 for everything longer.
-    std::uint8_t packed_rows[16];     // 0: instruction-count model; else rows per lane 4, 8, 12, 16
+    std::uint8_t packed_rows[16];     // 0: per-pair step-cost model; else rows per lane 4, 8, 12, 16
     std::uint8_t cell_bits[16];       // 0: narrowest safe; 32: never 16-bit cells
     std::uint32_t band_min_rows;      // shorter sides above this take the band (pairs on 32-bit cells)
     std::uint32_t band_min_rows_packed; // the same for pairs that fit 16-bit cells
+    std::uint16_t packed_step_cost[4];  // relative cost of one lane step with 4, 8, 12, 16 rows per lane
 };
 
 /** Per-bin counters the planner fills. */

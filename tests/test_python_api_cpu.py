@@ -132,10 +132,11 @@ def test_tuning_round_trip_and_validation():
     from stringzillas_gb300 import autotune, workloads as w
     engine = szs.NeedlemanWunschScores(*w.protein_table(), open=-11, extend=-1)
     assert engine.get_tuning() == {"packed_rows": [0] * 16, "cell_bits": [0] * 16, "band_min_rows": 0,
-                                   "packed_warps": [0] * 4, "band_min_rows_packed": 0, "pipeline_chunk_kb": 0}
+                                   "packed_warps": [0] * 4, "band_min_rows_packed": 0, "pipeline_chunk_kb": 0,
+                                   "packed_step_cost": [0] * 4}
     tuning = {"packed_rows": [0, 0, 0, 4, 4, 8, 8, 12, 16, 16, 16, 0, 0, 0, 0, 0], "cell_bits": [32] + [0] * 15,
               "band_min_rows": 2048, "packed_warps": [2, 4, 8, 4], "band_min_rows_packed": 3000,
-              "pipeline_chunk_kb": 8192}
+              "pipeline_chunk_kb": 8192, "packed_step_cost": [100, 170, 240, 320]}
     engine.set_tuning(tuning)
     assert engine.get_tuning() == tuning
     for bad in ({"packed_rows": [3] * 16}, {"cell_bits": [16] * 16}, {"packed_warps": [9, 0, 0, 0]},
@@ -166,3 +167,19 @@ def test_dense_table_constructor_validation():
         szs.NeedlemanWunschScores.dense(np.zeros((256, 256), dtype=np.int16))
     with pytest.raises(TypeError):
         szs.NeedlemanWunschScores.dense([[0] * 256] * 256)
+
+
+def test_step_cost_fit_recovers_planted_costs():
+    """The autotuner's step-cost fit: timings made from planted per-step costs give those costs back."""
+    from stringzillas_gb300 import autotune
+    rng = np.random.default_rng(2)
+    planted = [100, 170, 250, 340]
+    classes = []
+    for k in (6, 7, 8, 9):
+        la, lb = rng.integers(1 << k, 1 << (k + 1), size=(2, 5000))
+        n, m = np.minimum(la, lb), np.maximum(la, lb)
+        timings = {f"16x2 R={rows}": cost * autotune.lane_steps(n, m, rows) * 1e-9
+                   for rows, cost in zip(autotune.ROWS, planted)}
+        classes.append((timings, (n, m)))
+    assert autotune.fit_step_costs(classes) == planted
+    assert autotune.fit_step_costs([]) == [0, 0, 0, 0]
