@@ -46,7 +46,11 @@ METRIC = "GCUPS batched Levenshtein/NW/SW, 1 GB300, vs plain launch; serving p50
 #    (Xv, Eq&Pv, 2-op carried add, Xh, Ph, Mh, two funnel shifts, Pv, Mv); DNA needs B = 2 -> 13 / 32 per cell.
 #  - wavefront, 32-bit cells: linear 4 = opt(up, left) + (diag + s) + fused add-opt + cost unpack;
 #    affine 7 = E (add + fused add-opt) + F (add + fused add-opt) + (diag + s) + 3-way opt + cost unpack.
-OPS_PER_CELL = {"myers_dna": 13.0 / 32.0, "dp_linear": 4.0, "dp_affine": 7.0}
+#  - 16x2 packed cells (the NW / SW configurations run there: warp route and 16-bit band): per register of two
+#    cells, affine 5 DPX (E, diag + s against E, F, max, + open) + 1 byte permute of the two pairs' costs, plus the
+#    running maximum for local scores -> 3.0 (global) / 3.5 (local) per cell.
+OPS_PER_CELL = {"myers_dna": 13.0 / 32.0, "dp_linear": 4.0, "dp_affine": 7.0, "packed_affine": 3.0,
+                "packed_affine_local": 3.5}
 
 WORKLOADS = {
     "c1": "plain Levenshtein: 1,024 DNA pairs, len U[64,256], partner 5% subs + 2% indels, unit costs",
@@ -125,7 +129,9 @@ def oracle_costs(kind_and_tables):
 
 def ops_per_cell(kind_and_tables):
     kind = kind_and_tables[0]
-    return OPS_PER_CELL["myers_dna"] if kind == "lev" else OPS_PER_CELL["dp_affine"]
+    if kind == "lev":
+        return OPS_PER_CELL["myers_dna"]
+    return OPS_PER_CELL["packed_affine_local"] if kind == "sw" else OPS_PER_CELL["packed_affine"]
 
 
 class Clocks:
@@ -544,7 +550,7 @@ def run_ours(args):
         int_ops = cells_per_step * ops_per_cell(kind_and_tables)
         int_peak = None
         if peaks:
-            int_peak = peaks["lop3"] if kind_and_tables[0] == "lev" else peaks["dpx_viaddmax_s32"]
+            int_peak = peaks["lop3"] if kind_and_tables[0] == "lev" else peaks["dpx_viaddmax_s16x2"]
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,

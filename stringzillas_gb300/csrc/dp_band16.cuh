@@ -259,6 +259,8 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         std::uint32_t const steady_end = m >= 64u ? max(fill_end, min(steps, m - 1u)) : fill_end;
         std::uint32_t t = 0;
         for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
+        // Two steps per iteration: the row state alternates between two register sets instead of being copied back.
+#pragma unroll 2
         for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
         for (; t < steps && healthy; ++t) step(t, std::false_type {});
         __syncwarp();
