@@ -297,6 +297,7 @@ def cpu_baseline(first, second, kind_and_tables, seconds_budget):
 
 SERVING_RATE = 120.0      # offered load, requests per second (Poisson arrivals)
 SERVING_REQUESTS = 240    # requests per run, drawn from a pool of 48 distinct ones
+NW_SW_BURST = 64          # requests of the NW / SW-only burst, drawn from a pool of 32
 
 
 def serving_engines(szs):
@@ -371,6 +372,20 @@ def serving_leg(szs):
             "arena_peak_bytes": stats["arena_peak_bytes"], "kernel_launches": stats["kernel_launches"]}
     out["saturated_serving_over_plain"] = (out["serving"]["saturated_gcups"] /
                                            out["per_request_plain"]["saturated_gcups"])
+    # Mixed-length NW / SW only: a saturating burst of alignment requests, both forms.
+    nw_sw = w.serving_requests(32, seed=43, kinds=("nw", "sw"))
+    burst = rng.integers(0, len(nw_sw), size=NW_SW_BURST)
+    burst_cells = int(sum(nw_sw[k]["cells"] for k in burst))
+    mix = {"requests": NW_SW_BURST, "cells": burst_cells,
+           "mix": "NW:SW 1:1 (affine protein), 1-4,096 pairs per request, pair lengths log-uniform [16, 16,384]"}
+    for name, config in forms.items():
+        with szs.Server(**config) as server:
+            serve_stream(szs, server, engines, nw_sw, burst[:4], np.zeros(4))
+            infos, wall = serve_stream(szs, server, engines, nw_sw, burst, np.zeros(len(burst)))
+        mix[name] = {"saturated_gcups": burst_cells / wall / 1e9,
+                     "p99_ms": float(np.percentile([i["done_ms"] for i in infos], 99))}
+    mix["serving_over_plain"] = mix["serving"]["saturated_gcups"] / mix["per_request_plain"]["saturated_gcups"]
+    out["nw_sw_burst"] = mix
     return out
 
 
@@ -595,6 +610,7 @@ def run_ours(args):
                 row[schedule] = {"GCUPS": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms / 2,
                                  "compute_ms_per_step": cms / 2}
             row["batched_over_plain"] = row["batched"]["GCUPS"] / row["plain"]["GCUPS"]
+            row["cpu_baseline"] = cpu_baseline(f, s, kt, 3.0)
             extra[name] = row
             del batch
         line["extra"] = extra

@@ -139,12 +139,13 @@ def cells(first, second) -> int:
     return int(np.dot(np.diff(first[1]).astype(np.int64), np.diff(second[1]).astype(np.int64)))
 
 
-def serving_requests(count, min_pairs=1, max_pairs=4096, min_length=16, max_length=16384, seed=42):
+def serving_requests(count, min_pairs=1, max_pairs=4096, min_length=16, max_length=16384, seed=42,
+                     kinds=("lev", "lev", "nw", "sw")):
     """`count` requests of the serving stream: dicts with ``kind`` ("lev", "nw" or "sw"), ``first`` and ``second``
-    tapes, ``pairs`` and ``cells``. Kinds are drawn 2:1:1; each pair's first length is log-uniform and its partner
-    is a mutant of it."""
+    tapes, ``pairs`` and ``cells``. Kinds are drawn uniformly from `kinds` (2:1:1 by default); each pair's first
+    length is log-uniform and its partner is a mutant of it."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    kinds = rng.choice(np.array(["lev", "lev", "nw", "sw"]), size=count)
+    kinds = rng.choice(np.array(list(kinds)), size=count)
     pair_counts = np.exp(rng.uniform(np.log(min_pairs), np.log(max_pairs + 1), size=count)).astype(np.int64)
     pair_counts = np.clip(pair_counts, min_pairs, max_pairs)
     requests = []
