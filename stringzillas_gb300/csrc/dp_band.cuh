@@ -16,6 +16,12 @@
  *  wait is bounded: after `band_wait_limit_k` polls the warp raises the CTA's error flag, which also releases the
  *  other warps' waits, the pair is abandoned and the host reports an error for the call.
  *
+ *  Groups: when a call has fewer long pairs than the GPU holds CTAs, G co-resident CTAs (one cooperative launch)
+ *  share a pair and the ring spans all their G x W warps; its progress words, failure flag and a barrier counter
+ *  then live in global memory (`band_group_state_t`), published with GPU-scope fences. Between pairs the CTAs of a
+ *  group meet at a bounded barrier; the per-pair words are double-buffered by the pair's parity, so a CTA still
+ *  reading one pair's result never sees the next pair's reset.
+ *
  *  Inside a strip, lanes, steps, chunk staging and the shortened dependency chain are those of dp_packed.cuh, on
  *  32-bit cells with DPX `__viaddmax_s32` / `__viaddmin_s32`.
  */
@@ -58,6 +64,7 @@ struct band_shared_t {
     std::uint32_t pair_index;
     std::uint32_t failed;
     std::uint32_t redo; // 16-bit band: the pair reached the 16-bit limit and is scored again on 32-bit cells
+    std::uint32_t gate; // grouped kernels: the outcome of the last group barrier
 };
 
 template <typename policy_>
@@ -71,35 +78,103 @@ __host__ __device__ constexpr int band_shared_bytes(int classes) {
            band_warps_k * (band_profile_bytes_per_warp<policy_>(classes) + int(sizeof(band_chunk_t)));
 }
 
+/** The ring a warp takes part in: its progress words and failure flag (the CTA's shared memory, or global memory
+ *  for a group of CTAs), the number of warps in the ring and this warp's place in it. */
+struct band_ring_t {
+    unsigned long long *progress;
+    std::uint32_t *failed;
+    int members;
+    int member;
+    bool grid_scope; // progress and failure words are in global memory, shared with other CTAs
+};
+
+__device__ __forceinline__ band_ring_t band_cta_ring(band_shared_t &shared, int warp) {
+    return {shared.progress, &shared.failed, band_warps_k, warp, false};
+}
+
 /** Lane 0 of a warp waits (bounded) until ring slot `slot` has reached `target`; the warp then proceeds together. */
-__device__ __forceinline__ bool band_wait(band_shared_t &shared, int slot, unsigned long long target) {
+__device__ __forceinline__ bool band_wait(band_ring_t const &ring, int slot, unsigned long long target) {
     int const lane = threadIdx.x & 31;
     int ok = 1;
     if (lane == 0) {
         std::uint32_t polls = 0;
         while (true) {
-            unsigned long long const seen = *reinterpret_cast<volatile unsigned long long *>(&shared.progress[slot]);
+            unsigned long long const seen = *reinterpret_cast<volatile unsigned long long *>(&ring.progress[slot]);
             if (seen >= target) break;
-            if (*reinterpret_cast<volatile std::uint32_t *>(&shared.failed)) {
+            if (*reinterpret_cast<volatile std::uint32_t *>(ring.failed)) {
                 ok = 0;
                 break;
             }
             if (++polls > band_wait_limit_k) {
-                atomicExch(&shared.failed, 1u);
+                atomicExch(ring.failed, 1u);
                 ok = 0;
                 break;
             }
             __nanosleep(100);
         }
-        __threadfence_block();
+        if (ring.grid_scope) __threadfence();
+        else __threadfence_block();
     }
     ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+    if (ring.grid_scope) __threadfence(); // every lane's ring reads come after the producer's release
     return ok != 0;
 }
 
-__device__ __forceinline__ void band_publish(band_shared_t &shared, int slot, unsigned long long value) {
-    __threadfence_block();
-    *reinterpret_cast<volatile unsigned long long *>(&shared.progress[slot]) = value;
+__device__ __forceinline__ void band_publish(band_ring_t const &ring, int slot, unsigned long long value) {
+    if (ring.grid_scope) __threadfence();
+    else __threadfence_block();
+    *reinterpret_cast<volatile unsigned long long *>(&ring.progress[slot]) = value;
+}
+
+/** Most CTAs one long pair can share, and the ring words of a group. */
+constexpr int band_group_max_ctas_k = 16;
+constexpr int band_group_max_members_k = band_group_max_ctas_k * band_warps_k;
+constexpr std::uint32_t band_barrier_limit_k = 1u << 24; // polls of ~200 ns each, about 3 s
+
+/** One pass over a pair (16-bit or 32-bit cells): ring progress and the combined result. */
+struct band_pass_state_t {
+    unsigned long long progress[band_group_max_members_k];
+    std::int32_t best; // local scores: maximum over the group; global scores: the corner cell, from its owner
+    std::uint32_t reserved;
+};
+
+/** A group's words in global memory: two pair parities x two passes, the failure flag and the barrier counter.
+ *  Zeroed by the host before the launch. */
+struct band_group_state_t {
+    band_pass_state_t pass[2][2];
+    std::uint32_t failed;
+    std::uint32_t arrived;
+};
+
+/** Bounded barrier of the G CTAs of a group: the `number`-th meeting needs G * number arrivals. Returns false when the
+ *  group failed or the wait ran out (then the group's failure flag is set). */
+__device__ __forceinline__ bool band_group_barrier(band_group_state_t *group, int ctas, std::uint32_t number,
+                                                   std::uint32_t &flag_in_shared) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&group->arrived, 1u);
+        std::uint32_t const target = (std::uint32_t)ctas * number;
+        std::uint32_t polls = 0;
+        std::uint32_t ok = 1;
+        while (*reinterpret_cast<volatile std::uint32_t *>(&group->arrived) < target) {
+            if (*reinterpret_cast<volatile std::uint32_t *>(&group->failed)) {
+                ok = 0;
+                break;
+            }
+            if (++polls > band_barrier_limit_k) {
+                atomicExch(&group->failed, 1u);
+                ok = 0;
+                break;
+            }
+            __nanosleep(200);
+        }
+        if (*reinterpret_cast<volatile std::uint32_t *>(&group->failed)) ok = 0;
+        __threadfence();
+        flag_in_shared = ok;
+    }
+    __syncthreads();
+    return flag_in_shared != 0;
 }
 
 /**
@@ -108,15 +183,16 @@ __device__ __forceinline__ void band_publish(band_shared_t &shared, int slot, un
  */
 template <typename policy_>
 __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task, score_costs_t const &costs,
-                                                        band_shared_t &shared, std::int32_t *ring,
+                                                        band_ring_t const &sync, std::int32_t *ring,
                                                         std::size_t ring_cells_per_slot, std::int8_t *profile,
-                                                        band_chunk_t &chunk, int warp) {
+                                                        band_chunk_t &chunk) {
     using ops = typename policy_::ops_t;
     constexpr int R = policy_::rows_per_lane_k;
     constexpr int S = policy_::strip_rows_k;
     constexpr bool affine = policy_::affine_k;
     constexpr bool local = policy_::local_k;
-    constexpr int W = band_warps_k;
+    std::uint32_t const W = (std::uint32_t)sync.members;
+    int const warp = sync.member;
     static_assert(R % 4 == 0, "profile rows are read in 4-byte words");
     constexpr int words = R / 4;
 
@@ -187,7 +263,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             if (e == 0) {
                 // Stage lane 0's next columns; strips below the first wait for the strip above to write them.
                 std::uint32_t const need = min(m, t + band_chunk_k);
-                if (k > 0 && t + 1 <= m) healthy = band_wait(shared, slot_in, ((unsigned long long)k << 32) | need);
+                if (k > 0 && t + 1 <= m) healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
                 __syncwarp();
                 for (int c = lane; c < band_chunk_k; c += 32) {
                     std::uint32_t const j = t + 1 + c;
@@ -204,7 +280,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                 // The writer of the bottom row publishes its finished columns (it wrote column j at step j + 30).
                 if (write_bottom && lane == 31 && t > 31) {
                     std::uint32_t const done = min(m, t - 31);
-                    band_publish(shared, slot_out, ((unsigned long long)(k + 1) << 32) | done);
+                    band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | done);
                 }
             }
             std::int32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
@@ -273,7 +349,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             }
         }
         __syncwarp();
-        if (write_bottom && lane == 31) band_publish(shared, slot_out, ((unsigned long long)(k + 1) << 32) | m);
+        if (write_bottom && lane == 31) band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | m);
         if constexpr (local) {
 #pragma unroll
             for (int r = 0; r < R; ++r)
@@ -328,8 +404,9 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         std::uint32_t const index = shared.pair_index;
         if (index >= count) break;
         pair_task_t const task = tasks[begin + index];
-        std::int32_t const value = band_score_warp<policy_>(task, costs_s, shared, ring, ring_cells_per_slot,
-                                                            profiles + warp * profile_bytes, chunks[warp], warp);
+        std::int32_t const value = band_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp), ring,
+                                                            ring_cells_per_slot, profiles + warp * profile_bytes,
+                                                            chunks[warp]);
         if (lane == 0) shared.warp_result[warp] = value;
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -347,6 +424,80 @@ __global__ void __launch_bounds__(band_warps_k * 32)
             results[task.slot] = score;
         }
     }
+}
+
+/** Clears the next pair's words of a group (both passes): called by the group's first CTA after the barrier that
+ *  starts a pair, when every CTA has finished with the pair before it. */
+__device__ __forceinline__ void band_group_reset(band_group_state_t *state, int parity, int members) {
+    for (int i = threadIdx.x; i < members; i += blockDim.x) {
+        state->pass[parity][0].progress[i] = 0ull;
+        state->pass[parity][1].progress[i] = 0ull;
+    }
+    if (threadIdx.x == 0) state->pass[parity][0].best = 0, state->pass[parity][1].best = 0;
+    __threadfence();
+}
+
+/** A warp's share of a pass: local scores take the group's maximum, global scores the corner from its owner warp. */
+template <bool local_>
+__device__ __forceinline__ void band_group_contribute(band_pass_state_t &pass, std::int32_t value, bool owner) {
+    if ((threadIdx.x & 31) != 0) return;
+    if constexpr (local_) atomicMax(&pass.best, value);
+    else if (owner) {
+        *reinterpret_cast<volatile std::int32_t *>(&pass.best) = value;
+        __threadfence();
+    }
+}
+
+/**
+ *  Grouped band kernel: G co-resident CTAs (one cooperative launch, `group_ctas` = G) share each pair, their G x W
+ *  warps forming one ring; group g scores pairs g, g + groups, ... of bins [key_begin, key_end).
+ */
+template <typename policy_>
+__global__ void __launch_bounds__(band_warps_k * 32)
+    band_group_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t *__restrict__ bins, int key_begin,
+                      int key_end, score_costs_t const costs, std::int64_t *__restrict__ results,
+                      std::int32_t *__restrict__ scratch, std::size_t ring_cells_per_slot,
+                      band_group_state_t *__restrict__ group_states, int group_ctas) {
+    extern __shared__ __align__(16) unsigned char shared_bytes[];
+    score_costs_t &costs_s = *reinterpret_cast<score_costs_t *>(shared_bytes);
+    std::size_t const costs_bytes = (sizeof(score_costs_t) + 15) / 16 * 16;
+    band_shared_t &shared = *reinterpret_cast<band_shared_t *>(shared_bytes + costs_bytes);
+    std::size_t const shared_state_bytes = (sizeof(band_shared_t) + 15) / 16 * 16;
+    std::size_t const profile_bytes = (std::size_t)band_profile_bytes_per_warp<policy_>(costs.classes);
+    std::int8_t *profiles = reinterpret_cast<std::int8_t *>(shared_bytes + costs_bytes + shared_state_bytes);
+    auto *chunks = reinterpret_cast<band_chunk_t *>(profiles + band_warps_k * profile_bytes);
+    {
+        auto const *src = reinterpret_cast<std::uint32_t const *>(&costs);
+        auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
+        for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    int const warp = threadIdx.x >> 5;
+    int const group = (int)blockIdx.x / group_ctas, rank = (int)blockIdx.x % group_ctas;
+    int const groups = (int)gridDim.x / group_ctas;
+    int const members = group_ctas * band_warps_k;
+    band_group_state_t *state = group_states + group;
+    std::int32_t *ring = scratch + (std::size_t)group * members * ring_cells_per_slot;
+    std::uint32_t const begin = bins->begin[key_begin];
+    std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
+    std::uint32_t barriers = 0, iteration = 0;
+    for (std::uint32_t index = (std::uint32_t)group; index < count; index += (std::uint32_t)groups, ++iteration) {
+        int const parity = int(iteration & 1u);
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (rank == 0) band_group_reset(state, parity ^ 1, members);
+        pair_task_t const task = tasks[begin + index];
+        band_pass_state_t &pass = state->pass[parity][0];
+        band_ring_t const sync {pass.progress, &state->failed, members, rank * band_warps_k + warp, true};
+        std::int32_t const value = band_score_warp<policy_>(task, costs_s, sync, ring, ring_cells_per_slot,
+                                                            profiles + warp * profile_bytes, chunks[warp]);
+        std::uint32_t const strips = (task.rows_length + policy_::strip_rows_k - 1) / policy_::strip_rows_k;
+        band_group_contribute<policy_::local_k>(pass, value, (int)((strips - 1) % (std::uint32_t)members) == sync.member);
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (rank == 0 && threadIdx.x == 0)
+            results[task.slot] = *reinterpret_cast<volatile std::int32_t *>(&pass.best);
+    }
+    __syncthreads();
+    if (rank == 0 && threadIdx.x == 0 && *reinterpret_cast<volatile std::uint32_t *>(&state->failed))
+        atomicOr(&bins->error_flags, 1u);
 }
 
 } // namespace szs_gb300

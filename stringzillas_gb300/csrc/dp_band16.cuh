@@ -64,16 +64,17 @@ __host__ __device__ constexpr int band16_shared_bytes(int classes) {
  */
 template <typename policy_>
 __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &task, score_costs_t const &costs,
-                                                          band_shared_t &shared, std::uint32_t *ring,
+                                                          band_ring_t const &sync, std::uint32_t *ring,
                                                           std::size_t ring_words_per_slot, std::int8_t *profile,
-                                                          band16_chunk_t &chunk, int warp) {
+                                                          band16_chunk_t &chunk) {
     using ops = packed_ops_t<policy_::maximize_k>;
     constexpr int R = policy_::rows_per_lane_k;
     constexpr int S = policy_::strip_rows_k;
     constexpr int SS = policy_::super_rows_k;
     constexpr bool affine = policy_::affine_k;
     constexpr bool local = policy_::local_k;
-    constexpr int W = band_warps_k;
+    std::uint32_t const W = (std::uint32_t)sync.members;
+    int const warp = sync.member;
     static_assert(R % 4 == 0, "profile rows are read in 4-byte words");
     constexpr int words = R / 4;
 
@@ -150,9 +151,9 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
             if (e == 0) {
                 // The strip above must have published the columns staged now; this strip publishes its own.
                 std::uint32_t const need = min(m, t + band16_chunk_k);
-                if (k > 0 && t + 1 <= m) healthy = band_wait(shared, slot_in, ((unsigned long long)k << 32) | need);
+                if (k > 0 && t + 1 <= m) healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
                 if (bottom_writer && t > 63)
-                    band_publish(shared, slot_out, ((unsigned long long)(k + 1) << 32) | min(m, t - 63));
+                    band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | min(m, t - 63));
                 __syncwarp();
 #pragma unroll
                 for (int c = lane; c < band16_chunk_k; c += 32) {
@@ -264,7 +265,7 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
         for (; t < steps && healthy; ++t) step(t, std::false_type {});
         __syncwarp();
-        if (bottom_writer) band_publish(shared, slot_out, ((unsigned long long)(k + 1) << 32) | m);
+        if (bottom_writer) band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | m);
         if constexpr (local) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -322,8 +323,9 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         std::uint32_t const index = shared.pair_index;
         if (index >= count) break;
         pair_task_t const task = tasks[begin + index];
-        std::int32_t const value = band16_score_warp<policy_>(task, costs_s, shared, ring, ring_words_per_slot,
-                                                              profiles + warp * profile_bytes, chunks[warp], warp);
+        std::int32_t const value = band16_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp), ring,
+                                                              ring_words_per_slot, profiles + warp * profile_bytes,
+                                                              chunks[warp]);
         if (lane == 0) shared.warp_result[warp] = value;
         __syncthreads();
         if constexpr (policy_::local_k) {
@@ -345,8 +347,9 @@ __global__ void __launch_bounds__(band_warps_k * 32)
                 static_assert(sizeof(band_chunk_t) <= sizeof(band16_chunk_t), "chunk staging must fit");
                 std::size_t const wide_profile = (std::size_t)band_profile_bytes_per_warp<wide_t>(costs.classes);
                 std::int32_t const wide = band_score_warp<wide_t>(
-                    task, costs_s, shared, reinterpret_cast<std::int32_t *>(ring), 2 * ring_words_per_slot,
-                    profiles + warp * wide_profile, *reinterpret_cast<band_chunk_t *>(&chunks[warp]), warp);
+                    task, costs_s, band_cta_ring(shared, warp), reinterpret_cast<std::int32_t *>(ring),
+                    2 * ring_words_per_slot, profiles + warp * wide_profile,
+                    *reinterpret_cast<band_chunk_t *>(&chunks[warp]));
                 if (lane == 0) shared.warp_result[warp] = wide;
                 __syncthreads();
             }
@@ -366,6 +369,79 @@ __global__ void __launch_bounds__(band_warps_k * 32)
             results[task.slot] = score;
         }
     }
+}
+
+/**
+ *  Grouped 16-bit band kernel: G co-resident CTAs (one cooperative launch) share each pair, their G x W warps forming
+ *  one ring of super-strips (see `band_group_kernel`). A local pair whose group maximum reached the 16-bit limit is
+ *  scored again by the same group on 32-bit cells, with the second pass's ring words.
+ */
+template <typename policy_>
+__global__ void __launch_bounds__(band_warps_k * 32)
+    band16_group_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t *__restrict__ bins, int key_begin,
+                        int key_end, score_costs_t const costs, std::int64_t *__restrict__ results,
+                        std::uint32_t *__restrict__ scratch, std::size_t ring_words_per_slot,
+                        band_group_state_t *__restrict__ group_states, int group_ctas) {
+    extern __shared__ __align__(16) unsigned char shared_bytes[];
+    score_costs_t &costs_s = *reinterpret_cast<score_costs_t *>(shared_bytes);
+    std::size_t const costs_bytes = (sizeof(score_costs_t) + 15) / 16 * 16;
+    band_shared_t &shared = *reinterpret_cast<band_shared_t *>(shared_bytes + costs_bytes);
+    std::size_t const shared_state_bytes = (sizeof(band_shared_t) + 15) / 16 * 16;
+    std::size_t const profile_bytes = (std::size_t)band16_profile_bytes_per_warp<policy_>(costs.classes);
+    std::int8_t *profiles = reinterpret_cast<std::int8_t *>(shared_bytes + costs_bytes + shared_state_bytes);
+    auto *chunks = reinterpret_cast<band16_chunk_t *>(profiles + band_warps_k * profile_bytes);
+    {
+        auto const *src = reinterpret_cast<std::uint32_t const *>(&costs);
+        auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
+        for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    int const warp = threadIdx.x >> 5;
+    int const group = (int)blockIdx.x / group_ctas, rank = (int)blockIdx.x % group_ctas;
+    int const groups = (int)gridDim.x / group_ctas;
+    int const members = group_ctas * band_warps_k;
+    band_group_state_t *state = group_states + group;
+    constexpr std::size_t ring_scale = policy_::local_k ? 2 : 1;
+    std::uint32_t *ring = scratch + (std::size_t)group * members * ring_words_per_slot * ring_scale;
+    std::uint32_t const begin = bins->begin[key_begin];
+    std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
+    std::uint32_t barriers = 0, iteration = 0;
+    for (std::uint32_t index = (std::uint32_t)group; index < count; index += (std::uint32_t)groups, ++iteration) {
+        int const parity = int(iteration & 1u);
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (rank == 0) band_group_reset(state, parity ^ 1, members);
+        pair_task_t const task = tasks[begin + index];
+        int const member = rank * band_warps_k + warp;
+        band_pass_state_t *pass = &state->pass[parity][0];
+        {
+            band_ring_t const sync {pass->progress, &state->failed, members, member, true};
+            std::int32_t const value = band16_score_warp<policy_>(task, costs_s, sync, ring, ring_words_per_slot,
+                                                                  profiles + warp * profile_bytes, chunks[warp]);
+            std::uint32_t const super_strips =
+                (task.rows_length + policy_::super_rows_k - 1) / policy_::super_rows_k;
+            band_group_contribute<policy_::local_k>(*pass, value,
+                                                    (int)((super_strips - 1) % (std::uint32_t)members) == member);
+        }
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if constexpr (policy_::local_k) {
+            // The group's maximum decides, identically in every CTA, whether 16-bit values may have wrapped.
+            if (*reinterpret_cast<volatile std::int32_t *>(&pass->best) >= costs_s.local_limit16) {
+                using wide_t = band_policy_t<policy_::kind_k, policy_::affine_k, 8>;
+                std::size_t const wide_profile = (std::size_t)band_profile_bytes_per_warp<wide_t>(costs.classes);
+                pass = &state->pass[parity][1];
+                band_ring_t const sync {pass->progress, &state->failed, members, member, true};
+                std::int32_t const wide = band_score_warp<wide_t>(
+                    task, costs_s, sync, reinterpret_cast<std::int32_t *>(ring), 2 * ring_words_per_slot,
+                    profiles + warp * wide_profile, *reinterpret_cast<band_chunk_t *>(&chunks[warp]));
+                band_group_contribute<true>(*pass, wide, false);
+                if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+            }
+        }
+        if (rank == 0 && threadIdx.x == 0)
+            results[task.slot] = *reinterpret_cast<volatile std::int32_t *>(&pass->best);
+    }
+    __syncthreads();
+    if (rank == 0 && threadIdx.x == 0 && *reinterpret_cast<volatile std::uint32_t *>(&state->failed))
+        atomicOr(&bins->error_flags, 1u);
 }
 
 } // namespace szs_gb300

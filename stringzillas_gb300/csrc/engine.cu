@@ -841,25 +841,54 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t pairs;
         int ctas;
         std::size_t scratch_offset, scratch_bytes;
+        int group_ctas = 1;            // band jobs: CTAs sharing one pair (1 = one CTA per pair)
+        std::size_t state_offset = 0;  // grouped band jobs: the groups' state records in the scratch buffer
+        std::size_t state_bytes = 0;
     };
     job_t jobs[40];
     int job_count = 0;
     std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
     std::size_t const band16_words_per_slot = align_up((std::size_t)plan.max_cols + 1, 64);
     std::size_t scratch_total = 0;
+    // Long pairs: one CTA each while they fill the GPU; when fewer than half the resident CTA slots have a pair, the
+    // batched form gives each pair a group of CTAs (one cooperative launch) so a few long pairs still use every SM.
+    // A group never gets more warps than a pair can have strips: the shorter side is at most the longest row
+    // `max_cols`, so `max_cols / strip_rows` strips bound every pair of the call.
+    auto band_groups = [&](std::uint64_t pairs_here, dp_launch_shape_t const &shape, std::uint64_t strip_rows,
+                           int &ctas, int &group_ctas) {
+        ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+        group_ctas = 1;
+        if (schedule == szs_gb300_schedule_plain_k || shape.group_ctas_per_sm <= 0) return;
+        std::uint64_t const slots = (std::uint64_t)context->sm_count * shape.group_ctas_per_sm;
+        if (pairs_here * 2 > slots) return;
+        std::uint64_t const strips = ((std::uint64_t)plan.max_cols + strip_rows - 1) / strip_rows;
+        std::uint64_t const useful = (strips + band_warps_per_cta() - 1) / band_warps_per_cta();
+        std::uint64_t const size = std::min<std::uint64_t>({slots / pairs_here, (std::uint64_t)band_group_max_ctas(),
+                                                            useful});
+        if (size < 2) return;
+        group_ctas = (int)size;
+        ctas = (int)(std::min<std::uint64_t>(pairs_here, slots / group_ctas) * group_ctas);
+    };
     {
         std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
         if (pairs_here) {
             dp_launch_shape_t const shape = band16_shape(engine.kind, costs.affine != 0, packed_costs.classes);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
-            int const ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+            int ctas = 0, group_ctas = 1;
+            band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
             // Local scores keep room for a 32-bit ring: a pair that reaches the 16-bit limit is scored again.
             std::size_t const ring_scale = engine.kind == kind_smith_waterman_k ? 2 : 1;
             std::size_t const bytes = align_up(band16_words_per_slot * 4 * ring_scale * (std::size_t)ctas *
                                                    (std::size_t)band_warps_per_cta(), 256);
-            jobs[job_count++] = {job_band16_k, 16, 0, bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k,
-                                 pairs_here, ctas, scratch_total, bytes};
+            job_t job {job_band16_k, 16, 0, bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k, pairs_here,
+                       ctas, scratch_total, bytes};
             scratch_total += bytes;
+            if (group_ctas > 1) {
+                job.group_ctas = group_ctas, job.state_offset = scratch_total;
+                job.state_bytes = align_up((std::size_t)(ctas / group_ctas) * band_group_state_bytes(), 256);
+                scratch_total += job.state_bytes;
+            }
+            jobs[job_count++] = job;
         }
     }
     {
@@ -867,12 +896,19 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         if (pairs_here) {
             dp_launch_shape_t const shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
-            int const ctas = (int)std::min<std::uint64_t>(pairs_here, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+            int ctas = 0, group_ctas = 1;
+            band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
             std::size_t const bytes =
                 align_up(cells_per_warp * 4 * (std::size_t)ctas * (std::size_t)band_warps_per_cta(), 256);
-            jobs[job_count++] = {job_band_k, 32, 0, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here,
-                                 ctas, scratch_total, bytes};
+            job_t job {job_band_k, 32, 0, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here, ctas,
+                       scratch_total, bytes};
             scratch_total += bytes;
+            if (group_ctas > 1) {
+                job.group_ctas = group_ctas, job.state_offset = scratch_total;
+                job.state_bytes = align_up((std::size_t)(ctas / group_ctas) * band_group_state_bytes(), 256);
+                scratch_total += job.state_bytes;
+            }
+            jobs[job_count++] = job;
         }
     }
     for (int cell_bits : {64, 32}) {
@@ -939,6 +975,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             key_append(launch_key, jobs[i].warps);
             key_append(launch_key, jobs[i].key_begin), key_append(launch_key, jobs[i].key_end);
             key_append(launch_key, jobs[i].ctas), key_append(launch_key, jobs[i].scratch_offset);
+            key_append(launch_key, jobs[i].group_ctas), key_append(launch_key, jobs[i].state_offset);
         }
         key_append(launch_key, packed_costs), key_append(launch_key, call_costs);
         key_append(launch_key, tasks), key_append(launch_key, bins), key_append(launch_key, results);
@@ -956,13 +993,19 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             bool const traced = tracing && 2 * i + 1 < 64;
             if (traced) cudaEventRecord(context->trace_events[2 * i], lane_stream);
             void *scratch = static_cast<unsigned char *>(context->scratch.data) + job.scratch_offset;
+            void *group_states = nullptr;
+            if (job.group_ctas > 1) {
+                group_states = static_cast<unsigned char *>(context->scratch.data) + job.state_offset;
+                SZS_TRY_CUDA(cudaMemsetAsync(group_states, 0, job.state_bytes, lane_stream));
+            }
             if (job.kind == job_band_k)
                 SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
-                                         call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
+                                         call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,
+                                         group_states, job.group_ctas));
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
-                                           lane_stream));
+                                           lane_stream, group_states, job.group_ctas));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                        bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));

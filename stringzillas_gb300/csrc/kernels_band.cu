@@ -29,15 +29,37 @@ dp_launch_shape_t band_shape_of(int classes) {
         cudaSuccess)
         blocks = 0;
     shape.ctas_per_sm = blocks;
+    auto grouped = band_group_kernel<policy_t>;
+    cudaFuncSetAttribute(grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, shape.shared_bytes);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, grouped, shape.threads_per_cta, shape.shared_bytes) !=
+        cudaSuccess)
+        blocks = 0;
+    shape.group_ctas_per_sm = blocks;
     return shape;
 }
 
 template <int kind_, bool affine_>
 cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                            score_costs_t const &costs, std::int64_t *results, void *scratch,
-                           std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream) {
+                           std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
+                           int group_ctas) {
     using policy_t = band_instance_t<kind_, affine_>;
     int const shared = band_shared_bytes<policy_t>(costs.classes);
+    if (group_states) {
+        // The CTAs of a group wait on one another: a cooperative launch keeps the whole grid resident.
+        auto grouped = band_group_kernel<policy_t>;
+        cudaError_t status = cudaFuncSetAttribute(grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
+        if (status != cudaSuccess) return status;
+        cudaLaunchConfig_t config {};
+        config.gridDim = dim3((unsigned)ctas), config.blockDim = dim3(band_warps_k * 32);
+        config.dynamicSmemBytes = (std::size_t)shared, config.stream = stream;
+        cudaLaunchAttribute attribute {};
+        attribute.id = cudaLaunchAttributeCooperative, attribute.val.cooperative = 1;
+        config.attrs = &attribute, config.numAttrs = 1;
+        return cudaLaunchKernelEx(&config, grouped, tasks, bins, key_begin, key_end, costs, results,
+                                  static_cast<std::int32_t *>(scratch), ring_cells_per_slot,
+                                  static_cast<band_group_state_t *>(group_states), group_ctas);
+    }
     auto kernel = band_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
     if (status != cudaSuccess) return status;
@@ -68,10 +90,14 @@ dp_launch_shape_t band_shape(int kind, bool affine, int classes) {
 
 cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream) {
+                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
+                        int group_ctas) {
     SZS_BAND_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch, ring_cells_per_slot,
-                      ctas, stream)
+                      ctas, stream, group_states, group_ctas)
     return cudaErrorInvalidValue;
 }
+
+std::size_t band_group_state_bytes() { return sizeof(band_group_state_t); }
+int band_group_max_ctas() { return band_group_max_ctas_k; }
 
 } // namespace szs_gb300

@@ -68,6 +68,7 @@ struct dp_launch_shape_t {
     int shared_bytes;
     int ctas_per_sm; // from the occupancy calculator
     int rows_per_lane;
+    int group_ctas_per_sm = 0; // band kernels: the same for the grouped (several CTAs per pair) kernel
 };
 
 /** Launch shape of the wavefront kernel for (kind, affine, cell bits, classes); ctas_per_sm = 0 if unsupported. */
@@ -95,10 +96,16 @@ dp_launch_shape_t band_shape(int kind, bool affine, int classes);
 int band_warps_per_cta();
 
 /** Runs the band kernel over bins [key_begin, key_end). `scratch` holds `ctas * band_warps_per_cta()` ring slots of
- *  `ring_cells_per_slot` 32-bit cells. Bounded waits that give up set bit 0 of `bins->error_flags`. */
+ *  `ring_cells_per_slot` 32-bit cells. Bounded waits that give up set bit 0 of `bins->error_flags`. With
+ *  `group_states` (one zeroed `band_group_state_bytes()` record per group) the grouped kernel runs instead: a
+ *  cooperative launch of `ctas` CTAs in groups of `group_ctas`, each group sharing one pair at a time. */
 cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream);
+                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
+                        int group_ctas = 1);
+/** Bytes of one group's state record, and the most CTAs a group may have. */
+std::size_t band_group_state_bytes();
+int band_group_max_ctas();
 
 /** Launch shape of the 16-bit band kernel (one CTA per long pair, two row strips per warp in 16x2 cells). */
 dp_launch_shape_t band16_shape(int kind, bool affine, int classes);
@@ -108,7 +115,8 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes);
  *  cells). Bounded waits that give up set bit 0 of `bins->error_flags`. */
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                          std::size_t ring_words_per_slot, int ctas, cudaStream_t stream);
+                          std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
+                          int group_ctas = 1);
 
 /** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
  *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be

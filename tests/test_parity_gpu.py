@@ -268,8 +268,31 @@ def test_band_route_long_pairs(szs, port, family, costs):
     # A related pair, so local scores are large.
     second[2] = first[2][100:2900] + bytes(rng.choice(alphabet, size=300))
     engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
-    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
-    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    # Six long pairs leave most CTA slots free: the batched form gives each pair a group of CTAs; the plain form
+    # keeps one CTA per pair.
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 1, 1, 1)),
+                                          ("lev", (0, 2, 3, 1)), ("sw", (-3, -3))])
+def test_grouped_band_few_long_pairs(szs, port, family, costs):
+    """One or a few long pairs: each gets a group of up to 16 CTAs (one cooperative launch) whose warps share the
+    strip ring through global memory. Pairs with fewer strips than the group has warps leave warps idle."""
+    rng = np.random.default_rng(31)
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    for lengths in ([(6000, 7000)], [(1100, 20000)], [(3000, 3000), (2500, 9000), (1200, 1300)],
+                    [(1030, 1030)] * 2 + [(4000, 4100)]):
+        first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+        second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+        second[0] = first[0][: lengths[0][0] // 2] + second[0][lengths[0][0] // 2:]  # related: large local scores
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
 @pytest.mark.parametrize("family,costs,extreme", [
