@@ -546,6 +546,9 @@ typedef struct szs_gb300_server_config_t {
     sz_size_t max_batch_pairs;    /**< pairs merged into one batch at most (default 2^22) */
     sz_size_t max_batch_requests; /**< requests merged into one batch at most (default unlimited; 1 = per-request) */
     int schedule;                 /**< `szs_gb300_schedule_t` of the batches (default batched) */
+    sz_size_t max_batch_cells;    /**< cells (sum of len(a) * len(b)) merged into one batch at most while another lane
+                                       is idle, so small requests do not wait behind a large one's batch (default
+                                       2^33; a larger request still runs, alone; without an idle lane all merge) */
 } szs_gb300_server_config_t;
 
 /** What happened to one request. Times are host wall-clock milliseconds from its submission. */

@@ -168,6 +168,7 @@ class ServerConfig(ctypes.Structure):
         ("max_batch_pairs", c_size_t),
         ("max_batch_requests", c_size_t),
         ("schedule", c_int),
+        ("max_batch_cells", c_size_t),
     ]
 
 

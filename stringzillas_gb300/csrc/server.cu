@@ -7,8 +7,9 @@
  *  arena:
  *
  *  - Requests wait in arrival order. Whenever a lane is free, the admission thread takes the first waiting request
- *    and every later waiting request of the same engine that still fits the batch caps and the arena (continuous
- *    batching: whatever arrived while the other lanes were busy rides along), reserves one contiguous arena region
+ *    and every later waiting request of the same engine that still fits the batch caps (requests, pairs, cells) and
+ *    the arena (continuous batching: whatever arrived while the other lanes were busy rides along; the cells cap
+ *    keeps small requests out of a large request's batch), reserves one contiguous arena region
  *    for the merged batch and hands it to the lane. A batch that does not fit waits until a finishing batch returns
  *    its region (admission by HBM budget); a request larger than the whole arena fails alone.
  *  - A lane lays the batch out as one pair of u64 tapes over the region - offsets of all first strings, offsets of
@@ -239,7 +240,7 @@ void server_t::admit_loop() {
         // Merge: the first waiter, then later waiters of the same engine while the caps and the arena allow.
         auto batch = std::make_unique<batch_t>();
         batch->engine = waiting.front()->engine;
-        std::uint64_t pairs = 0, first_bytes = 0, second_bytes = 0;
+        std::uint64_t pairs = 0, first_bytes = 0, second_bytes = 0, cells = 0;
         std::size_t largest_free = 0;
         for (auto const &block : allocator.free_blocks) largest_free = std::max(largest_free, block.second);
         std::size_t const max_requests = config.max_batch_requests ? config.max_batch_requests : ~std::size_t(0);
@@ -253,11 +254,15 @@ void server_t::admit_loop() {
             std::uint64_t const grown_second = second_bytes + request->second.bytes();
             if (!batch->requests.empty()) {
                 if (grown_pairs > config.max_batch_pairs) break;
+                // The cells cap only holds while another lane is free to take the rest at once: under saturation
+                // every request of the engine merges, which keeps the device full.
+                if (cells + request->cells > config.max_batch_cells && idle_lanes.size() > 1) break;
                 if (batch_layout_t::of(grown_pairs, grown_first, grown_second).total > largest_free) break;
             }
             batch->requests.push_back(request);
             taken.push_back(it);
             pairs = grown_pairs, first_bytes = grown_first, second_bytes = grown_second;
+            cells += request->cells;
         }
         batch->layout = batch_layout_t::of(pairs, first_bytes, second_bytes);
         batch->first_bytes = first_bytes, batch->second_bytes = second_bytes;
@@ -450,6 +455,7 @@ SZS_GB300_API sz_status_t szs_gb300_server_init(szs_gb300_server_config_t const 
     if (!server->config.arena_bytes) server->config.arena_bytes = std::size_t(1) << 30;
     if (!server->config.lanes) server->config.lanes = 4;
     if (!server->config.max_batch_pairs) server->config.max_batch_pairs = std::size_t(1) << 22;
+    if (!server->config.max_batch_cells) server->config.max_batch_cells = std::size_t(1) << 33;
     server->device = (int)config->gpu_device;
     if (cudaSetDevice(server->device) != cudaSuccess ||
         cudaMalloc(&server->arena, server->config.arena_bytes) != cudaSuccess) {

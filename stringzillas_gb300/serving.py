@@ -55,16 +55,16 @@ class Ticket:
 
 class Server:
     """``Server(gpu_device=0, arena_bytes=1 << 30, lanes=4, max_batch_pairs=1 << 22, max_batch_requests=0,
-    schedule="batched")``.
+    schedule="batched", max_batch_cells=1 << 33)``.
 
     ``max_batch_requests=1, lanes=1, schedule="plain"`` gives the per-request form: every request on its own,
     one after another, with one plain launch each.
     """
 
     def __init__(self, gpu_device=0, arena_bytes=1 << 30, lanes=4, max_batch_pairs=1 << 22, max_batch_requests=0,
-                 schedule="batched"):
+                 schedule="batched", max_batch_cells=1 << 33):
         config = _native.ServerConfig(int(gpu_device), int(arena_bytes), int(lanes), int(max_batch_pairs),
-                                      int(max_batch_requests), _SCHEDULES[schedule])
+                                      int(max_batch_requests), _SCHEDULES[schedule], int(max_batch_cells))
         self._handle = ctypes.c_void_p()
         err = ctypes.c_char_p()
         status = lib.szs_gb300_server_init(ctypes.byref(config), ctypes.byref(self._handle), ctypes.byref(err))
