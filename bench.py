@@ -59,6 +59,11 @@ WORKLOADS = {
           "seeded symmetric int8 table (diag 4..11, off -4..3), open -11 extend -1",
     "c4": "Smith-Waterman affine DNA: 8,192 pairs, len log-uniform [1,000, 30,000], planted 500-5,000 bp shared "
           "segment with 10% divergence, match +2 mismatch -3 open -5 extend -2",
+    # Profiling cases for the 32-bit routes (not bench lines of the default run).
+    "p_band32": "profiling case, Needleman-Wunsch affine protein long pairs: 1,024 pairs, len lognormal(4000, 0.3) in "
+                "[2500, 8000], 70% identity, open -11 extend -1 (the reach bound exceeds int16: 32-bit band)",
+    "p_dp32": "profiling case, Needleman-Wunsch affine protein with a wide table: 65,536 pairs, len lognormal(350, 0.6) "
+              "in [50, 2000], diagonal 100..120, open -30 extend -2 (costs outside the int8 profile: 32-bit wavefront)",
 }
 
 
@@ -93,6 +98,16 @@ def make_workload(name, seed):
     if name == "c3":
         first, second = w.protein_pairs(262144, seed=seed)
         return first, second, ("nw", w.protein_table(seed=seed))
+    if name == "p_band32":
+        first, second = w.protein_pairs(1024, median=4000.0, sigma=0.3, low=2500, high=8000, seed=seed)
+        return first, second, ("nw32", (*w.protein_table(seed=seed), -11, -1))
+    if name == "p_dp32":
+        first, second = w.protein_pairs(65536, seed=seed)
+        byte_to_class, table = w.protein_table(seed=seed)
+        table = table.copy()
+        diagonal = np.arange(1, 21)
+        table[diagonal, diagonal] = 100 + np.arange(20)
+        return first, second, ("nw32", (byte_to_class, table, -30, -2))
     first, second = w.local_dna_pairs(8192, seed=seed)
     return first, second, ("sw", w.dna_table(2, -3))
 
@@ -106,6 +121,8 @@ def make_engine(kind_and_tables):
         engine = szs.LevenshteinDistances()
     elif kind == "nw":
         engine = szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
+    elif kind == "nw32":  # profiling cases of the 32-bit routes: (byte_to_class, table, open, extend)
+        engine = szs.NeedlemanWunschScores(*tables[:2], open=tables[2], extend=tables[3])
     else:
         engine = szs.SmithWatermanScores(*tables, open=-5, extend=-2)
     autotune.apply(engine)
@@ -124,6 +141,8 @@ def oracle_costs(kind_and_tables):
         return oracle.levenshtein_costs()
     if kind == "nw":
         return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables, -11, -1)
+    if kind == "nw32":
+        return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables)
     return oracle.alignment_costs(oracle.SMITH_WATERMAN, *tables, -5, -2)
 
 
@@ -131,6 +150,8 @@ def ops_per_cell(kind_and_tables):
     kind = kind_and_tables[0]
     if kind == "lev":
         return OPS_PER_CELL["myers_dna"]
+    if kind == "nw32":
+        return OPS_PER_CELL["dp_affine"]
     return OPS_PER_CELL["packed_affine_local"] if kind == "sw" else OPS_PER_CELL["packed_affine"]
 
 
@@ -565,7 +586,8 @@ def run_ours(args):
         int_ops = cells_per_step * ops_per_cell(kind_and_tables)
         int_peak = None
         if peaks:
-            int_peak = peaks["lop3"] if kind_and_tables[0] == "lev" else peaks["dpx_viaddmax_s16x2"]
+            int_peak = {"lev": peaks["lop3"], "nw32": peaks["dpx_viaddmax_s32"]}.get(
+                kind_and_tables[0], peaks["dpx_viaddmax_s16x2"])
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,

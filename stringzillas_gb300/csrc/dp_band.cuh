@@ -258,7 +258,10 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             load_profile_words<R>(profile + (int)code_now * S + lane * R, p_now);
         bool healthy = true;
 
-        for (std::uint32_t t = 0; t < steps && healthy; ++t) {
+        // One step of the sweep. `steady` steps are those where every lane is on a real column of a full strip
+        // (31 <= t < m, all 32 lanes hold rows): no range predicates and no corner capture.
+        auto step = [&](std::uint32_t t, auto steady_tag) {
+            constexpr bool steady = decltype(steady_tag)::value;
             std::uint32_t const e = t & (band_chunk_k - 1);
             if (e == 0) {
                 // Stage lane 0's next columns; strips below the first wait for the strip above to write them.
@@ -292,7 +295,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                 load_profile_words<R>(profile + (int)code_next * S + lane * R, p_next);
 
             std::int64_t const j = (std::int64_t)t + 1 - lane;
-            if (j >= 1 && j <= (std::int64_t)m && lane <= last_lane) {
+            if (steady || (j >= 1 && j <= (std::int64_t)m && lane <= last_lane)) {
                 std::int32_t diag = diag_up;
                 diag_up = up_h;
                 std::int32_t h_up = up_h, f_up = up_f;
@@ -335,7 +338,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                     __stcg(bottom + 2 * j, out_h);
                     __stcg(bottom + 2 * j + 1, out_f);
                 }
-                if constexpr (!local)
+                if constexpr (!local && !steady)
                     if (last_strip && lane == result_lane && j == (std::int64_t)m) {
 #pragma unroll
                         for (int r = 0; r < R; ++r)
@@ -347,7 +350,16 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
 #pragma unroll
                 for (int w = 0; w < words; ++w) p_now[w] = p_next[w];
             }
-        }
+        };
+
+        std::uint32_t const fill_end = min(steps, 31u);
+        std::uint32_t const steady_end = (last_lane == 31 && m >= 32u) ? max(fill_end, min(steps, m)) : fill_end;
+        std::uint32_t t = 0;
+        for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
+        // Two steps per iteration: the row state alternates between two register sets instead of being copied back.
+#pragma unroll 2
+        for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
+        for (; t < steps && healthy; ++t) step(t, std::false_type {});
         __syncwarp();
         if (write_bottom && lane == 31) band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | m);
         if constexpr (local) {
