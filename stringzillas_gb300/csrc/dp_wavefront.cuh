@@ -21,6 +21,7 @@
  *  (include/stringzillas/similarities/serial.hpp:663-1079) bit for bit.
  */
 #pragma once
+#include <type_traits>
 #include "dp_cells.cuh"
 #include "engine_types.cuh"
 #include "planner.cuh"
@@ -146,7 +147,10 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
         int out_code = 0;
         std::uint32_t const steps = m + (std::uint32_t)last_lane;
         bool const write_bottom = !last_strip;
-        for (std::uint32_t t = 0; t < steps; ++t) {
+        // One step of the sweep. `steady` steps are those where all 32 lanes hold rows of a full strip and real
+        // columns (31 <= t < m): no range predicates.
+        auto step = [&](std::uint32_t t, auto steady_tag) {
+            constexpr bool steady = decltype(steady_tag)::value;
             cell_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
             cell_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0;
             int code = __shfl_up_sync(0xFFFFFFFFu, out_code, 1);
@@ -160,7 +164,7 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
                 }
             }
             std::int64_t const j = (std::int64_t)t + 1 - lane;
-            if (j >= 1 && j <= (std::int64_t)m && lane <= last_lane) {
+            if (steady || (j >= 1 && j <= (std::int64_t)m && lane <= last_lane)) {
                 cell_t diag = diag_up;
                 diag_up = up_h;
                 cell_t h_up = up_h, f_up = up_f;
@@ -209,7 +213,15 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
                     if (affine) scratch[2 * j + 1] = out_f;
                 }
             }
-        }
+        };
+        std::uint32_t const fill_end = min(steps, 31u);
+        std::uint32_t const steady_end = (last_lane == 31 && m >= 32u) ? max(fill_end, min(steps, m)) : fill_end;
+        std::uint32_t t = 0;
+        for (; t < fill_end; ++t) step(t, std::false_type {});
+        // Two steps per iteration: the row state alternates between two register sets instead of being copied back.
+#pragma unroll 2
+        for (; t < steady_end; ++t) step(t, std::true_type {});
+        for (; t < steps; ++t) step(t, std::false_type {});
         // Fold this strip's contribution.
         if constexpr (local) {
 #pragma unroll
