@@ -118,6 +118,24 @@ def test_cross_and_symmetric_matrices(szs, port, name, family, costs):
     assert (out[:, 13:] == 7).all()
 
 
+@pytest.mark.parametrize("name,family,costs", ENGINES[:1] + ENGINES[5:6] + ENGINES[7:8],
+                         ids=["lev-unit", "nw-affine", "sw-affine"])
+def test_cross_and_symmetric_with_long_strings(szs, port, name, family, costs):
+    """Cross-product and symmetric calls whose few long pairs take the grouped band, mixed with empty and short
+    strings on the warp routes."""
+    rng = np.random.default_rng(8)
+    alphabet = DNA if family != "nw" else PROTEIN
+    b2c, table = dna_tables() if alphabet is DNA else protein_tables(rng)
+    queries = [bytes(rng.choice(alphabet, size=n)) for n in (3000, 0, 40, 2200)]
+    candidates = [bytes(rng.choice(alphabet, size=n)) for n in (2600, 1, 3500)]
+    candidates[2] = queries[0][:2000] + candidates[2][2000:]  # related: a large local score
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    got = engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.cross(oracle_costs, tape(queries), tape(candidates)))
+    got_sym = engine(szs.Strs(queries)).astype(np.int64)
+    np.testing.assert_array_equal(got_sym, port.cross(oracle_costs, tape(queries)))
+
+
 def test_myers_every_word_count(szs, port):
     """Unit-cost Levenshtein takes the bit-parallel route for shorter sides up to 512, the DP route above."""
     rng = np.random.default_rng(3)
