@@ -780,7 +780,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         return {};
     });
     if (!status.ok()) return status;
-    launches += 3 + (alphabet_pass ? 2 + (call.has_candidates ? 1 : 0) : 0);
+    launches += 3 + (alphabet_pass ? 2 : 0);
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
     batch_alphabet_t const &alphabet_host = *context->alphabet_host();

@@ -217,38 +217,74 @@ __global__ void plan_scan_kernel(plan_bins_t *__restrict__ bins) {
     if (i == threads - 1) bins->scheduled = scan[i];
 }
 
-/** Pass 3: write each routed pair into its bin; lanes sharing a bin reserve their slots with one atomic. */
+/**
+ *  Pass 3: write each routed pair into its bin. A CTA takes one contiguous range of pairs: it counts the range's
+ *  pairs per bin in shared memory, reserves each bin's slots with one global atomic, then routes the range again and
+ *  places every pair at its reserved base plus a shared-memory rank. Lanes of a warp that share a bin take their
+ *  ranks with one atomic in both passes.
+ */
 __global__ void plan_scatter_kernel(plan_args_t const args, plan_bins_t *__restrict__ bins,
                                     pair_task_t *__restrict__ tasks) {
+    __shared__ std::uint32_t counts[bin_keys_k];
+    __shared__ std::uint32_t bases[bin_keys_k];
     int const lane = threadIdx.x & 31;
-    std::uint64_t const warps = (std::uint64_t)gridDim.x * (blockDim.x / 32);
-    std::uint64_t const warp = (std::uint64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    for (std::uint64_t base = warp * 32; base < args.pairs; base += warps * 32) {
+    std::uint64_t const per_block = (args.pairs + gridDim.x - 1) / gridDim.x;
+    std::uint64_t const begin = min(args.pairs, (std::uint64_t)blockIdx.x * per_block);
+    std::uint64_t const end = min(args.pairs, begin + per_block);
+    for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x) counts[i] = 0;
+    __syncthreads();
+    // A warp's lanes that share a bin: one shared-memory atomic for all of them; returns this lane's rank.
+    auto claim = [&](unsigned key) -> std::uint32_t {
+        unsigned const peers = __match_any_sync(0xFFFFFFFFu, key);
+        int const leader = __ffs(peers) - 1;
+        std::uint32_t first = 0;
+        if (lane == leader && key != 0xFFFFFFFFu) first = atomicAdd(&counts[key], (unsigned)__popc(peers));
+        first = __shfl_sync(0xFFFFFFFFu, first, leader);
+        return first + __popc(peers & ((1u << lane) - 1u));
+    };
+    // The range is walked in warp-wide rounds so every lane of a warp takes part in each `claim`.
+    std::uint64_t const rounds_begin = begin + (threadIdx.x & ~31u);
+    for (std::uint64_t base = rounds_begin; base < end; base += blockDim.x) {
         std::uint64_t const p = base + lane;
         pair_route_info_t info;
         info.key = -1;
-        if (p < args.pairs) info = route_of_pair(args, p);
+        if (p < end) info = route_of_pair(args, p);
+        claim(info.key < 0 ? 0xFFFFFFFFu : (unsigned)info.key);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x) {
+        std::uint32_t const here = counts[i];
+        bases[i] = here ? bins->begin[i] + atomicAdd(&bins->fill[i], here) : 0u;
+        counts[i] = 0;
+    }
+    __syncthreads();
+    for (std::uint64_t base = rounds_begin; base < end; base += blockDim.x) {
+        std::uint64_t const p = base + lane;
+        pair_route_info_t info;
+        info.key = -1;
+        if (p < end) info = route_of_pair(args, p);
         unsigned const key = info.key < 0 ? 0xFFFFFFFFu : (unsigned)info.key;
-        unsigned const peers = __match_any_sync(0xFFFFFFFFu, key);
-        int const leader = __ffs(peers) - 1;
-        unsigned const rank = __popc(peers & ((1u << lane) - 1u));
-        std::uint32_t slot_base = 0;
-        if (lane == leader && key != 0xFFFFFFFFu) slot_base = atomicAdd(&bins->fill[key], (unsigned)__popc(peers));
-        slot_base = __shfl_sync(0xFFFFFFFFu, slot_base, leader);
+        std::uint32_t const rank = claim(key);
         if (key != 0xFFFFFFFFu) {
             pair_task_t task;
             task.rows = info.rows, task.cols = info.cols;
             task.rows_length = info.n, task.cols_length = info.m;
             task.slot = (std::uint32_t)p;
             task.transposed = info.transposed;
-            tasks[bins->begin[key] + slot_base + rank] = task;
+            tasks[bases[key] + rank] = task;
         }
     }
 }
 
 /** Marks every byte value present in a tape's data range [offsets[0], offsets[count]), read on the device; 16 bytes
- *  per load where aligned. Grid-stride, so the grid does not depend on the data size. */
-__global__ void alphabet_mark_kernel(tape_t const tape, std::uint32_t *__restrict__ symbol_mask) {
+ *  per load where aligned. Grid-stride over the CTAs given to the tape: the first `tape_ctas` CTAs take `first`, the
+ *  others `second` (both passes run in one launch, so their loads overlap). */
+__global__ void alphabet_mark_kernel(tape_t const first_tape, tape_t const second_tape, unsigned tape_ctas,
+                                     std::uint32_t *__restrict__ symbol_mask) {
+    bool const on_second = blockIdx.x >= tape_ctas;
+    tape_t const &tape = on_second ? second_tape : first_tape;
+    unsigned const block = on_second ? blockIdx.x - tape_ctas : blockIdx.x;
+    unsigned const blocks = on_second ? gridDim.x - tape_ctas : tape_ctas;
     // One flag byte per symbol, set with plain stores (every writer stores 1), folded into the mask at the end.
     __shared__ __align__(16) std::uint8_t seen[256];
     for (unsigned i = threadIdx.x; i < 256; i += blockDim.x) seen[i] = 0;
@@ -267,8 +303,8 @@ __global__ void alphabet_mark_kernel(tape_t const tape, std::uint32_t *__restric
     std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(data);
     std::uint64_t head = (16 - (address & 15)) & 15;
     if (head > length) head = length;
-    std::uint64_t const thread = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    std::uint64_t const threads = (std::uint64_t)gridDim.x * blockDim.x;
+    std::uint64_t const thread = (std::uint64_t)block * blockDim.x + threadIdx.x;
+    std::uint64_t const threads = (std::uint64_t)blocks * blockDim.x;
     if (thread < head) seen[data[thread]] = 1;
     std::uint64_t const body = (length - head) / 16;
     uint4 const *vectors = reinterpret_cast<uint4 const *>(data + head);
@@ -357,9 +393,9 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
 cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
                             batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream) {
     std::uint32_t *mask = alphabet->mask_scratch;
-    int const grid = sm_count * 8;
-    alphabet_mark_kernel<<<grid, 256, 0, stream>>>(queries, mask);
-    if (has_candidates) alphabet_mark_kernel<<<grid, 256, 0, stream>>>(candidates, mask);
+    unsigned const per_tape = (unsigned)sm_count * 8;
+    alphabet_mark_kernel<<<has_candidates ? 2 * per_tape : per_tape, 256, 0, stream>>>(
+        queries, has_candidates ? candidates : queries, per_tape, mask);
     alphabet_codes_kernel<<<1, 32, 0, stream>>>(mask, alphabet);
     return cudaGetLastError();
 }
