@@ -514,8 +514,8 @@ SZS_GB300_API sz_status_t szs_gb300_measure_integer_peaks(sz_size_t gpu_device, 
  *  Needleman-Wunsch / Smith-Waterman engines over a dense 256 x 256 table, `costs[a * 256 + b]` = cost of aligning
  *  byte a of the first string with byte b of the second, instead of the reference's 32-class fold. Every scoring
  *  entry point accepts these engines. Each call maps the bytes its batch actually uses onto dense codes on the
- *  device and scores over that sub-table, so a call may use at most 32 distinct byte values (more give
- *  `sz_unexpected_dimensions_k`); the allocation-free entry point does not accept them. No counterpart in the
+ *  device and scores over that sub-table; a call over more than 32 distinct byte values reads the whole table on the
+ *  32-bit routes instead. The allocation-free entry point does not accept these engines. No counterpart in the
  *  reference, whose engines take `byte_to_class` + a 32 x 32 table.
  */
 SZS_GB300_API sz_status_t szs_gb300_needleman_wunsch_scores_init_dense(sz_error_cost_t const *costs,

@@ -498,7 +498,7 @@ class _Alignment(_Engine):
     def dense(cls, substitution_matrix, open=-1, extend=-1, capabilities=None):
         """Extension: an engine over a dense 256 x 256 int8 table, ``substitution_matrix[a, b]`` = cost of aligning
         byte a of the first string with byte b of the second (no counterpart in the reference, which folds bytes
-        into 32 classes). Each call may use at most 32 distinct byte values."""
+        into 32 classes). Calls over more than 32 distinct byte values score on the 32-bit routes."""
         if not isinstance(substitution_matrix, np.ndarray):
             raise TypeError("substitution_matrix must be a NumPy array")
         if substitution_matrix.shape != (256, 256):

@@ -47,6 +47,7 @@ struct band_policy_t {
     static constexpr bool uniform_k = kind_ == kind_levenshtein_k;
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
+    static constexpr bool direct_k = false; // `direct_policy_t<>` reads costs from a dense table in shared memory
     using ops_t = cell_ops_t<std::int32_t, maximize_k>;
 };
 
@@ -69,13 +70,15 @@ struct band_shared_t {
 
 template <typename policy_>
 __host__ __device__ constexpr int band_profile_bytes_per_warp(int classes) {
-    return policy_::uniform_k ? 0 : classes * policy_::strip_rows_k;
+    return (policy_::uniform_k || policy_::direct_k) ? 0 : classes * policy_::strip_rows_k;
 }
 
+/** Costs, CTA state, per-warp profiles and chunk staging, then (direct-table instances) the dense table. */
 template <typename policy_>
 __host__ __device__ constexpr int band_shared_bytes(int classes) {
     return int((sizeof(score_costs_t) + 15) / 16 * 16) + int((sizeof(band_shared_t) + 15) / 16 * 16) +
-           band_warps_k * (band_profile_bytes_per_warp<policy_>(classes) + int(sizeof(band_chunk_t)));
+           band_warps_k * (band_profile_bytes_per_warp<policy_>(classes) + int(sizeof(band_chunk_t))) +
+           (policy_::direct_k ? direct_table_bytes_k : 0);
 }
 
 /** The ring a warp takes part in: its progress words and failure flag (the CTA's shared memory, or global memory
@@ -185,7 +188,7 @@ template <typename policy_>
 __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task, score_costs_t const &costs,
                                                         band_ring_t const &sync, std::int32_t *ring,
                                                         std::size_t ring_cells_per_slot, std::int8_t *profile,
-                                                        band_chunk_t &chunk) {
+                                                        band_chunk_t &chunk, std::int8_t const *table_s = nullptr) {
     using ops = typename policy_::ops_t;
     constexpr int R = policy_::rows_per_lane_k;
     constexpr int S = policy_::strip_rows_k;
@@ -205,7 +208,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
     auto gap_seed = [&](std::int64_t i) -> std::int32_t { return local ? extend : extend + edge.score(i); };
     auto column_code = [&](std::uint32_t j) -> std::uint32_t {
         std::uint32_t const byte = task.cols[j - 1];
-        if constexpr (policy_::uniform_k) return byte;
+        if constexpr (policy_::uniform_k || policy_::direct_k) return byte;
         else return costs.byte_to_compact[byte];
     };
 
@@ -231,7 +234,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             row_bytes[r] = i <= (std::int64_t)n ? task.rows[i - 1] : 0u;
         }
         __syncwarp();
-        if constexpr (!policy_::uniform_k) {
+        if constexpr (!policy_::uniform_k && !policy_::direct_k) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 int const row_class = costs.byte_to_class[row_bytes[r]];
@@ -254,7 +257,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
         std::uint32_t p_now[words];
-        if constexpr (!policy_::uniform_k)
+        if constexpr (!policy_::uniform_k && !policy_::direct_k)
             load_profile_words<R>(profile + (int)code_now * S + lane * R, p_now);
         bool healthy = true;
 
@@ -291,7 +294,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
             if (lane == 0) up_h = chunk.top_h[e], up_f = chunk.top_f[e], code_next = chunk.code[e];
             std::uint32_t p_next[words];
-            if constexpr (!policy_::uniform_k)
+            if constexpr (!policy_::uniform_k && !policy_::direct_k)
                 load_profile_words<R>(profile + (int)code_next * S + lane * R, p_next);
 
             std::int64_t const j = (std::int64_t)t + 1 - lane;
@@ -303,6 +306,12 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                 if constexpr (policy_::uniform_k) {
 #pragma unroll
                     for (int r = 0; r < R; ++r) subs[r] = row_bytes[r] == code_now ? costs.match : costs.mismatch;
+                }
+                else if constexpr (policy_::direct_k) {
+                    // table[first byte][second byte]: rows are the first string unless the pair was transposed.
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        subs[r] = table_s[task.transposed ? (code_now << 8) | row_bytes[r] : (row_bytes[r] << 8) | code_now];
                 }
                 else {
 #pragma unroll
@@ -346,7 +355,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                     }
             }
             code_now = code_next;
-            if constexpr (!policy_::uniform_k) {
+            if constexpr (!policy_::uniform_k && !policy_::direct_k) {
 #pragma unroll
                 for (int w = 0; w < words; ++w) p_now[w] = p_next[w];
             }
@@ -398,11 +407,13 @@ __global__ void __launch_bounds__(band_warps_k * 32)
     std::size_t const profile_bytes = (std::size_t)band_profile_bytes_per_warp<policy_>(costs.classes);
     std::int8_t *profiles = reinterpret_cast<std::int8_t *>(shared_bytes + costs_bytes + shared_state_bytes);
     auto *chunks = reinterpret_cast<band_chunk_t *>(profiles + band_warps_k * profile_bytes);
+    std::int8_t *table_s = reinterpret_cast<std::int8_t *>(chunks + band_warps_k);
     {
         auto const *src = reinterpret_cast<std::uint32_t const *>(&costs);
         auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
         for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
     }
+    if constexpr (policy_::direct_k) stage_direct_table(costs.direct_table, table_s);
     int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     std::int32_t *ring = scratch + (std::size_t)blockIdx.x * band_warps_k * ring_cells_per_slot;
     std::uint32_t const begin = bins->begin[key_begin];
@@ -418,7 +429,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         pair_task_t const task = tasks[begin + index];
         std::int32_t const value = band_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp), ring,
                                                             ring_cells_per_slot, profiles + warp * profile_bytes,
-                                                            chunks[warp]);
+                                                            chunks[warp], table_s);
         if (lane == 0) shared.warp_result[warp] = value;
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -478,11 +489,13 @@ __global__ void __launch_bounds__(band_warps_k * 32)
     std::size_t const profile_bytes = (std::size_t)band_profile_bytes_per_warp<policy_>(costs.classes);
     std::int8_t *profiles = reinterpret_cast<std::int8_t *>(shared_bytes + costs_bytes + shared_state_bytes);
     auto *chunks = reinterpret_cast<band_chunk_t *>(profiles + band_warps_k * profile_bytes);
+    std::int8_t *table_s = reinterpret_cast<std::int8_t *>(chunks + band_warps_k);
     {
         auto const *src = reinterpret_cast<std::uint32_t const *>(&costs);
         auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
         for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
     }
+    if constexpr (policy_::direct_k) stage_direct_table(costs.direct_table, table_s);
     int const warp = threadIdx.x >> 5;
     int const group = (int)blockIdx.x / group_ctas, rank = (int)blockIdx.x % group_ctas;
     int const groups = (int)gridDim.x / group_ctas;
@@ -500,7 +513,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         band_pass_state_t &pass = state->pass[parity][0];
         band_ring_t const sync {pass.progress, &state->failed, members, rank * band_warps_k + warp, true};
         std::int32_t const value = band_score_warp<policy_>(task, costs_s, sync, ring, ring_cells_per_slot,
-                                                            profiles + warp * profile_bytes, chunks[warp]);
+                                                            profiles + warp * profile_bytes, chunks[warp], table_s);
         std::uint32_t const strips = (task.rows_length + policy_::strip_rows_k - 1) / policy_::strip_rows_k;
         band_group_contribute<policy_::local_k>(pass, value, (int)((strips - 1) % (std::uint32_t)members) == sync.member);
         if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;

@@ -40,20 +40,38 @@ struct dp_policy_t {
     static constexpr bool uniform_k = kind_ == kind_levenshtein_k; // byte equality instead of a class table
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
+    static constexpr bool direct_k = false; // substitution costs from per-warp class profiles
     using cell_t = cell_type_;
     using ops_t = cell_ops_t<cell_t, maximize_k>;
 };
 
+/** The same kernel reading substitution costs straight from a dense 256 x 256 table that each CTA stages in shared
+ *  memory (dense-table calls over more than 32 distinct bytes, which no 32-class profile can hold). */
+template <typename policy_>
+struct direct_policy_t : policy_ {
+    static constexpr bool direct_k = true;
+};
+
+constexpr int direct_table_bytes_k = 256 * 256;
+
 /** Shared-memory bytes one warp needs for its substitution profile over @p classes column classes. */
 template <typename policy_>
 __host__ __device__ constexpr int dp_profile_bytes_per_warp(int classes) {
-    return policy_::uniform_k ? 0 : classes * policy_::strip_rows_k;
+    return (policy_::uniform_k || policy_::direct_k) ? 0 : classes * policy_::strip_rows_k;
 }
 
-/** Shared-memory bytes of one CTA: the staged costs plus one profile per warp. */
+/** Shared-memory bytes of one CTA: the staged costs plus one profile per warp (or the direct table). */
 template <typename policy_>
 __host__ __device__ constexpr int dp_shared_bytes(int warps_per_cta, int classes) {
-    return int((sizeof(score_costs_t) + 15) / 16 * 16) + warps_per_cta * dp_profile_bytes_per_warp<policy_>(classes);
+    return int((sizeof(score_costs_t) + 15) / 16 * 16) + warps_per_cta * dp_profile_bytes_per_warp<policy_>(classes) +
+           (policy_::direct_k ? direct_table_bytes_k : 0);
+}
+
+/** Copies the dense table into the CTA's shared memory (16 bytes per load); the caller synchronises. */
+__device__ __forceinline__ void stage_direct_table(std::int8_t const *table, std::int8_t *table_s) {
+    auto const *src = reinterpret_cast<uint4 const *>(table);
+    auto *dst = reinterpret_cast<uint4 *>(table_s);
+    for (unsigned i = threadIdx.x; i < direct_table_bytes_k / 16; i += blockDim.x) dst[i] = src[i];
 }
 
 /**
@@ -64,7 +82,8 @@ __host__ __device__ constexpr int dp_shared_bytes(int warps_per_cta, int classes
  */
 template <typename policy_>
 __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &task, score_costs_t const &costs,
-                                                           typename policy_::cell_t *scratch, std::int8_t *profile) {
+                                                           typename policy_::cell_t *scratch, std::int8_t *profile,
+                                                           std::int8_t const *table_s = nullptr) {
     using cell_t = typename policy_::cell_t;
     using ops = typename policy_::ops_t;
     constexpr int R = policy_::rows_per_lane_k;
@@ -96,7 +115,7 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
             std::int64_t const i = row0 + r;
             row_bytes[r] = i <= (std::int64_t)n ? task.rows[i - 1] : 0u;
         }
-        if constexpr (!policy_::uniform_k) {
+        if constexpr (!policy_::uniform_k && !policy_::direct_k) {
             // profile[cc * S + row_in_strip] = cost(row class, column class cc), oriented by `transposed`.
             __syncwarp();
             int const classes = costs.classes;
@@ -131,7 +150,7 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
             return strip_base == 0 ? edge.gap(j) : top[2 * j + 1];
         };
         auto column_code = [&](std::uint32_t byte) -> int {
-            if constexpr (policy_::uniform_k) return int(byte);
+            if constexpr (policy_::uniform_k || policy_::direct_k) return int(byte);
             else return costs.byte_to_compact[byte];
         };
         // Prefetched inputs of lane 0 for its next column.
@@ -174,6 +193,13 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
 #pragma unroll
                     for (int r = 0; r < R; ++r)
                         subs[r] = (row_bytes[r] == (std::uint32_t)code) ? (cell_t)costs.match : (cell_t)costs.mismatch;
+                }
+                else if constexpr (policy_::direct_k) {
+                    // table[first byte][second byte]: rows are the first string unless the pair was transposed.
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        subs[r] = (cell_t)table_s[task.transposed ? (code << 8) | (int)row_bytes[r]
+                                                                  : ((int)row_bytes[r] << 8) | code];
                 }
                 else {
                     static_assert(R % 8 == 0, "profile loads are 8 bytes wide");
@@ -268,6 +294,7 @@ __global__ void __launch_bounds__(256) dp_wavefront_kernel(pair_task_t const *__
         auto *dst = reinterpret_cast<std::uint32_t *>(&costs_s);
         for (unsigned i = threadIdx.x; i < sizeof(score_costs_t) / 4; i += blockDim.x) dst[i] = src[i];
     }
+    if constexpr (policy_::direct_k) stage_direct_table(costs.direct_table, profiles);
     __syncthreads();
 
     int const lane = threadIdx.x & 31;
@@ -284,7 +311,7 @@ __global__ void __launch_bounds__(256) dp_wavefront_kernel(pair_task_t const *__
         index = __shfl_sync(0xFFFFFFFFu, index, 0);
         if (index >= count) break;
         pair_task_t const task = tasks[begin + index];
-        std::int64_t const score = dp_score_pair_warp<policy_>(task, costs_s, warp_scratch, warp_profile);
+        std::int64_t const score = dp_score_pair_warp<policy_>(task, costs_s, warp_scratch, warp_profile, profiles);
         if (lane == 0) results[task.slot] = score;
     }
 }

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -225,6 +226,8 @@ struct device_context_t {
     device_buffer_t chunk_inputs;
     device_context_t *partner = nullptr; // second context of pipelined calls: its chunks alternate with this one's
     device_buffer_t utf8;                // UTF-8 calls: code-point set, counts, offsets and transcoded tapes
+    device_buffer_t dense_table;         // the 256 x 256 table of the dense engine last run here over > 32 bytes
+    std::uint64_t dense_table_id = 0;    // that engine's `dense_id` (0: none)
     bool deferred = false, deferred_compute = false;
     std::uint64_t deferred_launches = 0;
 
@@ -278,6 +281,7 @@ struct device_context_t {
         if (pipe_stop) cudaEventDestroy(pipe_stop);
         chunk_inputs.release();
         utf8.release();
+        dense_table.release(), dense_table_id = 0;
         if (partner) {
             partner->release();
             delete partner;
@@ -325,6 +329,7 @@ struct engine_t {
     szs_gb300_tuning_t tuning {};     // zeros: built-in choices
     int local_gain = -1;              // local scores with non-positive gaps: largest substitution gain (>= 0)
     std::vector<std::int8_t> dense;   // 256 x 256 [first byte][second byte] table of a dense engine, else empty
+    std::uint64_t dense_id = 0;       // unique per dense engine: device contexts cache its uploaded table by it
     bool utf8 = false;                // Levenshtein over UTF-8 code points (transcoded to one-byte codes per call)
     device_context_t devices[max_devices_k];
     szs_gb300_stats_t stats {};
@@ -709,6 +714,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.force_route = schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
     args.packed_allowed = engine.packed_profile_fits ? 1 : 0;
+    args.dense = engine.dense.empty() ? 0 : 1;
     std::memcpy(args.packed_rows, engine.tuning.packed_rows, 16);
     std::memcpy(args.cell_bits, engine.tuning.cell_bits, 16);
     args.band_min_rows = engine.tuning.band_min_rows ? engine.tuning.band_min_rows : (std::uint32_t)band_min_rows_k;
@@ -794,10 +800,24 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     // Dense-table engines score every route over the sub-table of the bytes this batch uses (dense codes from the
     // alphabet pass), which must fit the kernels' 32 compact classes.
     score_costs_t dense_costs;
-    if (dense) {
+    bool direct = false;
+    if (dense && alphabet_host.symbols > 32) {
+        // More distinct bytes than 32 classes: the 32-bit routes read the whole table from shared memory (the plan
+        // kept these pairs off the 16x2 routes, which need a 32-class profile).
+        if (context->dense_table_id != engine.dense_id) {
+            status = context->dense_table.reserve(engine.dense.size(), stream);
+            if (!status.ok()) return status;
+            SZS_TRY_CUDA(cudaMemcpyAsync(context->dense_table.data, engine.dense.data(), engine.dense.size(),
+                                         cudaMemcpyHostToDevice, stream));
+            context->dense_table_id = engine.dense_id;
+        }
+        dense_costs = engine.costs;
+        dense_costs.classes = 1;
+        dense_costs.direct_table = static_cast<std::int8_t const *>(context->dense_table.data);
+        direct = true;
+    }
+    else if (dense) {
         int const symbols = (int)alphabet_host.symbols;
-        if (symbols > 32)
-            return {sz_unexpected_dimensions_k, "A dense-table call may use at most 32 distinct byte values"};
         dense_costs = engine.costs;
         int byte_of_code[32] = {0};
         for (int b = 0; b < 256; ++b)
@@ -894,7 +914,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            dp_launch_shape_t const shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes);
+            dp_launch_shape_t const shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
             band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
@@ -915,7 +935,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int const key_begin = cell_bits == 32 ? bin_dp32_begin_k : bin_dp64_begin_k;
         std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + bin_dp_classes_k);
         if (!pairs_here) continue;
-        dp_launch_shape_t const shape = dp_shape(engine.kind, call_costs.affine != 0, cell_bits, call_costs.classes);
+        dp_launch_shape_t const shape =
+            dp_shape(engine.kind, call_costs.affine != 0, cell_bits, call_costs.classes, direct);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Wavefront kernel cannot be resident"};
         std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
@@ -1524,6 +1545,8 @@ sz_status_t create_dense_engine(int kind, int open, int extend, std::int8_t cons
     if (!engine) return report({sz_bad_alloc_k, "Failed to allocate the engine"}, error_message);
     engine->kind = kind;
     engine->dense.assign(table, table + 256 * 256);
+    static std::atomic<std::uint64_t> dense_ids {0};
+    engine->dense_id = ++dense_ids;
     score_costs_t &costs = engine->costs;
     std::memset(&costs, 0, sizeof(costs));
     costs.kind = kind;

@@ -46,6 +46,8 @@ struct score_costs_t {
     int classes;                    // number of compact column classes (NW / SW), <= 32
     int local_limit16;              // local scores on 16-bit cells are exact while every cell stays below this
                                     // (32767 - largest substitution gain); 0 when gaps may be positive
+    std::int8_t const *direct_table; // dense-table calls over more than 32 bytes: the 256 x 256 [first byte]
+                                     // [second byte] table in device memory, read by the direct-table kernels
     std::uint8_t byte_to_compact[256];  // byte -> compact class, indexing `profile_table` rows
     std::int8_t profile_table[32 * 32]; // [compact column class][row class] cost, already oriented for rows=first
     std::int8_t profile_table_t[32 * 32]; // same for rows=second (transposed lookups)

@@ -14,9 +14,10 @@ constexpr int band_rows_per_lane_k = 8;
 template <int kind_, bool affine_>
 using band_instance_t = band_policy_t<kind_, affine_, band_rows_per_lane_k>;
 
-template <int kind_, bool affine_>
+template <int kind_, bool affine_, bool direct_ = false>
 dp_launch_shape_t band_shape_of(int classes) {
-    using policy_t = band_instance_t<kind_, affine_>;
+    using policy_t = std::conditional_t<direct_, direct_policy_t<band_instance_t<kind_, affine_>>,
+                                        band_instance_t<kind_, affine_>>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = band_warps_k * 32;
     shape.warps_per_cta = band_warps_k;
@@ -38,12 +39,13 @@ dp_launch_shape_t band_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_>
+template <int kind_, bool affine_, bool direct_ = false>
 cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                            score_costs_t const &costs, std::int64_t *results, void *scratch,
                            std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
                            int group_ctas) {
-    using policy_t = band_instance_t<kind_, affine_>;
+    using policy_t = std::conditional_t<direct_, direct_policy_t<band_instance_t<kind_, affine_>>,
+                                        band_instance_t<kind_, affine_>>;
     int const shared = band_shared_bytes<policy_t>(costs.classes);
     if (group_states) {
         // The CTAs of a group wait on one another: a cooperative launch keeps the whole grid resident.
@@ -81,10 +83,25 @@ cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks,
     default: break;                                                                                                  \
     }
 
+/** Direct-table instances (dense tables over more than 32 bytes) exist for the alignment kinds only. */
+#define SZS_BAND_DIRECT_DISPATCH(call_, ...)                                                                         \
+    switch (kind * 2 + (affine ? 1 : 0)) {                                                                           \
+    case 2: return call_<kind_needleman_wunsch_k, false, true>(__VA_ARGS__);                                         \
+    case 3: return call_<kind_needleman_wunsch_k, true, true>(__VA_ARGS__);                                          \
+    case 4: return call_<kind_smith_waterman_k, false, true>(__VA_ARGS__);                                           \
+    case 5: return call_<kind_smith_waterman_k, true, true>(__VA_ARGS__);                                            \
+    default: break;                                                                                                  \
+    }
+
 int band_warps_per_cta() { return band_warps_k; }
 
-dp_launch_shape_t band_shape(int kind, bool affine, int classes) {
-    SZS_BAND_DISPATCH(band_shape_of, classes)
+dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct) {
+    if (direct) {
+        SZS_BAND_DIRECT_DISPATCH(band_shape_of, classes)
+    }
+    else {
+        SZS_BAND_DISPATCH(band_shape_of, classes)
+    }
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
@@ -92,8 +109,14 @@ cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
                         int group_ctas) {
-    SZS_BAND_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch, ring_cells_per_slot,
-                      ctas, stream, group_states, group_ctas)
+    if (costs.direct_table) {
+        SZS_BAND_DIRECT_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                                 ring_cells_per_slot, ctas, stream, group_states, group_ctas)
+    }
+    else {
+        SZS_BAND_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                          ring_cells_per_slot, ctas, stream, group_states, group_ctas)
+    }
     return cudaErrorInvalidValue;
 }
 

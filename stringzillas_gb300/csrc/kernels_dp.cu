@@ -15,9 +15,10 @@ constexpr int dp_threads_k = 256;
 template <int kind_, bool affine_, typename cell_t>
 using dp_instance_t = dp_policy_t<kind_, affine_, cell_t, dp_rows_per_lane_k>;
 
-template <int kind_, bool affine_, typename cell_t>
+template <int kind_, bool affine_, typename cell_t, bool direct_ = false>
 dp_launch_shape_t dp_shape_of(int classes) {
-    using policy_t = dp_instance_t<kind_, affine_, cell_t>;
+    using base_t = dp_instance_t<kind_, affine_, cell_t>;
+    using policy_t = std::conditional_t<direct_, direct_policy_t<base_t>, base_t>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = dp_threads_k;
     shape.warps_per_cta = dp_threads_k / 32;
@@ -33,11 +34,12 @@ dp_launch_shape_t dp_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_, typename cell_t>
+template <int kind_, bool affine_, typename cell_t, bool direct_ = false>
 cudaError_t dp_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                          score_costs_t const &costs, std::int64_t *results, void *scratch,
                          std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
-    using policy_t = dp_instance_t<kind_, affine_, cell_t>;
+    using base_t = dp_instance_t<kind_, affine_, cell_t>;
+    using policy_t = std::conditional_t<direct_, direct_policy_t<base_t>, base_t>;
     int const shared = dp_shared_bytes<policy_t>(dp_threads_k / 32, costs.classes);
     auto kernel = dp_wavefront_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
@@ -66,16 +68,42 @@ cudaError_t dp_launch_of(int key_begin, int key_end, pair_task_t const *tasks, p
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes) {
-    SZS_DP_DISPATCH(dp_shape_of, classes)
+/** Direct-table instances exist for the alignment kinds only (dense tables are a Needleman-Wunsch / Smith-Waterman
+ *  extension). */
+#define SZS_DP_DIRECT_DISPATCH(call_, ...)                                                                           \
+    switch (kind * 4 + (affine ? 2 : 0) + (cell_bits == 64 ? 1 : 0)) {                                               \
+    case 4: return call_<kind_needleman_wunsch_k, false, std::int32_t, true>(__VA_ARGS__);                           \
+    case 5: return call_<kind_needleman_wunsch_k, false, std::int64_t, true>(__VA_ARGS__);                           \
+    case 6: return call_<kind_needleman_wunsch_k, true, std::int32_t, true>(__VA_ARGS__);                            \
+    case 7: return call_<kind_needleman_wunsch_k, true, std::int64_t, true>(__VA_ARGS__);                            \
+    case 8: return call_<kind_smith_waterman_k, false, std::int32_t, true>(__VA_ARGS__);                             \
+    case 9: return call_<kind_smith_waterman_k, false, std::int64_t, true>(__VA_ARGS__);                             \
+    case 10: return call_<kind_smith_waterman_k, true, std::int32_t, true>(__VA_ARGS__);                             \
+    case 11: return call_<kind_smith_waterman_k, true, std::int64_t, true>(__VA_ARGS__);                             \
+    default: break;                                                                                                  \
+    }
+
+dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bool direct) {
+    if (direct) {
+        SZS_DP_DIRECT_DISPATCH(dp_shape_of, classes)
+    }
+    else {
+        SZS_DP_DISPATCH(dp_shape_of, classes)
+    }
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
 cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int key_end, pair_task_t const *tasks,
                       plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                       std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
-    SZS_DP_DISPATCH(dp_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
-                    ctas, stream)
+    if (costs.direct_table) {
+        SZS_DP_DIRECT_DISPATCH(dp_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                               scratch_cells_per_warp, ctas, stream)
+    }
+    else {
+        SZS_DP_DISPATCH(dp_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
+                        ctas, stream)
+    }
     return cudaErrorInvalidValue;
 }
 

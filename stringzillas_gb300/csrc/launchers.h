@@ -71,11 +71,12 @@ struct dp_launch_shape_t {
     int group_ctas_per_sm = 0; // band kernels: the same for the grouped (several CTAs per pair) kernel
 };
 
-/** Launch shape of the wavefront kernel for (kind, affine, cell bits, classes); ctas_per_sm = 0 if unsupported. */
-dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes);
+/** Launch shape of the wavefront kernel for (kind, affine, cell bits, classes); ctas_per_sm = 0 if unsupported.
+ *  `direct`: the direct-table instance (costs from a dense 256 x 256 table in shared memory). */
+dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bool direct = false);
 
 /** Runs the wavefront kernel over bins [key_begin, key_end). `scratch` holds `ctas * warps_per_cta` rows of
- *  `scratch_cells_per_warp` cells of `cell_bits` bits. */
+ *  `scratch_cells_per_warp` cells of `cell_bits` bits. Costs with a `direct_table` run the direct-table instance. */
 cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int key_end, pair_task_t const *tasks,
                       plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                       std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
@@ -90,8 +91,9 @@ cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream);
 
-/** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells). */
-dp_launch_shape_t band_shape(int kind, bool affine, int classes);
+/** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells); `direct`: the
+ *  direct-table instance. */
+dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct = false);
 /** Warps per band CTA (ring slots per CTA). */
 int band_warps_per_cta();
 
@@ -102,7 +104,7 @@ int band_warps_per_cta();
 cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
-                        int group_ctas = 1);
+                        int group_ctas = 1); // costs with a `direct_table` run the direct-table instance
 /** Bytes of one group's state record, and the most CTAs a group may have. */
 std::size_t band_group_state_bytes();
 int band_group_max_ctas();

@@ -73,6 +73,7 @@ struct plan_args_t {
     int steps_beyond_span;  // 1 linear, 3 affine (serial.hpp:126-140)
     int force_route;        // -1: normal planning; otherwise one bin per route, input order (the plain form)
     int packed_allowed;     // 1 if the 16x2 route may hold the substitution costs in int8 profiles
+    int dense;              // dense-table engine: its profile holds the batch's bytes, at most 32 of them
     batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)
     // Tuning by length class k = floor(log2(shorter side)), 15 for everything longer.
     std::uint8_t packed_rows[16];     // 0: per-pair step-cost model; else rows per lane 4, 8, 12, 16

@@ -513,10 +513,31 @@ def test_dense_tables(szs, port, family, costs):
     for q in range(20):
         np.testing.assert_array_equal(cross[q], port.pairs(oracle.dense_costs(kind, arbitrary, *costs),
                                                            tape([first[q]] * 15), tape(second[:15])))
-    # More than 32 distinct bytes in one call is refused.
-    wide = [bytes(range(40))]
-    with pytest.raises(ValueError):
-        engine.pairwise(szs.Strs(wide), szs.Strs(wide))
+
+
+@pytest.mark.parametrize("family,costs", [("nw", (-11, -1)), ("nw", (-4, -4)), ("sw", (-5, -2)), ("sw", (-3, -3))])
+def test_dense_tables_over_every_byte(szs, port, family, costs):
+    """Dense tables over more than 32 distinct bytes: the 32-bit routes read the whole 256 x 256 table from shared
+    memory (warp wavefront, band, grouped band), both orientations of a pair, against the oracle."""
+    rng = np.random.default_rng(29)
+    cls = szs.NeedlemanWunschScores if family == "nw" else szs.SmithWatermanScores
+    kind = oracle.NEEDLEMAN_WUNSCH if family == "nw" else oracle.SMITH_WATERMAN
+    table = rng.integers(-9, 10, size=(256, 256)).astype(np.int8)  # asymmetric
+    engine = cls.dense(table, open=costs[0], extend=costs[1])
+    want_costs = oracle.dense_costs(kind, table, *costs)
+    everything = np.arange(256, dtype=np.uint8)
+    for lengths in ([(int(rng.integers(0, 700)), int(rng.integers(0, 700))) for _ in range(120)] + [(1500, 1200)],
+                    [(2600, 3000)], [(40, 33), (33, 40)]):
+        first = [bytes(rng.choice(everything, size=n)) for n, _ in lengths]
+        second = [bytes(rng.choice(everything, size=m)) for _, m in lengths]
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, port.pairs(want_costs, tape(first), tape(second)))
+    # Forty distinct bytes, a cross product (queries shorter and longer than candidates: both orientations).
+    forty = np.arange(40, 80, dtype=np.uint8)
+    queries = [bytes(rng.choice(forty, size=n)) for n in (5, 300, 80)]
+    candidates = [bytes(rng.choice(forty, size=n)) for n in (120, 7, 300, 0)]
+    got = engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.cross(want_costs, tape(queries), tape(candidates)))
 
 
 def _golden_cases():
