@@ -210,7 +210,7 @@ struct device_context_t {
     pinned_buffer_t results_host;
     cudaEvent_t start = nullptr, stop = nullptr;
     cudaEvent_t compute_start = nullptr, compute_stop = nullptr;
-    static constexpr int lanes_k = 4; // auxiliary streams the routes of one call run on concurrently
+    static constexpr int lanes_k = 8; // auxiliary streams the routes of one call run on concurrently
     cudaStream_t lanes[lanes_k] = {nullptr};
     cudaEvent_t fork = nullptr;
     cudaEvent_t joins[lanes_k] = {nullptr};
@@ -353,6 +353,14 @@ cudaError_t launch_myers_planes3(int, bool, pair_task_t const *, plan_bins_t con
                                  std::int64_t *, int, cudaStream_t);
 cudaError_t launch_myers_planes5(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
                                  std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_warp_planes2(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
+                                     std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_warp_planes3(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
+                                     std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_warp_planes5(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
+                                     std::int64_t *, int, cudaStream_t);
+cudaError_t launch_myers_warp_planes8(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
+                                     std::int64_t *, int, cudaStream_t);
 cudaError_t launch_myers_planes8(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
                                  std::int64_t *, int, cudaStream_t);
 
@@ -364,6 +372,19 @@ int myers_planes_for(int bits_needed) {
 }
 
 int myers_threads_per_cta() { return 128; }
+
+/** Warp-per-pair bit-parallel kernel over the bins of `words` words per lane. */
+static cudaError_t launch_myers_warp(int words, int planes, pair_task_t const *tasks, plan_bins_t *bins,
+                                     batch_alphabet_t const *alphabet, std::int64_t *results, int ctas,
+                                     cudaStream_t stream) {
+    switch (planes) {
+    case 2: return launch_myers_warp_planes2(words, tasks, bins, alphabet, results, ctas, stream);
+    case 3: return launch_myers_warp_planes3(words, tasks, bins, alphabet, results, ctas, stream);
+    case 5: return launch_myers_warp_planes5(words, tasks, bins, alphabet, results, ctas, stream);
+    case 8: return launch_myers_warp_planes8(words, tasks, bins, alphabet, results, ctas, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_myers(int words, int planes, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
                          batch_alphabet_t const *alphabet, std::int64_t *results, int ctas, cudaStream_t stream) {
@@ -852,7 +873,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
 
     // The launch list, longest pairs first (64- and 32-bit wavefront, packed with the most rows per lane, then the
     // bit-parallel kernels by word count), so the routes' tails overlap each other instead of adding up.
-    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k };
+    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k, job_myers_warp_k };
     struct job_t {
         job_kind_t kind;
         int variant; // cell bits, rows per lane, or words
@@ -865,7 +886,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::size_t state_offset = 0;  // grouped band jobs: the groups' state records in the scratch buffer
         std::size_t state_bytes = 0;
     };
-    job_t jobs[40];
+    job_t jobs[64];
     int job_count = 0;
     std::size_t const cells_per_warp = align_up(((std::size_t)plan.max_cols + 1) * 2, 64);
     std::size_t const band16_words_per_slot = align_up((std::size_t)plan.max_cols + 1, 64);
@@ -964,6 +985,16 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     int myers_planes = 0;
     if (engine.unit_levenshtein) {
         myers_planes = myers_planes_for((int)alphabet_host.bits);
+        // Longer patterns first: one warp per pair, most words per lane first.
+        for (int words = myers_warp_max_words_k; words >= 1; --words) {
+            int const key_begin = bin_myers_warp_begin_k + (myers_warp_max_words_k - words) * myers_warp_classes_k;
+            std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + myers_warp_classes_k);
+            if (!pairs_here) continue;
+            std::uint64_t const needed = (pairs_here + 7) / 8; // eight warps per CTA
+            int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 2);
+            jobs[job_count++] = {job_myers_warp_k, words, 0, key_begin, key_begin + myers_warp_classes_k, pairs_here,
+                                 ctas, 0, 0};
+        }
         for (int words = myers_max_words_k; words >= 1; --words) {
             int const key_begin = bin_myers_begin_k + words * 16;
             std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + 16);
@@ -1034,6 +1065,9 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
                                          lane_stream));
+            else if (job.kind == job_myers_warp_k)
+                SZS_TRY_CUDA(launch_myers_warp(job.variant, myers_planes, tasks, bins, alphabet, results, job.ctas,
+                                               lane_stream));
             else
                 SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, schedule != szs_gb300_schedule_plain_k, tasks,
                                           bins, alphabet, results, job.ctas, lane_stream));

@@ -5,6 +5,7 @@
  */
 #include "launchers.h"
 #include "myers.cuh"
+#include "myers_warp.cuh"
 
 #ifndef SZS_MYERS_PLANES
 #error "compile with -DSZS_MYERS_PLANES=<2|3|5|8>"
@@ -51,6 +52,32 @@ cudaError_t SZS_CONCAT(launch_myers_planes, SZS_MYERS_PLANES)(int words, bool ex
     case 14: return myers_launch_words<14>(exact, tasks, bins, alphabet, results, ctas, stream);
     case 15: return myers_launch_words<15>(exact, tasks, bins, alphabet, results, ctas, stream);
     case 16: return myers_launch_words<16>(exact, tasks, bins, alphabet, results, ctas, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int words_>
+static cudaError_t myers_warp_launch_words(pair_task_t const *tasks, plan_bins_t *bins,
+                                           batch_alphabet_t const *alphabet, std::int64_t *results, int ctas,
+                                           cudaStream_t stream) {
+    myers_warp_kernel<words_, SZS_MYERS_PLANES><<<ctas, 256, 0, stream>>>(tasks, bins, alphabet, results);
+    return cudaGetLastError();
+}
+
+cudaError_t SZS_CONCAT(launch_myers_warp_planes, SZS_MYERS_PLANES)(int words, pair_task_t const *tasks,
+                                                                     plan_bins_t *bins,
+                                                                     batch_alphabet_t const *alphabet,
+                                                                     std::int64_t *results, int ctas,
+                                                                     cudaStream_t stream) {
+    switch (words) {
+    case 1: return myers_warp_launch_words<1>(tasks, bins, alphabet, results, ctas, stream);
+    case 2: return myers_warp_launch_words<2>(tasks, bins, alphabet, results, ctas, stream);
+    case 3: return myers_warp_launch_words<3>(tasks, bins, alphabet, results, ctas, stream);
+    case 4: return myers_warp_launch_words<4>(tasks, bins, alphabet, results, ctas, stream);
+    case 5: return myers_warp_launch_words<5>(tasks, bins, alphabet, results, ctas, stream);
+    case 6: return myers_warp_launch_words<6>(tasks, bins, alphabet, results, ctas, stream);
+    case 7: return myers_warp_launch_words<7>(tasks, bins, alphabet, results, ctas, stream);
+    case 8: return myers_warp_launch_words<8>(tasks, bins, alphabet, results, ctas, stream);
     default: return cudaErrorInvalidValue;
     }
 }

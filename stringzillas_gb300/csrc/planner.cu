@@ -83,6 +83,19 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         info.key = bin_myers_begin_k + words * 16 + text_class;
         return info;
     }
+    if (args.unit_levenshtein && n <= 32u * 32u * myers_warp_max_words_k) {
+        // Longer patterns: one warp per pair, W words per lane.
+        if (args.force_route >= 0) {
+            info.key = bin_myers_warp_begin_k; // plain form: one bin (16 words per lane), input order
+            return info;
+        }
+        int const words = int((n + 1023) / 1024);
+        int text_class = floor_log2_u64(m) - 9;
+        text_class = text_class < 0 ? 0 : (text_class > myers_warp_classes_k - 1 ? myers_warp_classes_k - 1 : text_class);
+        info.key = bin_myers_warp_begin_k + (myers_warp_max_words_k - words) * myers_warp_classes_k +
+                   (myers_warp_classes_k - 1 - text_class);
+        return info;
+    }
     bool const maximize = args.kind != kind_levenshtein_k;
     std::uint64_t const span = maximize ? n + m : (n > m ? n : m);
     std::uint64_t const reach = (span + (std::uint64_t)args.steps_beyond_span + 1) * (std::uint64_t)args.magnitude;

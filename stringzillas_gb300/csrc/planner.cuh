@@ -18,6 +18,8 @@
  *                pairs of a bin at once and pays for the larger of each dimension, so bins are narrow in both.
  *    [1360, 1392) band (one CTA per pair, 32-bit cells): key = 1360 + (31 - size class), size class ~ log2(n * m)
  *    [1392, 1424) 16-bit band (one CTA per pair, 16x2 cells): same layout from 1392
+ *    [1424, 1488) warp-per-pair Myers (unit Levenshtein, shorter side 513..8,192): key = 1424 + 8 * (8 - W)
+ *                 + (7 - text class), W = words per lane = ceil(n / 1024), text class ~ log2(m) - 9
  */
 #pragma once
 #include "engine_types.cuh"
@@ -43,6 +45,13 @@ constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shor
 constexpr int packed_step_cost_k[4] = {100, 165, 245, 330};
 constexpr int band_min_rows_packed_k = 2048; // default for pairs that fit 16-bit cells (the 16-bit band above it)
 constexpr int myers_max_words_k = 16;
+// Words per lane of the warp kernel: patterns up to 32 * 32 * 8 = 8,192 rows. Longer ones take the bands: a pair of
+// 8-16k characters keeps one warp busy for milliseconds, and a call rarely has enough of them to fill the GPU.
+constexpr int myers_warp_max_words_k = 8;
+constexpr int myers_warp_classes_k = 8;    // text-length classes per words count (longest first)
+constexpr int bin_myers_warp_begin_k = bin_band16_begin_k + bin_dp_classes_k; // 1424
+static_assert(bin_myers_warp_begin_k + myers_warp_max_words_k * myers_warp_classes_k <= bin_keys_k,
+              "bin layout exceeds the key space");
 
 /** Which pairs a call scores. */
 enum pair_mode_t : int {

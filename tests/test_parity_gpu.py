@@ -136,6 +136,31 @@ def test_cross_and_symmetric_with_long_strings(szs, port, name, family, costs):
     np.testing.assert_array_equal(got_sym, port.cross(oracle_costs, tape(queries)))
 
 
+@pytest.mark.parametrize("symbols", [4, 8, 30, 256])
+def test_warp_myers_long_patterns(szs, port, symbols):
+    """Unit-cost Levenshtein with shorter sides 513..8,192 takes the warp-per-pair bit-parallel route (W words per
+    lane, the carry and the shifted-out deltas passed down the lanes); longer ones take the bands. Code planes
+    follow the batch alphabet (2, 3, 5 or 8)."""
+    rng = np.random.default_rng(symbols + 100)
+    alphabet = np.arange(256, dtype=np.uint8)[:symbols] if symbols < 256 else np.arange(256, dtype=np.uint8)
+    lengths = [(512, 600), (513, 513), (514, 2000), (1023, 1100), (1024, 1024), (1025, 1030), (2048, 5000),
+               (3000, 3000), (4096, 4200), (4097, 4100)]
+    if symbols == 4:
+        lengths += [(3500, 16390), (700, 40000), (8192, 8200), (8193, 8193)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    # Related pairs (small distances) and one swapped orientation (the longer string first).
+    second[3] = first[3][:900] + second[3][900:]
+    second[6] = first[6] + second[6][2048:]
+    first[4], second[4] = second[4], first[4]
+    engine = szs.LevenshteinDistances()
+    want = port.pairs(oracle.levenshtein_costs(), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, want)
+
+
 def test_myers_every_word_count(szs, port):
     """Unit-cost Levenshtein takes the bit-parallel route for shorter sides up to 512, the DP route above."""
     rng = np.random.default_rng(3)
