@@ -203,8 +203,9 @@ SZS_GB300_API void szs_levenshtein_distances_free(szs_levenshtein_distances_t en
 
 /**
  *  Distances over UTF-8 code points. Each call decodes both tapes on the device the way the reference does
- *  (lead-byte lengths, continuation bytes not checked) and numbers the batch's distinct code points; a call may
- *  use at most 256 distinct code points (more give `sz_unexpected_dimensions_k`). Replaces stringzillas.h:239.
+ *  (lead-byte lengths, continuation bytes not checked) and numbers the batch's distinct code points: one-byte codes
+ *  up to 256 of them, 16-bit codes up to 65,536 (more give `sz_unexpected_dimensions_k`). Replaces
+ *  stringzillas.h:239.
  */
 SZS_GB300_API sz_status_t szs_levenshtein_distances_utf8_init(sz_error_cost_t match, sz_error_cost_t mismatch,
                                                               sz_error_cost_t open, sz_error_cost_t extend,

@@ -434,7 +434,7 @@ class LevenshteinDistances(_Engine):
 
 class LevenshteinDistancesUTF8(LevenshteinDistances):
     """Edit distances over UTF-8 code points (``LevenshteinDistancesUTF8`` of the reference). Each call numbers the
-    distinct code points of its batch on the device; a call may use at most 256 of them."""
+    distinct code points of its batch on the device (one-byte codes up to 256 of them, 16-bit codes up to 65,536)."""
 
     _algo = "levenshtein_distances_utf8"
     _name = "UTF-8 Levenshtein distances"

@@ -37,6 +37,7 @@ UNITS = [
     ("server", "server.cu", []),
     ("utf8", "utf8.cu", []),
     ("fingerprints", "fingerprints.cu", []),
+    ("myers_wide", "kernels_myers_wide.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),
     ("myers_p3", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=3"]),
     ("myers_p5", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=5"]),

@@ -48,6 +48,7 @@ struct band_policy_t {
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
     static constexpr bool direct_k = false; // `direct_policy_t<>` reads costs from a dense table in shared memory
+    static constexpr bool wide_k = false;   // `wide_policy_t<>`: strings of 16-bit codes
     using ops_t = cell_ops_t<std::int32_t, maximize_k>;
 };
 
@@ -207,7 +208,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
     std::int8_t const *table = task.transposed ? costs.profile_table_t : costs.profile_table;
     auto gap_seed = [&](std::int64_t i) -> std::int32_t { return local ? extend : extend + edge.score(i); };
     auto column_code = [&](std::uint32_t j) -> std::uint32_t {
-        std::uint32_t const byte = task.cols[j - 1];
+        std::uint32_t const byte = symbol_at<policy_::wide_k>(task.cols, j - 1);
         if constexpr (policy_::uniform_k || policy_::direct_k) return byte;
         else return costs.byte_to_compact[byte];
     };
@@ -231,7 +232,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             std::int64_t const i = row0 + r;
-            row_bytes[r] = i <= (std::int64_t)n ? task.rows[i - 1] : 0u;
+            row_bytes[r] = i <= (std::int64_t)n ? symbol_at<policy_::wide_k>(task.rows, i - 1) : 0u;
         }
         __syncwarp();
         if constexpr (!policy_::uniform_k && !policy_::direct_k) {

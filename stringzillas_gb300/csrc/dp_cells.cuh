@@ -105,4 +105,40 @@ struct byte_stream_t {
     }
 };
 
+/** Sequential reads of 16-bit codes in aligned 8-byte chunks: the `byte_stream_t` of tapes transcoded to 16-bit codes
+ *  (UTF-8 calls over more than 256 code points). */
+struct code16_stream_t {
+    std::uint64_t const *chunk;
+    std::uint64_t window;
+    int left; // codes remaining in `window`
+
+    __device__ __forceinline__ void open_at(std::uint8_t const *p) {
+        std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(p);
+        chunk = reinterpret_cast<std::uint64_t const *>(address & ~std::uintptr_t(7));
+        int const skip = int(address & 7) / 2;
+        window = __ldg(chunk) >> (16 * skip);
+        left = 4 - skip;
+        ++chunk;
+    }
+    /** Next code; the caller must not read past the string end by more than the chunk holding its last code. */
+    __device__ __forceinline__ std::uint32_t next() {
+        if (left == 0) {
+            window = __ldg(chunk);
+            ++chunk;
+            left = 4;
+        }
+        std::uint32_t const code = std::uint32_t(window & 0xFFFF);
+        window >>= 16;
+        --left;
+        return code;
+    }
+};
+
+/** Symbol `index` of a string: a byte, or a 16-bit code when `wide_`. */
+template <bool wide_>
+__device__ __forceinline__ std::uint32_t symbol_at(std::uint8_t const *string, std::uint64_t index) {
+    if constexpr (wide_) return reinterpret_cast<std::uint16_t const *>(string)[index];
+    else return string[index];
+}
+
 } // namespace szs_gb300

@@ -41,6 +41,7 @@ struct dp_policy_t {
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
     static constexpr bool direct_k = false; // substitution costs from per-warp class profiles
+    static constexpr bool wide_k = false;   // strings of bytes (16-bit codes: `wide_policy_t<>`)
     using cell_t = cell_type_;
     using ops_t = cell_ops_t<cell_t, maximize_k>;
 };
@@ -50,6 +51,13 @@ struct dp_policy_t {
 template <typename policy_>
 struct direct_policy_t : policy_ {
     static constexpr bool direct_k = true;
+};
+
+/** The same kernel over strings of 16-bit codes (UTF-8 Levenshtein over more than 256 code points); uniform costs. */
+template <typename policy_>
+struct wide_policy_t : policy_ {
+    static_assert(policy_::uniform_k, "16-bit codes are compared, not looked up in a table");
+    static constexpr bool wide_k = true;
 };
 
 constexpr int direct_table_bytes_k = 256 * 256;
@@ -113,7 +121,7 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             std::int64_t const i = row0 + r;
-            row_bytes[r] = i <= (std::int64_t)n ? task.rows[i - 1] : 0u;
+            row_bytes[r] = i <= (std::int64_t)n ? symbol_at<policy_::wide_k>(task.rows, i - 1) : 0u;
         }
         if constexpr (!policy_::uniform_k && !policy_::direct_k) {
             // profile[cc * S + row_in_strip] = cost(row class, column class cc), oriented by `transposed`.
@@ -140,7 +148,7 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
         cell_t diag_up = edge.score(row0 - 1);
 
         // Lane 0's top-boundary source.
-        byte_stream_t column_stream;
+        std::conditional_t<policy_::wide_k, code16_stream_t, byte_stream_t> column_stream;
         column_stream.open_at(task.cols);
         cell_t const *top = scratch;
         auto top_h = [&](std::uint32_t j) -> cell_t {

@@ -593,7 +593,7 @@ static status_t finish_deferred(device_context_t *context, szs_gb300_stats_t &st
  *  place of @p queries and @p candidates. A call may use at most 256 distinct code points.
  */
 static status_t transcode_utf8(device_context_t *context, cudaStream_t stream, tape_t &queries, tape_t &candidates,
-                               bool has_candidates) noexcept {
+                               bool has_candidates, bool &wide) noexcept {
     tape_t *tapes[2] = {&queries, has_candidates ? &candidates : nullptr};
     std::uint64_t first[2] = {0, 0}, end[2] = {0, 0};
     // The tapes' extents: the transcoded data can hold no more runes than bytes.
@@ -613,7 +613,8 @@ static status_t transcode_utf8(device_context_t *context, cudaStream_t stream, t
         std::uint64_t const count = tapes[t]->count;
         layout[t][0] = cursor, cursor += align_up((count + 1) * 8, 256);
         layout[t][1] = cursor, cursor += align_up((count + 1) * 8, 256);
-        layout[t][2] = cursor, cursor += align_up(end[t] - first[t] + 1, 256);
+        // Room for two bytes per code (more than 256 code points) and a whole 8-byte chunk past the end.
+        layout[t][2] = cursor, cursor += align_up(2 * (end[t] - first[t]) + 8, 256);
         scan_bytes = std::max(scan_bytes, utf8_scan_scratch_bytes(count));
     }
     std::size_t const scan_at = cursor;
@@ -632,15 +633,16 @@ static status_t transcode_utf8(device_context_t *context, cudaStream_t stream, t
     std::uint32_t seen[2] = {0, 0}; // symbols, overflow
     SZS_TRY_CUDA(cudaMemcpyAsync(seen, &set->symbols, sizeof(seen), cudaMemcpyDeviceToHost, stream));
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
-    if (seen[1] || seen[0] > 256)
-        return {sz_unexpected_dimensions_k, "A UTF-8 call may use at most 256 distinct code points"};
+    if (seen[1] || seen[0] > 65536)
+        return {sz_unexpected_dimensions_k, "A UTF-8 call may use at most 65,536 distinct code points"};
+    wide = seen[0] > 256; // 16-bit codes beyond 256 code points
     for (int t = 0; t < 2; ++t) {
         if (!tapes[t]) continue;
         auto const *counts = reinterpret_cast<std::uint64_t const *>(area + layout[t][0]);
         auto *offsets = reinterpret_cast<std::uint64_t *>(area + layout[t][1]);
         auto *data = reinterpret_cast<std::uint8_t *>(area + layout[t][2]);
         SZS_TRY_CUDA(launch_utf8_scan(counts, offsets, tapes[t]->count, area + scan_at, scan_bytes, stream));
-        SZS_TRY_CUDA(launch_utf8_write(*tapes[t], end[t], offsets, set, data, context->sm_count, stream));
+        SZS_TRY_CUDA(launch_utf8_write(*tapes[t], end[t], offsets, set, data, wide, context->sm_count, stream));
         tapes[t]->base = data;
         tapes[t]->offsets = offsets;
         tapes[t]->offset_bits = 64;
@@ -710,9 +712,11 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         }
         else args.candidates = args.queries;
     }
+    bool wide = false; // UTF-8 calls over more than 256 code points: 16-bit codes
     if (engine.utf8) {
-        status = transcode_utf8(context, stream, args.queries, args.candidates, call.has_candidates);
+        status = transcode_utf8(context, stream, args.queries, args.candidates, call.has_candidates, wide);
         if (!status.ok()) return status;
+        args.wide = wide ? 1 : 0;
     }
 
     // Work buffers: tasks, then dense results.
@@ -734,7 +738,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.steps_beyond_span = costs.affine ? 3 : 1;
     args.force_route = schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
-    args.packed_allowed = engine.packed_profile_fits ? 1 : 0;
+    args.packed_allowed = engine.packed_profile_fits && !wide ? 1 : 0; // 16-bit codes: no 32-class profile
     args.dense = engine.dense.empty() ? 0 : 1;
     std::memcpy(args.packed_rows, engine.tuning.packed_rows, 16);
     std::memcpy(args.cell_bits, engine.tuning.cell_bits, 16);
@@ -747,7 +751,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                             : (std::uint16_t)packed_step_cost_k[choice];
     bool const levenshtein = engine.kind == kind_levenshtein_k;
     bool const dense = !engine.dense.empty();
-    bool const alphabet_pass = levenshtein || dense; // both score over the batch's own byte codes
+    // Both score over the batch's own byte codes; 16-bit codes are already dense.
+    bool const alphabet_pass = (levenshtein || dense) && !wide;
 
     static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
     // Device-resident inputs make every launch of the call a function of bytes the call can key on, so both phases
@@ -935,7 +940,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            dp_launch_shape_t const shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct);
+            dp_launch_shape_t const shape =
+                band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
             band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
@@ -957,7 +963,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + bin_dp_classes_k);
         if (!pairs_here) continue;
         dp_launch_shape_t const shape =
-            dp_shape(engine.kind, call_costs.affine != 0, cell_bits, call_costs.classes, direct);
+            dp_shape(engine.kind, call_costs.affine != 0, cell_bits, call_costs.classes, direct, wide);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Wavefront kernel cannot be resident"};
         std::uint64_t const needed = (pairs_here + shape.warps_per_cta - 1) / shape.warps_per_cta;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
@@ -984,7 +990,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     }
     int myers_planes = 0;
     if (engine.unit_levenshtein) {
-        myers_planes = myers_planes_for((int)alphabet_host.bits);
+        myers_planes = wide ? 16 : myers_planes_for((int)alphabet_host.bits);
         // Longer patterns first: one warp per pair, most words per lane first.
         for (int words = myers_warp_max_words_k; words >= 1; --words) {
             int const key_begin = bin_myers_warp_begin_k + (myers_warp_max_words_k - words) * myers_warp_classes_k;
@@ -1032,7 +1038,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         key_append(launch_key, packed_costs), key_append(launch_key, call_costs);
         key_append(launch_key, tasks), key_append(launch_key, bins), key_append(launch_key, results);
         key_append(launch_key, context->scratch.data), key_append(launch_key, alphabet);
-        key_append(launch_key, cells_per_warp), key_append(launch_key, myers_planes);
+        key_append(launch_key, cells_per_warp), key_append(launch_key, myers_planes), key_append(launch_key, wide);
         key_append(launch_key, schedule), key_append(launch_key, lanes_used);
         key_append(launch_key, engine.kind);
     }
@@ -1053,21 +1059,27 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             if (job.kind == job_band_k)
                 SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                          call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,
-                                         group_states, job.group_ctas));
+                                         group_states, job.group_ctas, wide));
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
                                            lane_stream, group_states, job.group_ctas));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
-                                       bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream));
+                                       bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,
+                                       wide));
             else if (job.kind == job_dp16_k)
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
                                          lane_stream));
+            else if (job.kind == job_myers_warp_k && wide)
+                SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, results, job.ctas, lane_stream));
             else if (job.kind == job_myers_warp_k)
                 SZS_TRY_CUDA(launch_myers_warp(job.variant, myers_planes, tasks, bins, alphabet, results, job.ctas,
                                                lane_stream));
+            else if (wide)
+                SZS_TRY_CUDA(launch_myers_wide(job.variant, schedule != szs_gb300_schedule_plain_k, tasks, bins,
+                                               results, job.ctas, lane_stream));
             else
                 SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, schedule != szs_gb300_schedule_plain_k, tasks,
                                           bins, alphabet, results, job.ctas, lane_stream));

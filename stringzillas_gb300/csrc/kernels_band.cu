@@ -14,10 +14,17 @@ constexpr int band_rows_per_lane_k = 8;
 template <int kind_, bool affine_>
 using band_instance_t = band_policy_t<kind_, affine_, band_rows_per_lane_k>;
 
-template <int kind_, bool affine_, bool direct_ = false>
+/** The instance for (direct table, 16-bit codes): at most one of the two. */
+template <int kind_, bool affine_, bool direct_, bool wide_>
+struct band_variant {
+    using base_t = band_instance_t<kind_, affine_>;
+    using type = std::conditional_t<direct_, direct_policy_t<base_t>,
+                                    std::conditional_t<wide_, wide_policy_t<base_t>, base_t>>;
+};
+
+template <int kind_, bool affine_, bool direct_ = false, bool wide_ = false>
 dp_launch_shape_t band_shape_of(int classes) {
-    using policy_t = std::conditional_t<direct_, direct_policy_t<band_instance_t<kind_, affine_>>,
-                                        band_instance_t<kind_, affine_>>;
+    using policy_t = typename band_variant<kind_, affine_, direct_, wide_>::type;
     dp_launch_shape_t shape;
     shape.threads_per_cta = band_warps_k * 32;
     shape.warps_per_cta = band_warps_k;
@@ -39,13 +46,12 @@ dp_launch_shape_t band_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_, bool direct_ = false>
+template <int kind_, bool affine_, bool direct_ = false, bool wide_ = false>
 cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                            score_costs_t const &costs, std::int64_t *results, void *scratch,
                            std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
                            int group_ctas) {
-    using policy_t = std::conditional_t<direct_, direct_policy_t<band_instance_t<kind_, affine_>>,
-                                        band_instance_t<kind_, affine_>>;
+    using policy_t = typename band_variant<kind_, affine_, direct_, wide_>::type;
     int const shared = band_shared_bytes<policy_t>(costs.classes);
     if (group_states) {
         // The CTAs of a group wait on one another: a cooperative launch keeps the whole grid resident.
@@ -93,10 +99,21 @@ cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks,
     default: break;                                                                                                  \
     }
 
+/** 16-bit-code instances exist for Levenshtein only (UTF-8 calls). */
+#define SZS_BAND_WIDE_DISPATCH(call_, ...)                                                                           \
+    switch (kind * 2 + (affine ? 1 : 0)) {                                                                           \
+    case 0: return call_<kind_levenshtein_k, false, false, true>(__VA_ARGS__);                                       \
+    case 1: return call_<kind_levenshtein_k, true, false, true>(__VA_ARGS__);                                        \
+    default: break;                                                                                                  \
+    }
+
 int band_warps_per_cta() { return band_warps_k; }
 
-dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct) {
-    if (direct) {
+dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct, bool wide) {
+    if (wide) {
+        SZS_BAND_WIDE_DISPATCH(band_shape_of, classes)
+    }
+    else if (direct) {
         SZS_BAND_DIRECT_DISPATCH(band_shape_of, classes)
     }
     else {
@@ -108,8 +125,12 @@ dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct) {
 cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
-                        int group_ctas) {
-    if (costs.direct_table) {
+                        int group_ctas, bool wide) {
+    if (wide) {
+        SZS_BAND_WIDE_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                               ring_cells_per_slot, ctas, stream, group_states, group_ctas)
+    }
+    else if (costs.direct_table) {
         SZS_BAND_DIRECT_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
                                  ring_cells_per_slot, ctas, stream, group_states, group_ctas)
     }

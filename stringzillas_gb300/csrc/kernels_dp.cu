@@ -15,10 +15,17 @@ constexpr int dp_threads_k = 256;
 template <int kind_, bool affine_, typename cell_t>
 using dp_instance_t = dp_policy_t<kind_, affine_, cell_t, dp_rows_per_lane_k>;
 
-template <int kind_, bool affine_, typename cell_t, bool direct_ = false>
-dp_launch_shape_t dp_shape_of(int classes) {
+/** The instance for (direct table, 16-bit codes): at most one of the two. */
+template <int kind_, bool affine_, typename cell_t, bool direct_, bool wide_>
+struct dp_variant {
     using base_t = dp_instance_t<kind_, affine_, cell_t>;
-    using policy_t = std::conditional_t<direct_, direct_policy_t<base_t>, base_t>;
+    using type = std::conditional_t<direct_, direct_policy_t<base_t>,
+                                    std::conditional_t<wide_, wide_policy_t<base_t>, base_t>>;
+};
+
+template <int kind_, bool affine_, typename cell_t, bool direct_ = false, bool wide_ = false>
+dp_launch_shape_t dp_shape_of(int classes) {
+    using policy_t = typename dp_variant<kind_, affine_, cell_t, direct_, wide_>::type;
     dp_launch_shape_t shape;
     shape.threads_per_cta = dp_threads_k;
     shape.warps_per_cta = dp_threads_k / 32;
@@ -34,12 +41,11 @@ dp_launch_shape_t dp_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_, typename cell_t, bool direct_ = false>
+template <int kind_, bool affine_, typename cell_t, bool direct_ = false, bool wide_ = false>
 cudaError_t dp_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                          score_costs_t const &costs, std::int64_t *results, void *scratch,
                          std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
-    using base_t = dp_instance_t<kind_, affine_, cell_t>;
-    using policy_t = std::conditional_t<direct_, direct_policy_t<base_t>, base_t>;
+    using policy_t = typename dp_variant<kind_, affine_, cell_t, direct_, wide_>::type;
     int const shared = dp_shared_bytes<policy_t>(dp_threads_k / 32, costs.classes);
     auto kernel = dp_wavefront_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
@@ -83,8 +89,21 @@ cudaError_t dp_launch_of(int key_begin, int key_end, pair_task_t const *tasks, p
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bool direct) {
-    if (direct) {
+/** 16-bit-code instances exist for Levenshtein only (UTF-8 calls). */
+#define SZS_DP_WIDE_DISPATCH(call_, ...)                                                                             \
+    switch (kind * 4 + (affine ? 2 : 0) + (cell_bits == 64 ? 1 : 0)) {                                               \
+    case 0: return call_<kind_levenshtein_k, false, std::int32_t, false, true>(__VA_ARGS__);                         \
+    case 1: return call_<kind_levenshtein_k, false, std::int64_t, false, true>(__VA_ARGS__);                         \
+    case 2: return call_<kind_levenshtein_k, true, std::int32_t, false, true>(__VA_ARGS__);                          \
+    case 3: return call_<kind_levenshtein_k, true, std::int64_t, false, true>(__VA_ARGS__);                          \
+    default: break;                                                                                                  \
+    }
+
+dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bool direct, bool wide) {
+    if (wide) {
+        SZS_DP_WIDE_DISPATCH(dp_shape_of, classes)
+    }
+    else if (direct) {
         SZS_DP_DIRECT_DISPATCH(dp_shape_of, classes)
     }
     else {
@@ -95,8 +114,12 @@ dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bo
 
 cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int key_end, pair_task_t const *tasks,
                       plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                      std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream) {
-    if (costs.direct_table) {
+                      std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream, bool wide) {
+    if (wide) {
+        SZS_DP_WIDE_DISPATCH(dp_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                             scratch_cells_per_warp, ctas, stream)
+    }
+    else if (costs.direct_table) {
         SZS_DP_DIRECT_DISPATCH(dp_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
                                scratch_cells_per_warp, ctas, stream)
     }

@@ -38,7 +38,7 @@ cudaError_t launch_fingerprints(tape_t const &texts, fingerprint_dim_t const *pa
 
 /** The set of a batch's code points (UTF-8 Levenshtein): open addressing over `code point + 1` (0 = empty), then
  *  dense codes in slot order. */
-constexpr int rune_set_bits_k = 15;
+constexpr int rune_set_bits_k = 17; // 131,072 slots: room for 65,536 distinct code points at half load
 constexpr std::uint32_t rune_set_slots_k = 1u << rune_set_bits_k;
 struct rune_set_t {
     std::uint32_t keys[rune_set_slots_k];
@@ -57,9 +57,9 @@ std::size_t utf8_scan_scratch_bytes(std::uint64_t count);
 /** `offsets[0..count]` = exclusive scan of `counts[0..count]` (counts[count] must be 0). */
 cudaError_t launch_utf8_scan(std::uint64_t const *counts, std::uint64_t *offsets, std::uint64_t count, void *scratch,
                              std::size_t scratch_bytes, cudaStream_t stream);
-/** Writes each string's one-byte codes at `out + offsets[i]`. */
+/** Writes each string's codes at `out + offsets[i]` (in codes): one byte each, or 16 bits each when `wide`. */
 cudaError_t launch_utf8_write(tape_t const &tape, std::uint64_t end, std::uint64_t const *offsets,
-                              rune_set_t const *set, std::uint8_t *out, int sm_count, cudaStream_t stream);
+                              rune_set_t const *set, void *out, bool wide, int sm_count, cudaStream_t stream);
 
 /** Shape of a wavefront-DP launch for one engine configuration. */
 struct dp_launch_shape_t {
@@ -73,13 +73,14 @@ struct dp_launch_shape_t {
 
 /** Launch shape of the wavefront kernel for (kind, affine, cell bits, classes); ctas_per_sm = 0 if unsupported.
  *  `direct`: the direct-table instance (costs from a dense 256 x 256 table in shared memory). */
-dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bool direct = false);
+dp_launch_shape_t dp_shape(int kind, bool affine, int cell_bits, int classes, bool direct = false, bool wide = false);
 
 /** Runs the wavefront kernel over bins [key_begin, key_end). `scratch` holds `ctas * warps_per_cta` rows of
- *  `scratch_cells_per_warp` cells of `cell_bits` bits. Costs with a `direct_table` run the direct-table instance. */
+ *  `scratch_cells_per_warp` cells of `cell_bits` bits. Costs with a `direct_table` run the direct-table instance;
+ *  `wide`: strings of 16-bit codes (Levenshtein). */
 cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int key_end, pair_task_t const *tasks,
                       plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                      std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream);
+                      std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream, bool wide = false);
 
 /** Launch shape of the 16x2 packed wavefront kernel with `rows` (4, 8, 12, 16) rows per lane and `warps` (1..8)
  *  warps per CTA; ctas_per_sm = 0 if unsupported. */
@@ -93,7 +94,7 @@ cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_
 
 /** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells); `direct`: the
  *  direct-table instance. */
-dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct = false);
+dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct = false, bool wide = false);
 /** Warps per band CTA (ring slots per CTA). */
 int band_warps_per_cta();
 
@@ -104,7 +105,8 @@ int band_warps_per_cta();
 cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
-                        int group_ctas = 1); // costs with a `direct_table` run the direct-table instance
+                        int group_ctas = 1, bool wide = false); // costs with a `direct_table` run the
+                                                                 // direct-table instance; `wide`: 16-bit codes
 /** Bytes of one group's state record, and the most CTAs a group may have. */
 std::size_t band_group_state_bytes();
 int band_group_max_ctas();
@@ -119,6 +121,14 @@ cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pai
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
                           int group_ctas = 1);
+
+/** Bit-parallel kernels over strings of 16-bit codes (UTF-8 calls over more than 256 code points, 16 code planes):
+ *  thread per pair over the bins of `words` words (1..8), and warp per pair over the warp bins (1..8 words per
+ *  lane). */
+cudaError_t launch_myers_wide(int words, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
+                              std::int64_t *results, int ctas, cudaStream_t stream);
+cudaError_t launch_myers_warp_wide(int words, pair_task_t const *tasks, plan_bins_t *bins, std::int64_t *results,
+                                   int ctas, cudaStream_t stream);
 
 /** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
  *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be

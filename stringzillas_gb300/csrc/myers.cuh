@@ -160,4 +160,61 @@ __global__ void __launch_bounds__(128) myers_kernel(pair_task_t const *__restric
     }
 }
 
+/** Planes a 16-bit code needs: UTF-8 calls over more than 256 code points score with all 16. */
+constexpr int myers_wide_planes_k = 16;
+
+/** Selectors of a 16-bit code, from its bits (a 65,536-entry shared table would not fit): all-ones where the bit
+ *  is 0, as in `plane_selectors_t`. */
+template <int bits_>
+__device__ __forceinline__ void code_selectors(std::uint32_t code, std::uint32_t (&select)[bits_]) {
+#pragma unroll
+    for (int b = 0; b < bits_; ++b) select[b] = ((code >> b) & 1u) - 1u;
+}
+
+/** Thread-per-pair kernel over strings of 16-bit codes (UTF-8 calls over more than 256 code points). */
+template <int words_, bool exact_>
+__global__ void __launch_bounds__(128) myers_wide_kernel(pair_task_t const *__restrict__ tasks,
+                                                         plan_bins_t const *__restrict__ bins,
+                                                         std::int64_t *__restrict__ results) {
+    constexpr int W = words_, B = myers_wide_planes_k;
+    int const key_begin = bin_myers_begin_k + words_ * 16, key_end = key_begin + 16;
+    std::uint32_t const begin = bins->begin[key_begin];
+    std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
+    for (std::uint32_t index = blockIdx.x * blockDim.x + threadIdx.x; index < count;
+         index += gridDim.x * blockDim.x) {
+        pair_task_t const task = tasks[begin + index];
+        auto const *pattern = reinterpret_cast<std::uint16_t const *>(task.rows);
+        std::uint32_t const n = task.rows_length, m = task.cols_length;
+        myers_state_t<W, B, exact_> state;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            std::uint32_t acc[B];
+#pragma unroll
+            for (int b = 0; b < B; ++b) acc[b] = 0;
+            std::uint32_t const base = w * 32u;
+            std::uint32_t const valid = n > base ? min(32u, n - base) : 0u;
+            for (std::uint32_t k = 0; k < valid; ++k) {
+                std::uint32_t const c = pattern[base + k];
+#pragma unroll
+                for (int b = 0; b < B; ++b) acc[b] |= ((c >> b) & 1u) << k;
+            }
+#pragma unroll
+            for (int b = 0; b < B; ++b) state.planes[b][w] = acc[b];
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) state.pv[w] = 0xFFFFFFFFu, state.mv[w] = 0u;
+        state.last_bit = (n - 1) & 31u;
+        state.last_word = exact_ ? W - 1 : int((n - 1) / 32u);
+        state.score = (std::int32_t)n;
+        code16_stream_t text;
+        text.open_at(task.cols);
+        for (std::uint32_t j = 0; j < m; ++j) {
+            std::uint32_t select[B];
+            code_selectors<B>(text.next(), select);
+            state.step(select);
+        }
+        results[task.slot] = (std::uint32_t)state.score;
+    }
+}
+
 } // namespace szs_gb300

@@ -20,10 +20,11 @@
 
 namespace szs_gb300 {
 
-/** The distance of one pair, computed by the whole warp; every lane returns it. */
-template <int words_, int bits_>
+/** The distance of one pair, computed by the whole warp; every lane returns it. `wide_`: strings of 16-bit codes
+ *  (their own codes, selectors from the code's bits), else bytes mapped through the batch alphabet. */
+template <int words_, int bits_, bool wide_ = false>
 __device__ __forceinline__ std::uint32_t myers_warp_distance(pair_task_t const &task, std::uint8_t const *code,
-                                                             plane_selectors_t<bits_> const &selectors) {
+                                                             plane_selectors_t<bits_> const *selectors) {
     constexpr int W = words_, B = bits_;
     int const lane = threadIdx.x & 31;
     std::uint32_t const n = task.rows_length, m = task.cols_length;
@@ -40,7 +41,7 @@ __device__ __forceinline__ std::uint32_t myers_warp_distance(pair_task_t const &
         std::uint32_t const base = lane_base + 32u * w;
         std::uint32_t const valid = n > base ? min(32u, n - base) : 0u;
         for (std::uint32_t k = 0; k < valid; ++k) {
-            std::uint32_t const c = code[task.rows[base + k]];
+            std::uint32_t const c = wide_ ? symbol_at<true>(task.rows, base + k) : code[task.rows[base + k]];
 #pragma unroll
             for (int b = 0; b < B; ++b) acc[b] |= ((c >> b) & 1u) << k;
         }
@@ -57,20 +58,23 @@ __device__ __forceinline__ std::uint32_t myers_warp_distance(pair_task_t const &
     std::uint32_t const score_bit = last_row & 31u;
     std::int32_t score = (std::int32_t)n;
 
-    std::uint32_t out = 0;   // to lane + 1: byte | carry << 8 | top Ph bit << 9 | top Mh bit << 10
-    std::uint32_t chunk = 0; // the text byte of column (t & ~31) + lane
+    std::uint32_t out = 0;   // to lane + 1: symbol | carry << 16 | top Ph bit << 17 | top Mh bit << 18
+    std::uint32_t chunk = 0; // the text symbol of column (t & ~31) + lane
     std::uint32_t const steps = m + (std::uint32_t)lanes_used - 1;
     for (std::uint32_t t = 0; t < steps; ++t) {
-        if ((t & 31u) == 0) chunk = t + lane < m ? (std::uint32_t)task.cols[t + lane] : 0u;
+        if ((t & 31u) == 0) chunk = t + lane < m ? symbol_at<wide_>(task.cols, t + lane) : 0u;
         std::uint32_t const staged = __shfl_sync(0xFFFFFFFFu, chunk, int(t & 31u));
         std::uint32_t in = __shfl_up_sync(0xFFFFFFFFu, out, 1);
-        if (lane == 0) in = staged | (1u << 9); // no carry into row 0; +1 shifted into its horizontal delta
+        if (lane == 0) in = staged | (1u << 17); // no carry into row 0; +1 shifted into its horizontal delta
         int const j = (int)t - lane;
         if (lane < lanes_used && j >= 0 && j < (int)m) {
-            std::uint32_t const byte = in & 0xFFu;
+            std::uint32_t const byte = in & 0xFFFFu;
             std::uint32_t select[B];
+            if constexpr (wide_) code_selectors<B>(byte, select);
+            else {
 #pragma unroll
-            for (int b = 0; b < B; ++b) select[b] = selectors.select[byte][b];
+                for (int b = 0; b < B; ++b) select[b] = selectors->select[byte][b];
+            }
             std::uint32_t eq[W], xv[W], sum[W];
 #pragma unroll
             for (int w = 0; w < W; ++w) {
@@ -82,13 +86,13 @@ __device__ __forceinline__ std::uint32_t myers_warp_distance(pair_task_t const &
                 sum[w] = e & pv[w];
             }
             // Multi-word (Eq & Pv) + Pv with the carry from the lane below: the carry flag starts as that bit.
-            std::uint32_t const carry_in = (in >> 8) & 1u;
+            std::uint32_t const carry_in = (in >> 16) & 1u;
             std::uint32_t carry_out, scratch;
             asm volatile("add.cc.u32 %0, %1, 0xFFFFFFFF;" : "=r"(scratch) : "r"(carry_in));
 #pragma unroll
             for (int w = 0; w < W; ++w) asm volatile("addc.cc.u32 %0, %0, %1;" : "+r"(sum[w]) : "r"(pv[w]));
             asm volatile("addc.u32 %0, 0, 0;" : "=r"(carry_out));
-            std::uint32_t ph_prev = ((in >> 9) & 1u) << 31, mh_prev = ((in >> 10) & 1u) << 31;
+            std::uint32_t ph_prev = ((in >> 17) & 1u) << 31, mh_prev = ((in >> 18) & 1u) << 31;
 #pragma unroll
             for (int w = 0; w < W; ++w) {
                 std::uint32_t const xh = (sum[w] ^ pv[w]) | eq[w];
@@ -102,7 +106,7 @@ __device__ __forceinline__ std::uint32_t myers_warp_distance(pair_task_t const &
                 mv[w] = ph_shifted & xv[w];
                 ph_prev = ph, mh_prev = mh;
             }
-            out = byte | carry_out << 8 | (ph_prev >> 31) << 9 | (mh_prev >> 31) << 10;
+            out = byte | carry_out << 16 | (ph_prev >> 31) << 17 | (mh_prev >> 31) << 18;
         }
     }
     return (std::uint32_t)__shfl_sync(0xFFFFFFFFu, score, score_lane);
@@ -134,7 +138,29 @@ __global__ void __launch_bounds__(256) myers_warp_kernel(pair_task_t const *__re
         index = __shfl_sync(0xFFFFFFFFu, index, 0);
         if (index >= count) break;
         pair_task_t const task = tasks[begin + index];
-        std::uint32_t const distance = myers_warp_distance<words_, bits_>(task, code_s, selectors_s);
+        std::uint32_t const distance = myers_warp_distance<words_, bits_>(task, code_s, &selectors_s);
+        if (lane == 0) results[task.slot] = distance;
+    }
+}
+
+/** The same over strings of 16-bit codes (UTF-8 calls over more than 256 code points): 16 planes, no tables. */
+template <int words_>
+__global__ void __launch_bounds__(256) myers_warp_wide_kernel(pair_task_t const *__restrict__ tasks,
+                                                              plan_bins_t *__restrict__ bins,
+                                                              std::int64_t *__restrict__ results) {
+    int const lane = threadIdx.x & 31;
+    int const key_begin = bin_myers_warp_begin_k + (myers_warp_max_words_k - words_) * myers_warp_classes_k;
+    int const key_end = key_begin + myers_warp_classes_k;
+    std::uint32_t const begin = bins->begin[key_begin];
+    std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
+    while (true) {
+        std::uint32_t index = 0;
+        if (lane == 0) index = atomicAdd(&bins->cursor[key_begin], 1u);
+        index = __shfl_sync(0xFFFFFFFFu, index, 0);
+        if (index >= count) break;
+        pair_task_t const task = tasks[begin + index];
+        std::uint32_t const distance = myers_warp_distance<words_, myers_wide_planes_k, true>(
+            task, nullptr, static_cast<plane_selectors_t<myers_wide_planes_k> const *>(nullptr));
         if (lane == 0) results[task.slot] = distance;
     }
 }

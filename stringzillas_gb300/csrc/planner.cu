@@ -10,7 +10,7 @@
 namespace szs_gb300 {
 
 __device__ __forceinline__ void tape_string(tape_t const &tape, std::uint64_t index, std::uint8_t const *&start,
-                                            std::uint64_t &length) {
+                                            std::uint64_t &length, int wide) {
     std::uint64_t begin, end;
     if (tape.offset_bits == 32) {
         auto const *offsets = static_cast<std::uint32_t const *>(tape.offsets);
@@ -20,7 +20,7 @@ __device__ __forceinline__ void tape_string(tape_t const &tape, std::uint64_t in
         auto const *offsets = static_cast<std::uint64_t const *>(tape.offsets);
         begin = offsets[index], end = offsets[index + 1];
     }
-    start = tape.base + begin;
+    start = tape.base + (wide ? 2 * begin : begin); // 16-bit codes: lengths stay in codes
     length = end - begin;
 }
 
@@ -71,9 +71,10 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     info.transposed = swap ? 1u : 0u;
     if (first_length == 0 || second_length == 0) return info;
     std::uint64_t const n = info.n, m = info.m;
-    if (args.unit_levenshtein && n <= 32u * myers_max_words_k) {
+    int const thread_words = args.wide ? myers_wide_max_words_k : myers_max_words_k;
+    if (args.unit_levenshtein && n <= 32u * thread_words) {
         if (args.force_route >= 0) {
-            info.key = bin_myers_begin_k + myers_max_words_k * 16; // plain form: one bin, one kernel shape
+            info.key = bin_myers_begin_k + thread_words * 16; // plain form: one bin, one kernel shape
             return info;
         }
         int const words = int((n + 31) / 32);
@@ -173,8 +174,8 @@ __device__ __forceinline__ pair_route_info_t route_of_pair(plan_args_t const &ar
     pair_indices(args, p, q, c);
     std::uint8_t const *first, *second;
     std::uint64_t first_length, second_length;
-    tape_string(args.queries, q, first, first_length);
-    tape_string(args.mode == mode_symmetric_k ? args.queries : args.candidates, c, second, second_length);
+    tape_string(args.queries, q, first, first_length, args.wide);
+    tape_string(args.mode == mode_symmetric_k ? args.queries : args.candidates, c, second, second_length, args.wide);
     return route_pair(args, first, first_length, second, second_length);
 }
 

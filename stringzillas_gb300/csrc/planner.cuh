@@ -45,6 +45,7 @@ constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shor
 constexpr int packed_step_cost_k[4] = {100, 165, 245, 330};
 constexpr int band_min_rows_packed_k = 2048; // default for pairs that fit 16-bit cells (the 16-bit band above it)
 constexpr int myers_max_words_k = 16;
+constexpr int myers_wide_max_words_k = 8; // 16-bit codes take 16 code planes: the thread route stops at 8 words
 // Words per lane of the warp kernel: patterns up to 32 * 32 * 8 = 8,192 rows. Longer ones take the bands: a pair of
 // 8-16k characters keeps one warp busy for milliseconds, and a call rarely has enough of them to fill the GPU.
 constexpr int myers_warp_max_words_k = 8;
@@ -81,6 +82,7 @@ struct plan_args_t {
     int local_gain;         // local scores with non-positive gaps: max(0, largest substitution cost); else -1
     int steps_beyond_span;  // 1 linear, 3 affine (serial.hpp:126-140)
     int force_route;        // -1: normal planning; otherwise one bin per route, input order (the plain form)
+    int wide;               // UTF-8 calls over more than 256 code points: the tapes hold 16-bit codes, offsets in codes
     int packed_allowed;     // 1 if the 16x2 route may hold the substitution costs in int8 profiles
     int dense;              // dense-table engine: its profile holds the batch's bytes, at most 32 of them
     batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)

@@ -3,8 +3,9 @@
  *  @brief UTF-8 Levenshtein: code points of both tapes transcoded to one-byte codes on the device.
  *
  *  Edit distances over code points depend only on which code points are equal, so the batch's distinct code points
- *  are numbered 0..k-1 (k <= 256) and every string is rewritten as a byte string of those numbers; the byte-level
- *  Levenshtein routes then score the transcoded tapes unchanged. The reference decodes each string rune by rune
+ *  are numbered 0..k-1 and every string is rewritten as a string of those numbers: bytes when k <= 256 (the byte-level
+ *  Levenshtein routes then score the transcoded tapes unchanged), 16-bit codes up to k = 65,536 (scored by the
+ *  Levenshtein routes' 16-bit-symbol instances). The reference decodes each string rune by rune
  *  (include/stringzillas/similarities/serial.hpp:2288-2299) with `sz_rune_decode_unchecked`
  *  (include/stringzilla/utf8_runes/serial.h:101-115): the length comes from the lead byte alone and continuation
  *  bytes are not checked, so a sequence cut off by the end of a string reads on into the next string of the tape.
@@ -105,14 +106,15 @@ __global__ void utf8_codes_kernel(rune_set_t *__restrict__ set) {
     if (t == threads - 1) set->symbols = scan[t];
 }
 
-/** Pass 3: each string's codes at its scanned offset. */
+/** Pass 3: each string's codes at its scanned offset (one byte each, or two for more than 256 code points). */
+template <typename code_type_>
 __global__ void utf8_write_kernel(tape_t const tape, std::uint64_t const end, std::uint64_t const *__restrict__ offsets,
-                                  rune_set_t const *__restrict__ set, std::uint8_t *__restrict__ out) {
+                                  rune_set_t const *__restrict__ set, code_type_ *__restrict__ out) {
     for (std::uint64_t i = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tape.count;
          i += (std::uint64_t)gridDim.x * blockDim.x) {
         std::uint64_t position = tape_offset(tape, i);
         std::uint64_t const stop = tape_offset(tape, i + 1);
-        std::uint8_t *target = out + offsets[i];
+        code_type_ *target = out + offsets[i];
         std::uint32_t previous = 0xFFFFFFFFu, previous_code = 0;
         while (position < stop) {
             std::uint32_t length;
@@ -125,7 +127,7 @@ __global__ void utf8_write_kernel(tape_t const tape, std::uint64_t const end, st
                     slot = (slot + 1) & (rune_set_slots_k - 1);
                 previous = rune, previous_code = set->codes[slot];
             }
-            *target++ = (std::uint8_t)previous_code;
+            *target++ = (code_type_)previous_code;
         }
     }
 }
@@ -159,11 +161,12 @@ cudaError_t launch_utf8_scan(std::uint64_t const *counts, std::uint64_t *offsets
 }
 
 cudaError_t launch_utf8_write(tape_t const &tape, std::uint64_t end, std::uint64_t const *offsets,
-                              rune_set_t const *set, std::uint8_t *out, int sm_count, cudaStream_t stream) {
+                              rune_set_t const *set, void *out, bool wide, int sm_count, cudaStream_t stream) {
     if (!tape.count) return cudaSuccess;
     std::uint64_t const blocks = (tape.count + 255) / 256;
     int const grid = (int)(blocks < (std::uint64_t)sm_count * 8 ? blocks : (std::uint64_t)sm_count * 8);
-    utf8_write_kernel<<<grid, 256, 0, stream>>>(tape, end, offsets, set, out);
+    if (wide) utf8_write_kernel<<<grid, 256, 0, stream>>>(tape, end, offsets, set, static_cast<std::uint16_t *>(out));
+    else utf8_write_kernel<<<grid, 256, 0, stream>>>(tape, end, offsets, set, static_cast<std::uint8_t *>(out));
     return cudaGetLastError();
 }
 

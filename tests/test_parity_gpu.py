@@ -602,8 +602,8 @@ def test_engine_matches_reference_outputs(szs, name):
 
 @pytest.mark.parametrize("costs", [(0, 1, 1, 1), (0, 3, 2, 2), (0, 4, 5, 2), (1, 3, 4, 1)])
 def test_utf8_levenshtein_routes(szs, port, costs):
-    """Code-point distances across the routes: short and long pairs, up to 256 distinct code points, and more
-    refused."""
+    """Code-point distances across the routes: short and long pairs, up to 256 distinct code points (one-byte
+    codes)."""
     rng = np.random.default_rng(sum(costs) + 1)
     letters = [chr(c) for c in range(0x3041, 0x3041 + 80)] + [chr(c) for c in range(0x1F600, 0x1F600 + 60)] + \
         list("abcdefghij") + [chr(c) for c in range(0x400, 0x400 + 100)]
@@ -620,6 +620,28 @@ def test_utf8_levenshtein_routes(szs, port, costs):
     cross = engine(szs.Strs(first[:12]), szs.Strs(second[:9]))
     np.testing.assert_array_equal(cross.astype(np.int64), port.cross(oracle.levenshtein_utf8_costs(*costs),
                                                                      tape(first[:12]), tape(second[:9])))
-    too_many = ["".join(chr(0x4E00 + i) for i in range(300))]
-    with pytest.raises(ValueError):
-        engine(szs.Strs(too_many), szs.Strs(too_many))
+
+
+@pytest.mark.parametrize("costs", [(0, 1, 1, 1), (0, 2, 3, 1), (1, 3, 2, 2)])
+def test_utf8_levenshtein_over_many_code_points(szs, port, costs):
+    """More than 256 distinct code points: 16-bit codes on every route (thread and warp bit-parallel kernels with 16
+    code planes, 32-bit wavefront and band), short and long pairs, both orientations and a cross product."""
+    rng = np.random.default_rng(sum(costs) + 7)
+    letters = [chr(c) for c in range(0x4E00, 0x4E00 + 3000)] + list("abcdefghij")
+    lengths = [(int(rng.integers(0, 300)), int(rng.integers(0, 300))) for _ in range(150)]
+    lengths += [(255, 400), (256, 256), (257, 300), (700, 900), (1500, 1600), (3000, 2600), (9000, 9100)]
+    first = ["".join(rng.choice(letters, size=n)) for n, _ in lengths]
+    second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
+    second[-2] = first[-2][:2000] + second[-2][2000:]  # related: small distances on long pairs
+    second[-1] = first[-1][:8000] + second[-1][8000:]
+    first[-4], second[-4] = second[-4], first[-4]
+    engine = szs.LevenshteinDistancesUTF8(*costs)
+    want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, want)
+    engine.set_schedule("batched")
+    cross = engine(szs.Strs(first[:12]), szs.Strs(second[:9]))
+    np.testing.assert_array_equal(cross.astype(np.int64), port.cross(oracle.levenshtein_utf8_costs(*costs),
+                                                                     tape(first[:12]), tape(second[:9])))
