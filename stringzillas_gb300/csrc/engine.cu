@@ -1160,7 +1160,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     stats.last_compute_ms = compute;
     if (tracing) {
         static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits",
-                                            "band16 bits"};
+                                            "band16 bits", "warp bit-parallel"};
+        static_assert(sizeof(names) / sizeof(names[0]) == job_myers_warp_k + 1, "a name per job kind");
         for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
             float ms = 0, offset = 0;
             cudaEventElapsedTime(&ms, context->trace_events[2 * i], context->trace_events[2 * i + 1]);
