@@ -36,7 +36,9 @@
 
 namespace szs_gb300 {
 
-template <int kind_, bool affine_, int rows_per_lane_>
+/** `compare_`: Levenshtein over more than 32 byte values. No profile: every row keeps both pairs' row codes and a
+ *  cell's substitution cost is selected by comparing them with the column's codes. */
+template <int kind_, bool affine_, int rows_per_lane_, bool compare_ = false>
 struct dp16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -44,12 +46,14 @@ struct dp16_policy_t {
     static constexpr bool local_k = kind_ == kind_smith_waterman_k;
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
+    static constexpr bool compare_k = compare_;
+    static_assert(!compare_ || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
 };
 
-/** Per-warp shared profile bytes: two pairs x classes x strip rows, plus lane 0's column staging area. */
+/** Per-warp shared profile bytes: two pairs x classes x strip rows (none in compare mode). */
 template <typename policy_>
 __host__ __device__ constexpr int dp16_profile_bytes_per_warp(int classes) {
-    return 2 * classes * policy_::strip_rows_k;
+    return policy_::compare_k ? 0 : 2 * classes * policy_::strip_rows_k;
 }
 
 constexpr int dp16_chunk_bytes_k = 3 * 64 * 4;
@@ -122,6 +126,18 @@ __device__ __forceinline__ void load_profile_words(std::int8_t const *source, st
     }
 }
 
+/** Packed substitution costs of one row in compare mode: `row_codes` and `column_codes` hold pair A's code in the low
+ *  half and pair B's in the high half (codes below 256). A half of `row_codes ^ column_codes` is 0 exactly when the
+ *  codes are equal; adding 0x7FFF sets its top bit otherwise (and cannot carry out of the half), a byte permute with
+ *  sign replication widens that bit to a half mask, and one logic operation selects `mismatch` or `match` by it. */
+__device__ __forceinline__ std::uint32_t compare_costs(std::uint32_t row_codes, std::uint32_t column_codes,
+                                                       std::uint32_t match2, std::uint32_t mismatch2) {
+    std::uint32_t const differs = (row_codes ^ column_codes) + 0x7FFF7FFFu;
+    std::uint32_t mask;
+    asm("prmt.b32 %0, %1, 0, 0xBB99;" : "=r"(mask) : "r"(differs)); // bytes 1, 1, 3, 3 with their signs replicated
+    return (mask & mismatch2) | (~mask & match2);
+}
+
 /** Per-warp staging area for lane 0: top-boundary H (Ĥ for affine tracks) and F, and packed column codes, of the
  *  next 64 columns. */
 struct column_chunk_t {
@@ -153,8 +169,9 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
     constexpr int S = policy_::strip_rows_k;
     constexpr bool affine = policy_::affine_k;
     constexpr bool local = policy_::local_k;
+    constexpr bool compare = policy_::compare_k;
     static_assert(R % 4 == 0, "profile rows are read in 4-byte words");
-    constexpr int words = R / 4;
+    constexpr int words = compare ? 1 : R / 4; // profile words per pair (unused in compare mode)
 
     int const lane = threadIdx.x & 31;
     std::uint32_t const n_a = a.rows_length, m_a = a.cols_length;
@@ -179,11 +196,15 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
     auto gap_seed = [&](std::int64_t i) -> std::int32_t {
         return local ? open + extend : open + extend + edge.score(i);
     };
-    auto column_code = [&](std::uint32_t j) -> std::uint32_t { // packed codes of column j (1-based) of both pairs
+    // Packed codes of column j (1-based) of both pairs: 8-bit halves for profile lookups, 16-bit in compare mode.
+    auto column_code = [&](std::uint32_t j) -> std::uint32_t {
         std::uint32_t const ca = j <= m_a ? costs.byte_to_compact[a.cols[j - 1]] : 0u;
         std::uint32_t const cb = j <= m_b ? costs.byte_to_compact[cols_b[j - 1]] : 0u;
-        return ca | (cb << 8);
+        return ca | (cb << (compare ? 16 : 8));
     };
+    // Compare mode: costs of equal and different codes in both halves (shifted like the profile for affine tracks).
+    std::uint32_t const match2 = pack16(costs.match - (affine ? open : 0), costs.match - (affine ? open : 0));
+    std::uint32_t const mismatch2 = pack16(costs.mismatch - (affine ? open : 0), costs.mismatch - (affine ? open : 0));
 
     std::int32_t result_a = 0, result_b = 0;
     std::uint32_t lane_best = 0; // packed running maxima of valid cells (local scores), starts at 0 like the reference
@@ -194,17 +215,21 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
         int const last_lane = int((rows_here - 1) / R);
         std::int64_t const row0 = (std::int64_t)strip_base + lane * R + 1;
 
-        // Profiles of both pairs for this strip: profile[cc * S + row] = cost(row class, column class cc).
+        // Profiles of both pairs for this strip: profile[cc * S + row] = cost(row class, column class cc); in compare
+        // mode, the rows' packed codes instead.
+        std::uint32_t row_codes[compare ? R : 1];
         __syncwarp();
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             std::int64_t const i = row0 + r;
             int const class_a = costs.byte_to_class[i <= (std::int64_t)n_a ? a.rows[i - 1] : 0u];
             int const class_b = costs.byte_to_class[i <= (std::int64_t)n_b ? b.rows[i - 1] : 0u];
-            for (int cc = 0; cc < classes; ++cc) {
-                profile_a[cc * S + lane * R + r] = std::int8_t(table_a[cc * 32 + class_a] - h_shift);
-                profile_b[cc * S + lane * R + r] = std::int8_t(table_b[cc * 32 + class_b] - h_shift);
-            }
+            if constexpr (compare) row_codes[r] = std::uint32_t(class_a) | (std::uint32_t(class_b) << 16);
+            else
+                for (int cc = 0; cc < classes; ++cc) {
+                    profile_a[cc * S + lane * R + r] = std::int8_t(table_a[cc * 32 + class_a] - h_shift);
+                    profile_b[cc * S + lane * R + r] = std::int8_t(table_b[cc * 32 + class_b] - h_shift);
+                }
         }
 
         std::uint32_t h_col[R], e_col[R], best_row[R];
@@ -233,8 +258,10 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
         std::uint32_t pa_now[words], pb_now[words];
-        load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
-        load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
+        if constexpr (!compare) {
+            load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
+            load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
+        }
         int const lane_rows = lane * R;
 
         // One step of the sweep. `steady` steps are those where every lane is on a real column below both pairs'
@@ -271,8 +298,10 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
             std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
             if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
             std::uint32_t pa_next[words], pb_next[words];
-            load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane_rows, pa_next);
-            load_profile_words<R>(profile_b + (code_next >> 8) * S + lane_rows, pb_next);
+            if constexpr (!compare) {
+                load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane_rows, pa_next);
+                load_profile_words<R>(profile_b + (code_next >> 8) * S + lane_rows, pb_next);
+            }
 
             int const j = (int)t + 1 - lane;
             bool const active = steady || (j >= 1 && j <= (int)m_max && lane <= last_lane);
@@ -281,12 +310,18 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                 diag_up = up_h;
                 std::uint32_t h_up = up_h, f_up = up_f;
                 std::uint32_t subs[R], cell_h[R];
+                if constexpr (compare) {
 #pragma unroll
-                for (int w = 0; w < words; ++w) {
-                    subs[4 * w + 0] = interleave_signed_bytes<0>(pa_now[w], pb_now[w]);
-                    subs[4 * w + 1] = interleave_signed_bytes<1>(pa_now[w], pb_now[w]);
-                    subs[4 * w + 2] = interleave_signed_bytes<2>(pa_now[w], pb_now[w]);
-                    subs[4 * w + 3] = interleave_signed_bytes<3>(pa_now[w], pb_now[w]);
+                    for (int r = 0; r < R; ++r) subs[r] = compare_costs(row_codes[r], code_now, match2, mismatch2);
+                }
+                else {
+#pragma unroll
+                    for (int w = 0; w < words; ++w) {
+                        subs[4 * w + 0] = interleave_signed_bytes<0>(pa_now[w], pb_now[w]);
+                        subs[4 * w + 1] = interleave_signed_bytes<1>(pa_now[w], pb_now[w]);
+                        subs[4 * w + 2] = interleave_signed_bytes<2>(pa_now[w], pb_now[w]);
+                        subs[4 * w + 3] = interleave_signed_bytes<3>(pa_now[w], pb_now[w]);
+                    }
                 }
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
@@ -342,8 +377,10 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                 if (bottom_writer) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
             }
             code_now = code_next;
+            if constexpr (!compare) {
 #pragma unroll
-            for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
+                for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
+            }
         };
 
         std::uint32_t const fill_end = min(steps, 31u);

@@ -861,12 +861,15 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     }
     score_costs_t const &call_costs = dense ? dense_costs : costs;
 
-    // 16x2 routes (packed wavefront, 16-bit band): Levenshtein engines score over the batch alphabet's codes.
+    // 16x2 routes (packed wavefront, 16-bit band): Levenshtein engines score over the batch alphabet's codes, with a
+    // profile over at most 32 of them, else by comparing the codes (the wavefront's compare mode; the plan keeps such
+    // batches off the 16-bit band).
     score_costs_t packed_costs = call_costs;
+    bool const packed_compare = levenshtein && !wide && alphabet_host.symbols > 32;
     if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
                         pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k))) {
         int const symbols = (int)alphabet_host.symbols;
-        packed_costs.classes = symbols;
+        packed_costs.classes = packed_compare ? 1 : symbols;
         for (int b = 0; b < 256; ++b)
             packed_costs.byte_to_class[b] = packed_costs.byte_to_compact[b] = alphabet_host.code[b];
         for (int cc = 0; cc < 32; ++cc)
@@ -979,7 +982,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         if (!pairs_here) continue;
         int const rows = 4 * (choice + 1);
         int const warps = engine.tuning.packed_warps[choice] ? (int)engine.tuning.packed_warps[choice] : 4;
-        dp_launch_shape_t const shape = dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps);
+        dp_launch_shape_t const shape =
+            dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps, packed_compare);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
         std::uint64_t const warps_needed = (pairs_here + 1) / 2;
         std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
@@ -1040,7 +1044,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         key_append(launch_key, context->scratch.data), key_append(launch_key, alphabet);
         key_append(launch_key, cells_per_warp), key_append(launch_key, myers_planes), key_append(launch_key, wide);
         key_append(launch_key, schedule), key_append(launch_key, lanes_used);
-        key_append(launch_key, engine.kind);
+        key_append(launch_key, engine.kind), key_append(launch_key, packed_compare);
     }
     auto issue_jobs = [&](cudaStream_t s) -> status_t {
         SZS_TRY_CUDA(cudaEventRecord(context->fork, s));
@@ -1071,7 +1075,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             else if (job.kind == job_dp16_k)
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
-                                         lane_stream));
+                                         lane_stream, packed_compare));
             else if (job.kind == job_myers_warp_k && wide)
                 SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, results, job.ctas, lane_stream));
             else if (job.kind == job_myers_warp_k)

@@ -9,9 +9,9 @@ namespace szs_gb300 {
 
 namespace {
 
-template <int kind_, bool affine_, int rows_>
+template <int kind_, bool affine_, int rows_, bool compare_>
 dp_launch_shape_t dp16_shape_rows(int classes, int warps) {
-    using policy_t = dp16_policy_t<kind_, affine_, rows_>;
+    using policy_t = dp16_policy_t<kind_, affine_, rows_, compare_>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = warps * 32;
     shape.warps_per_cta = warps;
@@ -27,22 +27,22 @@ dp_launch_shape_t dp16_shape_rows(int classes, int warps) {
     return shape;
 }
 
-template <int kind_, bool affine_>
+template <int kind_, bool affine_, bool compare_ = false>
 dp_launch_shape_t dp16_shape_of(int rows, int classes, int warps) {
     switch (rows) {
-    case 4: return dp16_shape_rows<kind_, affine_, 4>(classes, warps);
-    case 8: return dp16_shape_rows<kind_, affine_, 8>(classes, warps);
-    case 12: return dp16_shape_rows<kind_, affine_, 12>(classes, warps);
-    case 16: return dp16_shape_rows<kind_, affine_, 16>(classes, warps);
+    case 4: return dp16_shape_rows<kind_, affine_, 4, compare_>(classes, warps);
+    case 8: return dp16_shape_rows<kind_, affine_, 8, compare_>(classes, warps);
+    case 12: return dp16_shape_rows<kind_, affine_, 12, compare_>(classes, warps);
+    case 16: return dp16_shape_rows<kind_, affine_, 16, compare_>(classes, warps);
     default: return dp_launch_shape_t {0, 0, 0, 0, 0};
     }
 }
 
-template <int kind_, bool affine_, int rows_>
+template <int kind_, bool affine_, int rows_, bool compare_>
 cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
                              std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
-    using policy_t = dp16_policy_t<kind_, affine_, rows_>;
+    using policy_t = dp16_policy_t<kind_, affine_, rows_, compare_>;
     int const shared = dp16_shared_bytes<policy_t>(warps, costs.classes);
     auto kernel = dp16_wavefront_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
@@ -52,15 +52,15 @@ cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *task
     return cudaGetLastError();
 }
 
-template <int kind_, bool affine_>
+template <int kind_, bool affine_, bool compare_ = false>
 cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                            score_costs_t const &costs, std::int64_t *results, void *scratch,
                            std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
     switch (rows) {
-    case 4: return dp16_launch_rows<kind_, affine_, 4>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
-    case 8: return dp16_launch_rows<kind_, affine_, 8>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
-    case 12: return dp16_launch_rows<kind_, affine_, 12>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
-    case 16: return dp16_launch_rows<kind_, affine_, 16>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 4: return dp16_launch_rows<kind_, affine_, 4, compare_>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 8: return dp16_launch_rows<kind_, affine_, 8, compare_>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 12: return dp16_launch_rows<kind_, affine_, 12, compare_>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
+    case 16: return dp16_launch_rows<kind_, affine_, 16, compare_>(key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp, ctas, warps, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -78,16 +78,30 @@ cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t con
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps) {
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps, bool compare) {
     if (warps < 1 || warps > 8) return dp_launch_shape_t {0, 0, 0, 0, 0};
+    if (compare) {
+        if (kind != kind_levenshtein_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
+        return affine ? dp16_shape_of<kind_levenshtein_k, true, true>(rows, classes, warps)
+                      : dp16_shape_of<kind_levenshtein_k, false, true>(rows, classes, warps);
+    }
     SZS_DP16_DISPATCH(dp16_shape_of, rows, classes, warps)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
 cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
+                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream, bool compare) {
     if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
+    if (compare) {
+        if (kind != kind_levenshtein_k) return cudaErrorInvalidValue;
+        return affine ? dp16_launch_of<kind_levenshtein_k, true, true>(rows, key_begin, key_end, tasks, bins, costs,
+                                                                      results, scratch, scratch_cells_per_warp, ctas,
+                                                                      warps, stream)
+                      : dp16_launch_of<kind_levenshtein_k, false, true>(rows, key_begin, key_end, tasks, bins, costs,
+                                                                       results, scratch, scratch_cells_per_warp, ctas,
+                                                                       warps, stream);
+    }
     SZS_DP16_DISPATCH(dp16_launch_of, rows, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
                       ctas, warps, stream)
     return cudaErrorInvalidValue;

@@ -83,14 +83,16 @@ cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int k
                       std::size_t scratch_cells_per_warp, int ctas, cudaStream_t stream, bool wide = false);
 
 /** Launch shape of the 16x2 packed wavefront kernel with `rows` (4, 8, 12, 16) rows per lane and `warps` (1..8)
- *  warps per CTA; ctas_per_sm = 0 if unsupported. */
-dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps);
+ *  warps per CTA; ctas_per_sm = 0 if unsupported. `compare`: the Levenshtein instance that compares codes instead of
+ *  reading a profile (batches over more than 32 byte values). */
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps, bool compare = false);
 
 /** Runs the 16x2 packed wavefront kernel over bins [key_begin, key_end): two scheduled pairs per warp. `scratch`
  *  holds `ctas * warps_per_cta` rows of `scratch_cells_per_warp` 32-bit words. */
 cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream);
+                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream,
+                        bool compare = false);
 
 /** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells); `direct`: the
  *  direct-table instance. */

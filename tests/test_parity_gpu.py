@@ -266,8 +266,8 @@ def test_needleman_wunsch_is_negative_levenshtein(szs, port):
 
 @pytest.mark.parametrize("symbols", [4, 32, 33, 256])
 def test_levenshtein_dp_over_alphabets(szs, port, symbols):
-    """Non-unit Levenshtein takes the 16x2 route over the batch alphabet when it has at most 32 symbols, the 32-bit
-    byte-comparing route otherwise."""
+    """Non-unit Levenshtein takes the 16x2 route over the batch alphabet: with a profile when it has at most 32
+    symbols, comparing codes otherwise."""
     rng = np.random.default_rng(symbols)
     alphabet = np.arange(256, dtype=np.uint8)[:symbols] if symbols < 256 else np.arange(256, dtype=np.uint8)
     first = random_strings(rng, 101, 0, 700, alphabet)
@@ -276,6 +276,37 @@ def test_levenshtein_dp_over_alphabets(szs, port, symbols):
         engine = szs.LevenshteinDistances(*costs)
         got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
         np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second)))
+
+
+TEXT = np.frombuffer(bytes(range(32, 127)), dtype=np.uint8)
+
+
+@pytest.mark.parametrize("rows", [4, 8, 12, 16])
+@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (1, 3, 4, 1), (0, 127, 100, 100), (3, 1, 5, 5),
+                                   (4, 4, 1, 6)])
+def test_levenshtein_compare_mode(szs, port, rows, costs):
+    """Levenshtein over more than 32 byte values on the 16x2 route selects each cell's cost by comparing the two
+    pairs' codes: every rows-per-lane instance, linear and affine gaps, costs near the byte limit (short pairs) and a
+    match dearer than a mismatch, partners of uneven shapes in one warp, codes 0 and 255 side by side, both
+    schedules."""
+    rng = np.random.default_rng(rows * 1000 + sum(map(abs, costs)))
+    extremes = np.array([0, 1, 127, 128, 254, 255], dtype=np.uint8)
+    first, second = [], []
+    for k in range(61):  # odd: one warp scores a single pair
+        alphabet = TEXT if k % 3 else np.arange(256, dtype=np.uint8)
+        first.append(bytes(rng.choice(alphabet, size=int(rng.integers(0, 700)))))
+        second.append(bytes(rng.choice(alphabet, size=int(rng.integers(0, 700)))))
+    first += [bytes(rng.choice(extremes, size=300)), b"", bytes(rng.choice(TEXT, size=1)), bytes(rng.choice(TEXT, size=650))]
+    second += [bytes(rng.choice(extremes, size=310)), bytes(rng.choice(TEXT, size=500)), bytes(rng.choice(TEXT, size=640)),
+               bytes(rng.choice(TEXT, size=3))]
+    second[5] = first[5][:200] + second[5][200:]  # a long shared stretch
+    engine = szs.LevenshteinDistances(*costs)
+    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 4096, "band_min_rows_packed": 4096})
+    want = port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, want)
 
 
 @pytest.mark.parametrize("family,costs", [("nw", (-11, -1)), ("sw", (-5, -2)), ("nw", (-4, -4)), ("sw", (-3, -3))])
