@@ -28,7 +28,8 @@
 
 namespace szs_gb300 {
 
-template <int kind_, bool affine_, int rows_per_lane_>
+/** `compare_`: Levenshtein over more than 32 byte values, costs selected by comparing codes (see dp_packed.cuh). */
+template <int kind_, bool affine_, int rows_per_lane_, bool compare_ = false>
 struct band16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -37,6 +38,8 @@ struct band16_policy_t {
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_; // rows of one half
     static constexpr int super_rows_k = 2 * strip_rows_k;             // rows of one warp's super-strip
+    static constexpr bool compare_k = compare_;
+    static_assert(!compare_ || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
 };
 
 constexpr int band16_chunk_k = 64; // lane 0's top values and codes are staged, waited for and published 64 at a time
@@ -49,7 +52,7 @@ struct band16_chunk_t {
 
 template <typename policy_>
 __host__ __device__ constexpr int band16_profile_bytes_per_warp(int classes) {
-    return 2 * classes * policy_::strip_rows_k;
+    return policy_::compare_k ? 0 : 2 * classes * policy_::strip_rows_k;
 }
 
 template <typename policy_>
@@ -75,8 +78,9 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
     constexpr bool local = policy_::local_k;
     std::uint32_t const W = (std::uint32_t)sync.members;
     int const warp = sync.member;
+    constexpr bool compare = policy_::compare_k;
     static_assert(R % 4 == 0, "profile rows are read in 4-byte words");
-    constexpr int words = R / 4;
+    constexpr int words = compare ? 1 : R / 4; // profile words per half (unused in compare mode)
 
     int const lane = threadIdx.x & 31;
     int const from_lane = (lane + 31) & 31; // the lane whose previous outputs feed this lane
@@ -93,6 +97,9 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         return local ? open + extend : open + extend + edge.score(i);
     };
     auto column_code = [&](std::uint32_t j) -> std::uint32_t { return costs.byte_to_compact[task.cols[j - 1]]; };
+    // Compare mode: costs of equal and different codes in both halves, shifted like the profile for affine tracks.
+    std::uint32_t const match2 = pack16(costs.match - h_shift, costs.match - h_shift);
+    std::uint32_t const mismatch2 = pack16(costs.mismatch - h_shift, costs.mismatch - h_shift);
 
     std::uint32_t const super_strips = (n + SS - 1) / SS;
     std::int32_t result = 0;
@@ -109,16 +116,19 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         std::uint32_t const *top = ring + (std::size_t)slot_in * ring_words_per_slot;
         std::uint32_t *bottom = ring + (std::size_t)slot_out * ring_words_per_slot;
 
+        std::uint32_t row_codes[compare ? R : 1]; // compare mode: both halves' row codes instead of profiles
         __syncwarp();
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             std::int64_t const i_lo = row0_lo + r, i_hi = row0_hi + r;
             int const class_lo = costs.byte_to_class[i_lo <= (std::int64_t)n ? task.rows[i_lo - 1] : 0u];
             int const class_hi = costs.byte_to_class[i_hi <= (std::int64_t)n ? task.rows[i_hi - 1] : 0u];
-            for (int cc = 0; cc < classes; ++cc) {
-                profile_lo[cc * S + lane_rows + r] = std::int8_t(table[cc * 32 + class_lo] - h_shift);
-                profile_hi[cc * S + lane_rows + r] = std::int8_t(table[cc * 32 + class_hi] - h_shift);
-            }
+            if constexpr (compare) row_codes[r] = std::uint32_t(class_lo) | (std::uint32_t(class_hi) << 16);
+            else
+                for (int cc = 0; cc < classes; ++cc) {
+                    profile_lo[cc * S + lane_rows + r] = std::int8_t(table[cc * 32 + class_lo] - h_shift);
+                    profile_hi[cc * S + lane_rows + r] = std::int8_t(table[cc * 32 + class_hi] - h_shift);
+                }
         }
         std::uint32_t h_col[R], e_col[R], best_row[R];
 #pragma unroll
@@ -140,8 +150,10 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
         std::uint32_t p_lo[words], p_hi[words];
-        load_profile_words<R>(profile_lo + (code_now & 0xFF) * S + lane_rows, p_lo);
-        load_profile_words<R>(profile_hi + ((code_now >> 8) & 0xFF) * S + lane_rows, p_hi);
+        if constexpr (!compare) {
+            load_profile_words<R>(profile_lo + (code_now & 0xFF) * S + lane_rows, p_lo);
+            load_profile_words<R>(profile_hi + ((code_now >> 8) & 0xFF) * S + lane_rows, p_hi);
+        }
         bool healthy = true;
 
         // `steady`: every lane's two columns are real and below m (63 <= t < m - 1): no masks, no capture.
@@ -176,11 +188,15 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                 // Low half: the strip's top row; high half: lane 31's low half (the row just above).
                 up_h = __byte_perm(staged_top, up_h, 0x5410);
                 up_f = __byte_perm(staged_top, up_f, 0x5432);
-                code_next = __byte_perm(staged_code, code_next, 0x1140);
+                // Codes: byte 0 the low half's, the high half's in byte 1 (profiles) or byte 2 (compare mode); the
+                // staged codes are below 256, so their byte 1 is a zero byte.
+                code_next = __byte_perm(staged_code, code_next, compare ? 0x1410 : 0x1140);
             }
             std::uint32_t q_lo[words], q_hi[words];
-            load_profile_words<R>(profile_lo + (code_next & 0xFF) * S + lane_rows, q_lo);
-            load_profile_words<R>(profile_hi + ((code_next >> 8) & 0xFF) * S + lane_rows, q_hi);
+            if constexpr (!compare) {
+                load_profile_words<R>(profile_lo + (code_next & 0xFF) * S + lane_rows, q_lo);
+                load_profile_words<R>(profile_hi + ((code_next >> 8) & 0xFF) * S + lane_rows, q_hi);
+            }
 
             int const j_lo = (int)t + 1 - lane, j_hi = j_lo - 32;
             // Low half past m, high half not yet started: a lane with neither real column skips the update.
@@ -192,12 +208,18 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                 diag_up = steady ? up_h : ((up_h & ~keep) | (diag_up & keep));
                 std::uint32_t h_up = up_h, f_up = up_f;
                 std::uint32_t subs[R], cell_h[R];
+                if constexpr (compare) {
 #pragma unroll
-                for (int w = 0; w < words; ++w) {
-                    subs[4 * w + 0] = interleave_signed_bytes<0>(p_lo[w], p_hi[w]);
-                    subs[4 * w + 1] = interleave_signed_bytes<1>(p_lo[w], p_hi[w]);
-                    subs[4 * w + 2] = interleave_signed_bytes<2>(p_lo[w], p_hi[w]);
-                    subs[4 * w + 3] = interleave_signed_bytes<3>(p_lo[w], p_hi[w]);
+                    for (int r = 0; r < R; ++r) subs[r] = compare_costs(row_codes[r], code_now, match2, mismatch2);
+                }
+                else {
+#pragma unroll
+                    for (int w = 0; w < words; ++w) {
+                        subs[4 * w + 0] = interleave_signed_bytes<0>(p_lo[w], p_hi[w]);
+                        subs[4 * w + 1] = interleave_signed_bytes<1>(p_lo[w], p_hi[w]);
+                        subs[4 * w + 2] = interleave_signed_bytes<2>(p_lo[w], p_hi[w]);
+                        subs[4 * w + 3] = interleave_signed_bytes<3>(p_lo[w], p_hi[w]);
+                    }
                 }
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
@@ -252,8 +274,10 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                     __stcg(bottom + j_hi, __byte_perm(out_h, out_f, 0x7632));
             }
             code_now = code_next;
+            if constexpr (!compare) {
 #pragma unroll
-            for (int w = 0; w < words; ++w) p_lo[w] = q_lo[w], p_hi[w] = q_hi[w];
+                for (int w = 0; w < words; ++w) p_lo[w] = q_lo[w], p_hi[w] = q_hi[w];
+            }
         };
 
         std::uint32_t const fill_end = min(steps, 63u);

@@ -862,8 +862,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     score_costs_t const &call_costs = dense ? dense_costs : costs;
 
     // 16x2 routes (packed wavefront, 16-bit band): Levenshtein engines score over the batch alphabet's codes, with a
-    // profile over at most 32 of them, else by comparing the codes (the wavefront's compare mode; the plan keeps such
-    // batches off the 16-bit band).
+    // profile over at most 32 of them, else by comparing the codes (the kernels' compare mode).
     score_costs_t packed_costs = call_costs;
     bool const packed_compare = levenshtein && !wide && alphabet_host.symbols > 32;
     if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
@@ -921,7 +920,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            dp_launch_shape_t const shape = band16_shape(engine.kind, costs.affine != 0, packed_costs.classes);
+            dp_launch_shape_t const shape =
+                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, packed_compare);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
             band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
@@ -1067,7 +1067,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
-                                           lane_stream, group_states, job.group_ctas));
+                                           lane_stream, group_states, job.group_ctas, packed_compare));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                        bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,

@@ -11,12 +11,12 @@ namespace {
 
 constexpr int band16_rows_per_lane_k = 8;
 
-template <int kind_, bool affine_>
-using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k>;
+template <int kind_, bool affine_, bool compare_ = false>
+using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_>;
 
-template <int kind_, bool affine_>
+template <int kind_, bool affine_, bool compare_ = false>
 dp_launch_shape_t band16_shape_of(int classes) {
-    using policy_t = band16_instance_t<kind_, affine_>;
+    using policy_t = band16_instance_t<kind_, affine_, compare_>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = band_warps_k * 32;
     shape.warps_per_cta = band_warps_k;
@@ -38,12 +38,12 @@ dp_launch_shape_t band16_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_>
+template <int kind_, bool affine_, bool compare_ = false>
 cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
                              std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
                              int group_ctas) {
-    using policy_t = band16_instance_t<kind_, affine_>;
+    using policy_t = band16_instance_t<kind_, affine_, compare_>;
     int const shared = band16_shared_bytes<policy_t>(costs.classes);
     if (group_states) {
         // The CTAs of a group wait on one another: a cooperative launch keeps the whole grid resident.
@@ -81,7 +81,12 @@ cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *task
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes) {
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, bool compare) {
+    if (compare) {
+        if (kind != kind_levenshtein_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
+        return affine ? band16_shape_of<kind_levenshtein_k, true, true>(classes)
+                      : band16_shape_of<kind_levenshtein_k, false, true>(classes);
+    }
     SZS_BAND16_DISPATCH(band16_shape_of, classes)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
@@ -89,7 +94,16 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes) {
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
-                          int group_ctas) {
+                          int group_ctas, bool compare) {
+    if (compare) {
+        if (kind != kind_levenshtein_k) return cudaErrorInvalidValue;
+        return affine ? band16_launch_of<kind_levenshtein_k, true, true>(key_begin, key_end, tasks, bins, costs,
+                                                                        results, scratch, ring_words_per_slot, ctas,
+                                                                        stream, group_states, group_ctas)
+                      : band16_launch_of<kind_levenshtein_k, false, true>(key_begin, key_end, tasks, bins, costs,
+                                                                         results, scratch, ring_words_per_slot, ctas,
+                                                                         stream, group_states, group_ctas);
+    }
     SZS_BAND16_DISPATCH(band16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
                         ring_words_per_slot, ctas, stream, group_states, group_ctas)
     return cudaErrorInvalidValue;

@@ -113,8 +113,9 @@ cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_
 std::size_t band_group_state_bytes();
 int band_group_max_ctas();
 
-/** Launch shape of the 16-bit band kernel (one CTA per long pair, two row strips per warp in 16x2 cells). */
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes);
+/** Launch shape of the 16-bit band kernel (one CTA per long pair, two row strips per warp in 16x2 cells);
+ *  `compare`: the Levenshtein instance that compares codes instead of reading a profile. */
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, bool compare = false);
 
 /** Runs the 16-bit band kernel over bins [key_begin, key_end). `scratch` holds `ctas * band_warps_per_cta()` ring
  *  slots of `ring_words_per_slot` 32-bit words (twice that for local scores, which may rescore a pair on 32-bit
@@ -122,7 +123,7 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes);
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
-                          int group_ctas = 1);
+                          int group_ctas = 1, bool compare = false);
 
 /** Bit-parallel kernels over strings of 16-bit codes (UTF-8 calls over more than 256 code points, 16 code planes):
  *  thread per pair over the bins of `words` words (1..8), and warp per pair over the warp bins (1..8 words per

@@ -107,15 +107,13 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     std::uint64_t const reach16 =
         args.local_gain >= 0 ? (std::uint64_t)args.local_gain * (n < m ? n : m) + 1 : reach;
     // The 16x2 routes hold costs in a 32-class profile: dense-table calls over more bytes than that stay on the
-    // 32-bit routes. Levenshtein calls over more bytes take the 16x2 wavefront in compare mode (codes compared, no
-    // profile), but not the 16-bit band, which has no such mode.
+    // 32-bit routes. Levenshtein calls over more bytes take them in compare mode (codes compared, no profile).
     bool const profile_fits = (args.kind != kind_levenshtein_k && !args.dense) ||
                               (args.alphabet && args.alphabet->symbols <= 32);
     bool const compare_fits = args.kind == kind_levenshtein_k && args.alphabet != nullptr;
     bool const packed = args.packed_allowed && (profile_fits || compare_fits) && reach16 < 32767 &&
                         args.cell_bits[length_class] != 32;
-    bool const packed_band = packed && profile_fits;
-    std::uint64_t const band_rows = packed_band ? args.band_min_rows_packed : args.band_min_rows;
+    std::uint64_t const band_rows = packed ? args.band_min_rows_packed : args.band_min_rows;
     // Local scores with non-positive gaps take the 16-bit band even beyond their proven bound: the kernel checks the
     // running maximum against the 16-bit limit and scores a pair that reached it again on 32-bit cells.
     bool const local_band16 =
@@ -123,7 +121,7 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     if (n > band_rows && fits32_early) {
         // Long pairs take a band in both forms (16-bit cells when they fit); the plain form keeps them in one bin,
         // in input order.
-        int const band_begin = (packed_band || local_band16) ? bin_band16_begin_k : bin_band_begin_k;
+        int const band_begin = (packed || local_band16) ? bin_band16_begin_k : bin_band_begin_k;
         if (args.force_route >= 0) {
             info.key = band_begin;
             return info;

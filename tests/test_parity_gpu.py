@@ -514,6 +514,30 @@ def test_band16_route(szs, port, family, costs):
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
+@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (1, 3, 4, 1), (3, 1, 5, 5)])
+def test_band16_compare_mode(szs, port, costs):
+    """Long Levenshtein pairs over more than 32 byte values take the 16-bit band in compare mode, one CTA per pair
+    and (few pairs) grouped CTAs: shapes around the super-strip size, a long shared stretch, codes 0 and 255."""
+    rng = np.random.default_rng(sum(costs) + 5)
+    lengths = [(601, 601), (700, 1400), (1023, 1024), (1025, 1300), (1400, 1500), (512 * 2 + 3, 1200), (2049, 2100)]
+    first = [bytes(rng.choice(TEXT, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(TEXT, size=m)) for _, m in lengths]
+    second[1] = first[1][:600] + second[1][600:]
+    first[3] = bytes(rng.choice(np.array([0, 255, 65], dtype=np.uint8), size=1025))
+    second[3] = bytes(rng.choice(np.array([0, 255, 66], dtype=np.uint8), size=1300))
+    engine = szs.LevenshteinDistances(*costs)
+    engine.set_tuning({"band_min_rows_packed": 600})
+    want = port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
+    engine.set_schedule("batched")
+    few = [1, 6]  # two long pairs: grouped CTAs
+    sub_first, sub_second = [first[i] for i in few], [second[i] for i in few]
+    np.testing.assert_array_equal(engine.pairwise(szs.Strs(sub_first), szs.Strs(sub_second)).astype(np.int64),
+                                  want[few])
+
+
 def test_band16_local_scores_past_the_16bit_limit(szs, port):
     """Local scores run on 16-bit cells beyond their proven bound; a pair whose maximum reaches 32767 minus the
     largest gain is scored again on 32-bit cells inside the same CTA. Identical long strings score 2 per base."""
