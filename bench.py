@@ -49,8 +49,10 @@ METRIC = "GCUPS batched Levenshtein/NW/SW, 1 GB300, vs plain launch; serving p50
 #  - 16x2 packed cells (the NW / SW configurations run there: warp route and 16-bit band): per register of two
 #    cells, affine 5 DPX (E, diag + s against E, F, max, + open) + 1 byte permute of the two pairs' costs, plus the
 #    running maximum for local scores -> 3.0 (global) / 3.5 (local) per cell.
+#  - 16x2 compare mode (Levenshtein over more than 32 byte values): per register of two cells, linear 3 DPX + 4 ops
+#    selecting the two pairs' costs by code equality -> 3.5 per cell.
 OPS_PER_CELL = {"myers_dna": 13.0 / 32.0, "dp_linear": 4.0, "dp_affine": 7.0, "packed_affine": 3.0,
-                "packed_affine_local": 3.5}
+                "packed_affine_local": 3.5, "packed_compare_linear": 3.5}
 
 WORKLOADS = {
     "c1": "plain Levenshtein: 1,024 DNA pairs, len U[64,256], partner 5% subs + 2% indels, unit costs",
@@ -64,6 +66,8 @@ WORKLOADS = {
                 "[2500, 8000], 70% identity, open -11 extend -1 (the reach bound exceeds int16: 32-bit band)",
     "p_dp32": "profiling case, Needleman-Wunsch affine protein with a wide table: 65,536 pairs, len lognormal(350, 0.6) "
               "in [50, 2000], diagonal 100..120, open -30 extend -2 (costs outside the int8 profile: 32-bit wavefront)",
+    "p_text": "profiling case, Levenshtein on printable text: 262,144 pairs, len U[100,300], 95 byte values, partner "
+              "5% subs + 2% indels, match 0 mismatch 2 open 3 extend 1 (16x2 wavefront in compare mode)",
 }
 
 
@@ -101,6 +105,9 @@ def make_workload(name, seed):
     if name == "p_band32":
         first, second = w.protein_pairs(1024, median=4000.0, sigma=0.3, low=2500, high=8000, seed=seed)
         return first, second, ("nw32", (*w.protein_table(seed=seed), -11, -1))
+    if name == "p_text":
+        first, second = w.text_pairs(262144, 100, 300, 0.05, 0.02, seed=seed)
+        return first, second, ("levc", (0, 2, 3, 1))
     if name == "p_dp32":
         first, second = w.protein_pairs(65536, seed=seed)
         byte_to_class, table = w.protein_table(seed=seed)
@@ -119,6 +126,8 @@ def make_engine(kind_and_tables):
     kind, tables = kind_and_tables
     if kind == "lev":
         engine = szs.LevenshteinDistances()
+    elif kind == "levc":  # Levenshtein with the given (match, mismatch, open, extend)
+        engine = szs.LevenshteinDistances(*tables)
     elif kind == "nw":
         engine = szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
     elif kind == "nw32":  # profiling cases of the 32-bit routes: (byte_to_class, table, open, extend)
@@ -139,6 +148,8 @@ def oracle_costs(kind_and_tables):
     kind, tables = kind_and_tables
     if kind == "lev":
         return oracle.levenshtein_costs()
+    if kind == "levc":
+        return oracle.levenshtein_costs(*tables)
     if kind == "nw":
         return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables, -11, -1)
     if kind == "nw32":
@@ -152,6 +163,8 @@ def ops_per_cell(kind_and_tables):
         return OPS_PER_CELL["myers_dna"]
     if kind == "nw32":
         return OPS_PER_CELL["dp_affine"]
+    if kind == "levc":
+        return OPS_PER_CELL["packed_compare_linear"]
     return OPS_PER_CELL["packed_affine_local"] if kind == "sw" else OPS_PER_CELL["packed_affine"]
 
 
@@ -591,7 +604,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32" if kind_and_tables[0] == "lev" else "int32",
+            "scaling": "weak", "vs_baseline": None, "dtype": {"lev": "u32", "levc": "int16x2"}.get(kind_and_tables[0], "int32"),
             "data": "synthetic (seeded numpy PCG64)",
             "config": {"workload": WORKLOADS[args.workload], "pairs": pairs, "cells_per_step": cells_per_step,
                        "input_bytes_per_step": input_bytes, "tuning": tuning_source(),

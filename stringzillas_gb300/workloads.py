@@ -23,6 +23,7 @@ import numpy as np
 
 DNA = np.frombuffer(b"ACGT", dtype=np.uint8)
 AMINO_ACIDS = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+PRINTABLE = np.arange(32, 127, dtype=np.uint8)  # the 95 printable ASCII bytes
 AMINO_FREQUENCIES = np.array([.074, .052, .045, .054, .025, .034, .054, .074, .026, .068,
                               .099, .058, .025, .047, .039, .057, .051, .013, .032, .073])
 
@@ -75,6 +76,16 @@ def levenshtein_reads(count, low, high, substitution_rate, indel_rate, seed=42):
     offsets = _offsets(lengths)
     first = _letters(rng, DNA, int(offsets[-1]))
     second, second_offsets = _mutate(rng, first, offsets, DNA, substitution_rate, indel_rate)
+    return (first, offsets), (second, second_offsets)
+
+
+def text_pairs(count, low, high, substitution_rate, indel_rate, seed=42):
+    """Printable-text pairs (95 byte values, uniform) for Levenshtein with non-unit costs."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = rng.integers(low, high + 1, size=count)
+    offsets = _offsets(lengths)
+    first = _letters(rng, PRINTABLE, int(offsets[-1]))
+    second, second_offsets = _mutate(rng, first, offsets, PRINTABLE, substitution_rate, indel_rate)
     return (first, offsets), (second, second_offsets)
 
 
