@@ -49,10 +49,10 @@ METRIC = "GCUPS batched Levenshtein/NW/SW, 1 GB300, vs plain launch; serving p50
 #  - 16x2 packed cells (the NW / SW configurations run there: warp route and 16-bit band): per register of two
 #    cells, affine 5 DPX (E, diag + s against E, F, max, + open) + 1 byte permute of the two pairs' costs, plus the
 #    running maximum for local scores -> 3.0 (global) / 3.5 (local) per cell.
-#  - 16x2 compare mode (Levenshtein over more than 32 byte values): per register of two cells, linear 3 DPX + 4 ops
-#    selecting the two pairs' costs by code equality -> 3.5 per cell.
+#  - 16x2 compare mode (Levenshtein over more than 32 byte values): per register of two cells, affine 5 DPX + 1 DPX
+#    add-min (0 where the codes are equal, else 1) + 1 multiply-add giving both pairs' costs -> 3.5 per cell.
 OPS_PER_CELL = {"myers_dna": 13.0 / 32.0, "dp_linear": 4.0, "dp_affine": 7.0, "packed_affine": 3.0,
-                "packed_affine_local": 3.5, "packed_compare_linear": 3.5}
+                "packed_affine_local": 3.5, "packed_compare_affine": 3.5}
 
 WORKLOADS = {
     "c1": "plain Levenshtein: 1,024 DNA pairs, len U[64,256], partner 5% subs + 2% indels, unit costs",
@@ -164,7 +164,7 @@ def ops_per_cell(kind_and_tables):
     if kind == "nw32":
         return OPS_PER_CELL["dp_affine"]
     if kind == "levc":
-        return OPS_PER_CELL["packed_compare_linear"]
+        return OPS_PER_CELL["packed_compare_affine"]
     return OPS_PER_CELL["packed_affine_local"] if kind == "sw" else OPS_PER_CELL["packed_affine"]
 
 

@@ -28,8 +28,8 @@
 
 namespace szs_gb300 {
 
-/** `compare_`: Levenshtein over more than 32 byte values, costs selected by comparing codes (see dp_packed.cuh). */
-template <int kind_, bool affine_, int rows_per_lane_, bool compare_ = false>
+/** `compare_`: Levenshtein over more than 32 byte values, costs from comparing codes (`compare_mode_t`). */
+template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k>
 struct band16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -38,8 +38,9 @@ struct band16_policy_t {
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_; // rows of one half
     static constexpr int super_rows_k = 2 * strip_rows_k;             // rows of one warp's super-strip
-    static constexpr bool compare_k = compare_;
-    static_assert(!compare_ || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
+    static constexpr bool compare_k = compare_ != compare_none_k;
+    static constexpr bool multiply_k = compare_ == compare_multiply_k;
+    static_assert(!compare_k || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
 };
 
 constexpr int band16_chunk_k = 64; // lane 0's top values and codes are staged, waited for and published 64 at a time
@@ -96,10 +97,13 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
     auto gap_seed = [&](std::int64_t i) -> std::int32_t {
         return local ? open + extend : open + extend + edge.score(i);
     };
-    auto column_code = [&](std::uint32_t j) -> std::uint32_t { return costs.byte_to_compact[task.cols[j - 1]]; };
-    // Compare mode: costs of equal and different codes in both halves, shifted like the profile for affine tracks.
-    std::uint32_t const match2 = pack16(costs.match - h_shift, costs.match - h_shift);
-    std::uint32_t const mismatch2 = pack16(costs.mismatch - h_shift, costs.mismatch - h_shift);
+    // The code of column j; in compare mode negated within 16 bits (see compare_costs_t).
+    auto column_code = [&](std::uint32_t j) -> std::uint32_t {
+        std::uint32_t const c = costs.byte_to_compact[task.cols[j - 1]];
+        return compare ? (0u - c) & 0xFFFFu : c;
+    };
+    // Compare mode: costs of equal and different codes, shifted like the profile for affine tracks.
+    compare_costs_t const compared(costs.match - h_shift, costs.mismatch - h_shift);
 
     std::uint32_t const super_strips = (n + SS - 1) / SS;
     std::int32_t result = 0;
@@ -188,9 +192,9 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                 // Low half: the strip's top row; high half: lane 31's low half (the row just above).
                 up_h = __byte_perm(staged_top, up_h, 0x5410);
                 up_f = __byte_perm(staged_top, up_f, 0x5432);
-                // Codes: byte 0 the low half's, the high half's in byte 1 (profiles) or byte 2 (compare mode); the
-                // staged codes are below 256, so their byte 1 is a zero byte.
-                code_next = __byte_perm(staged_code, code_next, compare ? 0x1410 : 0x1140);
+                // Codes: the low half's in byte 0 and the high half's in byte 1 (profiles; the staged codes are below
+                // 256, so their byte 1 is a zero byte), or in bits 0-15 and 16-31 (compare mode).
+                code_next = __byte_perm(staged_code, code_next, compare ? 0x5410 : 0x1140);
             }
             std::uint32_t q_lo[words], q_hi[words];
             if constexpr (!compare) {
@@ -208,10 +212,7 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                 diag_up = steady ? up_h : ((up_h & ~keep) | (diag_up & keep));
                 std::uint32_t h_up = up_h, f_up = up_f;
                 std::uint32_t subs[R], cell_h[R];
-                if constexpr (compare) {
-#pragma unroll
-                    for (int r = 0; r < R; ++r) subs[r] = compare_costs(row_codes[r], code_now, match2, mismatch2);
-                }
+                if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code_now, subs);
                 else {
 #pragma unroll
                     for (int w = 0; w < words; ++w) {

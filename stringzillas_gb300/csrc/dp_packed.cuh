@@ -36,9 +36,9 @@
 
 namespace szs_gb300 {
 
-/** `compare_`: Levenshtein over more than 32 byte values. No profile: every row keeps both pairs' row codes and a
- *  cell's substitution cost is selected by comparing them with the column's codes. */
-template <int kind_, bool affine_, int rows_per_lane_, bool compare_ = false>
+/** `compare_`: a `compare_mode_t` (engine_types.cuh); other than `compare_none_k`, Levenshtein over more than 32 byte
+ *  values with costs from comparing codes instead of profiles. */
+template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k>
 struct dp16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -46,8 +46,9 @@ struct dp16_policy_t {
     static constexpr bool local_k = kind_ == kind_smith_waterman_k;
     static constexpr int rows_per_lane_k = rows_per_lane_;
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
-    static constexpr bool compare_k = compare_;
-    static_assert(!compare_ || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
+    static constexpr bool compare_k = compare_ != compare_none_k;
+    static constexpr bool multiply_k = compare_ == compare_multiply_k;
+    static_assert(!compare_k || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
 };
 
 /** Per-warp shared profile bytes: two pairs x classes x strip rows (none in compare mode). */
@@ -126,17 +127,46 @@ __device__ __forceinline__ void load_profile_words(std::int8_t const *source, st
     }
 }
 
-/** Packed substitution costs of one row in compare mode: `row_codes` and `column_codes` hold pair A's code in the low
- *  half and pair B's in the high half (codes below 256). A half of `row_codes ^ column_codes` is 0 exactly when the
- *  codes are equal; adding 0x7FFF sets its top bit otherwise (and cannot carry out of the half), a byte permute with
- *  sign replication widens that bit to a half mask, and one logic operation selects `mismatch` or `match` by it. */
-__device__ __forceinline__ std::uint32_t compare_costs(std::uint32_t row_codes, std::uint32_t column_codes,
-                                                       std::uint32_t match2, std::uint32_t mismatch2) {
-    std::uint32_t const differs = (row_codes ^ column_codes) + 0x7FFF7FFFu;
-    std::uint32_t mask;
-    asm("prmt.b32 %0, %1, 0, 0xBB99;" : "=r"(mask) : "r"(differs)); // bytes 1, 1, 3, 3 with their signs replicated
-    return (mask & mismatch2) | (~mask & match2);
-}
+/**
+ *  Packed substitution costs in compare mode. Row codes hold pair A's code in the low half and pair B's in the high
+ *  half (codes below 256); column codes travel negated per half (`-c mod 2^16`), so one DPX add-min,
+ *  `min(row + column, 1)` per unsigned half with the add wrapping inside the half, is 0 exactly where the codes are
+ *  equal and 1 where they differ. Then either
+ *
+ *  - `multiply`: one integer multiply-add, `differs * (mismatch - match) + match2`, on the multiply-add pipe. Exact
+ *    when `match` and `mismatch` (as shifted for the call) have the same sign: the low half's value and `match` then
+ *    borrow from the high half alike (both negative) or not at all (both non-negative);
+ *  - or a half mask `differs * 0xFFFF` and one logic operation selecting `mismatch` or `match`.
+ */
+struct compare_costs_t {
+    std::uint32_t match2, mismatch2; // both halves
+    std::uint32_t delta;             // mismatch - match, two's complement
+
+    __device__ __forceinline__ compare_costs_t(std::int32_t match, std::int32_t mismatch)
+        : match2(pack16(match, match)), mismatch2(pack16(mismatch, mismatch)), delta(std::uint32_t(mismatch - match)) {}
+
+    /** Column codes `ca`, `cb` as they travel: negated per half. */
+    __device__ __forceinline__ static std::uint32_t column_codes(std::uint32_t ca, std::uint32_t cb) {
+        return ((0u - ca) & 0xFFFFu) | ((0u - cb) << 16);
+    }
+    /** Costs of R rows against one column. */
+    template <bool multiply_, int rows_>
+    __device__ __forceinline__ void rows(std::uint32_t const (&row_codes)[rows_], std::uint32_t negated_column_codes,
+                                         std::uint32_t (&out)[rows_]) const {
+        if constexpr (multiply_) {
+#pragma unroll
+            for (int r = 0; r < rows_; ++r)
+                out[r] = __viaddmin_u16x2(row_codes[r], negated_column_codes, 0x00010001u) * delta + match2;
+        }
+        else {
+#pragma unroll
+            for (int r = 0; r < rows_; ++r) {
+                std::uint32_t const mask = __viaddmin_u16x2(row_codes[r], negated_column_codes, 0x00010001u) * 0xFFFFu;
+                out[r] = (mask & mismatch2) | (~mask & match2);
+            }
+        }
+    }
+};
 
 /** Per-warp staging area for lane 0: top-boundary H (Ĥ for affine tracks) and F, and packed column codes, of the
  *  next 64 columns. */
@@ -196,15 +226,15 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
     auto gap_seed = [&](std::int64_t i) -> std::int32_t {
         return local ? open + extend : open + extend + edge.score(i);
     };
-    // Packed codes of column j (1-based) of both pairs: 8-bit halves for profile lookups, 16-bit in compare mode.
+    // Packed codes of column j (1-based) of both pairs: 8-bit halves for profile lookups, negated 16-bit halves in
+    // compare mode.
     auto column_code = [&](std::uint32_t j) -> std::uint32_t {
         std::uint32_t const ca = j <= m_a ? costs.byte_to_compact[a.cols[j - 1]] : 0u;
         std::uint32_t const cb = j <= m_b ? costs.byte_to_compact[cols_b[j - 1]] : 0u;
-        return ca | (cb << (compare ? 16 : 8));
+        return compare ? compare_costs_t::column_codes(ca, cb) : ca | (cb << 8);
     };
-    // Compare mode: costs of equal and different codes in both halves (shifted like the profile for affine tracks).
-    std::uint32_t const match2 = pack16(costs.match - (affine ? open : 0), costs.match - (affine ? open : 0));
-    std::uint32_t const mismatch2 = pack16(costs.mismatch - (affine ? open : 0), costs.mismatch - (affine ? open : 0));
+    // Compare mode: costs of equal and different codes (shifted like the profile for affine tracks).
+    compare_costs_t const compared(costs.match - (affine ? open : 0), costs.mismatch - (affine ? open : 0));
 
     std::int32_t result_a = 0, result_b = 0;
     std::uint32_t lane_best = 0; // packed running maxima of valid cells (local scores), starts at 0 like the reference
@@ -310,10 +340,7 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
                 diag_up = up_h;
                 std::uint32_t h_up = up_h, f_up = up_f;
                 std::uint32_t subs[R], cell_h[R];
-                if constexpr (compare) {
-#pragma unroll
-                    for (int r = 0; r < R; ++r) subs[r] = compare_costs(row_codes[r], code_now, match2, mismatch2);
-                }
+                if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code_now, subs);
                 else {
 #pragma unroll
                     for (int w = 0; w < words; ++w) {

@@ -865,6 +865,11 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     // profile over at most 32 of them, else by comparing the codes (the kernels' compare mode).
     score_costs_t packed_costs = call_costs;
     bool const packed_compare = levenshtein && !wide && alphabet_host.symbols > 32;
+    // Compare mode's form: one multiply-add per row when match and mismatch, as the kernels shift them (minus `open`
+    // for affine tracks), have the same sign, else a mask and a select.
+    int const shift = costs.affine ? costs.open : 0;
+    int const compare_mode =
+        packed_compare ? compare_mode_for(costs.match - shift, costs.mismatch - shift) : (int)compare_none_k;
     if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
                         pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k))) {
         int const symbols = (int)alphabet_host.symbols;
@@ -921,7 +926,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
         if (pairs_here) {
             dp_launch_shape_t const shape =
-                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, packed_compare);
+                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
             band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
@@ -983,7 +988,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int const rows = 4 * (choice + 1);
         int const warps = engine.tuning.packed_warps[choice] ? (int)engine.tuning.packed_warps[choice] : 4;
         dp_launch_shape_t const shape =
-            dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps, packed_compare);
+            dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps, compare_mode);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
         std::uint64_t const warps_needed = (pairs_here + 1) / 2;
         std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
@@ -1044,7 +1049,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         key_append(launch_key, context->scratch.data), key_append(launch_key, alphabet);
         key_append(launch_key, cells_per_warp), key_append(launch_key, myers_planes), key_append(launch_key, wide);
         key_append(launch_key, schedule), key_append(launch_key, lanes_used);
-        key_append(launch_key, engine.kind), key_append(launch_key, packed_compare);
+        key_append(launch_key, engine.kind), key_append(launch_key, compare_mode);
     }
     auto issue_jobs = [&](cudaStream_t s) -> status_t {
         SZS_TRY_CUDA(cudaEventRecord(context->fork, s));
@@ -1067,7 +1072,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
-                                           lane_stream, group_states, job.group_ctas, packed_compare));
+                                           lane_stream, group_states, job.group_ctas, compare_mode));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                        bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,
@@ -1075,7 +1080,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             else if (job.kind == job_dp16_k)
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
-                                         lane_stream, packed_compare));
+                                         lane_stream, compare_mode));
             else if (job.kind == job_myers_warp_k && wide)
                 SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, results, job.ctas, lane_stream));
             else if (job.kind == job_myers_warp_k)

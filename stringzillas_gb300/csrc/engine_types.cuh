@@ -27,6 +27,20 @@ enum pair_route_t : int {
     route_dp64_k = 3,    // wavefront DP, 64-bit cells, warp per pair (only when 32-bit could overflow)
 };
 
+/** Compare modes of the 16x2 kernels: Levenshtein over more than 32 byte values keeps both pairs' row codes instead
+ *  of a profile, and a cell's substitution cost follows from comparing them with the column's codes. */
+enum compare_mode_t : int {
+    compare_none_k = 0,     // costs from the int8 profiles
+    compare_multiply_k = 1, // costs by one multiply-add: exact when match and mismatch, as shifted, have one sign
+    compare_select_k = 2,   // costs by a half mask and one logic operation
+};
+
+/** The compare mode for Levenshtein costs `match` and `mismatch` as the 16x2 kernels hold them (minus `open` for
+ *  affine tracks). */
+inline int compare_mode_for(int match, int mismatch) {
+    return (match < 0) == (mismatch < 0) ? compare_multiply_k : compare_select_k;
+}
+
 /** One scheduled pair. 32 bytes; the planner writes these in scheduled order. */
 struct pair_task_t {
     std::uint8_t const *rows;  // the string laid along DP rows (the shorter one)

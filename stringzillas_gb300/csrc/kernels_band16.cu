@@ -11,10 +11,10 @@ namespace {
 
 constexpr int band16_rows_per_lane_k = 8;
 
-template <int kind_, bool affine_, bool compare_ = false>
+template <int kind_, bool affine_, int compare_ = compare_none_k>
 using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_>;
 
-template <int kind_, bool affine_, bool compare_ = false>
+template <int kind_, bool affine_, int compare_ = compare_none_k>
 dp_launch_shape_t band16_shape_of(int classes) {
     using policy_t = band16_instance_t<kind_, affine_, compare_>;
     dp_launch_shape_t shape;
@@ -38,7 +38,7 @@ dp_launch_shape_t band16_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_, bool compare_ = false>
+template <int kind_, bool affine_, int compare_ = compare_none_k>
 cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
                              std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
@@ -81,11 +81,15 @@ cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *task
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes, bool compare) {
-    if (compare) {
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare) {
+    if (compare != compare_none_k) {
         if (kind != kind_levenshtein_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
-        return affine ? band16_shape_of<kind_levenshtein_k, true, true>(classes)
-                      : band16_shape_of<kind_levenshtein_k, false, true>(classes);
+        switch ((affine ? 2 : 0) + (compare == compare_multiply_k ? 1 : 0)) {
+        case 0: return band16_shape_of<kind_levenshtein_k, false, compare_select_k>(classes);
+        case 1: return band16_shape_of<kind_levenshtein_k, false, compare_multiply_k>(classes);
+        case 2: return band16_shape_of<kind_levenshtein_k, true, compare_select_k>(classes);
+        default: return band16_shape_of<kind_levenshtein_k, true, compare_multiply_k>(classes);
+        }
     }
     SZS_BAND16_DISPATCH(band16_shape_of, classes)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
@@ -94,15 +98,19 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes, bool compare)
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
-                          int group_ctas, bool compare) {
-    if (compare) {
+                          int group_ctas, int compare) {
+    if (compare != compare_none_k) {
         if (kind != kind_levenshtein_k) return cudaErrorInvalidValue;
-        return affine ? band16_launch_of<kind_levenshtein_k, true, true>(key_begin, key_end, tasks, bins, costs,
-                                                                        results, scratch, ring_words_per_slot, ctas,
-                                                                        stream, group_states, group_ctas)
-                      : band16_launch_of<kind_levenshtein_k, false, true>(key_begin, key_end, tasks, bins, costs,
-                                                                         results, scratch, ring_words_per_slot, ctas,
-                                                                         stream, group_states, group_ctas);
+#define SZS_BAND16_COMPARE(affine_, mode_)                                                                            \
+    band16_launch_of<kind_levenshtein_k, affine_, mode_>(key_begin, key_end, tasks, bins, costs, results, scratch,     \
+                                                         ring_words_per_slot, ctas, stream, group_states, group_ctas)
+        switch ((affine ? 2 : 0) + (compare == compare_multiply_k ? 1 : 0)) {
+        case 0: return SZS_BAND16_COMPARE(false, compare_select_k);
+        case 1: return SZS_BAND16_COMPARE(false, compare_multiply_k);
+        case 2: return SZS_BAND16_COMPARE(true, compare_select_k);
+        default: return SZS_BAND16_COMPARE(true, compare_multiply_k);
+        }
+#undef SZS_BAND16_COMPARE
     }
     SZS_BAND16_DISPATCH(band16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
                         ring_words_per_slot, ctas, stream, group_states, group_ctas)

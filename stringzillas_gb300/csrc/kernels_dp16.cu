@@ -9,7 +9,7 @@ namespace szs_gb300 {
 
 namespace {
 
-template <int kind_, bool affine_, int rows_, bool compare_>
+template <int kind_, bool affine_, int rows_, int compare_>
 dp_launch_shape_t dp16_shape_rows(int classes, int warps) {
     using policy_t = dp16_policy_t<kind_, affine_, rows_, compare_>;
     dp_launch_shape_t shape;
@@ -27,7 +27,7 @@ dp_launch_shape_t dp16_shape_rows(int classes, int warps) {
     return shape;
 }
 
-template <int kind_, bool affine_, bool compare_ = false>
+template <int kind_, bool affine_, int compare_ = compare_none_k>
 dp_launch_shape_t dp16_shape_of(int rows, int classes, int warps) {
     switch (rows) {
     case 4: return dp16_shape_rows<kind_, affine_, 4, compare_>(classes, warps);
@@ -38,7 +38,7 @@ dp_launch_shape_t dp16_shape_of(int rows, int classes, int warps) {
     }
 }
 
-template <int kind_, bool affine_, int rows_, bool compare_>
+template <int kind_, bool affine_, int rows_, int compare_>
 cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
                              std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
@@ -52,7 +52,7 @@ cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *task
     return cudaGetLastError();
 }
 
-template <int kind_, bool affine_, bool compare_ = false>
+template <int kind_, bool affine_, int compare_ = compare_none_k>
 cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                            score_costs_t const &costs, std::int64_t *results, void *scratch,
                            std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
@@ -78,12 +78,16 @@ cudaError_t dp16_launch_of(int rows, int key_begin, int key_end, pair_task_t con
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps, bool compare) {
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps, int compare) {
     if (warps < 1 || warps > 8) return dp_launch_shape_t {0, 0, 0, 0, 0};
-    if (compare) {
+    if (compare != compare_none_k) {
         if (kind != kind_levenshtein_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
-        return affine ? dp16_shape_of<kind_levenshtein_k, true, true>(rows, classes, warps)
-                      : dp16_shape_of<kind_levenshtein_k, false, true>(rows, classes, warps);
+        switch ((affine ? 2 : 0) + (compare == compare_multiply_k ? 1 : 0)) {
+        case 0: return dp16_shape_of<kind_levenshtein_k, false, compare_select_k>(rows, classes, warps);
+        case 1: return dp16_shape_of<kind_levenshtein_k, false, compare_multiply_k>(rows, classes, warps);
+        case 2: return dp16_shape_of<kind_levenshtein_k, true, compare_select_k>(rows, classes, warps);
+        default: return dp16_shape_of<kind_levenshtein_k, true, compare_multiply_k>(rows, classes, warps);
+        }
     }
     SZS_DP16_DISPATCH(dp16_shape_of, rows, classes, warps)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
@@ -91,16 +95,20 @@ dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int w
 
 cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream, bool compare) {
+                        std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream, int compare) {
     if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
-    if (compare) {
+    if (compare != compare_none_k) {
         if (kind != kind_levenshtein_k) return cudaErrorInvalidValue;
-        return affine ? dp16_launch_of<kind_levenshtein_k, true, true>(rows, key_begin, key_end, tasks, bins, costs,
-                                                                      results, scratch, scratch_cells_per_warp, ctas,
-                                                                      warps, stream)
-                      : dp16_launch_of<kind_levenshtein_k, false, true>(rows, key_begin, key_end, tasks, bins, costs,
-                                                                       results, scratch, scratch_cells_per_warp, ctas,
-                                                                       warps, stream);
+#define SZS_DP16_COMPARE(affine_, mode_)                                                                              \
+    dp16_launch_of<kind_levenshtein_k, affine_, mode_>(rows, key_begin, key_end, tasks, bins, costs, results, scratch, \
+                                                       scratch_cells_per_warp, ctas, warps, stream)
+        switch ((affine ? 2 : 0) + (compare == compare_multiply_k ? 1 : 0)) {
+        case 0: return SZS_DP16_COMPARE(false, compare_select_k);
+        case 1: return SZS_DP16_COMPARE(false, compare_multiply_k);
+        case 2: return SZS_DP16_COMPARE(true, compare_select_k);
+        default: return SZS_DP16_COMPARE(true, compare_multiply_k);
+        }
+#undef SZS_DP16_COMPARE
     }
     SZS_DP16_DISPATCH(dp16_launch_of, rows, key_begin, key_end, tasks, bins, costs, results, scratch, scratch_cells_per_warp,
                       ctas, warps, stream)

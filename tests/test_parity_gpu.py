@@ -283,12 +283,13 @@ TEXT = np.frombuffer(bytes(range(32, 127)), dtype=np.uint8)
 
 @pytest.mark.parametrize("rows", [4, 8, 12, 16])
 @pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (1, 3, 4, 1), (0, 127, 100, 100), (3, 1, 5, 5),
-                                   (4, 4, 1, 6)])
+                                   (4, 4, 1, 6), (0, 5, 3, 1), (1, 9, 4, 2)])
 def test_levenshtein_compare_mode(szs, port, rows, costs):
-    """Levenshtein over more than 32 byte values on the 16x2 route selects each cell's cost by comparing the two
-    pairs' codes: every rows-per-lane instance, linear and affine gaps, costs near the byte limit (short pairs) and a
-    match dearer than a mismatch, partners of uneven shapes in one warp, codes 0 and 255 side by side, both
-    schedules."""
+    """Levenshtein over more than 32 byte values on the 16x2 route takes each cell's cost from comparing the two
+    pairs' codes: every rows-per-lane instance, linear and affine gaps, both forms (one multiply-add when match and
+    mismatch minus the affine shift have one sign, a mask and a select when they straddle zero: the last two cost
+    sets), costs near the byte limit (short pairs) and a match dearer than a mismatch, partners of uneven shapes in
+    one warp, codes 0 and 255 side by side, both schedules."""
     rng = np.random.default_rng(rows * 1000 + sum(map(abs, costs)))
     extremes = np.array([0, 1, 127, 128, 254, 255], dtype=np.uint8)
     first, second = [], []
@@ -514,7 +515,7 @@ def test_band16_route(szs, port, family, costs):
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
-@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (1, 3, 4, 1), (3, 1, 5, 5)])
+@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (1, 3, 4, 1), (3, 1, 5, 5), (0, 5, 3, 1)])
 def test_band16_compare_mode(szs, port, costs):
     """Long Levenshtein pairs over more than 32 byte values take the 16-bit band in compare mode, one CTA per pair
     and (few pairs) grouped CTAs: shapes around the super-strip size, a long shared stretch, codes 0 and 255."""
