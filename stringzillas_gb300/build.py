@@ -30,6 +30,7 @@ UNITS = [
     ("planner", "planner.cu", []),
     ("kernels_dp", "kernels_dp.cu", []),
     ("kernels_dp16", "kernels_dp16.cu", []),
+    ("kernels_dp16_compare", "kernels_dp16.cu", ["-DSZS_DP16_COMPARE_UNIT"]),
     ("kernels_band", "kernels_band.cu", []),
     ("kernels_band16", "kernels_band16.cu", []),
     ("probe", "probe.cu", []),

@@ -294,7 +294,7 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             std::int32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0;
             std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
             if (lane == 0) up_h = chunk.top_h[e], up_f = chunk.top_f[e], code_next = chunk.code[e];
-            std::uint32_t p_next[words];
+            [[maybe_unused]] std::uint32_t p_next[words]; // profile words (unused by uniform and direct instances)
             if constexpr (!policy_::uniform_k && !policy_::direct_k)
                 load_profile_words<R>(profile + (int)code_next * S + lane * R, p_next);
 

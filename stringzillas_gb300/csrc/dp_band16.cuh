@@ -28,8 +28,9 @@
 
 namespace szs_gb300 {
 
-/** `compare_`: Levenshtein over more than 32 byte values, costs from comparing codes (`compare_mode_t`). */
-template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k>
+/** `compare_`: Levenshtein over more than 32 byte values, costs from comparing codes (`compare_mode_t`); `wide_`
+ *  (compare modes only): strings of 16-bit codes. */
+template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k, bool wide_ = false>
 struct band16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -40,7 +41,9 @@ struct band16_policy_t {
     static constexpr int super_rows_k = 2 * strip_rows_k;             // rows of one warp's super-strip
     static constexpr bool compare_k = compare_ != compare_none_k;
     static constexpr bool multiply_k = compare_ == compare_multiply_k;
+    static constexpr bool wide_k = wide_;
     static_assert(!compare_k || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
+    static_assert(!wide_ || compare_k, "16-bit codes have no profile");
 };
 
 constexpr int band16_chunk_k = 64; // lane 0's top values and codes are staged, waited for and published 64 at a time
@@ -99,7 +102,8 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
     };
     // The code of column j; in compare mode negated within 16 bits (see compare_costs_t).
     auto column_code = [&](std::uint32_t j) -> std::uint32_t {
-        std::uint32_t const c = costs.byte_to_compact[task.cols[j - 1]];
+        std::uint32_t const c =
+            policy_::wide_k ? symbol_at<true>(task.cols, j - 1) : (std::uint32_t)costs.byte_to_compact[task.cols[j - 1]];
         return compare ? (0u - c) & 0xFFFFu : c;
     };
     // Compare mode: costs of equal and different codes, shifted like the profile for affine tracks.
@@ -125,6 +129,12 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             std::int64_t const i_lo = row0_lo + r, i_hi = row0_hi + r;
+            if constexpr (policy_::wide_k) {
+                std::uint32_t const code_lo = i_lo <= (std::int64_t)n ? symbol_at<true>(task.rows, i_lo - 1) : 0u;
+                std::uint32_t const code_hi = i_hi <= (std::int64_t)n ? symbol_at<true>(task.rows, i_hi - 1) : 0u;
+                row_codes[r] = code_lo | (code_hi << 16);
+                continue;
+            }
             int const class_lo = costs.byte_to_class[i_lo <= (std::int64_t)n ? task.rows[i_lo - 1] : 0u];
             int const class_hi = costs.byte_to_class[i_hi <= (std::int64_t)n ? task.rows[i_hi - 1] : 0u];
             if constexpr (compare) row_codes[r] = std::uint32_t(class_lo) | (std::uint32_t(class_hi) << 16);
@@ -153,7 +163,7 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         std::uint32_t out_h = 0, out_f = 0;
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
-        std::uint32_t p_lo[words], p_hi[words];
+        [[maybe_unused]] std::uint32_t p_lo[words], p_hi[words]; // profile words (unused in compare mode)
         if constexpr (!compare) {
             load_profile_words<R>(profile_lo + (code_now & 0xFF) * S + lane_rows, p_lo);
             load_profile_words<R>(profile_hi + ((code_now >> 8) & 0xFF) * S + lane_rows, p_hi);
@@ -196,7 +206,7 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                 // 256, so their byte 1 is a zero byte), or in bits 0-15 and 16-31 (compare mode).
                 code_next = __byte_perm(staged_code, code_next, compare ? 0x5410 : 0x1140);
             }
-            std::uint32_t q_lo[words], q_hi[words];
+            [[maybe_unused]] std::uint32_t q_lo[words], q_hi[words];
             if constexpr (!compare) {
                 load_profile_words<R>(profile_lo + (code_next & 0xFF) * S + lane_rows, q_lo);
                 load_profile_words<R>(profile_hi + ((code_next >> 8) & 0xFF) * S + lane_rows, q_hi);
@@ -224,7 +234,8 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                 }
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    std::uint32_t h, kept, e_new = 0;
+                    std::uint32_t h, kept;
+                    [[maybe_unused]] std::uint32_t e_new = 0; // affine tracks only
                     if constexpr (affine) {
                         e_new = ops::add_opt(e_col[r], extend2, h_col[r]);
                         std::uint32_t const x = ops::add_opt(diag, subs[r], e_new);

@@ -37,8 +37,9 @@
 namespace szs_gb300 {
 
 /** `compare_`: a `compare_mode_t` (engine_types.cuh); other than `compare_none_k`, Levenshtein over more than 32 byte
- *  values with costs from comparing codes instead of profiles. */
-template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k>
+ *  values with costs from comparing codes instead of profiles. `wide_` (compare modes only): strings of 16-bit codes
+ *  (UTF-8 calls over more than 256 code points), compared as they are. */
+template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k, bool wide_ = false>
 struct dp16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -48,7 +49,9 @@ struct dp16_policy_t {
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
     static constexpr bool compare_k = compare_ != compare_none_k;
     static constexpr bool multiply_k = compare_ == compare_multiply_k;
+    static constexpr bool wide_k = wide_;
     static_assert(!compare_k || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
+    static_assert(!wide_ || compare_k, "16-bit codes have no profile");
 };
 
 /** Per-warp shared profile bytes: two pairs x classes x strip rows (none in compare mode). */
@@ -129,7 +132,7 @@ __device__ __forceinline__ void load_profile_words(std::int8_t const *source, st
 
 /**
  *  Packed substitution costs in compare mode. Row codes hold pair A's code in the low half and pair B's in the high
- *  half (codes below 256); column codes travel negated per half (`-c mod 2^16`), so one DPX add-min,
+ *  half (byte codes, or 16-bit codes); column codes travel negated per half (`-c mod 2^16`), so one DPX add-min,
  *  `min(row + column, 1)` per unsigned half with the add wrapping inside the half, is 0 exactly where the codes are
  *  equal and 1 where they differ. Then either
  *
@@ -227,11 +230,18 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
         return local ? open + extend : open + extend + edge.score(i);
     };
     // Packed codes of column j (1-based) of both pairs: 8-bit halves for profile lookups, negated 16-bit halves in
-    // compare mode.
+    // compare mode (16-bit strings: their own codes).
     auto column_code = [&](std::uint32_t j) -> std::uint32_t {
-        std::uint32_t const ca = j <= m_a ? costs.byte_to_compact[a.cols[j - 1]] : 0u;
-        std::uint32_t const cb = j <= m_b ? costs.byte_to_compact[cols_b[j - 1]] : 0u;
-        return compare ? compare_costs_t::column_codes(ca, cb) : ca | (cb << 8);
+        if constexpr (policy_::wide_k) {
+            std::uint32_t const ca = j <= m_a ? symbol_at<true>(a.cols, j - 1) : 0u;
+            std::uint32_t const cb = j <= m_b ? symbol_at<true>(cols_b, j - 1) : 0u;
+            return compare_costs_t::column_codes(ca, cb);
+        }
+        else {
+            std::uint32_t const ca = j <= m_a ? costs.byte_to_compact[a.cols[j - 1]] : 0u;
+            std::uint32_t const cb = j <= m_b ? costs.byte_to_compact[cols_b[j - 1]] : 0u;
+            return compare ? compare_costs_t::column_codes(ca, cb) : ca | (cb << 8);
+        }
     };
     // Compare mode: costs of equal and different codes (shifted like the profile for affine tracks).
     compare_costs_t const compared(costs.match - (affine ? open : 0), costs.mismatch - (affine ? open : 0));
@@ -252,6 +262,12 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             std::int64_t const i = row0 + r;
+            if constexpr (policy_::wide_k) {
+                std::uint32_t const code_a = i <= (std::int64_t)n_a ? symbol_at<true>(a.rows, i - 1) : 0u;
+                std::uint32_t const code_b = i <= (std::int64_t)n_b ? symbol_at<true>(b.rows, i - 1) : 0u;
+                row_codes[r] = code_a | (code_b << 16);
+                continue;
+            }
             int const class_a = costs.byte_to_class[i <= (std::int64_t)n_a ? a.rows[i - 1] : 0u];
             int const class_b = costs.byte_to_class[i <= (std::int64_t)n_b ? b.rows[i - 1] : 0u];
             if constexpr (compare) row_codes[r] = std::uint32_t(class_a) | (std::uint32_t(class_b) << 16);
@@ -287,7 +303,7 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
         std::uint32_t out_h = 0, out_f = 0;
         std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
         __syncwarp();
-        std::uint32_t pa_now[words], pb_now[words];
+        [[maybe_unused]] std::uint32_t pa_now[words], pb_now[words]; // profile words (unused in compare mode)
         if constexpr (!compare) {
             load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
             load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
@@ -327,7 +343,7 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
             std::uint32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0u;
             std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
             if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
-            std::uint32_t pa_next[words], pb_next[words];
+            [[maybe_unused]] std::uint32_t pa_next[words], pb_next[words];
             if constexpr (!compare) {
                 load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane_rows, pa_next);
                 load_profile_words<R>(profile_b + (code_next >> 8) * S + lane_rows, pb_next);

@@ -738,7 +738,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.steps_beyond_span = costs.affine ? 3 : 1;
     args.force_route = schedule == szs_gb300_schedule_plain_k ? 1 : -1;
 
-    args.packed_allowed = engine.packed_profile_fits && !wide ? 1 : 0; // 16-bit codes: no 32-class profile
+    args.packed_allowed = engine.packed_profile_fits ? 1 : 0; // 16-bit codes (Levenshtein): compare mode
     args.dense = engine.dense.empty() ? 0 : 1;
     std::memcpy(args.packed_rows, engine.tuning.packed_rows, 16);
     std::memcpy(args.cell_bits, engine.tuning.cell_bits, 16);
@@ -862,9 +862,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     score_costs_t const &call_costs = dense ? dense_costs : costs;
 
     // 16x2 routes (packed wavefront, 16-bit band): Levenshtein engines score over the batch alphabet's codes, with a
-    // profile over at most 32 of them, else by comparing the codes (the kernels' compare mode).
+    // profile over at most 32 of them, else by comparing the codes (the kernels' compare mode), which is also how
+    // 16-bit codes are scored.
     score_costs_t packed_costs = call_costs;
-    bool const packed_compare = levenshtein && !wide && alphabet_host.symbols > 32;
+    bool const packed_compare = levenshtein && (wide || alphabet_host.symbols > 32);
     // Compare mode's form: one multiply-add per row when match and mismatch, as the kernels shift them (minus `open`
     // for affine tracks), have the same sign, else a mask and a select.
     int const shift = costs.affine ? costs.open : 0;
@@ -872,10 +873,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         packed_compare ? compare_mode_for(costs.match - shift, costs.mismatch - shift) : (int)compare_none_k;
     if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
                         pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k))) {
-        int const symbols = (int)alphabet_host.symbols;
-        packed_costs.classes = packed_compare ? 1 : symbols;
-        for (int b = 0; b < 256; ++b)
-            packed_costs.byte_to_class[b] = packed_costs.byte_to_compact[b] = alphabet_host.code[b];
+        packed_costs.classes = packed_compare ? 1 : (int)alphabet_host.symbols;
+        if (!wide) // 16-bit codes are compared as they are; no alphabet pass ran
+            for (int b = 0; b < 256; ++b)
+                packed_costs.byte_to_class[b] = packed_costs.byte_to_compact[b] = alphabet_host.code[b];
         for (int cc = 0; cc < 32; ++cc)
             for (int rc = 0; rc < 32; ++rc) {
                 std::int8_t const cost = (std::int8_t)(cc == rc ? costs.match : costs.mismatch);
@@ -926,7 +927,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
         if (pairs_here) {
             dp_launch_shape_t const shape =
-                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode);
+                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide);
             if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
             band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
@@ -988,7 +989,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int const rows = 4 * (choice + 1);
         int const warps = engine.tuning.packed_warps[choice] ? (int)engine.tuning.packed_warps[choice] : 4;
         dp_launch_shape_t const shape =
-            dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps, compare_mode);
+            dp16_shape(engine.kind, costs.affine != 0, rows, packed_costs.classes, warps, compare_mode, wide);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Packed wavefront kernel cannot be resident"};
         std::uint64_t const warps_needed = (pairs_here + 1) / 2;
         std::uint64_t const needed = (warps_needed + shape.warps_per_cta - 1) / shape.warps_per_cta;
@@ -1072,7 +1073,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
-                                           lane_stream, group_states, job.group_ctas, compare_mode));
+                                           lane_stream, group_states, job.group_ctas, compare_mode, wide));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                        bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,
@@ -1080,7 +1081,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             else if (job.kind == job_dp16_k)
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
-                                         lane_stream, compare_mode));
+                                         lane_stream, compare_mode, wide));
             else if (job.kind == job_myers_warp_k && wide)
                 SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, results, job.ctas, lane_stream));
             else if (job.kind == job_myers_warp_k)
@@ -1759,11 +1760,6 @@ sz_status_t fingerprint_call(void *engine_handle, void *scope_handle, tape_view_
     if (error == cudaSuccess) error = cudaStreamSynchronize(stream);
     if (error != cudaSuccess) return report(from_cuda(error), error_message);
     return report({}, error_message);
-}
-
-sz_status_t not_in_scope(char const **error_message) {
-    return report({sz_status_unknown_k, "Not implemented by the GB300 engine (outside its scoring scope)"},
-                  error_message);
 }
 
 } // namespace

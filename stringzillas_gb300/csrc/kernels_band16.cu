@@ -11,12 +11,12 @@ namespace {
 
 constexpr int band16_rows_per_lane_k = 8;
 
-template <int kind_, bool affine_, int compare_ = compare_none_k>
-using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_>;
+template <int kind_, bool affine_, int compare_ = compare_none_k, bool wide_ = false>
+using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_, wide_>;
 
-template <int kind_, bool affine_, int compare_ = compare_none_k>
+template <int kind_, bool affine_, int compare_ = compare_none_k, bool wide_ = false>
 dp_launch_shape_t band16_shape_of(int classes) {
-    using policy_t = band16_instance_t<kind_, affine_, compare_>;
+    using policy_t = band16_instance_t<kind_, affine_, compare_, wide_>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = band_warps_k * 32;
     shape.warps_per_cta = band_warps_k;
@@ -38,12 +38,12 @@ dp_launch_shape_t band16_shape_of(int classes) {
     return shape;
 }
 
-template <int kind_, bool affine_, int compare_ = compare_none_k>
+template <int kind_, bool affine_, int compare_ = compare_none_k, bool wide_ = false>
 cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
                              std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
                              int group_ctas) {
-    using policy_t = band16_instance_t<kind_, affine_, compare_>;
+    using policy_t = band16_instance_t<kind_, affine_, compare_, wide_>;
     int const shared = band16_shared_bytes<policy_t>(costs.classes);
     if (group_states) {
         // The CTAs of a group wait on one another: a cooperative launch keeps the whole grid resident.
@@ -81,15 +81,23 @@ cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *task
     default: break;                                                                                                  \
     }
 
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare) {
-    if (compare != compare_none_k) {
-        if (kind != kind_levenshtein_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
-        switch ((affine ? 2 : 0) + (compare == compare_multiply_k ? 1 : 0)) {
-        case 0: return band16_shape_of<kind_levenshtein_k, false, compare_select_k>(classes);
-        case 1: return band16_shape_of<kind_levenshtein_k, false, compare_multiply_k>(classes);
-        case 2: return band16_shape_of<kind_levenshtein_k, true, compare_select_k>(classes);
-        default: return band16_shape_of<kind_levenshtein_k, true, compare_multiply_k>(classes);
-        }
+// Compare-mode instances: affine or not, multiply-add or select form, bytes or 16-bit codes.
+#define SZS_BAND16_COMPARE_DISPATCH(call_, ...)                                                                      \
+    switch ((affine ? 4 : 0) + (compare == compare_multiply_k ? 2 : 0) + (wide ? 1 : 0)) {                           \
+    case 0: return call_<kind_levenshtein_k, false, compare_select_k, false>(__VA_ARGS__);                           \
+    case 1: return call_<kind_levenshtein_k, false, compare_select_k, true>(__VA_ARGS__);                            \
+    case 2: return call_<kind_levenshtein_k, false, compare_multiply_k, false>(__VA_ARGS__);                         \
+    case 3: return call_<kind_levenshtein_k, false, compare_multiply_k, true>(__VA_ARGS__);                          \
+    case 4: return call_<kind_levenshtein_k, true, compare_select_k, false>(__VA_ARGS__);                            \
+    case 5: return call_<kind_levenshtein_k, true, compare_select_k, true>(__VA_ARGS__);                             \
+    case 6: return call_<kind_levenshtein_k, true, compare_multiply_k, false>(__VA_ARGS__);                          \
+    default: return call_<kind_levenshtein_k, true, compare_multiply_k, true>(__VA_ARGS__);                          \
+    }
+
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare, bool wide) {
+    if (compare != compare_none_k || wide) {
+        if (kind != kind_levenshtein_k || compare == compare_none_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
+        SZS_BAND16_COMPARE_DISPATCH(band16_shape_of, classes)
     }
     SZS_BAND16_DISPATCH(band16_shape_of, classes)
     return dp_launch_shape_t {0, 0, 0, 0, 0};
@@ -98,19 +106,11 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare) 
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
-                          int group_ctas, int compare) {
-    if (compare != compare_none_k) {
-        if (kind != kind_levenshtein_k) return cudaErrorInvalidValue;
-#define SZS_BAND16_COMPARE(affine_, mode_)                                                                            \
-    band16_launch_of<kind_levenshtein_k, affine_, mode_>(key_begin, key_end, tasks, bins, costs, results, scratch,     \
-                                                         ring_words_per_slot, ctas, stream, group_states, group_ctas)
-        switch ((affine ? 2 : 0) + (compare == compare_multiply_k ? 1 : 0)) {
-        case 0: return SZS_BAND16_COMPARE(false, compare_select_k);
-        case 1: return SZS_BAND16_COMPARE(false, compare_multiply_k);
-        case 2: return SZS_BAND16_COMPARE(true, compare_select_k);
-        default: return SZS_BAND16_COMPARE(true, compare_multiply_k);
-        }
-#undef SZS_BAND16_COMPARE
+                          int group_ctas, int compare, bool wide) {
+    if (compare != compare_none_k || wide) {
+        if (kind != kind_levenshtein_k || compare == compare_none_k) return cudaErrorInvalidValue;
+        SZS_BAND16_COMPARE_DISPATCH(band16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
+                                    ring_words_per_slot, ctas, stream, group_states, group_ctas)
     }
     SZS_BAND16_DISPATCH(band16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
                         ring_words_per_slot, ctas, stream, group_states, group_ctas)

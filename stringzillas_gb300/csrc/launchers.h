@@ -85,14 +85,23 @@ cudaError_t launch_dp(int kind, bool affine, int cell_bits, int key_begin, int k
 /** Launch shape of the 16x2 packed wavefront kernel with `rows` (4, 8, 12, 16) rows per lane and `warps` (1..8)
  *  warps per CTA; ctas_per_sm = 0 if unsupported. `compare` (a `compare_mode_t`, dp_packed.cuh): the Levenshtein
  *  instances that compare codes instead of reading a profile (batches over more than 32 byte values). */
-dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps, int compare = 0);
+dp_launch_shape_t dp16_shape(int kind, bool affine, int rows, int classes, int warps, int compare = 0,
+                             bool wide = false);
 
 /** Runs the 16x2 packed wavefront kernel over bins [key_begin, key_end): two scheduled pairs per warp. `scratch`
  *  holds `ctas * warps_per_cta` rows of `scratch_cells_per_warp` 32-bit words. */
 cudaError_t launch_dp16(int kind, bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream,
-                        int compare = 0);
+                        int compare = 0, bool wide = false);
+
+/** The compare-mode halves of `dp16_shape` and `launch_dp16` (Levenshtein only; `wide`: strings of 16-bit codes),
+ *  built in their own translation unit. */
+dp_launch_shape_t dp16_compare_shape(bool affine, int rows, int classes, int warps, int compare, bool wide);
+cudaError_t launch_dp16_compare(bool affine, int rows, int key_begin, int key_end, pair_task_t const *tasks,
+                                plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                                std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream,
+                                int compare, bool wide);
 
 /** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells); `direct`: the
  *  direct-table instance. */
@@ -115,7 +124,7 @@ int band_group_max_ctas();
 
 /** Launch shape of the 16-bit band kernel (one CTA per long pair, two row strips per warp in 16x2 cells);
  *  `compare` (a `compare_mode_t`): the Levenshtein instances that compare codes instead of reading a profile. */
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare = 0);
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare = 0, bool wide = false);
 
 /** Runs the 16-bit band kernel over bins [key_begin, key_end). `scratch` holds `ctas * band_warps_per_cta()` ring
  *  slots of `ring_words_per_slot` 32-bit words (twice that for local scores, which may rescore a pair on 32-bit
@@ -123,7 +132,7 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare =
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
-                          int group_ctas = 1, int compare = 0);
+                          int group_ctas = 1, int compare = 0, bool wide = false);
 
 /** Bit-parallel kernels over strings of 16-bit codes (UTF-8 calls over more than 256 code points, 16 code planes):
  *  thread per pair over the bins of `words` words (1..8), and warp per pair over the warp bins (1..8 words per

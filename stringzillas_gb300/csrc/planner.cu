@@ -107,10 +107,11 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     std::uint64_t const reach16 =
         args.local_gain >= 0 ? (std::uint64_t)args.local_gain * (n < m ? n : m) + 1 : reach;
     // The 16x2 routes hold costs in a 32-class profile: dense-table calls over more bytes than that stay on the
-    // 32-bit routes. Levenshtein calls over more bytes take them in compare mode (codes compared, no profile).
+    // 32-bit routes. Levenshtein calls over more bytes, or over 16-bit codes, take them in compare mode (codes
+    // compared, no profile).
     bool const profile_fits = (args.kind != kind_levenshtein_k && !args.dense) ||
                               (args.alphabet && args.alphabet->symbols <= 32);
-    bool const compare_fits = args.kind == kind_levenshtein_k && args.alphabet != nullptr;
+    bool const compare_fits = args.kind == kind_levenshtein_k && (args.alphabet != nullptr || args.wide);
     bool const packed = args.packed_allowed && (profile_fits || compare_fits) && reach16 < 32767 &&
                         args.cell_bits[length_class] != 32;
     std::uint64_t const band_rows = packed ? args.band_min_rows_packed : args.band_min_rows;

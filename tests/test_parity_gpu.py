@@ -678,10 +678,32 @@ def test_utf8_levenshtein_routes(szs, port, costs):
                                                                      tape(first[:12]), tape(second[:9])))
 
 
-@pytest.mark.parametrize("costs", [(0, 1, 1, 1), (0, 2, 3, 1), (1, 3, 2, 2)])
+@pytest.mark.parametrize("rows", [4, 8, 12, 16])
+@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (3, 1, 5, 5), (0, 5, 3, 1)])
+def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
+    """16-bit codes on the 16x2 routes: every rows-per-lane instance of the wavefront and the 16-bit band (tuned down
+    to 600 rows), codes that differ only in their high byte, uneven partners, odd counts."""
+    rng = np.random.default_rng(rows * 100 + sum(costs))
+    # 300 distinct code points: the codes above 255 share their low byte with codes below it.
+    letters = [chr(c) for c in range(0x3041, 0x3041 + 86)] + [chr(c) for c in range(0xAC00, 0xAC00 + 214)]
+    lengths = [(int(rng.integers(0, 500)), int(rng.integers(0, 500))) for _ in range(41)]
+    lengths += [(601, 700), (1025, 1300), (700, 1400), (2049, 2100)]
+    first = ["".join(rng.choice(letters, size=n)) for n, _ in lengths]
+    second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
+    second[-3] = first[-3][:500] + second[-3][500:]
+    engine = szs.LevenshteinDistancesUTF8(*costs)
+    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600})
+    want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
+
+
+@pytest.mark.parametrize("costs", [(0, 1, 1, 1), (0, 2, 3, 1), (1, 3, 2, 2), (0, 5, 3, 1)])
 def test_utf8_levenshtein_over_many_code_points(szs, port, costs):
     """More than 256 distinct code points: 16-bit codes on every route (thread and warp bit-parallel kernels with 16
-    code planes, 32-bit wavefront and band), short and long pairs, both orientations and a cross product."""
+    code planes, the 16x2 wavefront and 16-bit band in compare mode, both cost forms, the 32-bit wavefront and band
+    where the bound needs them), short and long pairs, both orientations and a cross product."""
     rng = np.random.default_rng(sum(costs) + 7)
     letters = [chr(c) for c in range(0x4E00, 0x4E00 + 3000)] + list("abcdefghij")
     lengths = [(int(rng.integers(0, 300)), int(rng.integers(0, 300))) for _ in range(150)]
@@ -701,3 +723,24 @@ def test_utf8_levenshtein_over_many_code_points(szs, port, costs):
     cross = engine(szs.Strs(first[:12]), szs.Strs(second[:9]))
     np.testing.assert_array_equal(cross.astype(np.int64), port.cross(oracle.levenshtein_utf8_costs(*costs),
                                                                      tape(first[:12]), tape(second[:9])))
+
+
+@pytest.mark.parametrize("rows", [4, 8, 12, 16])
+@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (3, 1, 5, 5), (0, 5, 3, 1)])
+def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
+    """16-bit codes on the 16x2 routes: every rows-per-lane instance of the wavefront and the 16-bit band (tuned down
+    to 600 rows), codes that differ only in their high byte, uneven partners, odd counts."""
+    rng = np.random.default_rng(rows * 100 + sum(costs))
+    # 300 distinct code points: the codes above 255 share their low byte with codes below it.
+    letters = [chr(c) for c in range(0x3041, 0x3041 + 86)] + [chr(c) for c in range(0xAC00, 0xAC00 + 214)]
+    lengths = [(int(rng.integers(0, 500)), int(rng.integers(0, 500))) for _ in range(41)]
+    lengths += [(601, 700), (1025, 1300), (700, 1400), (2049, 2100)]
+    first = ["".join(rng.choice(letters, size=n)) for n, _ in lengths]
+    second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
+    second[-3] = first[-3][:500] + second[-3][500:]
+    engine = szs.LevenshteinDistancesUTF8(*costs)
+    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600})
+    want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
