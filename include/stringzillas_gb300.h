@@ -465,6 +465,10 @@ typedef struct szs_gb300_tuning_t {
         the planner gives each pair the rows per lane of least `strips x (m + 31) x cost` (0 = built-in 100, 165,
         245, 330). */
     sz_u16_t packed_step_cost[4];
+    /** Calls of the batched form with fewer pairs than 32 per SM (less than one wave of the 16x2 route's warps, two
+        pairs each) give pairs whose shorter side exceeds this a band instead, whatever the two thresholds above say
+        (0 = 512): a band spreads one pair over a CTA's warps, where the wavefront would leave SMs idle. */
+    sz_u32_t band_min_rows_few;
 } szs_gb300_tuning_t;
 
 /** Installs @p tuning on @p engine (NULL restores the built-in choices); out-of-range values are rejected with

@@ -150,6 +150,7 @@ class Tuning(ctypes.Structure):
         ("band_min_rows_packed", ctypes.c_uint32),
         ("pipeline_chunk_kb", ctypes.c_uint32),
         ("packed_step_cost", ctypes.c_uint16 * 4),
+        ("band_min_rows_few", ctypes.c_uint32),
     ]
 
 

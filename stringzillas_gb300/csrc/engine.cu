@@ -745,6 +745,14 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.band_min_rows = engine.tuning.band_min_rows ? engine.tuning.band_min_rows : (std::uint32_t)band_min_rows_k;
     args.band_min_rows_packed = engine.tuning.band_min_rows_packed ? engine.tuning.band_min_rows_packed
                                                                    : (std::uint32_t)band_min_rows_packed_k;
+    // A batched call with fewer pairs than one wave of the 16x2 route (two pairs per warp, about 16 resident warps
+    // per SM) would leave SMs idle on the wavefront: its longer pairs spread over a band CTA's warps instead.
+    if (schedule != szs_gb300_schedule_plain_k && args.pairs < 32ull * (std::uint64_t)context->sm_count) {
+        std::uint32_t const few = engine.tuning.band_min_rows_few ? engine.tuning.band_min_rows_few
+                                                                  : (std::uint32_t)band_min_rows_few_k;
+        args.band_min_rows = std::min(args.band_min_rows, few);
+        args.band_min_rows_packed = std::min(args.band_min_rows_packed, few);
+    }
     for (int choice = 0; choice < 4; ++choice)
         args.packed_step_cost[choice] = engine.tuning.packed_step_cost[choice]
                                             ? engine.tuning.packed_step_cost[choice]

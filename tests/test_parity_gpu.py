@@ -79,6 +79,9 @@ def test_pairwise_matches_oracle(szs, port, name, family, costs, lengths):
     want = port.pairs(oracle_costs, tape(first), tape(second))
     bad = np.flatnonzero(got != want)
     assert bad.size == 0, f"{name}: {bad.size} mismatches, first {bad[:5]}: got {got[bad[:5]]} want {want[bad[:5]]}"
+    if lengths[1] > 512:  # few pairs: the longer ones took the bands; the wavefront routes must agree
+        engine.set_tuning({"band_min_rows_few": 1 << 20})
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
 
 
 @pytest.mark.parametrize("family,costs", [("nw", (-3, -1)), ("sw", (-3, -1)), ("nw", (-2, -2)), ("sw", (-4, -4))])
@@ -302,7 +305,8 @@ def test_levenshtein_compare_mode(szs, port, rows, costs):
                bytes(rng.choice(TEXT, size=3))]
     second[5] = first[5][:200] + second[5][200:]  # a long shared stretch
     engine = szs.LevenshteinDistances(*costs)
-    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 4096, "band_min_rows_packed": 4096})
+    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 4096, "band_min_rows_packed": 4096,
+                       "band_min_rows_few": 4096})
     want = port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
@@ -324,6 +328,7 @@ def test_packed_couples_with_uneven_partners(szs, port, family, costs):
     first += [bytes(rng.choice(PROTEIN, size=1))] * 3 + [bytes(rng.choice(PROTEIN, size=800))]
     second += [bytes(rng.choice(PROTEIN, size=800))] * 3 + [bytes(rng.choice(PROTEIN, size=2))]
     engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    engine.set_tuning({"band_min_rows_few": 1 << 20})  # keep the longer pairs on the 16x2 wavefront
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
         got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
@@ -692,7 +697,8 @@ def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
     second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
     second[-3] = first[-3][:500] + second[-3][500:]
     engine = szs.LevenshteinDistancesUTF8(*costs)
-    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600})
+    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600,
+                       "band_min_rows_few": 600})
     want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
@@ -739,7 +745,8 @@ def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
     second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
     second[-3] = first[-3][:500] + second[-3][500:]
     engine = szs.LevenshteinDistancesUTF8(*costs)
-    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600})
+    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600,
+                       "band_min_rows_few": 600})
     want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
