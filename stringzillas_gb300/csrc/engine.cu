@@ -906,6 +906,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int group_ctas = 1;            // band jobs: CTAs sharing one pair (1 = one CTA per pair)
         std::size_t state_offset = 0;  // grouped band jobs: the groups' state records in the scratch buffer
         std::size_t state_bytes = 0;
+        bool fills = true;             // the grid takes every resident CTA slot of its kernel on the device
     };
     job_t jobs[64];
     int job_count = 0;
@@ -945,6 +946,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                                    (std::size_t)band_warps_per_cta(), 256);
             job_t job {job_band16_k, 16, 0, bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k, pairs_here,
                        ctas, scratch_total, bytes};
+            job.fills = group_ctas > 1 || ctas >= context->sm_count * shape.ctas_per_sm;
             scratch_total += bytes;
             if (group_ctas > 1) {
                 job.group_ctas = group_ctas, job.state_offset = scratch_total;
@@ -966,6 +968,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                 align_up(cells_per_warp * 4 * (std::size_t)ctas * (std::size_t)band_warps_per_cta(), 256);
             job_t job {job_band_k, 32, 0, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here, ctas,
                        scratch_total, bytes};
+            job.fills = group_ctas > 1 || ctas >= context->sm_count * shape.ctas_per_sm;
             scratch_total += bytes;
             if (group_ctas > 1) {
                 job.group_ctas = group_ctas, job.state_offset = scratch_total;
@@ -987,6 +990,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::size_t const bytes = align_up(cells_per_warp * (cell_bits / 8) * (std::size_t)ctas * shape.warps_per_cta, 256);
         jobs[job_count++] = {job_dp_k, cell_bits, 0, key_begin, key_begin + bin_dp_classes_k, pairs_here, ctas,
                              scratch_total, bytes};
+        jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * shape.ctas_per_sm;
         scratch_total += bytes;
     }
     for (int choice = dp16_row_choices_k - 1; choice >= 0; --choice) {
@@ -1004,6 +1008,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
         std::size_t const bytes = align_up(cells_per_warp * 4 * (std::size_t)ctas * shape.warps_per_cta, 256);
         jobs[job_count++] = {job_dp16_k, rows, warps, key_begin, key_end, pairs_here, ctas, scratch_total, bytes};
+        jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * shape.ctas_per_sm;
         scratch_total += bytes;
     }
     int myers_planes = 0;
@@ -1018,6 +1023,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 2);
             jobs[job_count++] = {job_myers_warp_k, words, 0, key_begin, key_begin + myers_warp_classes_k, pairs_here,
                                  ctas, 0, 0};
+            jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * 2;
         }
         for (int words = myers_max_words_k; words >= 1; --words) {
             int const key_begin = bin_myers_begin_k + words * 16;
@@ -1027,8 +1033,14 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             std::uint64_t const needed = (pairs_here + threads - 1) / threads;
             int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
             jobs[job_count++] = {job_myers_k, words, 0, key_begin, key_begin + 16, pairs_here, ctas, 0, 0};
+            jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * 16;
         }
     }
+    // Jobs whose grids leave slots free go first: a persistent grid that fills the device holds its slots until its
+    // last pair, so a small job launched after it would only start at the end and add its whole time to the call.
+    // Launched first, it takes its few slots and runs beside the large grids, which balance over their cursor.
+    if (schedule != szs_gb300_schedule_plain_k)
+        std::stable_partition(jobs, jobs + job_count, [](job_t const &job) { return !job.fills; });
     if (scratch_total) {
         status = context->scratch.reserve(scratch_total, stream);
         if (!status.ok()) return status;
