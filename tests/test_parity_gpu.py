@@ -375,6 +375,25 @@ def test_grouped_band_few_long_pairs(szs, port, family, costs):
         np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
+@pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 2, 3, 1))])
+def test_grouped_band_beside_small_launches(szs, port, family, costs):
+    """A cooperative grouped-band launch queued behind small launches that take a few CTA slots first (grids that
+    do not fill the device go first): the group still meets, every score equals the oracle, no wait gives up."""
+    rng = np.random.default_rng(47)
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
+    lengths = [(6000, 6500), (5000, 9000)] + [(int(rng.integers(20, 300)), int(rng.integers(20, 300)))
+                                              for _ in range(50)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    second[0] = first[0][:3000] + second[0][3000:]
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    for _ in range(3):
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, want)
+
+
 @pytest.mark.parametrize("family,costs,extreme", [
     ("nw", (-30, -2), 120),    # 120 - (-30) leaves a signed byte: the affine pairs leave the 16x2 route
     ("sw", (-30, -2), 110),
