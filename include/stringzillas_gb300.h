@@ -467,7 +467,7 @@ typedef struct szs_gb300_tuning_t {
     sz_u16_t packed_step_cost[4];
     /** Calls of the batched form with fewer pairs than 32 per SM (less than one wave of the 16x2 route's warps, two
         pairs each) give pairs whose shorter side exceeds this a band instead, whatever the two thresholds above say
-        (0 = 512): a band spreads one pair over a CTA's warps, where the wavefront would leave SMs idle. */
+        (0 = 1,024): a band spreads one pair over a CTA's warps, where the wavefront would leave SMs idle. */
     sz_u32_t band_min_rows_few;
 } szs_gb300_tuning_t;
 

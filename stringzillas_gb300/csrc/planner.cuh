@@ -44,7 +44,7 @@ constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shor
  *  (affine protein alignment, shorter sides 128-1,023). */
 constexpr int packed_step_cost_k[4] = {100, 165, 245, 330};
 constexpr int band_min_rows_packed_k = 2048; // default for pairs that fit 16-bit cells (the 16-bit band above it)
-constexpr int band_min_rows_few_k = 512;     // default for calls with fewer pairs than one 16x2 wave (32 per SM)
+constexpr int band_min_rows_few_k = 1024;    // default for calls with fewer pairs than one 16x2 wave (32 per SM)
 constexpr int myers_max_words_k = 16;
 constexpr int myers_wide_max_words_k = 8; // 16-bit codes take 16 code planes: the thread route stops at 8 words
 // Words per lane of the warp kernel: patterns up to 32 * 32 * 8 = 8,192 rows. Longer ones take the bands: a pair of

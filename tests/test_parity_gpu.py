@@ -79,7 +79,7 @@ def test_pairwise_matches_oracle(szs, port, name, family, costs, lengths):
     want = port.pairs(oracle_costs, tape(first), tape(second))
     bad = np.flatnonzero(got != want)
     assert bad.size == 0, f"{name}: {bad.size} mismatches, first {bad[:5]}: got {got[bad[:5]]} want {want[bad[:5]]}"
-    if lengths[1] > 512:  # few pairs: the longer ones took the bands; the wavefront routes must agree
+    if lengths[1] > 1024:  # few pairs: the longer ones took the bands; the wavefront routes must agree
         engine.set_tuning({"band_min_rows_few": 1 << 20})
         np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
 
