@@ -66,8 +66,8 @@ WORKLOADS = {
                 "[2500, 8000], 70% identity, open -11 extend -1 (the reach bound exceeds int16: 32-bit band)",
     "p_dp32": "profiling case, Needleman-Wunsch affine protein with a wide table: 65,536 pairs, len lognormal(350, 0.6) "
               "in [50, 2000], diagonal 100..120, open -30 extend -2 (costs outside the int8 profile: 32-bit wavefront)",
-    "p_text": "profiling case, Levenshtein on printable text: 262,144 pairs, len U[100,300], 95 byte values, partner "
-              "5% subs + 2% indels, match 0 mismatch 2 open 3 extend 1 (16x2 wavefront in compare mode)",
+    "text": "Levenshtein on printable text: 262,144 pairs, len U[100,300], 95 byte values, partner 5% subs + 2% indels, "
+            "match 0 mismatch 2 open 3 extend 1 (16x2 wavefront in compare mode)",
 }
 
 
@@ -105,7 +105,7 @@ def make_workload(name, seed):
     if name == "p_band32":
         first, second = w.protein_pairs(1024, median=4000.0, sigma=0.3, low=2500, high=8000, seed=seed)
         return first, second, ("nw32", (*w.protein_table(seed=seed), -11, -1))
-    if name == "p_text":
+    if name == "text":
         first, second = w.text_pairs(262144, 100, 300, 0.05, 0.02, seed=seed)
         return first, second, ("levc", (0, 2, 3, 1))
     if name == "p_dp32":
@@ -632,7 +632,7 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_extra:
         line["cpu_baseline"] = cpu_baseline(first, second, kind_and_tables, args.cpu_seconds)
         extra = {}
-        for name in ("c3", "c4"):
+        for name in ("c3", "c4", "text"):
             if name == args.workload:
                 continue
             f, s, kt = make_workload(name, 42)
