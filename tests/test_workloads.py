@@ -15,6 +15,15 @@ def test_levenshtein_reads_shape_and_mutation_rates():
     assert np.array_equal(a, a2) and np.array_equal(b, b2)
 
 
+def test_text_pairs_use_the_printable_bytes():
+    (a, ao), (b, bo) = w.text_pairs(4096, 100, 300, 0.05, 0.02, seed=5)
+    lengths = np.diff(ao)
+    assert lengths.min() >= 100 and lengths.max() <= 300
+    assert set(np.unique(a)) == set(range(32, 127)) and set(np.unique(b)) <= set(range(32, 127))
+    (a2, _), (b2, _) = w.text_pairs(4096, 100, 300, 0.05, 0.02, seed=5)
+    assert np.array_equal(a, a2) and np.array_equal(b, b2)
+
+
 def test_protein_pairs_lengths_and_identity():
     (a, ao), (b, bo) = w.protein_pairs(2000, seed=1)
     lengths = np.diff(ao)
