@@ -68,6 +68,8 @@ WORKLOADS = {
               "in [50, 2000], diagonal 100..120, open -30 extend -2 (costs outside the int8 profile: 32-bit wavefront)",
     "text": "Levenshtein on printable text: 262,144 pairs, len U[100,300], 95 byte values, partner 5% subs + 2% indels, "
             "match 0 mismatch 2 open 3 extend 1 (16x2 wavefront in compare mode)",
+    "p_long_lev": "profiling case, unit-cost Levenshtein on long DNA reads: 16,384 pairs, len U[1,000, 4,000], partner 3% "
+                  "subs + 1% indels (warp-per-pair bit-parallel kernel)",
 }
 
 
@@ -105,6 +107,9 @@ def make_workload(name, seed):
     if name == "p_band32":
         first, second = w.protein_pairs(1024, median=4000.0, sigma=0.3, low=2500, high=8000, seed=seed)
         return first, second, ("nw32", (*w.protein_table(seed=seed), -11, -1))
+    if name == "p_long_lev":
+        first, second = w.levenshtein_reads(16384, 1000, 4000, 0.03, 0.01, seed=seed)
+        return first, second, ("lev", None)
     if name == "text":
         first, second = w.text_pairs(262144, 100, 300, 0.05, 0.02, seed=seed)
         return first, second, ("levc", (0, 2, 3, 1))
