@@ -68,6 +68,9 @@ WORKLOADS = {
               "in [50, 2000], diagonal 100..120, open -30 extend -2 (costs outside the int8 profile: 32-bit wavefront)",
     "text": "Levenshtein on printable text: 262,144 pairs, len U[100,300], 95 byte values, partner 5% subs + 2% indels, "
             "match 0 mismatch 2 open 3 extend 1 (16x2 wavefront in compare mode)",
+    "p_cjk": "profiling case, UTF-8 Levenshtein on CJK text: 65,536 pairs, len U[100,300] code points of 3,000 "
+             "ideographs (three UTF-8 bytes each), partner 5% subs + 2% indels, match 0 mismatch 2 open 3 extend 1 "
+             "(16-bit codes; 16x2 wavefront in compare mode)",
     "p_long_lev": "profiling case, unit-cost Levenshtein on long DNA reads: 16,384 pairs, len U[1,000, 4,000], partner 3% "
                   "subs + 1% indels (warp-per-pair bit-parallel kernel)",
 }
@@ -107,6 +110,9 @@ def make_workload(name, seed):
     if name == "p_band32":
         first, second = w.protein_pairs(1024, median=4000.0, sigma=0.3, low=2500, high=8000, seed=seed)
         return first, second, ("nw32", (*w.protein_table(seed=seed), -11, -1))
+    if name == "p_cjk":
+        first, second = w.cjk_pairs(65536, 100, 300, 0.05, 0.02, seed=seed)
+        return first, second, ("levu", (0, 2, 3, 1))
     if name == "p_long_lev":
         first, second = w.levenshtein_reads(16384, 1000, 4000, 0.03, 0.01, seed=seed)
         return first, second, ("lev", None)
@@ -133,6 +139,8 @@ def make_engine(kind_and_tables):
         engine = szs.LevenshteinDistances()
     elif kind == "levc":  # Levenshtein with the given (match, mismatch, open, extend)
         engine = szs.LevenshteinDistances(*tables)
+    elif kind == "levu":  # UTF-8 Levenshtein with the given (match, mismatch, open, extend)
+        engine = szs.LevenshteinDistancesUTF8(*tables)
     elif kind == "nw":
         engine = szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
     elif kind == "nw32":  # profiling cases of the 32-bit routes: (byte_to_class, table, open, extend)
@@ -155,6 +163,8 @@ def oracle_costs(kind_and_tables):
         return oracle.levenshtein_costs()
     if kind == "levc":
         return oracle.levenshtein_costs(*tables)
+    if kind == "levu":
+        return oracle.levenshtein_utf8_costs(*tables)
     if kind == "nw":
         return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables, -11, -1)
     if kind == "nw32":
@@ -168,7 +178,7 @@ def ops_per_cell(kind_and_tables):
         return OPS_PER_CELL["myers_dna"]
     if kind == "nw32":
         return OPS_PER_CELL["dp_affine"]
-    if kind == "levc":
+    if kind in ("levc", "levu"):
         return OPS_PER_CELL["packed_compare_affine"]
     return OPS_PER_CELL["packed_affine_local"] if kind == "sw" else OPS_PER_CELL["packed_affine"]
 
@@ -609,7 +619,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": {"lev": "u32", "levc": "int16x2"}.get(kind_and_tables[0], "int32"),
+            "scaling": "weak", "vs_baseline": None, "dtype": {"lev": "u32", "levc": "int16x2", "levu": "int16x2"}.get(kind_and_tables[0], "int32"),
             "data": "synthetic (seeded numpy PCG64)",
             "config": {"workload": WORKLOADS[args.workload], "pairs": pairs, "cells_per_step": cells_per_step,
                        "input_bytes_per_step": input_bytes, "tuning": tuning_source(),

@@ -37,7 +37,8 @@ def _offsets(lengths) -> np.ndarray:
 def _letters(rng, alphabet, size, probabilities=None):
     """`size` letters drawn from `alphabet` (uniform, or by `probabilities` at 1/65536 resolution)."""
     if probabilities is None:
-        return alphabet[rng.integers(0, len(alphabet), size=size, dtype=np.uint8)]
+        index_type = np.uint8 if len(alphabet) <= 256 else np.int64
+        return alphabet[rng.integers(0, len(alphabet), size=size, dtype=index_type)]
     edges = np.cumsum(probabilities / np.sum(probabilities)) * 65536.0
     lut = alphabet[np.minimum(np.searchsorted(edges, np.arange(65536) + 0.5), len(alphabet) - 1)]
     return lut[rng.integers(0, 65536, size=size, dtype=np.uint16)]
@@ -87,6 +88,30 @@ def text_pairs(count, low, high, substitution_rate, indel_rate, seed=42):
     first = _letters(rng, PRINTABLE, int(offsets[-1]))
     second, second_offsets = _mutate(rng, first, offsets, PRINTABLE, substitution_rate, indel_rate)
     return (first, offsets), (second, second_offsets)
+
+
+CJK_FIRST, CJK_COUNT = 0x4E00, 3000  # the first 3,000 CJK unified ideographs: three UTF-8 bytes each
+
+
+def cjk_pairs(count, low, high, substitution_rate, indel_rate, seed=42):
+    """UTF-8 pairs of CJK text (3,000 code points, uniform) for UTF-8 Levenshtein over 16-bit codes: lengths in code
+    points; the returned tapes hold UTF-8 bytes, three per code point."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = rng.integers(low, high + 1, size=count)
+    offsets = _offsets(lengths)
+    alphabet = np.arange(CJK_COUNT, dtype=np.int64)
+    first = _letters(rng, alphabet, int(offsets[-1]))
+    second, second_offsets = _mutate(rng, first, offsets, alphabet, substitution_rate, indel_rate)
+
+    def encode(indices):
+        points = indices + CJK_FIRST
+        out = np.empty((points.shape[0], 3), dtype=np.uint8)
+        out[:, 0] = 0xE0 | (points >> 12)
+        out[:, 1] = 0x80 | ((points >> 6) & 0x3F)
+        out[:, 2] = 0x80 | (points & 0x3F)
+        return out.reshape(-1)
+
+    return (encode(first), offsets * 3), (encode(second), second_offsets * 3)
 
 
 def protein_pairs(count, median=350.0, sigma=0.6, low=50, high=2000, identity=0.70, indel_rate=0.02, seed=42):

@@ -24,6 +24,15 @@ def test_text_pairs_use_the_printable_bytes():
     assert np.array_equal(a, a2) and np.array_equal(b, b2)
 
 
+def test_cjk_pairs_are_utf8_of_the_ideographs():
+    (a, ao), (b, bo) = w.cjk_pairs(512, 100, 300, 0.05, 0.02, seed=3)
+    lengths = np.diff(ao) // 3
+    assert lengths.min() >= 100 and lengths.max() <= 300 and (np.diff(ao) % 3 == 0).all()
+    text = a[ao[0]:ao[1]].tobytes().decode("utf-8")
+    assert len(text) == lengths[0] and all(0x4E00 <= ord(c) < 0x4E00 + 3000 for c in text)
+    assert len(b[bo[0]:bo[1]].tobytes().decode("utf-8")) > 0
+
+
 def test_protein_pairs_lengths_and_identity():
     (a, ao), (b, bo) = w.protein_pairs(2000, seed=1)
     lengths = np.diff(ao)
