@@ -290,7 +290,9 @@ class HostBatch:
 def call_pairwise(engine, scope, batch):
     from stringzillas_gb300._native import lib
     err = ctypes.c_char_p()
-    fn = getattr(lib, f"szs_{engine._algo}_pairwise_u64tape")
+    # The Levenshtein pairwise entry point serves the UTF-8 engines too (no separate _utf8 pairwise symbol).
+    algo = "levenshtein_distances" if engine._algo.startswith("levenshtein_distances") else engine._algo
+    fn = getattr(lib, f"szs_{algo}_pairwise_u64tape")
     status = fn(engine.handle, scope.handle, ctypes.byref(batch.tapes[0]), ctypes.byref(batch.tapes[1]),
                 ctypes.c_void_p(batch.out.data_ptr()), ctypes.byref(err))
     if status != 0:
