@@ -589,8 +589,9 @@ static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &str
 static status_t finish_deferred(device_context_t *context, szs_gb300_stats_t &stats) noexcept;
 
 /**
- *  UTF-8 Levenshtein: rewrites both device-resident tapes as one-byte codes of their code points (see utf8.cu), in
- *  place of @p queries and @p candidates. A call may use at most 256 distinct code points.
+ *  UTF-8 Levenshtein: rewrites both device-resident tapes as codes of their code points (see utf8.cu), in place of
+ *  @p queries and @p candidates: one byte each for up to 256 distinct code points, else 16 bits each (@p wide). A
+ *  call may use at most 65,536 distinct code points.
  */
 static status_t transcode_utf8(device_context_t *context, cudaStream_t stream, tape_t &queries, tape_t &candidates,
                                bool has_candidates, bool &wide) noexcept {

@@ -36,21 +36,22 @@ cudaError_t launch_fingerprints(tape_t const &texts, fingerprint_dim_t const *pa
                                 std::uint32_t *hashes, std::uint64_t hashes_stride, std::uint32_t *counts,
                                 std::uint64_t counts_stride, int sm_count, cudaStream_t stream);
 
-/** The set of a batch's code points (UTF-8 Levenshtein): open addressing over `code point + 1` (0 = empty), then
- *  dense codes in slot order. */
-constexpr int rune_set_bits_k = 17; // 131,072 slots: room for 65,536 distinct code points at half load
-constexpr std::uint32_t rune_set_slots_k = 1u << rune_set_bits_k;
+/** The set of a batch's code points (UTF-8 Levenshtein) as a bitmap over every value the decoder can produce (lead
+ *  bytes give at most 21 bits), and the rank of each bitmap word: a code point's code is the number of distinct code
+ *  points below it. */
+constexpr int rune_bits_k = 21;
+constexpr std::uint32_t rune_words_k = (1u << rune_bits_k) / 32; // 65,536 words of 32 code points
 struct rune_set_t {
-    std::uint32_t keys[rune_set_slots_k];
-    std::uint32_t codes[rune_set_slots_k];
-    std::uint32_t symbols;  // distinct code points
-    std::uint32_t overflow; // set if an insertion found no free slot
+    std::uint32_t present[rune_words_k]; // bit (r & 31) of word r >> 5: code point r occurs in the batch
+    std::uint32_t rank[rune_words_k];    // distinct code points below word w's first
+    std::uint32_t symbols;               // distinct code points
+    std::uint32_t overflow;              // always 0: every decodable value has its bit
 };
-/** Counts each string's code points into `counts[i]` and inserts them into `set` (both zeroed by the caller);
+/** Counts each string's code points into `counts[i]` and marks them in `set` (both zeroed by the caller);
  *  `end` is the tape's last offset: a sequence cut off there reads zeros beyond it. */
 cudaError_t launch_utf8_count(tape_t const &tape, std::uint64_t end, std::uint64_t *counts, rune_set_t *set,
                               int sm_count, cudaStream_t stream);
-/** Numbers the set's occupied slots 0..symbols-1. */
+/** Ranks the set's bitmap words and counts the distinct code points (one CTA). */
 cudaError_t launch_utf8_codes(rune_set_t *set, cudaStream_t stream);
 /** Device scratch the exclusive scan of `count + 1` counts needs. */
 std::size_t utf8_scan_scratch_bytes(std::uint64_t count);
