@@ -16,7 +16,7 @@
  *  rarer code points are marked in the global bitmap directly); (2) one CTA ranks the bitmap's words, so a code
  *  point's code is the number of distinct code points below it; (3) after an exclusive scan of the counts, one warp
  *  per string writes its codes, each the word's rank plus a population count (the Basic Multilingual Plane's ranks and
- *  bits staged in shared memory, 16 KB). A warp decodes 32 bytes at once when the string is well formed
+ *  bits staged in shared memory, 16 KB). A warp decodes 128 bytes at once when the string is well formed
  *  (`warp_walk`), else its first lane walks the string with the sequential rule above.
  */
 #include <cub/device/device_scan.cuh>
@@ -50,67 +50,84 @@ __device__ __forceinline__ std::uint64_t tape_offset(tape_t const &tape, std::ui
 constexpr std::uint32_t plane_words_k = 65536 / 32; // the Basic Multilingual Plane's 2,048 bitmap words
 constexpr int utf8_threads_k = 128;
 
-__device__ __forceinline__ std::uint32_t tape_byte(tape_t const &tape, std::uint64_t end, std::uint64_t position) {
-    return position < end ? (std::uint32_t)tape.base[position] : 0u;
+/** Bit k (k < 4) set where byte k of `x` is a continuation byte (10xxxxxx). */
+__device__ __forceinline__ std::uint32_t continuation_bits(std::uint32_t x) {
+    std::uint32_t const tops = x & ~(x << 1) & 0x80808080u; // bit 7 of a byte: its bit 7 set and bit 6 clear
+    return ((tops >> 7) * 0x01020408u) >> 24;                // gather bits 0, 8, 16, 24 into bits 0..3
 }
 
 /**
- *  One warp walks the string [begin, stop) 32 bytes at a time, lanes on consecutive bytes (coalesced loads), and
- *  calls `visit(rune, index)` on the lane of each code point's lead byte, `index` counting code points from the
- *  string's start. This holds only when the string is well formed in the decoder's sense: its first byte is a lead
- *  byte and every lead byte's length covers exactly the continuation bytes (10xxxxxx) that follow it, ending at
- *  `stop`; then the code points start exactly at the lead bytes, as a sequential walk would find them. Returns
- *  false, warp-uniformly, as soon as a window breaks that (code points visited before stay visited: both passes
- *  then walk the whole string again sequentially). Sets `count` to the string's code points on success.
+ *  One warp walks the string [begin, stop) 128 bytes at a time, lane L on bytes 4L..4L+3 of each window (coalesced
+ *  loads), and calls `visit(rune, index)` once per code point, on the lane holding its lead byte, `index` counting
+ *  code points from the string's start. This holds only when the string is well formed in the decoder's sense: its
+ *  first byte is a lead byte and every lead byte's length covers exactly the continuation bytes (10xxxxxx) that follow
+ *  it, ending at `stop`; then the code points start exactly at the lead bytes, as a sequential walk would find them,
+ *  and no byte past `stop` is needed. Returns false, warp-uniformly, as soon as a window breaks that (code points
+ *  visited before stay visited: both passes then walk the whole string again sequentially), or for strings of 2^31
+ *  bytes or more. Sets `count` to the string's code points on success. Offsets inside the string are 32-bit and the
+ *  checks are mask arithmetic, without branches.
  */
 template <typename visit_>
-__device__ __forceinline__ bool warp_walk(tape_t const &tape, std::uint64_t end, std::uint64_t begin,
-                                          std::uint64_t stop, std::uint64_t &count, visit_ &&visit) {
+__device__ __forceinline__ bool warp_walk(tape_t const &tape, std::uint64_t begin, std::uint64_t stop,
+                                          std::uint64_t &count, visit_ &&visit) {
+    if (stop - begin >= (1ull << 31)) return false;
+    std::uint32_t const n = (std::uint32_t)(stop - begin);
+    std::uint8_t const *string = tape.base + begin;
     int const lane = threadIdx.x & 31;
-    auto is_continuation = [](std::uint32_t byte) { return (byte & 0xC0u) == 0x80u; };
+    std::uint32_t const lower = (1u << lane) - 1u;
     std::uint64_t runes = 0;
-    for (std::uint64_t window = begin; window < stop; window += 32) {
-        std::uint64_t const position = window + (std::uint64_t)lane;
-        std::uint32_t const here = tape_byte(tape, end, position);
-        std::uint32_t const ahead = lane < 4 ? tape_byte(tape, end, window + 32 + (std::uint64_t)lane) : 0u;
-        std::uint32_t following[5]; // bytes at position + 0 .. position + 4
-        following[0] = here;
+    for (std::uint32_t window = 0; window < n; window += 128) {
+        std::uint32_t const rel = window + 4u * (std::uint32_t)lane;
+        // This lane's four bytes, and the four after them (the next lane's, or the next window's for lane 31);
+        // bytes past the string read as 0 and never decide a well-formed string.
+        std::uint32_t own = 0, ahead = 0;
 #pragma unroll
-        for (int k = 1; k <= 4; ++k) {
-            std::uint32_t const inside = __shfl_sync(0xFFFFFFFFu, here, (lane + k) & 31);
-            std::uint32_t const beyond = __shfl_sync(0xFFFFFFFFu, ahead, (lane + k) & 31);
-            following[k] = lane + k < 32 ? inside : beyond;
+        for (std::uint32_t k = 0; k < 4; ++k) {
+            own |= (rel + k < n ? (std::uint32_t)string[rel + k] : 0u) << (8 * k);
+            if (lane == 0) ahead |= (window + 128 + k < n ? (std::uint32_t)string[window + 128 + k] : 0u) << (8 * k);
         }
-        bool const active = position < stop;
-        bool const lead = active && !is_continuation(here);
-        std::uint32_t const length = 1u + (here >= 0xC0u) + (here >= 0xE0u) + (here >= 0xF0u);
-        bool ok = !active || lead || position != begin; // the string starts on a lead byte
-        if (lead) {
-            ok = position + length <= stop;
+        std::uint32_t const next_lane = __shfl_sync(0xFFFFFFFFu, own, (lane + 1) & 31);
+        std::uint32_t const next_window = __shfl_sync(0xFFFFFFFFu, ahead, 0);
+        std::uint32_t const high = lane == 31 ? next_window : next_lane;
+        std::uint32_t const continuation = continuation_bits(own) | continuation_bits(high) << 4;
+
+        bool ok = !(rel == 0 && (continuation & 1u)); // the string starts on a lead byte
+        std::uint32_t leads = 0, lengths = 0;          // lengths: 4 bits per byte slot
 #pragma unroll
-            for (int k = 1; k < 4; ++k)
-                if ((std::uint32_t)k < length) ok = ok && is_continuation(following[k]);
-            std::uint32_t next = following[1];
-#pragma unroll
-            for (int k = 2; k <= 4; ++k)
-                if ((std::uint32_t)k == length) next = following[k];
-            ok = ok && (position + length == stop || !is_continuation(next));
+        for (std::uint32_t j = 0; j < 4; ++j) {
+            std::uint32_t const position = rel + j;
+            std::uint32_t const byte = (own >> (8 * j)) & 0xFFu;
+            bool const lead = position < n && !((continuation >> j) & 1u);
+            // Lead bytes' lengths from their leading ones: 0 -> 1, 2 -> 2, 3 -> 3, 4 or more -> 4.
+            std::uint32_t const length = min(max((std::uint32_t)__clz(~(byte << 24)), 1u), 4u);
+            std::uint32_t const needed = ((1u << (length - 1)) - 1u) << (j + 1);
+            bool const covered = position + length <= n && (continuation & needed) == needed &&
+                                 (position + length == n || !((continuation >> (j + length)) & 1u));
+            ok = ok && (!lead || covered);
+            leads |= (lead ? 1u : 0u) << j;
+            lengths |= length << (4 * j);
         }
         if (!__all_sync(0xFFFFFFFFu, ok)) return false;
-        std::uint32_t const leads = __ballot_sync(0xFFFFFFFFu, lead);
-        if (lead) {
-            std::uint32_t rune;
-            switch (length) {
-            case 1: rune = here; break;
-            case 2: rune = (here & 0x1Fu) << 6 | (following[1] & 0x3Fu); break;
-            case 3: rune = (here & 0x0Fu) << 12 | (following[1] & 0x3Fu) << 6 | (following[2] & 0x3Fu); break;
-            default:
-                rune = (here & 0x07u) << 18 | (following[1] & 0x3Fu) << 12 | (following[2] & 0x3Fu) << 6 |
-                       (following[3] & 0x3Fu);
-            }
-            visit(rune, runes + (std::uint64_t)__popc(leads & ((1u << lane) - 1u)));
+        std::uint32_t before = 0, total = 0; // code points of lower lanes in this window, and of the whole window
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            std::uint32_t const slot = __ballot_sync(0xFFFFFFFFu, (leads >> j) & 1u);
+            before += __popc(slot & lower), total += __popc(slot);
         }
-        runes += (std::uint64_t)__popc(leads);
+#pragma unroll
+        for (std::uint32_t j = 0; j < 4; ++j) {
+            if (!((leads >> j) & 1u)) continue;
+            std::uint32_t const word = __funnelshift_r(own, high, 8 * j); // bytes j..j+3
+            std::uint32_t const length = (lengths >> (4 * j)) & 0xFu;
+            std::uint32_t const b0 = word & 0xFFu, c1 = (word >> 8) & 0x3Fu, c2 = (word >> 16) & 0x3Fu,
+                                c3 = (word >> 24) & 0x3Fu;
+            std::uint32_t const rune = length == 1   ? b0
+                                       : length == 2 ? (b0 & 0x1Fu) << 6 | c1
+                                       : length == 3 ? (b0 & 0x0Fu) << 12 | c1 << 6 | c2
+                                                     : (b0 & 0x07u) << 18 | c1 << 12 | c2 << 6 | c3;
+            visit(rune, runes + before + (std::uint64_t)__popc(leads & ((1u << j) - 1u)));
+        }
+        runes += total;
     }
     count = runes;
     return true;
@@ -136,7 +153,7 @@ __global__ void __launch_bounds__(utf8_threads_k) utf8_count_kernel(tape_t const
          i += warps) {
         std::uint64_t const begin = tape_offset(tape, i), stop = tape_offset(tape, i + 1);
         std::uint64_t runes = 0;
-        bool const walked = warp_walk(tape, end, begin, stop, runes,
+        bool const walked = warp_walk(tape, begin, stop, runes,
                                       [&](std::uint32_t rune, std::uint64_t) { mark(rune); });
         if (!walked && lane == 0) { // the decoder's sequential rule, as the reference applies it
             runes = 0;
@@ -153,36 +170,38 @@ __global__ void __launch_bounds__(utf8_threads_k) utf8_count_kernel(tape_t const
         if (plane_s[k]) atomicOr(&set->present[k], plane_s[k]);
 }
 
-/** Pass 2: the rank of every bitmap word and the number of distinct code points (one CTA of 1,024 threads, each
- *  over 64 consecutive words). */
+/** Pass 2: the rank of every bitmap word and the number of distinct code points (one CTA of 32 warps, each over a
+ *  contiguous block of 2,048 words read 32 consecutive words at a time). */
 __global__ void __launch_bounds__(1024) utf8_codes_kernel(rune_set_t *__restrict__ set) {
-    constexpr int threads = 1024;
-    constexpr int per_thread = rune_words_k / threads;
-    static_assert(per_thread % 4 == 0, "words are read four at a time");
-    __shared__ std::uint32_t scan[threads];
-    int const t = threadIdx.x;
-    auto const *words = reinterpret_cast<uint4 const *>(set->present + t * per_thread);
-    std::uint32_t own = 0;
-#pragma unroll 4
-    for (int k = 0; k < per_thread / 4; ++k) {
-        uint4 const w = words[k];
-        own += __popc(w.x) + __popc(w.y) + __popc(w.z) + __popc(w.w);
-    }
-    scan[t] = own;
+    constexpr int warps = 32;
+    constexpr std::uint32_t per_warp = rune_words_k / warps;
+    __shared__ std::uint32_t warp_totals[warps];
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    std::uint32_t const *present = set->present + warp * per_warp;
+    std::uint32_t *rank = set->rank + warp * per_warp;
+    std::uint32_t sum = 0;
+    for (std::uint32_t k = lane; k < per_warp; k += 32) sum += __popc(present[k]);
+    sum = __reduce_add_sync(0xFFFFFFFFu, sum);
+    if (lane == 0) warp_totals[warp] = sum;
     __syncthreads();
-    for (int offset = 1; offset < threads; offset <<= 1) {
-        std::uint32_t const add = t >= offset ? scan[t - offset] : 0u;
-        __syncthreads();
-        scan[t] += add;
-        __syncthreads();
+    std::uint32_t offset = 0; // distinct code points in the blocks before this warp's
+    for (int w = 0; w < warp; ++w) offset += warp_totals[w];
+    for (std::uint32_t base = 0; base < per_warp; base += 32) {
+        std::uint32_t const own = __popc(present[base + lane]);
+        std::uint32_t scan = own; // inclusive over the 32 words
+#pragma unroll
+        for (int distance = 1; distance < 32; distance <<= 1) {
+            std::uint32_t const lower = __shfl_up_sync(0xFFFFFFFFu, scan, distance);
+            if (lane >= distance) scan += lower;
+        }
+        rank[base + lane] = offset + scan - own;
+        offset += __shfl_sync(0xFFFFFFFFu, scan, 31);
     }
-    std::uint32_t rank = scan[t] - own;
-    for (int k = 0; k < per_thread; ++k) {
-        std::uint32_t const word = t * per_thread + k;
-        set->rank[word] = rank;
-        rank += __popc(set->present[word]);
+    if (threadIdx.x == 0) {
+        std::uint32_t symbols = 0;
+        for (int w = 0; w < warps; ++w) symbols += warp_totals[w];
+        set->symbols = symbols;
     }
-    if (t == threads - 1) set->symbols = scan[t];
 }
 
 /** Pass 3: each string's codes at its scanned offset (one byte each, or two for more than 256 code points): one warp
@@ -207,7 +226,7 @@ __global__ void __launch_bounds__(utf8_threads_k)
         std::uint64_t const begin = tape_offset(tape, i), stop = tape_offset(tape, i + 1);
         code_type_ *target = out + offsets[i];
         std::uint64_t runes = 0;
-        bool const walked = warp_walk(tape, end, begin, stop, runes, [&](std::uint32_t rune, std::uint64_t index) {
+        bool const walked = warp_walk(tape, begin, stop, runes, [&](std::uint32_t rune, std::uint64_t index) {
             target[index] = (code_type_)code_of(rune);
         });
         if (!walked && lane == 0) // the decoder's sequential rule, as the reference applies it
