@@ -142,9 +142,7 @@ __global__ void __launch_bounds__(utf8_threads_k) utf8_count_kernel(tape_t const
     __syncthreads();
     auto mark = [&](std::uint32_t rune) {
         std::uint32_t const bit = 1u << (rune & 31u);
-        if (rune < 65536u) {
-            if (!(plane_s[rune >> 5] & bit)) atomicOr(&plane_s[rune >> 5], bit);
-        }
+        if (rune < 65536u) atomicOr(&plane_s[rune >> 5], bit);
         else atomicOr(&set->present[rune >> 5], bit);
     };
     int const lane = threadIdx.x & 31;
