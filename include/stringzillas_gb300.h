@@ -469,6 +469,10 @@ typedef struct szs_gb300_tuning_t {
         pairs each) give pairs whose shorter side exceeds this a band instead, whatever the two thresholds above say
         (0 = 1,024): a band spreads one pair over a CTA's warps, where the wavefront would leave SMs idle. */
     sz_u32_t band_min_rows_few;
+    /** The 16-bit band threshold for Levenshtein pairs scored by comparing codes (more than 32 byte values, or UTF-8
+        over more than 256 code points) instead of `band_min_rows_packed` (0 = 2,048: on text the band overtakes the
+        wavefront only past about 2,000 rows). */
+    sz_u32_t band_min_rows_compare;
 } szs_gb300_tuning_t;
 
 /** Installs @p tuning on @p engine (NULL restores the built-in choices); out-of-range values are rejected with

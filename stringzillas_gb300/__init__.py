@@ -357,14 +357,15 @@ class _Engine:
     def set_tuning(self, tuning=None):
         """Extension: per-length-bin choices (see ``szs_gb300_tuning_t``): a dict with any of ``packed_rows`` (16
         values), ``cell_bits`` (16 values), ``band_min_rows``, ``packed_warps`` (4 values),
-        ``band_min_rows_packed``, ``pipeline_chunk_kb``, ``packed_step_cost`` (4 values) and ``band_min_rows_few``;
-        None restores the built-in choices."""
+        ``band_min_rows_packed``, ``pipeline_chunk_kb``, ``packed_step_cost`` (4 values), ``band_min_rows_few`` and
+        ``band_min_rows_compare``; None restores the built-in choices."""
         err = ctypes.c_char_p()
         if tuning is None:
             status = lib.szs_gb300_engine_set_tuning(self.handle, None, ctypes.byref(err))
         else:
             unknown = set(tuning) - {"packed_rows", "cell_bits", "band_min_rows", "packed_warps", "band_min_rows_packed",
-                                     "pipeline_chunk_kb", "packed_step_cost", "band_min_rows_few"}
+                                     "pipeline_chunk_kb", "packed_step_cost", "band_min_rows_few",
+                                     "band_min_rows_compare"}
             if unknown:
                 raise ValueError(f"unknown tuning fields {sorted(unknown)}")
             t = _native.Tuning()
@@ -377,6 +378,7 @@ class _Engine:
             t.band_min_rows_packed = int(tuning.get("band_min_rows_packed", 0))
             t.pipeline_chunk_kb = int(tuning.get("pipeline_chunk_kb", 0))
             t.band_min_rows_few = int(tuning.get("band_min_rows_few", 0))
+            t.band_min_rows_compare = int(tuning.get("band_min_rows_compare", 0))
             status = lib.szs_gb300_engine_set_tuning(self.handle, ctypes.byref(t), ctypes.byref(err))
         _native.raise_for(status, err.value, "set_tuning")
 
@@ -389,7 +391,8 @@ class _Engine:
         return {"packed_rows": list(t.packed_rows), "cell_bits": list(t.cell_bits),
                 "band_min_rows": t.band_min_rows, "packed_warps": list(t.packed_warps),
                 "band_min_rows_packed": t.band_min_rows_packed, "pipeline_chunk_kb": t.pipeline_chunk_kb,
-                "packed_step_cost": list(t.packed_step_cost), "band_min_rows_few": t.band_min_rows_few}
+                "packed_step_cost": list(t.packed_step_cost), "band_min_rows_few": t.band_min_rows_few,
+                "band_min_rows_compare": t.band_min_rows_compare}
 
     def stats(self) -> dict:
         """Extension: counters of the last call (device time, cells, pairs, launches)."""

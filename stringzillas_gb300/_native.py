@@ -151,6 +151,7 @@ class Tuning(ctypes.Structure):
         ("pipeline_chunk_kb", ctypes.c_uint32),
         ("packed_step_cost", ctypes.c_uint16 * 4),
         ("band_min_rows_few", ctypes.c_uint32),
+        ("band_min_rows_compare", ctypes.c_uint32),
     ]
 
 

@@ -746,6 +746,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     args.band_min_rows = engine.tuning.band_min_rows ? engine.tuning.band_min_rows : (std::uint32_t)band_min_rows_k;
     args.band_min_rows_packed = engine.tuning.band_min_rows_packed ? engine.tuning.band_min_rows_packed
                                                                    : (std::uint32_t)band_min_rows_packed_k;
+    args.band_min_rows_compare = engine.tuning.band_min_rows_compare ? engine.tuning.band_min_rows_compare
+                                                                     : (std::uint32_t)band_min_rows_compare_k;
     // A batched call with fewer pairs than one wave of the 16x2 route (two pairs per warp, about 16 resident warps
     // per SM) would leave SMs idle on the wavefront: its longer pairs spread over a band CTA's warps instead.
     if (schedule != szs_gb300_schedule_plain_k && args.pairs < 32ull * (std::uint64_t)context->sm_count) {
@@ -753,6 +755,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                                                   : (std::uint32_t)band_min_rows_few_k;
         args.band_min_rows = std::min(args.band_min_rows, few);
         args.band_min_rows_packed = std::min(args.band_min_rows_packed, few);
+        args.band_min_rows_compare = std::min(args.band_min_rows_compare, few);
     }
     for (int choice = 0; choice < 4; ++choice)
         args.packed_step_cost[choice] = engine.tuning.packed_step_cost[choice]

@@ -114,7 +114,9 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     bool const compare_fits = args.kind == kind_levenshtein_k && (args.alphabet != nullptr || args.wide);
     bool const packed = args.packed_allowed && (profile_fits || compare_fits) && reach16 < 32767 &&
                         args.cell_bits[length_class] != 32;
-    std::uint64_t const band_rows = packed ? args.band_min_rows_packed : args.band_min_rows;
+    std::uint64_t const band_rows = !packed        ? args.band_min_rows
+                                    : profile_fits ? args.band_min_rows_packed
+                                                   : args.band_min_rows_compare;
     // Local scores with non-positive gaps take the 16-bit band even beyond their proven bound: the kernel checks the
     // running maximum against the 16-bit limit and scores a pair that reached it again on 32-bit cells.
     bool const local_band16 =

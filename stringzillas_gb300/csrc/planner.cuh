@@ -45,6 +45,7 @@ constexpr int band_min_rows_k = 1024;        // default: 32-bit pairs whose shor
 constexpr int packed_step_cost_k[4] = {100, 165, 245, 330};
 constexpr int band_min_rows_packed_k = 2048; // default for pairs that fit 16-bit cells (the 16-bit band above it)
 constexpr int band_min_rows_few_k = 1024;    // default for calls with fewer pairs than one 16x2 wave (32 per SM)
+constexpr int band_min_rows_compare_k = 2048; // default for compare-mode Levenshtein pairs on 16-bit cells
 constexpr int myers_max_words_k = 16;
 constexpr int myers_wide_max_words_k = 8; // 16-bit codes take 16 code planes: the thread route stops at 8 words
 // Words per lane of the warp kernel: patterns up to 32 * 32 * 8 = 8,192 rows. Longer ones take the bands: a pair of
@@ -93,6 +94,7 @@ struct plan_args_t {
     std::uint32_t band_min_rows;      // shorter sides above this take the band (pairs on 32-bit cells)
     std::uint32_t band_min_rows_packed; // the same for pairs that fit 16-bit cells
     std::uint16_t packed_step_cost[4];  // relative cost of one lane step with 4, 8, 12, 16 rows per lane
+    std::uint32_t band_min_rows_compare; // the same for compare-mode Levenshtein pairs (no profile)
 };
 
 /** Per-bin counters the planner fills. */

@@ -306,7 +306,7 @@ def test_levenshtein_compare_mode(szs, port, rows, costs):
     second[5] = first[5][:200] + second[5][200:]  # a long shared stretch
     engine = szs.LevenshteinDistances(*costs)
     engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 4096, "band_min_rows_packed": 4096,
-                       "band_min_rows_few": 4096})
+                       "band_min_rows_few": 4096, "band_min_rows_compare": 4096})
     want = port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
@@ -551,7 +551,7 @@ def test_band16_compare_mode(szs, port, costs):
     first[3] = bytes(rng.choice(np.array([0, 255, 65], dtype=np.uint8), size=1025))
     second[3] = bytes(rng.choice(np.array([0, 255, 66], dtype=np.uint8), size=1300))
     engine = szs.LevenshteinDistances(*costs)
-    engine.set_tuning({"band_min_rows_packed": 600})
+    engine.set_tuning({"band_min_rows_packed": 600, "band_min_rows_compare": 600})
     want = port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
@@ -717,7 +717,7 @@ def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
     second[-3] = first[-3][:500] + second[-3][500:]
     engine = szs.LevenshteinDistancesUTF8(*costs)
     engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600,
-                       "band_min_rows_few": 600})
+                       "band_min_rows_few": 600, "band_min_rows_compare": 600})
     want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
@@ -765,7 +765,7 @@ def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
     second[-3] = first[-3][:500] + second[-3][500:]
     engine = szs.LevenshteinDistancesUTF8(*costs)
     engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600,
-                       "band_min_rows_few": 600})
+                       "band_min_rows_few": 600, "band_min_rows_compare": 600})
     want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
