@@ -183,9 +183,10 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
         measurements[f"warps per CTA, R={rows}"] = {str(w_): cells / (ms * 1e6) for w_, ms in timings.items()}
         log(f"  {family:10s} R={rows:2d}: warps per CTA {best} "
             + " ".join(f"{w_}={cells / (ms * 1e6):7.0f}" for w_, ms in timings.items()))
-    # Band thresholds on batches of long pairs (shorter sides log-uniform in [256, 8192]): first for pairs on
-    # 32-bit cells (16-bit cells switched off while measuring), then for pairs that fit 16-bit cells.
-    count = 512
+    # Band thresholds on a full wave of long pairs (shorter sides log-uniform in [256, 8192]; calls with fewer pairs
+    # than 32 per SM follow `band_min_rows_few` instead, switched off here): first for pairs on 32-bit cells (16-bit
+    # cells switched off while measuring), then for pairs that fit 16-bit cells.
+    count = 8192
     lengths = [np.exp(rng.uniform(np.log(256), np.log(8192), size=count)).astype(np.int64) for _ in range(2)]
     tapes = []
     for lens in lengths:
@@ -200,7 +201,7 @@ def tune_family(szs, make_engine, family, rng, target_cells=4e9, log=print):
             ("band_min_rows_packed", PACKED_BAND_THRESHOLDS, dict(table))):
         timings = {}
         for threshold in thresholds:
-            engine.set_tuning(dict(trial_base, **{field: threshold}))
+            engine.set_tuning(dict(trial_base, band_min_rows_few=1 << 30, **{field: threshold}))
             timings[threshold] = _time(engine, tapes[0], tapes[1], out, repeats=2)
         best = min(timings, key=timings.get)
         table[field] = best
