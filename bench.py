@@ -96,8 +96,21 @@ def parse_args():
     return parser.parse_args()
 
 
+def _workloads_module():
+    """The seeded generators, loaded from their file alone: importing the package would load the engine's library,
+    which the CPU arm (``--impl reference``) must not map."""
+    import importlib.util
+    name = "szs_bench_workloads"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, os.path.join(HERE, "stringzillas_gb300", "workloads.py"))
+        module = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(module)
+        sys.modules[name] = module
+    return sys.modules[name]
+
+
 def make_workload(name, seed):
-    from stringzillas_gb300 import workloads as w
+    w = _workloads_module()
     if name == "c1":
         first, second = w.levenshtein_reads(1024, 64, 256, 0.05, 0.02, seed=seed)
         return first, second, ("lev", None)
@@ -151,9 +164,21 @@ def make_engine(kind_and_tables):
     return engine
 
 
+TUNING_TABLE = os.path.join("stringzillas_gb300", "tuning", "gb300.json")
+
+
 def tuning_source():
-    from stringzillas_gb300 import autotune
-    return "autotuned table " + os.path.relpath(autotune.DEFAULT_TABLE, HERE) if autotune.load() else "built-in"
+    # Read from the file path (not through the package) so both arms print the same key without loading the engine.
+    return "autotuned table " + TUNING_TABLE if os.path.exists(os.path.join(HERE, TUNING_TABLE)) else "built-in"
+
+
+def workload_config(name, first, second, world):
+    """The ``config`` object both arms print for a workload."""
+    cells = int(np.dot(np.diff(first[1]).astype(np.int64), np.diff(second[1]).astype(np.int64)))
+    return {"workload": WORKLOADS[name], "pairs": len(first[1]) - 1, "cells_per_step": cells,
+            "input_bytes_per_step": int(first[0].shape[0] + second[0].shape[0]), "tuning": tuning_source(),
+            "l2": "inputs larger than L2 (129 MB), no flush between steps",
+            "parallelism": f"pairs: each of {world} ranks scores its own batch, no collective"}
 
 
 def oracle_costs(kind_and_tables):
@@ -541,12 +566,13 @@ def run_reference(args):
         if step >= args.warmup:
             values.append(baseline["value"])
     value = statistics.median(values)
-    cells = int(np.dot(np.diff(first[1]).astype(np.int64), np.diff(second[1]).astype(np.int64)))
+    config = workload_config(args.workload, first, second, int(os.environ.get("WORLD_SIZE", "1")))
+    cells = config["cells_per_step"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / (value * 1e9) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit-vectors / int64",
-        "data": "synthetic (seeded)", "config": {"workload": WORKLOADS[args.workload], "pairs": len(first[1]) - 1},
+        "data": "synthetic (seeded numpy PCG64)", "config": config,
         "cpu_baseline": dict(baseline, value=value),
         "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -623,10 +649,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": {"lev": "u32", "levc": "int16x2", "levu": "int16x2"}.get(kind_and_tables[0], "int32"),
             "data": "synthetic (seeded numpy PCG64)",
-            "config": {"workload": WORKLOADS[args.workload], "pairs": pairs, "cells_per_step": cells_per_step,
-                       "input_bytes_per_step": input_bytes, "tuning": tuning_source(),
-                       "l2": "inputs larger than L2 (129 MB), no flush between steps",
-                       "parallelism": f"pairs: each of {world} ranks scores its own batch, no collective"},
+            "config": workload_config(args.workload, first, second, world),
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved_gbs / hbm_peak, "traffic": DRAM_TRAFFIC_PER_STEP.get(args.workload),
                          "traffic_unit": "bytes per step (all scoring launches of one step)",

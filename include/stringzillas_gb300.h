@@ -473,6 +473,11 @@ typedef struct szs_gb300_tuning_t {
         over more than 256 code points) instead of `band_min_rows_packed` (0 = 2,048: on text the band overtakes the
         wavefront only past about 2,000 rows). */
     sz_u32_t band_min_rows_compare;
+    /** Polls (about 100 ns each) before a band kernel's wait for the strip above gives up, raises the call's error
+        and abandons the pair; group barriers get four times as many (0 = 4,194,304, about 0.4 s, and 3 s at a
+        barrier). Values above the built-in bounds are clamped to them, so every wait stays bounded; small values
+        only make calls with long pairs fail early with `sz_status_unknown_k` (a wait that gives up never faults). */
+    sz_u32_t band_wait_polls;
 } szs_gb300_tuning_t;
 
 /** Installs @p tuning on @p engine (NULL restores the built-in choices); out-of-range values are rejected with
@@ -494,13 +499,16 @@ SZS_GB300_API sz_status_t szs_gb300_engine_get_stats(void *engine, szs_gb300_sta
  *  in the reference. For callers that cannot call `cudaMalloc` / `cudaFree` - for example a host application whose
  *  own allocator already reserves the device memory, or a latency-bound loop that cannot afford the device-wide
  *  synchronisation of `cudaFree`.
- *  - Tapes (data and offsets) and `results` must already be in device or managed memory, else
- *    `sz_device_memory_mismatch_k`. The engine's staging buffers are not used.
+ *  - Tapes (data and offsets, non-null) and `results` must already be in the scope device's memory or in managed
+ *    memory, else `sz_device_memory_mismatch_k`. The engine's staging buffers are not used.
  *  - Scratch comes from a fixed 16 MiB (+ 256 B) device array inside the library, held by every GPU that loads it
  *    until exit. A pair whose two sides both exceed 256 bytes must have both sides below 2,048 bytes; longer ones
- *    fail the call with `sz_overflow_risk_k` (other pairs' results are still written).
- *  - The first call on each device resolves the array's address with that device current; make that first call
- *    before any stream capture. Every call shares the array: calls whose kernels overlap on the GPU race.
+ *    fail the call with `sz_overflow_risk_k`. The other pairs' results are still written, and every rejected pair's
+ *    slot is set to 0 (which is also a valid score: check the status).
+ *  - The first call on each device resolves the array's address with that device current and keeps it; make that
+ *    first call before any stream capture, and do not use this entry point across a `cudaDeviceReset` of the device.
+ *    Every call shares the array: calls whose kernels overlap on the GPU race.
+ *  - The calling thread's current device is the same after the call as before it.
  *  The default scope runs on the legacy default stream; GPU scopes use their own stream. Synchronous, like the rest.
  */
 SZS_GB300_API sz_status_t szs_gb300_score_pairwise_noalloc_u64tape(void *engine, szs_device_scope_t device,

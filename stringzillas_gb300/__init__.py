@@ -357,15 +357,16 @@ class _Engine:
     def set_tuning(self, tuning=None):
         """Extension: per-length-bin choices (see ``szs_gb300_tuning_t``): a dict with any of ``packed_rows`` (16
         values), ``cell_bits`` (16 values), ``band_min_rows``, ``packed_warps`` (4 values),
-        ``band_min_rows_packed``, ``pipeline_chunk_kb``, ``packed_step_cost`` (4 values), ``band_min_rows_few`` and
-        ``band_min_rows_compare``; None restores the built-in choices."""
+        ``band_min_rows_packed``, ``pipeline_chunk_kb``, ``packed_step_cost`` (4 values), ``band_min_rows_few``,
+        ``band_min_rows_compare`` and ``band_wait_polls`` (the band kernels' wait bound, clamped to the built-in
+        one); None restores the built-in choices."""
         err = ctypes.c_char_p()
         if tuning is None:
             status = lib.szs_gb300_engine_set_tuning(self.handle, None, ctypes.byref(err))
         else:
             unknown = set(tuning) - {"packed_rows", "cell_bits", "band_min_rows", "packed_warps", "band_min_rows_packed",
                                      "pipeline_chunk_kb", "packed_step_cost", "band_min_rows_few",
-                                     "band_min_rows_compare"}
+                                     "band_min_rows_compare", "band_wait_polls"}
             if unknown:
                 raise ValueError(f"unknown tuning fields {sorted(unknown)}")
             t = _native.Tuning()
@@ -379,6 +380,7 @@ class _Engine:
             t.pipeline_chunk_kb = int(tuning.get("pipeline_chunk_kb", 0))
             t.band_min_rows_few = int(tuning.get("band_min_rows_few", 0))
             t.band_min_rows_compare = int(tuning.get("band_min_rows_compare", 0))
+            t.band_wait_polls = int(tuning.get("band_wait_polls", 0))
             status = lib.szs_gb300_engine_set_tuning(self.handle, ctypes.byref(t), ctypes.byref(err))
         _native.raise_for(status, err.value, "set_tuning")
 
@@ -392,7 +394,7 @@ class _Engine:
                 "band_min_rows": t.band_min_rows, "packed_warps": list(t.packed_warps),
                 "band_min_rows_packed": t.band_min_rows_packed, "pipeline_chunk_kb": t.pipeline_chunk_kb,
                 "packed_step_cost": list(t.packed_step_cost), "band_min_rows_few": t.band_min_rows_few,
-                "band_min_rows_compare": t.band_min_rows_compare}
+                "band_min_rows_compare": t.band_min_rows_compare, "band_wait_polls": t.band_wait_polls}
 
     def stats(self) -> dict:
         """Extension: counters of the last call (device time, cells, pairs, launches)."""

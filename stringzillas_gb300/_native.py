@@ -28,6 +28,17 @@ class U64Tape(ctypes.Structure):
     _fields_ = [("data", c_void_p), ("offsets", c_void_p), ("count", c_size_t)]
 
 
+# ``sz_sequence_member_start_t`` / ``sz_sequence_member_length_t``: (handle, index) -> start pointer / length.
+SequenceStart = ctypes.CFUNCTYPE(c_void_p, c_void_p, c_size_t)
+SequenceLength = ctypes.CFUNCTYPE(c_size_t, c_void_p, c_size_t)
+
+
+class Sequence(ctypes.Structure):
+    """``sz_sequence_t``: strings reached through two callbacks."""
+    _fields_ = [("handle", c_void_p), ("count", c_size_t), ("get_start", SequenceStart),
+                ("get_length", SequenceLength)]
+
+
 class Stats(ctypes.Structure):
     """``szs_gb300_stats_t``"""
     _fields_ = [
@@ -152,6 +163,7 @@ class Tuning(ctypes.Structure):
         ("packed_step_cost", ctypes.c_uint16 * 4),
         ("band_min_rows_few", ctypes.c_uint32),
         ("band_min_rows_compare", ctypes.c_uint32),
+        ("band_wait_polls", ctypes.c_uint32),
     ]
 
 

@@ -13,7 +13,7 @@
  *  Progress: ring slot s holds one 64-bit word in shared memory, `(strip + 1) << 32 | columns written`. Slots are
  *  reused every W strips, so the word only grows; a consumer of strip k - 1's row waits until the word reaches
  *  `k << 32 | columns needed`. Only warps of the same CTA wait on each other (co-resident by construction), and every
- *  wait is bounded: after `band_wait_limit_k` polls the warp raises the CTA's error flag, which also releases the
+ *  wait is bounded: after `costs.wait_polls` polls (at most `band_wait_polls_default_k`) the warp raises the CTA's error flag, which also releases the
  *  other warps' waits, the pair is abandoned and the host reports an error for the call.
  *
  *  Groups: when a call has fewer long pairs than the GPU holds CTAs, G co-resident CTAs (one cooperative launch)
@@ -35,7 +35,6 @@
 namespace szs_gb300 {
 
 constexpr int band_warps_k = 8;
-constexpr std::uint32_t band_wait_limit_k = 1u << 22; // polls of ~100 ns each, about 0.4 s
 constexpr int band_chunk_k = 32;                      // columns staged and published at a time
 
 template <int kind_, bool affine_, int rows_per_lane_>
@@ -90,10 +89,11 @@ struct band_ring_t {
     int members;
     int member;
     bool grid_scope; // progress and failure words are in global memory, shared with other CTAs
+    std::uint32_t wait_polls; // polls before a wait gives up
 };
 
-__device__ __forceinline__ band_ring_t band_cta_ring(band_shared_t &shared, int warp) {
-    return {shared.progress, &shared.failed, band_warps_k, warp, false};
+__device__ __forceinline__ band_ring_t band_cta_ring(band_shared_t &shared, int warp, std::uint32_t wait_polls) {
+    return {shared.progress, &shared.failed, band_warps_k, warp, false, wait_polls};
 }
 
 /** Lane 0 of a warp waits (bounded) until ring slot `slot` has reached `target`; the warp then proceeds together. */
@@ -109,7 +109,7 @@ __device__ __forceinline__ bool band_wait(band_ring_t const &ring, int slot, uns
                 ok = 0;
                 break;
             }
-            if (++polls > band_wait_limit_k) {
+            if (++polls > ring.wait_polls) {
                 atomicExch(ring.failed, 1u);
                 ok = 0;
                 break;
@@ -133,7 +133,6 @@ __device__ __forceinline__ void band_publish(band_ring_t const &ring, int slot, 
 /** Most CTAs one long pair can share, and the ring words of a group. */
 constexpr int band_group_max_ctas_k = 16;
 constexpr int band_group_max_members_k = band_group_max_ctas_k * band_warps_k;
-constexpr std::uint32_t band_barrier_limit_k = 1u << 24; // polls of ~200 ns each, about 3 s
 
 /** One pass over a pair (16-bit or 32-bit cells): ring progress and the combined result. */
 struct band_pass_state_t {
@@ -153,7 +152,7 @@ struct band_group_state_t {
 /** Bounded barrier of the G CTAs of a group: the `number`-th meeting needs G * number arrivals. Returns false when the
  *  group failed or the wait ran out (then the group's failure flag is set). */
 __device__ __forceinline__ bool band_group_barrier(band_group_state_t *group, int ctas, std::uint32_t number,
-                                                   std::uint32_t &flag_in_shared) {
+                                                   std::uint32_t &flag_in_shared, std::uint32_t barrier_polls) {
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -166,7 +165,7 @@ __device__ __forceinline__ bool band_group_barrier(band_group_state_t *group, in
                 ok = 0;
                 break;
             }
-            if (++polls > band_barrier_limit_k) {
+            if (++polls > barrier_polls) {
                 atomicExch(&group->failed, 1u);
                 ok = 0;
                 break;
@@ -428,7 +427,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         std::uint32_t const index = shared.pair_index;
         if (index >= count) break;
         pair_task_t const task = tasks[begin + index];
-        std::int32_t const value = band_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp), ring,
+        std::int32_t const value = band_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp, costs_s.wait_polls), ring,
                                                             ring_cells_per_slot, profiles + warp * profile_bytes,
                                                             chunks[warp], table_s);
         if (lane == 0) shared.warp_result[warp] = value;
@@ -508,16 +507,17 @@ __global__ void __launch_bounds__(band_warps_k * 32)
     std::uint32_t barriers = 0, iteration = 0;
     for (std::uint32_t index = (std::uint32_t)group; index < count; index += (std::uint32_t)groups, ++iteration) {
         int const parity = int(iteration & 1u);
-        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate, costs_s.barrier_polls)) break;
         if (rank == 0) band_group_reset(state, parity ^ 1, members);
         pair_task_t const task = tasks[begin + index];
         band_pass_state_t &pass = state->pass[parity][0];
-        band_ring_t const sync {pass.progress, &state->failed, members, rank * band_warps_k + warp, true};
+        band_ring_t const sync {pass.progress, &state->failed, members, rank * band_warps_k + warp, true,
+                                costs_s.wait_polls};
         std::int32_t const value = band_score_warp<policy_>(task, costs_s, sync, ring, ring_cells_per_slot,
                                                             profiles + warp * profile_bytes, chunks[warp], table_s);
         std::uint32_t const strips = (task.rows_length + policy_::strip_rows_k - 1) / policy_::strip_rows_k;
         band_group_contribute<policy_::local_k>(pass, value, (int)((strips - 1) % (std::uint32_t)members) == sync.member);
-        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate, costs_s.barrier_polls)) break;
         if (rank == 0 && threadIdx.x == 0)
             results[task.slot] = *reinterpret_cast<volatile std::int32_t *>(&pass.best);
     }

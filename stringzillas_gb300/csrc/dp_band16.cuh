@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         std::uint32_t const index = shared.pair_index;
         if (index >= count) break;
         pair_task_t const task = tasks[begin + index];
-        std::int32_t const value = band16_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp), ring,
+        std::int32_t const value = band16_score_warp<policy_>(task, costs_s, band_cta_ring(shared, warp, costs_s.wait_polls), ring,
                                                               ring_words_per_slot, profiles + warp * profile_bytes,
                                                               chunks[warp]);
         if (lane == 0) shared.warp_result[warp] = value;
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
                 static_assert(sizeof(band_chunk_t) <= sizeof(band16_chunk_t), "chunk staging must fit");
                 std::size_t const wide_profile = (std::size_t)band_profile_bytes_per_warp<wide_t>(costs.classes);
                 std::int32_t const wide = band_score_warp<wide_t>(
-                    task, costs_s, band_cta_ring(shared, warp), reinterpret_cast<std::int32_t *>(ring),
+                    task, costs_s, band_cta_ring(shared, warp, costs_s.wait_polls), reinterpret_cast<std::int32_t *>(ring),
                     2 * ring_words_per_slot, profiles + warp * wide_profile,
                     *reinterpret_cast<band_chunk_t *>(&chunks[warp]));
                 if (lane == 0) shared.warp_result[warp] = wide;
@@ -443,13 +443,13 @@ __global__ void __launch_bounds__(band_warps_k * 32)
     std::uint32_t barriers = 0, iteration = 0;
     for (std::uint32_t index = (std::uint32_t)group; index < count; index += (std::uint32_t)groups, ++iteration) {
         int const parity = int(iteration & 1u);
-        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate, costs_s.barrier_polls)) break;
         if (rank == 0) band_group_reset(state, parity ^ 1, members);
         pair_task_t const task = tasks[begin + index];
         int const member = rank * band_warps_k + warp;
         band_pass_state_t *pass = &state->pass[parity][0];
         {
-            band_ring_t const sync {pass->progress, &state->failed, members, member, true};
+            band_ring_t const sync {pass->progress, &state->failed, members, member, true, costs_s.wait_polls};
             std::int32_t const value = band16_score_warp<policy_>(task, costs_s, sync, ring, ring_words_per_slot,
                                                                   profiles + warp * profile_bytes, chunks[warp]);
             std::uint32_t const super_strips =
@@ -457,19 +457,19 @@ __global__ void __launch_bounds__(band_warps_k * 32)
             band_group_contribute<policy_::local_k>(*pass, value,
                                                     (int)((super_strips - 1) % (std::uint32_t)members) == member);
         }
-        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+        if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate, costs_s.barrier_polls)) break;
         if constexpr (policy_::local_k) {
             // The group's maximum decides, identically in every CTA, whether 16-bit values may have wrapped.
             if (*reinterpret_cast<volatile std::int32_t *>(&pass->best) >= costs_s.local_limit16) {
                 using wide_t = band_policy_t<policy_::kind_k, policy_::affine_k, 8>;
                 std::size_t const wide_profile = (std::size_t)band_profile_bytes_per_warp<wide_t>(costs.classes);
                 pass = &state->pass[parity][1];
-                band_ring_t const sync {pass->progress, &state->failed, members, member, true};
+                band_ring_t const sync {pass->progress, &state->failed, members, member, true, costs_s.wait_polls};
                 std::int32_t const wide = band_score_warp<wide_t>(
                     task, costs_s, sync, reinterpret_cast<std::int32_t *>(ring), 2 * ring_words_per_slot,
                     profiles + warp * wide_profile, *reinterpret_cast<band_chunk_t *>(&chunks[warp]));
                 band_group_contribute<true>(*pass, wide, false);
-                if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate)) break;
+                if (!band_group_barrier(state, group_ctas, ++barriers, shared.gate, costs_s.barrier_polls)) break;
             }
         }
         if (rank == 0 && threadIdx.x == 0)

@@ -1459,11 +1459,22 @@ sz_status_t exec_pairwise(void *engine_handle, void *handle, sz_sequence_u64tape
 
 bool engine_handle_valid(void *engine_handle) noexcept { return as_engine(engine_handle, -1) != nullptr; }
 
+/** The band kernels' wait bounds from the tuning: 0 keeps the built-in bounds, a smaller value lowers both (the
+ *  barrier keeps four times the ring wait's polls), a larger one is clamped to the built-in bounds. */
+static void apply_wait_bounds(engine_t &engine) noexcept {
+    std::uint32_t const polls = engine.tuning.band_wait_polls;
+    engine.costs.wait_polls = polls ? std::min(polls, band_wait_polls_default_k) : band_wait_polls_default_k;
+    engine.costs.barrier_polls =
+        polls ? (std::uint32_t)std::min<std::uint64_t>(4ull * polls, band_barrier_polls_default_k)
+              : band_barrier_polls_default_k;
+}
+
 sz_status_t set_tuning(void *engine_handle, szs_gb300_tuning_t const *tuning, char const **error_message) noexcept {
     engine_t *engine = as_engine(engine_handle, -1);
     if (!engine) return report({sz_status_unknown_k, "Invalid engine handle"}, error_message);
     if (!tuning) {
         engine->tuning = szs_gb300_tuning_t {};
+        apply_wait_bounds(*engine);
         return report({}, error_message);
     }
     for (int k = 0; k < 16; ++k) {
@@ -1477,6 +1488,7 @@ sz_status_t set_tuning(void *engine_handle, szs_gb300_tuning_t const *tuning, ch
         if (tuning->packed_warps[choice] > 8)
             return report({sz_unexpected_dimensions_k, "Warps per CTA must be at most 8"}, error_message);
     engine->tuning = *tuning;
+    apply_wait_bounds(*engine);
     return report({}, error_message);
 }
 
@@ -1585,6 +1597,7 @@ sz_status_t create_engine(int kind, int match, int mismatch, int open, int exten
     engine->kind = kind;
     score_costs_t &costs = engine->costs;
     std::memset(&costs, 0, sizeof(costs));
+    apply_wait_bounds(*engine);
     costs.kind = kind;
     costs.open = open, costs.extend = extend;
     costs.affine = open != extend; // `open == extend` selects the linear engine, as the reference's init does
@@ -1630,6 +1643,7 @@ sz_status_t create_dense_engine(int kind, int open, int extend, std::int8_t cons
     engine->dense_id = ++dense_ids;
     score_costs_t &costs = engine->costs;
     std::memset(&costs, 0, sizeof(costs));
+    apply_wait_bounds(*engine);
     costs.kind = kind;
     costs.open = open, costs.extend = extend;
     costs.affine = open != extend;

@@ -60,6 +60,8 @@ struct score_costs_t {
     int classes;                    // number of compact column classes (NW / SW), <= 32
     int local_limit16;              // local scores on 16-bit cells are exact while every cell stays below this
                                     // (32767 - largest substitution gain); 0 when gaps may be positive
+    std::uint32_t wait_polls;       // band kernels: polls before a ring wait gives up and fails the call
+    std::uint32_t barrier_polls;    // grouped band kernels: polls before a group barrier gives up
     std::int8_t const *direct_table; // dense-table calls over more than 32 bytes: the 256 x 256 [first byte]
                                      // [second byte] table in device memory, read by the direct-table kernels
     std::uint8_t byte_to_compact[256];  // byte -> compact class, indexing `profile_table` rows
@@ -67,6 +69,11 @@ struct score_costs_t {
     std::int8_t profile_table_t[32 * 32]; // same for rows=second (transposed lookups)
     std::uint8_t byte_to_class[256];      // byte -> full class of the reference's 32x32 table
 };
+
+/** Bounds of the band kernels' waits (each poll sleeps about 100 ns in a ring wait, 200 ns at a barrier): about
+ *  0.4 s and 3 s. A tuning may lower them, never raise them. */
+constexpr std::uint32_t band_wait_polls_default_k = 1u << 22;
+constexpr std::uint32_t band_barrier_polls_default_k = 1u << 24;
 
 /** Alphabet of a batch: byte -> dense code, and the number of code bits the bit-parallel kernel needs. */
 struct batch_alphabet_t {

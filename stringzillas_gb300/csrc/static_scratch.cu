@@ -43,7 +43,6 @@ enum static_scratch_error_t : std::uint32_t {
 
 struct static_scratch_control_t {
     std::uint32_t errors;
-    std::uint32_t longest_rejected;
 };
 
 template <typename policy_>
@@ -98,11 +97,8 @@ __global__ void __launch_bounds__(static_scratch_threads_k)
             bool const fits = (span + (std::uint64_t)steps_beyond_span + 1) * (std::uint64_t)magnitude < (1ull << 31) - 1;
             bool const needs_row = n > (std::uint64_t)policy_::strip_rows_k;
             if (!fits || (needs_row && m + 1 > static_scratch_columns_k)) {
-                if (lane == 0) {
-                    atomicOr(&control->errors, fits ? static_scratch_too_long_k : static_scratch_too_wide_k);
-                    atomicMax(&control->longest_rejected, (std::uint32_t)m);
-                }
-                score = 0;
+                if (lane == 0) atomicOr(&control->errors, fits ? static_scratch_too_long_k : static_scratch_too_wide_k);
+                score = 0; // a rejected pair's slot reads 0; the call's status says that some pair was rejected
             }
             else score = dp_score_pair_warp<policy_>(task, costs_s, row, profile);
         }
@@ -115,7 +111,9 @@ namespace {
 std::mutex static_scratch_mutex;
 unsigned char *static_scratch_address[64] = {nullptr};
 
-/** Resolves the array's device address once per device (with that device current). */
+/** Resolves the array's device address once per device (with that device current) and keeps it for the life of the
+ *  process. The address belongs to the device's primary context: after a `cudaDeviceReset` of that device it is
+ *  stale, so this entry point must not be used across a reset. */
 cudaError_t static_scratch_pointer(int device, unsigned char *&pointer) {
     std::lock_guard<std::mutex> lock(static_scratch_mutex);
     if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
@@ -128,6 +126,20 @@ cudaError_t static_scratch_pointer(int device, unsigned char *&pointer) {
     pointer = static_scratch_address[device];
     return cudaSuccess;
 }
+
+/** Restores the calling thread's current device on every return path. */
+struct current_device_guard_t {
+    int saved = -1;
+    current_device_guard_t() {
+        if (cudaGetDevice(&saved) != cudaSuccess) {
+            cudaGetLastError();
+            saved = -1;
+        }
+    }
+    ~current_device_guard_t() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
 
 template <int kind_, bool affine_>
 cudaError_t launch_static(tape_t const &first, tape_t const &second, std::uint64_t count, score_costs_t const &costs,
@@ -143,14 +155,16 @@ cudaError_t launch_static(tape_t const &first, tape_t const &second, std::uint64
     return cudaGetLastError();
 }
 
-bool on_device(void const *pointer) {
+/** True for managed memory, and for device memory of `device` itself (another GPU's memory is not mapped here). */
+bool on_device(void const *pointer, int device) {
     if (!pointer) return false;
     cudaPointerAttributes attributes;
     if (cudaPointerGetAttributes(&attributes, pointer) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return attributes.type == cudaMemoryTypeDevice || attributes.type == cudaMemoryTypeManaged;
+    if (attributes.type == cudaMemoryTypeManaged) return true;
+    return attributes.type == cudaMemoryTypeDevice && attributes.device == device;
 }
 
 } // namespace
@@ -175,10 +189,13 @@ sz_status_t static_scratch_pairwise(static_call_t const &call, sz_sequence_u64ta
     if (first->count != second->count) return fail(sz_unexpected_dimensions_k, "Pairwise inputs must hold the same count");
     if (first->count == 0) return fail(sz_success_k, nullptr);
     if (first->count > 0xFFFFFFFFull) return fail(sz_overflow_risk_k, "More than 2^32 pairs in one call");
-    if (!on_device(first->offsets) || !on_device(second->offsets) || !on_device(results) ||
-        (first->data && !on_device(first->data)) || (second->data && !on_device(second->data)))
+    if (!on_device(first->offsets, call.device) || !on_device(second->offsets, call.device) ||
+        !on_device(results, call.device) || !on_device(first->data, call.device) ||
+        !on_device(second->data, call.device))
         return fail(sz_device_memory_mismatch_k,
-                    "The allocation-free entry point needs device-resident tapes and results");
+                    "The allocation-free entry point needs tapes and results in the scope device's memory "
+                    "(or managed memory), with non-null data pointers");
+    current_device_guard_t const device_guard;
     cudaError_t status = cudaSetDevice(call.device);
     unsigned char *scratch = nullptr;
     if (status == cudaSuccess) status = static_scratch_pointer(call.device, scratch);
@@ -201,7 +218,7 @@ sz_status_t static_scratch_pairwise(static_call_t const &call, sz_sequence_u64ta
     case 5: status = launch_static<kind_smith_waterman_k, true>(a, b, first->count, *call.costs, steps, call.magnitude, results, scratch, ctas, call.stream); break;
     default: status = cudaErrorInvalidValue; break;
     }
-    static_scratch_control_t control {0, 0};
+    static_scratch_control_t control {0};
     if (status == cudaSuccess)
         status = cudaMemcpyAsync(&control, scratch, sizeof(control), cudaMemcpyDeviceToHost, call.stream);
     if (status == cudaSuccess) status = cudaStreamSynchronize(call.stream);

@@ -69,8 +69,9 @@ def test_protein_needleman_wunsch_full_size(szs, port):
 
 def test_long_dna_smith_waterman_full_size(szs, port):
     """8,192 long DNA pairs (lengths log-uniform [1,000, 30,000], planted shared segments, +2/-3, -5/-2): the 48
-    smallest pairs equal the oracle, scores are swap-invariant and within [0, 2 min(n, m)], and each string aligned
-    with itself scores 2 per base."""
+    smallest pairs and 16 of the largest (8 with both sides of 25k-30k characters, 8 more from the top decile by
+    cells, which holds half of the batch's cells) equal the oracle on all host cores, scores are swap-invariant and within [0, 2 min(n, m)], and each
+    string aligned with itself scores 2 per base."""
     first, second = w.local_dna_pairs(8192, seed=42)
     b2c, table = w.dna_table(2, -3)
     engine = szs.SmithWatermanScores(b2c, table, open=-5, extend=-2)
@@ -82,6 +83,14 @@ def test_long_dna_smith_waterman_full_size(szs, port):
     want = port.pairs(oracle.alignment_costs(oracle.SMITH_WATERMAN, b2c, table, -5, -2),
                       _subset(first, smallest), _subset(second, smallest))
     np.testing.assert_array_equal(got[smallest], want)
+    cells, shorter = n * m, np.minimum(n, m)
+    pick = np.random.default_rng(2)
+    longest = pick.choice(np.flatnonzero(shorter >= 25000), size=8, replace=False)
+    top_decile = np.setdiff1d(np.flatnonzero(cells >= np.percentile(cells, 90)), longest)
+    largest = np.sort(np.concatenate([longest, pick.choice(top_decile, size=8, replace=False)]))
+    want = port.pairs(oracle.alignment_costs(oracle.SMITH_WATERMAN, b2c, table, -5, -2),
+                      _subset(first, largest), _subset(second, largest))
+    np.testing.assert_array_equal(got[largest], want)
     np.testing.assert_array_equal(engine.pairwise(b, a).astype(np.int64), got)
     picks = np.sort(np.random.default_rng(1).choice(8192, size=256, replace=False))
     sub = _strs(szs, _subset(first, picks))

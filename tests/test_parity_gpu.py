@@ -702,28 +702,6 @@ def test_utf8_levenshtein_routes(szs, port, costs):
                                                                      tape(first[:12]), tape(second[:9])))
 
 
-@pytest.mark.parametrize("rows", [4, 8, 12, 16])
-@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (3, 1, 5, 5), (0, 5, 3, 1)])
-def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
-    """16-bit codes on the 16x2 routes: every rows-per-lane instance of the wavefront and the 16-bit band (tuned down
-    to 600 rows), codes that differ only in their high byte, uneven partners, odd counts."""
-    rng = np.random.default_rng(rows * 100 + sum(costs))
-    # 300 distinct code points: the codes above 255 share their low byte with codes below it.
-    letters = [chr(c) for c in range(0x3041, 0x3041 + 86)] + [chr(c) for c in range(0xAC00, 0xAC00 + 214)]
-    lengths = [(int(rng.integers(0, 500)), int(rng.integers(0, 500))) for _ in range(41)]
-    lengths += [(601, 700), (1025, 1300), (700, 1400), (2049, 2100)]
-    first = ["".join(rng.choice(letters, size=n)) for n, _ in lengths]
-    second = ["".join(rng.choice(letters, size=m)) for _, m in lengths]
-    second[-3] = first[-3][:500] + second[-3][500:]
-    engine = szs.LevenshteinDistancesUTF8(*costs)
-    engine.set_tuning({"packed_rows": [rows] * 16, "band_min_rows": 600, "band_min_rows_packed": 600,
-                       "band_min_rows_few": 600, "band_min_rows_compare": 600})
-    want = port.pairs(oracle.levenshtein_utf8_costs(*costs), tape(first), tape(second))
-    for schedule in ("batched", "plain"):
-        engine.set_schedule(schedule)
-        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
-
-
 @pytest.mark.parametrize("costs", [(0, 1, 1, 1), (0, 2, 3, 1), (1, 3, 2, 2), (0, 5, 3, 1)])
 def test_utf8_levenshtein_over_many_code_points(szs, port, costs):
     """More than 256 distinct code points: 16-bit codes on every route (thread and warp bit-parallel kernels with 16
@@ -770,3 +748,32 @@ def test_utf8_compare_mode_over_16bit_codes(szs, port, rows, costs):
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
         np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
+
+
+@pytest.mark.parametrize("schedule", ["batched", "plain"], ids=["grouped-band", "one-cta-band"])
+@pytest.mark.parametrize("family", ["nw", "sw"], ids=["band32-nw", "band16-sw"])
+def test_bounded_wait_gives_up_and_next_call_is_exact(szs, port, family, schedule):
+    """The band kernels' waits are bounded. With the bound tuned down to one poll (about 100 ns), the strips below
+    the first cannot find the strip above ready (it needs dozens of column steps first), so the waits give up: the
+    call returns an error status instead of hanging, and nothing faults. The next call at the built-in bound is
+    bit-exact. Few long pairs in the batched form take the cooperative grouped band (its barrier is bounded the same
+    way); the plain form gives each pair one CTA. Protein NW at -11/-1 needs 32-bit cells, DNA SW 16-bit ones."""
+    rng = np.random.default_rng(77 if family == "nw" else 78)
+    if family == "nw":
+        b2c, table = protein_tables(rng)
+        first = random_strings(rng, 3, 5000, 6000, PROTEIN)
+        second = random_strings(rng, 3, 5000, 6000, PROTEIN)
+        engine, oracle_costs = make_engine(szs, "nw", (-11, -1), b2c, table)
+    else:
+        b2c, table = dna_tables()
+        first = random_strings(rng, 3, 5000, 6000, DNA)
+        second = random_strings(rng, 3, 5000, 6000, DNA)
+        engine, oracle_costs = make_engine(szs, "sw", (-5, -2), b2c, table)
+    engine.set_schedule(schedule)
+    a, b = szs.Strs(first), szs.Strs(second)
+    engine.set_tuning({"band_wait_polls": 1})
+    with pytest.raises(RuntimeError, match="bounded wait"):
+        engine.pairwise(a, b)
+    engine.set_tuning(None)
+    got = engine.pairwise(a, b).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))

@@ -66,7 +66,12 @@ def engines(szs):
         ("sw-linear", szs.SmithWatermanScores(dna_b2c, dna, open=-4, extend=-4), DNA),
         ("lev-affine", szs.LevenshteinDistances(0, 4, 5, 2), DNA),
         ("lev-unit", szs.LevenshteinDistances(), DNA),
+        ("nw-linear", szs.NeedlemanWunschScores(b2c, table, open=-5, extend=-5), PROTEIN),
+        ("sw-affine", szs.SmithWatermanScores(dna_b2c, dna, open=-5, extend=-2), DNA),
     ]
+
+
+ENGINE_NAMES = ["nw-affine", "sw-linear", "lev-affine", "lev-unit", "nw-linear", "sw-affine"]
 
 
 def regular(env, engine, a, b, count):
@@ -88,13 +93,16 @@ def allocation_free(env, engine, a, b, out):
     return status, err.value
 
 
-@pytest.mark.parametrize("index", range(4), ids=["nw-affine", "sw-linear", "lev-affine", "lev-unit"])
+@pytest.mark.parametrize("index", range(len(ENGINE_NAMES)), ids=ENGINE_NAMES)
 def test_matches_regular_entry_point_twice(env, index):
+    """Every kernel instance (kind x linear / affine), with empty sides on either string, on two calls in a row."""
     torch, szs, native = env
     name, engine, alphabet = engines(szs)[index]
     rng = np.random.default_rng(100 + index)
     for call, count in enumerate((40, 23)):  # two calls in a row, different shapes
         first, second = workload(rng, alphabet, count)
+        first += [b"", b"", bytes(rng.choice(alphabet, size=300))]
+        second += [bytes(rng.choice(alphabet, size=7)), b"", b""]
         a, keep_a = device_tape(torch, native, first)
         b, keep_b = device_tape(torch, native, second)
         want = regular(env, engine, a, b, len(first))
@@ -115,9 +123,12 @@ def test_rejects_what_the_fixed_scratch_cannot_hold(env):
     a, keep_a = device_tape(torch, native, first)
     b, keep_b = device_tape(torch, native, second)
     out = torch.zeros(2, dtype=torch.int64, device="cuda")
+    out.fill_(-777)
     status, message = allocation_free(env, engine, a, b, out.data_ptr())
     assert status == native.OVERFLOW_RISK and b"2,048" in message
-    # The pair that fits is still scored, and the next call starts from a cleared error word.
+    # The rejected pair's slot reads 0, the pair that fits is still scored, and the next call starts from a cleared
+    # error word.
+    assert int(out[0]) == 0
     assert int(out[1]) == int(regular(env, engine, a, b, 2)[1])
     first, second = first[1:], second[1:]
     a, keep_a = device_tape(torch, native, first)
@@ -134,4 +145,30 @@ def test_rejects_host_memory(env):
     a = native.U64Tape(data.ctypes.data, offsets.ctypes.data, 2)
     out = np.zeros(2, dtype=np.int64)
     status, _ = allocation_free(env, engine, a, a, out.ctypes.data)
+    assert status == native.DEVICE_MEMORY_MISMATCH
+
+
+def test_keeps_the_callers_current_device(env):
+    torch, szs, native = env
+    _, engine, alphabet = engines(szs)[3]
+    a, keep = device_tape(torch, native, [b"ACGT", b"GATTACA"])
+    out = torch.zeros(2, dtype=torch.int64, device="cuda")
+    before = torch.cuda.current_device()
+    status, message = allocation_free(env, engine, a, a, out.data_ptr())
+    assert status == 0, message
+    assert torch.cuda.current_device() == before
+    assert out.cpu().tolist() == [0, 0]
+
+
+def test_rejects_another_gpus_memory(env):
+    """Tapes on GPU 1 with a scope on GPU 0 would be read without a peer mapping: refused before any launch."""
+    torch, szs, native = env
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two visible GPUs")
+    _, engine, _ = engines(szs)[3]
+    data = torch.frombuffer(bytearray(b"ACGTACGT"), dtype=torch.uint8).to("cuda:1")
+    offsets = torch.tensor([0, 4, 8], dtype=torch.int64, device="cuda:1")
+    a = native.U64Tape(data.data_ptr(), offsets.data_ptr(), 2)
+    out = torch.zeros(2, dtype=torch.int64, device="cuda:1")
+    status, _ = allocation_free(env, engine, a, a, out.data_ptr())
     assert status == native.DEVICE_MEMORY_MISMATCH
