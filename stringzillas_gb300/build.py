@@ -40,6 +40,7 @@ UNITS = [
     ("fingerprints", "fingerprints.cu", []),
     ("myers_wide", "kernels_myers_wide.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),
+    ("myers_table", "kernels_myers_table.cu", []),
     ("myers_p3", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=3"]),
     ("myers_p5", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=5"]),
     ("myers_p8", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=8"]),

@@ -347,22 +347,18 @@ static engine_t *as_engine(void *handle, int kind) noexcept {
 
 static int cost_abs(int x) noexcept { return x < 0 ? -x : x; }
 
-cudaError_t launch_myers_planes2(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
-                                 std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_planes3(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
-                                 std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_planes5(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
-                                 std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_warp_planes2(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
-                                     std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_warp_planes3(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
-                                     std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_warp_planes5(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
-                                     std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_warp_planes8(int, pair_task_t const *, plan_bins_t *, batch_alphabet_t const *,
-                                     std::int64_t *, int, cudaStream_t);
-cudaError_t launch_myers_planes8(int, bool, pair_task_t const *, plan_bins_t const *, batch_alphabet_t const *,
-                                 std::int64_t *, int, cudaStream_t);
+// Per plane count, built from kernels_myers.cu once per count: (words, exact, tasks, bins, key_begin, key_end,
+// alphabet, results, ctas, stream), and the warp forms without `exact`.
+#define SZS_DECLARE_MYERS_PLANES(planes)                                                                            \
+    cudaError_t launch_myers_planes##planes(int, bool, pair_task_t const *, plan_bins_t const *, int, int,           \
+                                            batch_alphabet_t const *, std::int64_t *, int, cudaStream_t);           \
+    cudaError_t launch_myers_warp_planes##planes(int, pair_task_t const *, plan_bins_t *, int, int,                 \
+                                                 batch_alphabet_t const *, std::int64_t *, int, cudaStream_t);
+SZS_DECLARE_MYERS_PLANES(2)
+SZS_DECLARE_MYERS_PLANES(3)
+SZS_DECLARE_MYERS_PLANES(5)
+SZS_DECLARE_MYERS_PLANES(8)
+#undef SZS_DECLARE_MYERS_PLANES
 
 int myers_planes_for(int bits_needed) {
     if (bits_needed <= 2) return 2;
@@ -373,26 +369,27 @@ int myers_planes_for(int bits_needed) {
 
 int myers_threads_per_cta() { return 128; }
 
-/** Warp-per-pair bit-parallel kernel over the bins of `words` words per lane. */
+/** Warp-per-pair bit-parallel kernel over bins [key_begin, key_end) with `words` words per lane. */
 static cudaError_t launch_myers_warp(int words, int planes, pair_task_t const *tasks, plan_bins_t *bins,
-                                     batch_alphabet_t const *alphabet, std::int64_t *results, int ctas,
-                                     cudaStream_t stream) {
+                                     int key_begin, int key_end, batch_alphabet_t const *alphabet,
+                                     std::int64_t *results, int ctas, cudaStream_t stream) {
     switch (planes) {
-    case 2: return launch_myers_warp_planes2(words, tasks, bins, alphabet, results, ctas, stream);
-    case 3: return launch_myers_warp_planes3(words, tasks, bins, alphabet, results, ctas, stream);
-    case 5: return launch_myers_warp_planes5(words, tasks, bins, alphabet, results, ctas, stream);
-    case 8: return launch_myers_warp_planes8(words, tasks, bins, alphabet, results, ctas, stream);
+    case 2: return launch_myers_warp_planes2(words, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
+    case 3: return launch_myers_warp_planes3(words, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
+    case 5: return launch_myers_warp_planes5(words, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
+    case 8: return launch_myers_warp_planes8(words, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
     default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_myers(int words, int planes, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
-                         batch_alphabet_t const *alphabet, std::int64_t *results, int ctas, cudaStream_t stream) {
+                         int key_begin, int key_end, batch_alphabet_t const *alphabet, std::int64_t *results, int ctas,
+                         cudaStream_t stream) {
     switch (planes) {
-    case 2: return launch_myers_planes2(words, exact, tasks, bins, alphabet, results, ctas, stream);
-    case 3: return launch_myers_planes3(words, exact, tasks, bins, alphabet, results, ctas, stream);
-    case 5: return launch_myers_planes5(words, exact, tasks, bins, alphabet, results, ctas, stream);
-    case 8: return launch_myers_planes8(words, exact, tasks, bins, alphabet, results, ctas, stream);
+    case 2: return launch_myers_planes2(words, exact, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
+    case 3: return launch_myers_planes3(words, exact, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
+    case 5: return launch_myers_planes5(words, exact, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
+    case 8: return launch_myers_planes8(words, exact, tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -1018,25 +1015,31 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     int myers_planes = 0;
     if (engine.unit_levenshtein) {
         myers_planes = wide ? 16 : myers_planes_for((int)alphabet_host.bits);
+        // The plain form keeps each bit-parallel route in one bin and launches the word count of the batch's longest
+        // pattern on it (the binned form launches each bin with its own word count).
+        bool const plain = schedule == szs_gb300_schedule_plain_k;
         // Longer patterns first: one warp per pair, most words per lane first.
         for (int words = myers_warp_max_words_k; words >= 1; --words) {
             int const key_begin = bin_myers_warp_begin_k + (myers_warp_max_words_k - words) * myers_warp_classes_k;
             std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + myers_warp_classes_k);
             if (!pairs_here) continue;
+            int const launch_words =
+                plain ? std::max(1, (int)((plan.max_myers_warp_rows + 32u * 32u - 1) / (32u * 32u))) : words;
             std::uint64_t const needed = (pairs_here + 7) / 8; // eight warps per CTA
             int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 2);
-            jobs[job_count++] = {job_myers_warp_k, words, 0, key_begin, key_begin + myers_warp_classes_k, pairs_here,
-                                 ctas, 0, 0};
+            jobs[job_count++] = {job_myers_warp_k, launch_words, 0, key_begin, key_begin + myers_warp_classes_k,
+                                 pairs_here, ctas, 0, 0};
             jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * 2;
         }
         for (int words = myers_max_words_k; words >= 1; --words) {
             int const key_begin = bin_myers_begin_k + words * 16;
             std::uint64_t const pairs_here = pairs_in(key_begin, key_begin + 16);
             if (!pairs_here) continue;
+            int const launch_words = plain ? std::max(1, (int)((plan.max_myers_rows + 31u) / 32u)) : words;
             int const threads = myers_threads_per_cta();
             std::uint64_t const needed = (pairs_here + threads - 1) / threads;
             int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * 16);
-            jobs[job_count++] = {job_myers_k, words, 0, key_begin, key_begin + 16, pairs_here, ctas, 0, 0};
+            jobs[job_count++] = {job_myers_k, launch_words, 0, key_begin, key_begin + 16, pairs_here, ctas, 0, 0};
             jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * 16;
         }
     }
@@ -1107,16 +1110,21 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
                                          lane_stream, compare_mode, wide));
             else if (job.kind == job_myers_warp_k && wide)
-                SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, results, job.ctas, lane_stream));
+                SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, job.key_begin, job.key_end, results,
+                                                    job.ctas, lane_stream));
             else if (job.kind == job_myers_warp_k)
-                SZS_TRY_CUDA(launch_myers_warp(job.variant, myers_planes, tasks, bins, alphabet, results, job.ctas,
-                                               lane_stream));
+                SZS_TRY_CUDA(launch_myers_warp(job.variant, myers_planes, tasks, bins, job.key_begin, job.key_end,
+                                               alphabet, results, job.ctas, lane_stream));
             else if (wide)
                 SZS_TRY_CUDA(launch_myers_wide(job.variant, schedule != szs_gb300_schedule_plain_k, tasks, bins,
-                                               results, job.ctas, lane_stream));
+                                               job.key_begin, job.key_end, results, job.ctas, lane_stream));
+            else if (myers_planes == 2)
+                SZS_TRY_CUDA(launch_myers_table(job.variant, job.key_begin, job.key_end, tasks, bins, alphabet,
+                                                results, job.ctas, lane_stream));
             else
                 SZS_TRY_CUDA(launch_myers(job.variant, myers_planes, schedule != szs_gb300_schedule_plain_k, tasks,
-                                          bins, alphabet, results, job.ctas, lane_stream));
+                                          bins, job.key_begin, job.key_end, alphabet, results, job.ctas,
+                                          lane_stream));
             if (traced) cudaEventRecord(context->trace_events[2 * i + 1], lane_stream);
         }
         for (int lane = 0; lane < lanes_used; ++lane) {

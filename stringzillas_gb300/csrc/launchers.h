@@ -138,17 +138,24 @@ cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pai
 /** Bit-parallel kernels over strings of 16-bit codes (UTF-8 calls over more than 256 code points, 16 code planes):
  *  thread per pair over the bins of `words` words (1..8), and warp per pair over the warp bins (1..8 words per
  *  lane). */
-cudaError_t launch_myers_wide(int words, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
-                              std::int64_t *results, int ctas, cudaStream_t stream);
-cudaError_t launch_myers_warp_wide(int words, pair_task_t const *tasks, plan_bins_t *bins, std::int64_t *results,
-                                   int ctas, cudaStream_t stream);
+cudaError_t launch_myers_wide(int words, bool exact, pair_task_t const *tasks, plan_bins_t const *bins, int key_begin,
+                              int key_end, std::int64_t *results, int ctas, cudaStream_t stream);
+cudaError_t launch_myers_warp_wide(int words, pair_task_t const *tasks, plan_bins_t *bins, int key_begin, int key_end,
+                                   std::int64_t *results, int ctas, cudaStream_t stream);
 
-/** Runs the bit-parallel kernel over the bins of one word count (1..16) with `planes` code planes (2, 3, 5 or 8).
- *  `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise pairs may be
- *  shorter (the plain schedule puts every bit-parallel pair in the 16-word bin). */
+/** Runs the bit-parallel kernel over bins [key_begin, key_end) with `words` words (1..16) and `planes` code planes
+ *  (2, 3, 5 or 8). `exact` = every pair in the bins needs exactly `words` words (the binned schedule); otherwise
+ *  pairs may be shorter (the plain schedule puts every bit-parallel pair in one bin and launches the word count of
+ *  the batch's longest pattern). */
 cudaError_t launch_myers(int words, int planes, bool exact, pair_task_t const *tasks, plan_bins_t const *bins,
-                         batch_alphabet_t const *alphabet, std::int64_t *results, int ctas, cudaStream_t stream);
+                         int key_begin, int key_end, batch_alphabet_t const *alphabet, std::int64_t *results, int ctas,
+                         cudaStream_t stream);
 int myers_threads_per_cta();
+/** The shared-table bit-parallel kernel for batches over at most four symbol codes: bins [key_begin, key_end),
+ *  patterns of at most 32 x `words` rows (1..16). */
+cudaError_t launch_myers_table(int words, int key_begin, int key_end, pair_task_t const *tasks,
+                               plan_bins_t const *bins, batch_alphabet_t const *alphabet, std::int64_t *results,
+                               int ctas, cudaStream_t stream);
 /** Planes actually instantiated for a requested minimum. */
 int myers_planes_for(int bits_needed);
 

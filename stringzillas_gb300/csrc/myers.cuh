@@ -133,10 +133,11 @@ __device__ __forceinline__ std::uint32_t myers_distance(std::uint8_t const *patt
     return (std::uint32_t)state.score;
 }
 
-/** Thread-per-pair kernel over the Myers bin of one word count. */
+/** Thread-per-pair kernel over bins [key_begin, key_end), patterns of at most 32 x `words_` rows (exactly that many
+ *  words when `exact_`). */
 template <int words_, int bits_, bool exact_>
 __global__ void __launch_bounds__(128) myers_kernel(pair_task_t const *__restrict__ tasks,
-                                                    plan_bins_t const *__restrict__ bins,
+                                                    plan_bins_t const *__restrict__ bins, int key_begin, int key_end,
                                                     batch_alphabet_t const *__restrict__ alphabet,
                                                     std::int64_t *__restrict__ results) {
     __shared__ std::uint8_t code_s[256];
@@ -148,7 +149,6 @@ __global__ void __launch_bounds__(128) myers_kernel(pair_task_t const *__restric
         for (int b = 0; b < bits_; ++b) selectors_s.select[i][b] = ((c >> b) & 1u) ? 0u : 0xFFFFFFFFu;
     }
     __syncthreads();
-    int const key_begin = bin_myers_begin_k + words_ * 16, key_end = key_begin + 16;
     std::uint32_t const begin = bins->begin[key_begin];
     std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
     for (std::uint32_t index = blockIdx.x * blockDim.x + threadIdx.x; index < count;
@@ -174,10 +174,9 @@ __device__ __forceinline__ void code_selectors(std::uint32_t code, std::uint32_t
 /** Thread-per-pair kernel over strings of 16-bit codes (UTF-8 calls over more than 256 code points). */
 template <int words_, bool exact_>
 __global__ void __launch_bounds__(128) myers_wide_kernel(pair_task_t const *__restrict__ tasks,
-                                                         plan_bins_t const *__restrict__ bins,
-                                                         std::int64_t *__restrict__ results) {
+                                                         plan_bins_t const *__restrict__ bins, int key_begin,
+                                                         int key_end, std::int64_t *__restrict__ results) {
     constexpr int W = words_, B = myers_wide_planes_k;
-    int const key_begin = bin_myers_begin_k + words_ * 16, key_end = key_begin + 16;
     std::uint32_t const begin = bins->begin[key_begin];
     std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
     for (std::uint32_t index = blockIdx.x * blockDim.x + threadIdx.x; index < count;

@@ -112,10 +112,11 @@ __device__ __forceinline__ std::uint32_t myers_warp_distance(pair_task_t const &
     return (std::uint32_t)__shfl_sync(0xFFFFFFFFu, score, score_lane);
 }
 
-/** Warp-per-pair kernel over the bins of one words-per-lane count; warps pull pairs from the bins' cursor. */
+/** Warp-per-pair kernel over bins [key_begin, key_end) with at most `words_` words per lane; warps pull pairs from
+ *  the first bin's cursor. */
 template <int words_, int bits_>
 __global__ void __launch_bounds__(256) myers_warp_kernel(pair_task_t const *__restrict__ tasks,
-                                                         plan_bins_t *__restrict__ bins,
+                                                         plan_bins_t *__restrict__ bins, int key_begin, int key_end,
                                                          batch_alphabet_t const *__restrict__ alphabet,
                                                          std::int64_t *__restrict__ results) {
     __shared__ std::uint8_t code_s[256];
@@ -128,8 +129,6 @@ __global__ void __launch_bounds__(256) myers_warp_kernel(pair_task_t const *__re
     }
     __syncthreads();
     int const lane = threadIdx.x & 31;
-    int const key_begin = bin_myers_warp_begin_k + (myers_warp_max_words_k - words_) * myers_warp_classes_k;
-    int const key_end = key_begin + myers_warp_classes_k;
     std::uint32_t const begin = bins->begin[key_begin];
     std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
     while (true) {
@@ -146,11 +145,9 @@ __global__ void __launch_bounds__(256) myers_warp_kernel(pair_task_t const *__re
 /** The same over strings of 16-bit codes (UTF-8 calls over more than 256 code points): 16 planes, no tables. */
 template <int words_>
 __global__ void __launch_bounds__(256) myers_warp_wide_kernel(pair_task_t const *__restrict__ tasks,
-                                                              plan_bins_t *__restrict__ bins,
-                                                              std::int64_t *__restrict__ results) {
+                                                              plan_bins_t *__restrict__ bins, int key_begin,
+                                                              int key_end, std::int64_t *__restrict__ results) {
     int const lane = threadIdx.x & 31;
-    int const key_begin = bin_myers_warp_begin_k + (myers_warp_max_words_k - words_) * myers_warp_classes_k;
-    int const key_end = key_begin + myers_warp_classes_k;
     std::uint32_t const begin = bins->begin[key_begin];
     std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
     while (true) {

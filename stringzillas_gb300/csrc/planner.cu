@@ -189,12 +189,12 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
                                   std::int64_t *__restrict__ results) {
     __shared__ std::uint32_t histogram[bin_keys_k];
     __shared__ unsigned long long block_cells;
-    __shared__ std::uint32_t block_max_cols;
+    __shared__ std::uint32_t block_max_cols, block_max_myers, block_max_myers_warp;
     for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x) histogram[i] = 0;
-    if (threadIdx.x == 0) block_cells = 0, block_max_cols = 0;
+    if (threadIdx.x == 0) block_cells = 0, block_max_cols = 0, block_max_myers = 0, block_max_myers_warp = 0;
     __syncthreads();
     std::uint64_t thread_cells = 0;
-    std::uint32_t thread_max_cols = 0;
+    std::uint32_t thread_max_cols = 0, thread_max_myers = 0, thread_max_myers_warp = 0;
     for (std::uint64_t p = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < args.pairs;
          p += (std::uint64_t)gridDim.x * blockDim.x) {
         pair_route_info_t const info = route_of_pair(args, p);
@@ -205,15 +205,22 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
         }
         atomicAdd(&histogram[info.key], 1u);
         if (info.key >= bin_dp32_begin_k) thread_max_cols = max(thread_max_cols, info.m);
+        if (info.key >= bin_myers_warp_begin_k) thread_max_myers_warp = max(thread_max_myers_warp, info.n);
+        else if (info.key < bin_myers_begin_k + (myers_max_words_k + 1) * 16)
+            thread_max_myers = max(thread_max_myers, info.n);
     }
     atomicAdd(&block_cells, (unsigned long long)thread_cells);
     atomicMax(&block_max_cols, thread_max_cols);
+    atomicMax(&block_max_myers, thread_max_myers);
+    atomicMax(&block_max_myers_warp, thread_max_myers_warp);
     __syncthreads();
     for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x)
         if (histogram[i]) atomicAdd(&bins->count[i], histogram[i]);
     if (threadIdx.x == 0) {
         atomicAdd((unsigned long long *)&bins->cells, block_cells);
         atomicMax(&bins->max_cols, block_max_cols);
+        atomicMax(&bins->max_myers_rows, block_max_myers);
+        atomicMax(&bins->max_myers_warp_rows, block_max_myers_warp);
     }
 }
 

@@ -107,6 +107,8 @@ struct plan_bins_t {
     std::uint32_t error_flags;
     std::uint64_t cells;
     std::uint64_t scheduled;
+    std::uint32_t max_myers_rows;      // longest pattern on the thread-per-pair bit-parallel route
+    std::uint32_t max_myers_warp_rows; // longest pattern on the warp-per-pair bit-parallel route
 };
 
 } // namespace szs_gb300

@@ -164,24 +164,32 @@ def test_warp_myers_long_patterns(szs, port, symbols):
         np.testing.assert_array_equal(got, want)
 
 
-def test_myers_every_word_count(szs, port):
-    """Unit-cost Levenshtein takes the bit-parallel route for shorter sides up to 512, the DP route above."""
-    rng = np.random.default_rng(3)
+@pytest.mark.parametrize("schedule", ["batched", "plain"])
+@pytest.mark.parametrize("symbols", [1, 2, 4, 7, 256], ids=["1sym", "2sym", "4sym", "7sym", "256sym"])
+def test_myers_every_word_count(szs, port, symbols, schedule):
+    """Unit-cost Levenshtein takes the bit-parallel routes: one thread per pair for shorter sides up to 512 (the
+    shared-table kernel over at most four symbol codes, code planes above), one warp per pair up to 8,192. Every word
+    count, texts shorter and longer than the pattern, empty partners; the plain form runs each route with the word
+    count of the batch's longest pattern, checked here on a batch whose patterns are all short as well."""
+    rng = np.random.default_rng(3 + symbols)
+    alphabet = np.frombuffer(b"ACGTNRYK", dtype=np.uint8)[:symbols] if symbols < 256 else \
+        np.arange(256, dtype=np.uint8)
     first, second = [], []
-    for n in list(range(1, 70)) + list(range(90, 530, 7)):
-        first.append(bytes(rng.choice(DNA, size=n)))
-        second.append(bytes(rng.choice(DNA, size=int(rng.integers(n, n + 400)))))
+    for n in list(range(1, 70)) + list(range(90, 530, 7)) + [600, 1100, 2100]:
+        first.append(bytes(rng.choice(alphabet, size=n)))
+        second.append(bytes(rng.choice(alphabet, size=int(rng.integers(max(0, n - 60), n + 400)))))
+    first[5], second[5] = second[5], first[5]  # the pattern on the second side
+    first += [b"", bytes(rng.choice(alphabet, size=40))]
+    second += [bytes(rng.choice(alphabet, size=40)), b""]
     engine = szs.LevenshteinDistances()
+    engine.set_schedule(schedule)
     got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
     want = port.pairs(oracle.levenshtein_costs(), tape(first), tape(second))
     np.testing.assert_array_equal(got, want)
-    # Large alphabets need more code planes.
-    text = np.arange(256, dtype=np.uint8)
-    first = [bytes(rng.choice(text, size=int(rng.integers(1, 300)))) for _ in range(100)]
-    second = [bytes(rng.choice(text, size=int(rng.integers(1, 300)))) for _ in range(100)]
-    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
-    want = port.pairs(oracle.levenshtein_costs(), tape(first), tape(second))
-    np.testing.assert_array_equal(got, want)
+    short_first = [bytes(rng.choice(alphabet, size=int(rng.integers(1, 70)))) for _ in range(300)]
+    short_second = [bytes(rng.choice(alphabet, size=int(rng.integers(1, 300)))) for _ in range(300)]
+    got = engine.pairwise(szs.Strs(short_first), szs.Strs(short_second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(), tape(short_first), tape(short_second)))
 
 
 @pytest.mark.parametrize("schedule", ["batched", "plain"])
