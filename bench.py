@@ -429,6 +429,9 @@ def serving_leg(szs):
     cells = int(sum(pool[k]["cells"] for k in order))
     forms = {"serving": dict(lanes=4, arena_bytes=4 << 30),
              "per_request_plain": dict(lanes=1, max_batch_requests=1, schedule="plain", arena_bytes=4 << 30)}
+    # The same four lanes without batching: one request per batch, plain schedule (isolates what batching buys).
+    same_lanes = {"per_request_plain_4_lanes": dict(lanes=4, max_batch_requests=1, schedule="plain",
+                                                    arena_bytes=4 << 30)}
     out = {"offered_requests_per_s": SERVING_RATE, "requests": SERVING_REQUESTS,
            "offered_gcups": cells / arrivals[-1] / 1e9, "cells": cells,
            "mix": "Levenshtein:NW:SW 2:1:1, 1-4,096 pairs per request, pair lengths log-uniform [16, 16,384]"}
@@ -454,13 +457,15 @@ def serving_leg(szs):
     burst_cells = int(sum(nw_sw[k]["cells"] for k in burst))
     mix = {"requests": NW_SW_BURST, "cells": burst_cells,
            "mix": "NW:SW 1:1 (affine protein), 1-4,096 pairs per request, pair lengths log-uniform [16, 16,384]"}
-    for name, config in forms.items():
+    for name, config in {**forms, **same_lanes}.items():
         with szs.Server(**config) as server:
             serve_stream(szs, server, engines, nw_sw, burst[:4], np.zeros(4))
             infos, wall = serve_stream(szs, server, engines, nw_sw, burst, np.zeros(len(burst)))
         mix[name] = {"saturated_gcups": burst_cells / wall / 1e9,
                      "p99_ms": float(np.percentile([i["done_ms"] for i in infos], 99))}
     mix["serving_over_plain"] = mix["serving"]["saturated_gcups"] / mix["per_request_plain"]["saturated_gcups"]
+    mix["serving_over_plain_same_lanes"] = (mix["serving"]["saturated_gcups"] /
+                                            mix["per_request_plain_4_lanes"]["saturated_gcups"])
     out["nw_sw_burst"] = mix
     return out
 
@@ -661,6 +666,7 @@ def run_ours(args):
                                  None if peaks is None else {k: v / 1e12 for k, v in peaks.items()}},
             "plain": {"value": plain_cells / (plain_ms * 1e-3) / 1e9, "unit": "GCUPS",
                       "ms_per_step": plain_ms / plain_steps, "compute_ms_per_step": plain_compute_ms / plain_steps},
+            "batched_over_plain": value / (plain_cells / (plain_ms * 1e-3) / 1e9 * world),
             "e2e": {"value": e2e_cells / (e2e_ms * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": e2e_ms / e2e_steps,
                     "h2d_bytes_per_step": host_batch.bytes_in, "d2h_bytes_per_step": host_batch.bytes_out},
             "clocks": clock_summary,

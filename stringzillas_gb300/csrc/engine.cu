@@ -562,6 +562,7 @@ struct call_t {
     std::size_t stride = 0;
     bool pre_staged = false;           // the tapes below are already on the device (a chunk of a pipelined call)
     tape_t staged_queries {}, staged_candidates {};
+    bool exact_alphabet = false;       // mark every byte of the batch, no sampled guess
 };
 
 static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &stream, device_context_t *contexts,
@@ -653,6 +654,8 @@ static status_t transcode_utf8(device_context_t *context, cudaStream_t stream, t
  *  @param defer  pairwise calls with host results only: return once the work is queued, without waiting for it;
  *                `finish_deferred` later waits and fills @p stats (the pipelined driver keeps two chunks in flight).
  */
+constexpr std::uint64_t alphabet_sample_bytes_k = std::uint64_t(1) << 20; // bytes per tape of a guessed alphabet
+
 static status_t run_on(engine_t const &engine, device_context_t *context, cudaStream_t stream, call_t const &call,
                        int schedule, szs_gb300_stats_t &stats, bool defer = false) noexcept {
     status_t status;
@@ -762,6 +765,11 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     bool const dense = !engine.dense.empty();
     // Both score over the batch's own byte codes; 16-bit codes are already dense.
     bool const alphabet_pass = (levenshtein || dense) && !wide;
+    // Unit-cost Levenshtein: the alphabet is guessed from the first bytes of each tape instead of a pass over all of
+    // them, and the shared-table kernel checks every byte it reads against the guess. A guess with more than four
+    // symbols, a plan with pairs on other routes, or a byte the guess missed is answered by scoring the call again
+    // with the exact alphabet, so results never depend on the guess.
+    bool const speculative = alphabet_pass && engine.unit_levenshtein && !call.exact_alphabet && !defer;
 
     static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
     // Device-resident inputs make every launch of the call a function of bytes the call can key on, so both phases
@@ -806,14 +814,14 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         key_append(prologue_key, args);
         key_append(prologue_key, bins), key_append(prologue_key, tasks), key_append(prologue_key, results);
         key_append(prologue_key, context->readback.data), key_append(prologue_key, context->sm_count);
-        key_append(prologue_key, call.has_candidates);
+        key_append(prologue_key, call.has_candidates), key_append(prologue_key, speculative);
     }
     status = issue_or_replay(context->prologue_graphs, prologue_key, prologue_replayed, [&](cudaStream_t s) -> status_t {
         // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code planes
         // by it, and the 16x2 route builds its substitution profile over it (when it has at most 32 symbols).
         if (alphabet_pass)
             SZS_TRY_CUDA(launch_alphabet(args.queries, args.candidates, call.has_candidates, alphabet,
-                                         context->sm_count, s));
+                                         context->sm_count, s, speculative ? alphabet_sample_bytes_k : 0));
         SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, s));
         // Read the plan (and the alphabet, stored right after it) back: which bins are non-empty, column lengths.
         SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t) + sizeof(batch_alphabet_t),
@@ -825,6 +833,17 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
     batch_alphabet_t const &alphabet_host = *context->alphabet_host();
+    auto run_exact = [&]() -> status_t {
+        call_t exact = call;
+        exact.exact_alphabet = true;
+        return run_on(engine, context, stream, exact, schedule, stats, defer);
+    };
+    if (speculative) {
+        bool thread_route_only = alphabet_host.bits <= 2; // at most four codes: the shared-table kernel
+        for (int key = bin_dp32_begin_k; key < bin_keys_k && thread_route_only; ++key)
+            thread_route_only = plan.count[key] == 0;
+        if (!thread_route_only) return run_exact();
+    }
     stats.last_cells = plan.cells;
     auto pairs_in = [&](int key_begin, int key_end) {
         std::uint64_t total = 0;
@@ -1191,9 +1210,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         }
     }
     SZS_TRY_CUDA(cudaGetLastError());
-    if (context->bins_host()->error_flags)
+    if (context->bins_host()->error_flags & 1u)
         return {sz_status_unknown_k, "A long pair's band of warps stopped waiting for its neighbour (bounded wait "
                                      "expired); its score was not computed"};
+    if (speculative && (context->bins_host()->error_flags & 2u)) return run_exact(); // the guessed alphabet missed
     float elapsed = 0;
     cudaEventElapsedTime(&elapsed, context->start, context->stop);
     stats.last_call_ms = elapsed;
@@ -1223,7 +1243,7 @@ static status_t finish_deferred(device_context_t *context, szs_gb300_stats_t &st
     context->deferred = false;
     SZS_TRY_CUDA(cudaEventSynchronize(context->stop));
     SZS_TRY_CUDA(cudaGetLastError());
-    if (context->bins_host()->error_flags)
+    if (context->bins_host()->error_flags & 1u)
         return {sz_status_unknown_k, "A long pair's band of warps stopped waiting for its neighbour (bounded wait "
                                      "expired); its score was not computed"};
     float elapsed = 0, compute = 0;

@@ -9,7 +9,7 @@
 namespace szs_gb300 {
 
 template <int words_>
-static cudaError_t myers_table_launch_words(pair_task_t const *tasks, plan_bins_t const *bins, int key_begin,
+static cudaError_t myers_table_launch_words(pair_task_t const *tasks, plan_bins_t *bins, int key_begin,
                                             int key_end, batch_alphabet_t const *alphabet, std::int64_t *results,
                                             int ctas, cudaStream_t stream) {
     int const shared = myers_table_shared_bytes(words_);
@@ -23,7 +23,7 @@ static cudaError_t myers_table_launch_words(pair_task_t const *tasks, plan_bins_
 }
 
 cudaError_t launch_myers_table(int words, int key_begin, int key_end, pair_task_t const *tasks,
-                               plan_bins_t const *bins, batch_alphabet_t const *alphabet, std::int64_t *results,
+                               plan_bins_t *bins, batch_alphabet_t const *alphabet, std::int64_t *results,
                                int ctas, cudaStream_t stream) {
     switch (words) {
     case 1: return myers_table_launch_words<1>(tasks, bins, key_begin, key_end, alphabet, results, ctas, stream);

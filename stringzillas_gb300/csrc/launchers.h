@@ -16,10 +16,13 @@ namespace szs_gb300 {
 
 cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t *tasks, std::int64_t *results,
                         int sm_count, cudaStream_t stream);
-/** Marks the bytes of both tapes and assigns dense codes (`alphabet->code`, `symbols`, `bits`), on the device.
- *  The alphabet's mark words must be zero on entry (they start zeroed and the code pass clears them again). */
+/** Marks the bytes of both tapes and assigns dense codes (`alphabet->code`, `symbols`, `bits`, `present`), on the
+ *  device. With `sample_bytes` > 0 only the first `sample_bytes` of each tape's data are marked: a guess of the
+ *  alphabet that the kernels reading it must verify. The alphabet's mark words must be zero on entry (they start
+ *  zeroed and the code pass clears them again). */
 cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
-                            batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream);
+                            batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream,
+                            std::uint64_t sample_bytes = 0);
 cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
                                   std::uint64_t stride, int sm_count, cudaStream_t stream);
 
@@ -152,9 +155,10 @@ cudaError_t launch_myers(int words, int planes, bool exact, pair_task_t const *t
                          cudaStream_t stream);
 int myers_threads_per_cta();
 /** The shared-table bit-parallel kernel for batches over at most four symbol codes: bins [key_begin, key_end),
- *  patterns of at most 32 x `words` rows (1..16). */
+ *  patterns of at most 32 x `words` rows (1..16). A pair holding a byte outside `alphabet->present` sets bit 1 of
+ *  `bins->error_flags` (its score is then not valid). */
 cudaError_t launch_myers_table(int words, int key_begin, int key_end, pair_task_t const *tasks,
-                               plan_bins_t const *bins, batch_alphabet_t const *alphabet, std::int64_t *results,
+                               plan_bins_t *bins, batch_alphabet_t const *alphabet, std::int64_t *results,
                                int ctas, cudaStream_t stream);
 /** Planes actually instantiated for a requested minimum. */
 int myers_planes_for(int bits_needed);

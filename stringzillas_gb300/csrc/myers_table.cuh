@@ -14,9 +14,14 @@
  *  - **No per-column score tracking.** The distance is read once, after the last column: the vertical deltas of the
  *    last column give `D[n][m] = D[0][m] + sum(Pv[i] - Mv[i], i = 1..n) = m + popc(Pv) - popc(Mv)` over the rows
  *    1..n, where the top row D[0][j] = j is the boundary of the global distance.
- *  - **Loads ahead of use.** The next pair's task, the text's first words (during the pattern's setup) and each next
- *    aligned 8-byte word of the text (while the current one is scored) are in flight before they are needed; the
- *    pattern is read in aligned 8-byte words too, not byte by byte.
+ *  - **Loads ahead of use.** The text's first words (during the pattern's setup) and each next aligned 8-byte word of
+ *    the text (while the current one is scored) are in flight before they are needed; the pattern is read in aligned
+ *    8-byte words too, not byte by byte.
+ *
+ *  The alphabet may be a guess from a sample of the batch (`alphabet->present`): a byte outside it gets a marker code
+ *  and a table offset that still lands inside the table, every pair ORs its codes and offsets together, and a pair
+ *  that met a marker sets bit 1 of the plan's error word, on which the host scores the call again with the exact
+ *  alphabet. Known codes (0..3) and offsets (multiples of 2,048) never carry the marker bit.
  *
  *  Per text character and pattern word the step is ten ALU operations (Xv, Eq & Pv, the carried add, Xh, Ph, Mh,
  *  two funnel shifts, Pv, Mv). The kernel takes its bins as a key range, so the plain form can run every pair with
@@ -33,6 +38,7 @@ namespace szs_gb300 {
 
 constexpr int myers_table_threads_k = 128;
 constexpr int myers_table_symbols_k = 4;
+constexpr std::uint32_t myers_table_unknown_k = 16; // code and offset marker of a byte outside the alphabet
 
 /** Bytes of the shared match-mask table of one CTA for patterns of `words` words. */
 __host__ __device__ constexpr int myers_table_shared_bytes(int words) {
@@ -90,7 +96,7 @@ __host__ __device__ constexpr int myers_table_min_ctas(int words) {
 
 template <int words_>
 __global__ void __launch_bounds__(myers_table_threads_k, myers_table_min_ctas(words_))
-    myers_table_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t const *__restrict__ bins, int key_begin,
+    myers_table_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t *__restrict__ bins, int key_begin,
                        int key_end, batch_alphabet_t const *__restrict__ alphabet,
                        std::int64_t *__restrict__ results) {
     constexpr int W = words_, Q = (words_ + 3) / 4;
@@ -101,20 +107,17 @@ __global__ void __launch_bounds__(myers_table_threads_k, myers_table_min_ctas(wo
     __shared__ std::uint8_t code_s[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
         std::uint32_t const c = alphabet->code[i] & (myers_table_symbols_k - 1);
-        code_s[i] = (std::uint8_t)c;
-        offset_s[i] = c * code_stride;
+        bool const known = (alphabet->present[i >> 5] >> (i & 31)) & 1u;
+        code_s[i] = known ? (std::uint8_t)c : (std::uint8_t)myers_table_unknown_k;
+        offset_s[i] = known ? c * code_stride : myers_table_unknown_k; // 16 bytes on: still inside the table
     }
     __syncthreads();
     unsigned char *const mine = table_s + threadIdx.x * 16u;
     std::uint32_t const begin = bins->begin[key_begin];
     std::uint32_t const count = bins->begin[key_end - 1] + bins->count[key_end - 1] - begin;
-    std::uint32_t const stride = gridDim.x * blockDim.x;
-    std::uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
-    pair_task_t upcoming; // the next pair's task, loaded while the current one is scored
-    if (index < count) upcoming = tasks[begin + index];
-    for (; index < count; index += stride) {
-        pair_task_t const task = upcoming;
-        if (index + stride < count) upcoming = tasks[begin + index + stride];
+    for (std::uint32_t index = blockIdx.x * blockDim.x + threadIdx.x; index < count;
+         index += gridDim.x * blockDim.x) {
+        pair_task_t const task = tasks[begin + index];
         std::uint8_t const *pattern = task.rows;
         std::uint32_t const n = task.rows_length, m = task.cols_length;
 
@@ -142,27 +145,47 @@ __global__ void __launch_bounds__(myers_table_threads_k, myers_table_min_ctas(wo
         std::uint32_t const last_word = (skew + n - 1) >> 3;              // the aligned word holding row n - 1
         std::uint32_t const select = 0x3210u + 0x1111u * (skew & 3u);
         bool const upper = skew >= 4;
+        std::uint32_t seen = 0; // OR of every code and table offset of the pair: the marker bit flags a guess missed
+        std::uint32_t first_bytes = 0; // the pattern's first byte, four times
         std::uint32_t plane0[W], plane1[W];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
             std::uint32_t a0 = 0, a1 = 0;
             if (32u * w < n) {
-                std::uint32_t v[10];
-#pragma unroll
-                for (int i = 0; i < 5; ++i) {
-                    uint2 const two = __ldg(aligned + min(4u * w + i, last_word));
-                    v[2 * i] = two.x, v[2 * i + 1] = two.y;
-                }
-                std::uint32_t r[8]; // r[j] = rows 32 w + 4 j .. + 3
-#pragma unroll
-                for (int j = 0; j < 8; ++j) r[j] = __byte_perm(upper ? v[j + 1] : v[j], upper ? v[j + 2] : v[j + 1], select);
+                std::uint32_t const valid = min(32u, n - 32u * w); // rows of this word inside the pattern
                 std::uint32_t halves[2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
+                    // Rows 32 w + 16 h .. + 15 from three aligned 8-byte words (clamped to the last one).
+                    std::uint32_t v[6];
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        uint2 const two = __ldg(aligned + min(4u * w + 2u * h + i, last_word));
+                        v[2 * i] = two.x, v[2 * i + 1] = two.y;
+                    }
+                    std::uint32_t r[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        r[j] = __byte_perm(upper ? v[j + 1] : v[j], upper ? v[j + 2] : v[j + 1], select);
+                    if (w == 0 && h == 0) first_bytes = __byte_perm(r[0], 0u, 0u);
+                    // Rows past the pattern's end may hold other strings' bytes or bytes past the tape: they take
+                    // the pattern's first byte instead, so they never raise the marker on their own.
+                    if (valid < 32u) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            int const keep = (int)valid - 16 * h - 4 * j; // bytes of r[j] inside the pattern
+                            std::uint32_t const mask =
+                                keep >= 4 ? 0xFFFFFFFFu : (keep <= 0 ? 0u : 0xFFFFFFFFu >> (32 - 8 * keep));
+                            r[j] = (r[j] & mask) | (first_bytes & ~mask);
+                        }
+                    }
                     std::uint32_t x = 0; // row 16 h + k's code at bits 2k (plane 0) and 2k + 1 (plane 1)
 #pragma unroll
-                    for (int k = 15; k >= 0; --k)
-                        x = x * 4u + code_s[__byte_perm(r[4 * h + k / 4], 0u, 0x4440u + (k & 3))];
+                    for (int k = 15; k >= 0; --k) {
+                        std::uint32_t const code = code_s[__byte_perm(r[k / 4], 0u, 0x4440u + (k & 3))];
+                        x = x * 4u + code;
+                        seen |= code;
+                    }
                     // Unshuffle: even bits to the low half, odd bits to the high half.
                     std::uint32_t t;
                     t = (x ^ (x >> 1)) & 0x22222222u, x ^= t ^ (t << 1);
@@ -197,20 +220,23 @@ __global__ void __launch_bounds__(myers_table_threads_k, myers_table_min_ctas(wo
 #pragma unroll
         for (int w = 0; w < W; ++w) state.pv[w] = 0xFFFFFFFFu, state.mv[w] = 0u;
 
-        for (std::uint32_t j = 0; j < head; ++j)
-            state.step(mine + offset_s[(std::uint32_t)(first_word >> (8 * (text_skew + j))) & 0xFFu]);
+        auto column = [&](std::uint32_t byte) {
+            std::uint32_t const offset = offset_s[byte];
+            seen |= offset;
+            state.step(mine + offset);
+        };
+        for (std::uint32_t j = 0; j < head; ++j) column((std::uint32_t)(first_word >> (8 * (text_skew + j))) & 0xFFu);
         for (std::uint32_t c = 0; c < full; ++c) {
             std::uint64_t const word = next;
             std::uint32_t const upcoming_word = start_word + c + 1;
             if (upcoming_word <= text_last) next = __ldg(text_words + upcoming_word);
             std::uint32_t const lo = (std::uint32_t)word, hi = (std::uint32_t)(word >> 32);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) state.step(mine + offset_s[__byte_perm(lo, 0u, 0x4440u + k)]);
+            for (int k = 0; k < 4; ++k) column(__byte_perm(lo, 0u, 0x4440u + k));
 #pragma unroll
-            for (int k = 0; k < 4; ++k) state.step(mine + offset_s[__byte_perm(hi, 0u, 0x4440u + k)]);
+            for (int k = 0; k < 4; ++k) column(__byte_perm(hi, 0u, 0x4440u + k));
         }
-        for (std::uint32_t j = 0; j < tail; ++j) // `next` holds the word after the whole ones
-            state.step(mine + offset_s[(std::uint32_t)(next >> (8 * j)) & 0xFFu]);
+        for (std::uint32_t j = 0; j < tail; ++j) column((std::uint32_t)(next >> (8 * j)) & 0xFFu); // the last word
 
         // D[n][m] = m + (rows 1..n of the last column's +1 deltas) - (its -1 deltas).
         std::int32_t score = (std::int32_t)m;
@@ -221,6 +247,7 @@ __global__ void __launch_bounds__(myers_table_threads_k, myers_table_min_ctas(wo
             score += __popc(state.pv[w] & mask) - __popc(state.mv[w] & mask);
         }
         results[task.slot] = score;
+        if (seen & myers_table_unknown_k) atomicOr(&bins->error_flags, 2u);
     }
 }
 

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 namespace szs_gb300 {
 
 __device__ __forceinline__ void tape_string(tape_t const &tape, std::uint64_t index, std::uint8_t const *&start,
@@ -310,7 +312,7 @@ __global__ void plan_scatter_kernel(plan_args_t const args, plan_bins_t *__restr
  *  per load where aligned. Grid-stride over the CTAs given to the tape: the first `tape_ctas` CTAs take `first`, the
  *  others `second` (both passes run in one launch, so their loads overlap). */
 __global__ void alphabet_mark_kernel(tape_t const first_tape, tape_t const second_tape, unsigned tape_ctas,
-                                     std::uint32_t *__restrict__ symbol_mask) {
+                                     std::uint64_t sample_bytes, std::uint32_t *__restrict__ symbol_mask) {
     bool const on_second = blockIdx.x >= tape_ctas;
     tape_t const &tape = on_second ? second_tape : first_tape;
     unsigned const block = on_second ? blockIdx.x - tape_ctas : blockIdx.x;
@@ -329,7 +331,7 @@ __global__ void alphabet_mark_kernel(tape_t const first_tape, tape_t const secon
         first = offsets[0], last = offsets[tape.count];
     }
     std::uint8_t const *data = tape.base + first;
-    std::uint64_t const length = last - first;
+    std::uint64_t const length = sample_bytes && last - first > sample_bytes ? sample_bytes : last - first;
     std::uintptr_t const address = reinterpret_cast<std::uintptr_t>(data);
     std::uint64_t head = (16 - (address & 15)) & 15;
     if (head > length) head = length;
@@ -421,11 +423,14 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
 }
 
 cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
-                            batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream) {
+                            batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream, std::uint64_t sample_bytes) {
     std::uint32_t *mask = alphabet->mask_scratch;
-    unsigned const per_tape = (unsigned)sm_count * 8;
+    // A sample needs few CTAs: 16 bytes per thread and load.
+    unsigned const per_tape = sample_bytes ? (unsigned)std::min<std::uint64_t>((std::uint64_t)sm_count * 8,
+                                                                                sample_bytes / (256 * 16 * 4) + 1)
+                                           : (unsigned)sm_count * 8;
     alphabet_mark_kernel<<<has_candidates ? 2 * per_tape : per_tape, 256, 0, stream>>>(
-        queries, has_candidates ? candidates : queries, per_tape, mask);
+        queries, has_candidates ? candidates : queries, per_tape, sample_bytes, mask);
     alphabet_codes_kernel<<<1, 32, 0, stream>>>(mask, alphabet);
     return cudaGetLastError();
 }

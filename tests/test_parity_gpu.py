@@ -785,3 +785,53 @@ def test_bounded_wait_gives_up_and_next_call_is_exact(szs, port, family, schedul
     engine.set_tuning(None)
     got = engine.pairwise(a, b).astype(np.int64)
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("where", ["pattern", "text", "both", "none"])
+def test_sampled_alphabet_guess_is_verified(szs, port, where):
+    """Unit-cost Levenshtein guesses the batch alphabet from the first MiB of each tape and the shared-table kernel
+    checks every byte against the guess; a byte the sample missed makes the engine score the call again with the
+    exact alphabet. Batches of more than 1 MiB per tape whose last pairs hold a fifth symbol in the shorter string,
+    the longer one, or both, all equal the oracle, as does a device-resident tape whose bytes after its last string
+    lie outside the alphabet."""
+    rng = np.random.default_rng(101)
+    count = 9000
+    first = random_strings(rng, count, 100, 200, DNA)
+    second = random_strings(rng, count, 150, 300, DNA)  # second strings are the longer ones (texts)
+    if where in ("pattern", "both"):
+        first[-3] = first[-3][:50] + b"N" + first[-3][51:]
+    if where in ("text", "both"):
+        second[-2] = second[-2][:70] + b"NN" + second[-2][72:]
+    engine = szs.LevenshteinDistances()
+    want = port.pairs(oracle.levenshtein_costs(), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, want)
+    engine.set_schedule("batched")
+    # Device-resident tapes with bytes outside the alphabet right after the last string.
+    import torch
+    data_a, offsets_a = tape(first)
+    data_b, offsets_b = tape(second)
+    padded_a = np.concatenate([data_a, np.frombuffer(b"ZZZZZZZZZZZZZZZZ", dtype=np.uint8)])
+    padded_b = np.concatenate([data_b, np.frombuffer(b"\x00" * 16, dtype=np.uint8)])
+    a = szs.Strs.from_buffers(torch.from_numpy(padded_a).cuda(), torch.from_numpy(offsets_a.astype(np.int64)).cuda())
+    b = szs.Strs.from_buffers(torch.from_numpy(padded_b).cuda(), torch.from_numpy(offsets_b.astype(np.int64)).cuda())
+    np.testing.assert_array_equal(engine.pairwise(a, b).astype(np.int64), want)
+    np.testing.assert_array_equal(engine.pairwise(b, a).astype(np.int64), want)
+
+
+def test_sampled_alphabet_with_other_routes(szs, port):
+    """A guessed DNA alphabet with a long pair on the warp-per-pair route, and a cross product over a five-symbol
+    batch: both fall back to the exact alphabet before scoring."""
+    rng = np.random.default_rng(102)
+    first = random_strings(rng, 7000, 100, 200, DNA) + [bytes(rng.choice(DNA, size=3000))]
+    second = random_strings(rng, 7000, 100, 300, DNA) + [bytes(rng.choice(DNA, size=3200))]
+    engine = szs.LevenshteinDistances()
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(), tape(first), tape(second)))
+    five = np.frombuffer(b"ACGTN", dtype=np.uint8)
+    queries = random_strings(rng, 40, 0, 300, five)
+    candidates = random_strings(rng, 30, 0, 300, DNA)
+    got = engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.cross(oracle.levenshtein_costs(), tape(queries), tape(candidates)))
