@@ -73,6 +73,12 @@ WORKLOADS = {
              "(16-bit codes; 16x2 wavefront in compare mode)",
     "p_long_lev": "profiling case, unit-cost Levenshtein on long DNA reads: 16,384 pairs, len U[1,000, 4,000], partner 3% "
                   "subs + 1% indels (warp-per-pair bit-parallel kernel)",
+    "short_nw": "short pairs, Needleman-Wunsch affine protein: 1,048,576 pairs, len U[16, 128], 70% identity, the protein "
+                "configuration's table, open -11 extend -1 (segmented short-pair kernel)",
+    "short_sw": "short pairs, Smith-Waterman affine DNA: 1,048,576 pairs, len U[16, 128], partner 10% subs + 2% indels, "
+                "match +2 mismatch -3 open -5 extend -2 (segmented short-pair kernel)",
+    "short_lev": "short pairs, Levenshtein with costs (0, 2, 3, 1) on DNA: 1,048,576 pairs, len U[16, 128], partner 5% "
+                 "subs + 2% indels (segmented short-pair kernel)",
 }
 
 
@@ -132,6 +138,15 @@ def make_workload(name, seed):
     if name == "text":
         first, second = w.text_pairs(262144, 100, 300, 0.05, 0.02, seed=seed)
         return first, second, ("levc", (0, 2, 3, 1))
+    if name == "short_nw":
+        first, second = w.short_pairs(1 << 20, 16, 128, "protein", 0.28, 0.02, seed=seed)
+        return first, second, ("nw", w.protein_table(seed=seed))
+    if name == "short_sw":
+        first, second = w.short_pairs(1 << 20, 16, 128, "dna", 0.10, 0.02, seed=seed)
+        return first, second, ("sw", w.dna_table(2, -3))
+    if name == "short_lev":
+        first, second = w.short_pairs(1 << 20, 16, 128, "dna", 0.05, 0.02, seed=seed)
+        return first, second, ("levp", (0, 2, 3, 1))
     if name == "p_dp32":
         first, second = w.protein_pairs(65536, seed=seed)
         byte_to_class, table = w.protein_table(seed=seed)
@@ -150,7 +165,7 @@ def make_engine(kind_and_tables):
     kind, tables = kind_and_tables
     if kind == "lev":
         engine = szs.LevenshteinDistances()
-    elif kind == "levc":  # Levenshtein with the given (match, mismatch, open, extend)
+    elif kind in ("levc", "levp"):  # Levenshtein with the given (match, mismatch, open, extend)
         engine = szs.LevenshteinDistances(*tables)
     elif kind == "levu":  # UTF-8 Levenshtein with the given (match, mismatch, open, extend)
         engine = szs.LevenshteinDistancesUTF8(*tables)
@@ -186,7 +201,7 @@ def oracle_costs(kind_and_tables):
     kind, tables = kind_and_tables
     if kind == "lev":
         return oracle.levenshtein_costs()
-    if kind == "levc":
+    if kind in ("levc", "levp"):
         return oracle.levenshtein_costs(*tables)
     if kind == "levu":
         return oracle.levenshtein_utf8_costs(*tables)
@@ -205,6 +220,8 @@ def ops_per_cell(kind_and_tables):
         return OPS_PER_CELL["dp_affine"]
     if kind in ("levc", "levu"):
         return OPS_PER_CELL["packed_compare_affine"]
+    if kind == "levp":
+        return OPS_PER_CELL["packed_affine"]
     return OPS_PER_CELL["packed_affine_local"] if kind == "sw" else OPS_PER_CELL["packed_affine"]
 
 
@@ -652,7 +669,8 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": slowest_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": {"lev": "u32", "levc": "int16x2", "levu": "int16x2"}.get(kind_and_tables[0], "int32"),
+            "scaling": "weak", "vs_baseline": None, "dtype": {"lev": "u32", "levc": "int16x2", "levu": "int16x2",
+                                                     "levp": "int16x2"}.get(kind_and_tables[0], "int32"),
             "data": "synthetic (seeded numpy PCG64)",
             "config": workload_config(args.workload, first, second, world),
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -678,7 +696,7 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_extra:
         line["cpu_baseline"] = cpu_baseline(first, second, kind_and_tables, args.cpu_seconds)
         extra = {}
-        for name in ("c3", "c4", "text"):
+        for name in ("c3", "c4", "text", "short_nw", "short_sw", "short_lev"):
             if name == args.workload:
                 continue
             f, s, kt = make_workload(name, 42)
@@ -691,6 +709,14 @@ def run_ours(args):
                 row[schedule] = {"GCUPS": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms / 2,
                                  "compute_ms_per_step": cms / 2}
             row["batched_over_plain"] = row["batched"]["GCUPS"] / row["plain"]["GCUPS"]
+            if peaks:
+                ops = ops_per_cell(kt)
+                achieved = (row["batched"]["GCUPS"] * 1e9 * row["batched"]["ms_per_step"] /
+                            row["batched"]["compute_ms_per_step"] * ops)
+                row["roofline_int"] = {"ops_per_cell": ops, "achieved_tops": achieved / 1e12,
+                                       "peak_tops": peaks["dpx_viaddmax_s16x2"] / 1e12,
+                                       "frac": achieved / peaks["dpx_viaddmax_s16x2"],
+                                       "note": "over the scoring kernels' event-timed duration"}
             row["cpu_baseline"] = cpu_baseline(f, s, kt, 3.0)
             extra[name] = row
             del batch

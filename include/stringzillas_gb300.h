@@ -478,6 +478,9 @@ typedef struct szs_gb300_tuning_t {
         barrier). Values above the built-in bounds are clamped to them, so every wait stays bounded; small values
         only make calls with long pairs fail early with `sz_status_unknown_k` (a wait that gives up never faults). */
     sz_u32_t band_wait_polls;
+    /** Pairs on 16-bit cells whose shorter side is at most this take the short-pair kernel, several pairs per warp
+        (0 = 128; larger values are clamped to 128). */
+    sz_u32_t short_max_rows;
 } szs_gb300_tuning_t;
 
 /** Installs @p tuning on @p engine (NULL restores the built-in choices); out-of-range values are rejected with

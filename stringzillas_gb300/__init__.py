@@ -358,15 +358,16 @@ class _Engine:
         """Extension: per-length-bin choices (see ``szs_gb300_tuning_t``): a dict with any of ``packed_rows`` (16
         values), ``cell_bits`` (16 values), ``band_min_rows``, ``packed_warps`` (4 values),
         ``band_min_rows_packed``, ``pipeline_chunk_kb``, ``packed_step_cost`` (4 values), ``band_min_rows_few``,
-        ``band_min_rows_compare`` and ``band_wait_polls`` (the band kernels' wait bound, clamped to the built-in
-        one); None restores the built-in choices."""
+        ``band_min_rows_compare``, ``band_wait_polls`` (the band kernels' wait bound, clamped to the built-in
+        one) and ``short_max_rows`` (shorter sides up to this take the short-pair kernel; at most 128); None restores
+        the built-in choices."""
         err = ctypes.c_char_p()
         if tuning is None:
             status = lib.szs_gb300_engine_set_tuning(self.handle, None, ctypes.byref(err))
         else:
             unknown = set(tuning) - {"packed_rows", "cell_bits", "band_min_rows", "packed_warps", "band_min_rows_packed",
                                      "pipeline_chunk_kb", "packed_step_cost", "band_min_rows_few",
-                                     "band_min_rows_compare", "band_wait_polls"}
+                                     "band_min_rows_compare", "band_wait_polls", "short_max_rows"}
             if unknown:
                 raise ValueError(f"unknown tuning fields {sorted(unknown)}")
             t = _native.Tuning()
@@ -381,6 +382,7 @@ class _Engine:
             t.band_min_rows_few = int(tuning.get("band_min_rows_few", 0))
             t.band_min_rows_compare = int(tuning.get("band_min_rows_compare", 0))
             t.band_wait_polls = int(tuning.get("band_wait_polls", 0))
+            t.short_max_rows = int(tuning.get("short_max_rows", 0))
             status = lib.szs_gb300_engine_set_tuning(self.handle, ctypes.byref(t), ctypes.byref(err))
         _native.raise_for(status, err.value, "set_tuning")
 
@@ -394,7 +396,8 @@ class _Engine:
                 "band_min_rows": t.band_min_rows, "packed_warps": list(t.packed_warps),
                 "band_min_rows_packed": t.band_min_rows_packed, "pipeline_chunk_kb": t.pipeline_chunk_kb,
                 "packed_step_cost": list(t.packed_step_cost), "band_min_rows_few": t.band_min_rows_few,
-                "band_min_rows_compare": t.band_min_rows_compare, "band_wait_polls": t.band_wait_polls}
+                "band_min_rows_compare": t.band_min_rows_compare, "band_wait_polls": t.band_wait_polls,
+                "short_max_rows": t.short_max_rows}
 
     def stats(self) -> dict:
         """Extension: counters of the last call (device time, cells, pairs, launches)."""

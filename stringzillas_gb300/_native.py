@@ -164,6 +164,7 @@ class Tuning(ctypes.Structure):
         ("band_min_rows_few", ctypes.c_uint32),
         ("band_min_rows_compare", ctypes.c_uint32),
         ("band_wait_polls", ctypes.c_uint32),
+        ("short_max_rows", ctypes.c_uint32),
     ]
 
 

@@ -33,6 +33,8 @@ UNITS = [
     ("kernels_dp16_compare", "kernels_dp16.cu", ["-DSZS_DP16_COMPARE_UNIT"]),
     ("kernels_band", "kernels_band.cu", []),
     ("kernels_band16", "kernels_band16.cu", []),
+    ("kernels_short8", "kernels_short.cu", ["-DSZS_SHORT_ROWS=8"]),
+    ("kernels_short16", "kernels_short.cu", ["-DSZS_SHORT_ROWS=16"]),
     ("probe", "probe.cu", []),
     ("static_scratch", "static_scratch.cu", []),
     ("server", "server.cu", []),

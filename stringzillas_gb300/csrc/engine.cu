@@ -748,6 +748,9 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                                                    : (std::uint32_t)band_min_rows_packed_k;
     args.band_min_rows_compare = engine.tuning.band_min_rows_compare ? engine.tuning.band_min_rows_compare
                                                                      : (std::uint32_t)band_min_rows_compare_k;
+    args.short_max_rows = engine.tuning.short_max_rows
+                              ? std::min<std::uint32_t>(engine.tuning.short_max_rows, (std::uint32_t)short_max_rows_k)
+                              : (std::uint32_t)short_max_rows_k;
     // A batched call with fewer pairs than one wave of the 16x2 route (two pairs per warp, about 16 resident warps
     // per SM) would leave SMs idle on the wavefront: its longer pairs spread over a band CTA's warps instead.
     if (schedule != szs_gb300_schedule_plain_k && args.pairs < 32ull * (std::uint64_t)context->sm_count) {
@@ -900,6 +903,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     int const compare_mode =
         packed_compare ? compare_mode_for(costs.match - shift, costs.mismatch - shift) : (int)compare_none_k;
     if (levenshtein && (pairs_in(bin_dp16_begin_k, bin_dp16_begin_k + bin_dp16_classes_k) ||
+                        pairs_in(bin_short_begin_k, bin_short_begin_k + short_shapes_k * short_m_classes_k) ||
                         pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k))) {
         packed_costs.classes = packed_compare ? 1 : (int)alphabet_host.symbols;
         if (!wide) // 16-bit codes are compared as they are; no alphabet pass ran
@@ -914,7 +918,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
 
     // The launch list, longest pairs first (64- and 32-bit wavefront, packed with the most rows per lane, then the
     // bit-parallel kernels by word count), so the routes' tails overlap each other instead of adding up.
-    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k, job_myers_warp_k };
+    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k, job_myers_warp_k, job_short_k };
     struct job_t {
         job_kind_t kind;
         int variant; // cell bits, rows per lane, or words
@@ -1031,6 +1035,24 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * shape.ctas_per_sm;
         scratch_total += bytes;
     }
+    // Short pairs: one job per segment shape, most rows first.
+    for (int shape_index = short_shapes_k - 1; shape_index >= 0; --shape_index) {
+        int const key_begin = bin_short_begin_k + shape_index * short_m_classes_k;
+        int const key_end = key_begin + short_m_classes_k;
+        std::uint64_t const pairs_here = pairs_in(key_begin, key_end);
+        if (!pairs_here) continue;
+        int const warps = 4;
+        dp_launch_shape_t const shape =
+            short_shape(engine.kind, costs.affine != 0, shape_index, packed_costs.classes, warps, compare_mode);
+        if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Short-pair kernel cannot be resident"};
+        int const rows = short_rows_for(packed_costs.classes, compare_mode);
+        std::uint64_t const per_warp = 2u * (32u / (std::uint64_t)((16 << shape_index) / rows)); // pairs per warp
+        std::uint64_t const warps_needed = (pairs_here + per_warp - 1) / per_warp;
+        std::uint64_t const needed = (warps_needed + warps - 1) / warps;
+        int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);
+        jobs[job_count++] = {job_short_k, shape_index, warps, key_begin, key_end, pairs_here, ctas, 0, 0};
+        jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * shape.ctas_per_sm;
+    }
     int myers_planes = 0;
     if (engine.unit_levenshtein) {
         myers_planes = wide ? 16 : myers_planes_for((int)alphabet_host.bits);
@@ -1128,6 +1150,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
                                          lane_stream, compare_mode, wide));
+            else if (job.kind == job_short_k)
+                SZS_TRY_CUDA(launch_short(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end,
+                                          tasks, bins, packed_costs, results, job.ctas, job.warps, lane_stream,
+                                          compare_mode));
             else if (job.kind == job_myers_warp_k && wide)
                 SZS_TRY_CUDA(launch_myers_warp_wide(job.variant, tasks, bins, job.key_begin, job.key_end, results,
                                                     job.ctas, lane_stream));
@@ -1222,8 +1248,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     stats.last_compute_ms = compute;
     if (tracing) {
         static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits",
-                                            "band16 bits", "warp bit-parallel"};
-        static_assert(sizeof(names) / sizeof(names[0]) == job_myers_warp_k + 1, "a name per job kind");
+                                            "band16 bits", "warp bit-parallel", "short shape"};
+        static_assert(sizeof(names) / sizeof(names[0]) == job_short_k + 1, "a name per job kind");
         for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
             float ms = 0, offset = 0;
             cudaEventElapsedTime(&ms, context->trace_events[2 * i], context->trace_events[2 * i + 1]);

@@ -138,6 +138,15 @@ cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pai
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
                           int group_ctas = 1, int compare = 0, bool wide = false);
 
+/** Short pairs (shorter side at most 128) on the segmented 16x2 kernel: `shape` 0, 1, 2, 3 for shorter sides up to
+ *  16, 32, 64, 128; segments of 16 rows per lane when `short_rows_for` says 16 (compare mode or at most 8 classes),
+ *  else of 8 rows per lane; `compare` as for the 16x2 wavefront (Levenshtein only). */
+int short_rows_for(int classes, int compare);
+dp_launch_shape_t short_shape(int kind, bool affine, int shape, int classes, int warps, int compare = 0);
+cudaError_t launch_short(int kind, bool affine, int shape, int key_begin, int key_end, pair_task_t const *tasks,
+                         plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, int ctas, int warps,
+                         cudaStream_t stream, int compare = 0);
+
 /** Bit-parallel kernels over strings of 16-bit codes (UTF-8 calls over more than 256 code points, 16 code planes):
  *  thread per pair over the bins of `words` words (1..8), and warp per pair over the warp bins (1..8 words per
  *  lane). */

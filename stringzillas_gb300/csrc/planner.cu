@@ -123,6 +123,18 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     // running maximum against the 16-bit limit and scores a pair that reached it again on 32-bit cells.
     bool const local_band16 =
         args.local_gain >= 0 && args.packed_allowed && profile_fits && args.cell_bits[length_class] != 32;
+    // Short pairs: a few lanes per pair instead of a warp (dp_short.cuh).
+    if (packed && !args.wide && n <= args.short_max_rows) {
+        if (args.force_route >= 0) {
+            info.key = bin_short_begin_k + 3 * short_m_classes_k; // plain form: one bin (128-row segments), input order
+            return info;
+        }
+        int const shape = n <= 16 ? 0 : (n <= 32 ? 1 : (n <= 64 ? 2 : 3));
+        int m_class = m < 512 ? int(m / 16) : 32 + floor_log2_u64(m) - 9;
+        m_class = m_class > short_m_classes_k - 1 ? short_m_classes_k - 1 : m_class;
+        info.key = bin_short_begin_k + shape * short_m_classes_k + (short_m_classes_k - 1 - m_class);
+        return info;
+    }
     if (n > band_rows && fits32_early) {
         // Long pairs take a band in both forms (16-bit cells when they fit); the plain form keeps them in one bin,
         // in input order.
@@ -207,7 +219,8 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
         }
         atomicAdd(&histogram[info.key], 1u);
         if (info.key >= bin_dp32_begin_k) thread_max_cols = max(thread_max_cols, info.m);
-        if (info.key >= bin_myers_warp_begin_k) thread_max_myers_warp = max(thread_max_myers_warp, info.n);
+        if (info.key >= bin_myers_warp_begin_k && info.key < bin_short_begin_k)
+            thread_max_myers_warp = max(thread_max_myers_warp, info.n);
         else if (info.key < bin_myers_begin_k + (myers_max_words_k + 1) * 16)
             thread_max_myers = max(thread_max_myers, info.n);
     }

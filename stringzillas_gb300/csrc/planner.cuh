@@ -20,6 +20,8 @@
  *    [1392, 1424) 16-bit band (one CTA per pair, 16x2 cells): same layout from 1392
  *    [1424, 1488) warp-per-pair Myers (unit Levenshtein, shorter side 513..8,192): key = 1424 + 8 * (8 - W)
  *                 + (7 - text class), W = words per lane = ceil(n / 1024), text class ~ log2(m) - 9
+ *    [1488, 1680) short pairs on 16x2 cells (shorter side <= 128): key = 1488 + 48 * shape + (47 - m class),
+ *                 shape 0/1/2/3 for n <= 16/32/64/128, m class = m / 16 below 512, then 32 + log2(m) - 9
  */
 #pragma once
 #include "engine_types.cuh"
@@ -55,6 +57,11 @@ constexpr int myers_warp_classes_k = 8;    // text-length classes per words coun
 constexpr int bin_myers_warp_begin_k = bin_band16_begin_k + bin_dp_classes_k; // 1424
 static_assert(bin_myers_warp_begin_k + myers_warp_max_words_k * myers_warp_classes_k <= bin_keys_k,
               "bin layout exceeds the key space");
+constexpr int bin_short_begin_k = bin_myers_warp_begin_k + myers_warp_max_words_k * myers_warp_classes_k; // 1488
+constexpr int short_shapes_k = 4;      // segments holding 16, 32, 64 and 128 rows
+constexpr int short_m_classes_k = 48;  // text-length classes per shape
+constexpr int short_max_rows_k = 128;  // default: shorter sides up to this take the short route
+static_assert(bin_short_begin_k + short_shapes_k * short_m_classes_k <= bin_keys_k, "bin layout exceeds the key space");
 
 /** Which pairs a call scores. */
 enum pair_mode_t : int {
@@ -95,6 +102,7 @@ struct plan_args_t {
     std::uint32_t band_min_rows_packed; // the same for pairs that fit 16-bit cells
     std::uint16_t packed_step_cost[4];  // relative cost of one lane step with 4, 8, 12, 16 rows per lane
     std::uint32_t band_min_rows_compare; // the same for compare-mode Levenshtein pairs (no profile)
+    std::uint32_t short_max_rows;        // 16x2 pairs whose shorter side is at most this take the short route
 };
 
 /** Per-bin counters the planner fills. */

@@ -6,6 +6,8 @@ Each generator returns tapes as ``(data: uint8[], offsets: int64[count + 1])`` p
 * ``levenshtein_reads``: DNA pairs, first string length uniform in [low, high], second derived from the first by
   per-base substitutions and single-character insertions/deletions (configs "plain Levenshtein" 1,024 pairs
   U[64,256] 5%/2%, and "batched Levenshtein" 1,048,576 pairs U[100,300] 3%/1%).
+* ``short_pairs``: DNA or protein pairs with first lengths uniform in [low, high] (16-128 by default) and a mutant
+  partner, for the short-pair kernel.
 * ``protein_pairs``: 20 amino acids at background frequencies, length log-normal (median 350, sigma 0.6) clipped to
   [50, 2000], partner = a mutant with the requested identity (substitutions plus a small indel rate).
 * ``protein_table``: symmetric int8 20x20 scores, diagonal U{4..11}, off-diagonal U{-4..3}, folded into the
@@ -112,6 +114,23 @@ def cjk_pairs(count, low, high, substitution_rate, indel_rate, seed=42):
         return out.reshape(-1)
 
     return (encode(first), offsets * 3), (encode(second), second_offsets * 3)
+
+
+def short_pairs(count, low=16, high=128, alphabet="dna", substitution_rate=0.10, indel_rate=0.02, seed=42):
+    """Short pairs, first length uniform in [low, high], partner a mutant of it: DNA (uniform letters) or protein
+    (background frequencies)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = rng.integers(low, high + 1, size=count)
+    offsets = _offsets(lengths)
+    if alphabet == "protein":
+        p = AMINO_FREQUENCIES / AMINO_FREQUENCIES.sum()
+        first = _letters(rng, AMINO_ACIDS, int(offsets[-1]), p)
+        second, second_offsets = _mutate(rng, first, offsets, AMINO_ACIDS, substitution_rate, indel_rate,
+                                         probabilities=p)
+    else:
+        first = _letters(rng, DNA, int(offsets[-1]))
+        second, second_offsets = _mutate(rng, first, offsets, DNA, substitution_rate, indel_rate)
+    return (first, offsets), (second, second_offsets)
 
 
 def protein_pairs(count, median=350.0, sigma=0.6, low=50, high=2000, identity=0.70, indel_rate=0.02, seed=42):

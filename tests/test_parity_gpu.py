@@ -19,6 +19,11 @@ def szs():
     return stringzillas_gb300
 
 
+def zlib_seed(*parts):
+    import zlib
+    return zlib.crc32(repr(parts).encode())
+
+
 def random_strings(rng, count, low, high, alphabet):
     return [bytes(rng.choice(alphabet, size=int(rng.integers(low, high + 1)))) for _ in range(count)]
 
@@ -835,3 +840,51 @@ def test_sampled_alphabet_with_other_routes(szs, port):
     candidates = random_strings(rng, 30, 0, 300, DNA)
     got = engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64)
     np.testing.assert_array_equal(got, port.cross(oracle.levenshtein_costs(), tape(queries), tape(candidates)))
+
+
+@pytest.mark.parametrize("name,family,costs", ENGINES, ids=[e[0] for e in ENGINES])
+def test_short_pairs_every_segment_shape(szs, port, name, family, costs):
+    """Shorter sides up to 128 take the segmented short-pair kernel (segments of 16 to 128 rows, two pairs per
+    segment; 8 rows per lane for protein profiles, 16 for DNA): every shape, partners from 1 to 600 characters, odd
+    counts that leave segments and halves empty, both schedules, and the short threshold tuned down."""
+    rng = np.random.default_rng(zlib_seed(name))
+    alphabet = DNA if family != "nw" or name == "nw-positive-gaps" else PROTEIN
+    b2c, table = dna_tables() if alphabet is DNA else protein_tables(rng, symmetric=False)
+    lengths = [(int(rng.integers(1, 129)), int(rng.integers(1, 300))) for _ in range(333)]
+    lengths += [(n, m) for n in (1, 2, 15, 16, 17, 31, 32, 33, 63, 64, 65, 127, 128) for m in (1, 3, 64, 65, 600)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    for k in range(0, len(first), 7):
+        first[k], second[k] = second[k], first[k]  # the short string on the second side
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        bad = np.flatnonzero(got != want)
+        assert bad.size == 0, f"{name} {schedule}: {bad.size} mismatches, first {bad[:5]}: {got[bad[:5]]} vs {want[bad[:5]]}"
+    engine.set_schedule("batched")
+    for short_rows in (16, 32, 64):
+        engine.set_tuning({"short_max_rows": short_rows})
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
+    engine.set_tuning(None)
+    queries, candidates = first[:23], second[:17]
+    np.testing.assert_array_equal(engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64),
+                                  port.cross(oracle_costs, tape(queries), tape(candidates)))
+
+
+@pytest.mark.parametrize("costs", [(0, 2, 3, 1), (0, 3, 2, 2), (3, 1, 5, 5), (0, 5, 3, 1)])
+def test_short_pairs_compare_mode(szs, port, costs):
+    """Levenshtein over more than 32 byte values on the short-pair kernel compares codes: both cost forms, codes 0 and
+    255 side by side."""
+    rng = np.random.default_rng(sum(costs) + 500)
+    letters = np.arange(256, dtype=np.uint8)
+    lengths = [(int(rng.integers(1, 129)), int(rng.integers(1, 200))) for _ in range(301)]
+    first = [bytes(rng.choice(letters, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(letters, size=m)) for _, m in lengths]
+    first[0], second[0] = b"\x00\xff" * 20, b"\xff\x00" * 30
+    engine = szs.LevenshteinDistances(*costs)
+    want = port.pairs(oracle.levenshtein_costs(*costs), tape(first), tape(second))
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)

@@ -134,11 +134,11 @@ def test_tuning_round_trip_and_validation():
     assert engine.get_tuning() == {"packed_rows": [0] * 16, "cell_bits": [0] * 16, "band_min_rows": 0,
                                    "packed_warps": [0] * 4, "band_min_rows_packed": 0, "pipeline_chunk_kb": 0,
                                    "packed_step_cost": [0] * 4, "band_min_rows_few": 0, "band_min_rows_compare": 0,
-                                   "band_wait_polls": 0}
+                                   "band_wait_polls": 0, "short_max_rows": 0}
     tuning = {"packed_rows": [0, 0, 0, 4, 4, 8, 8, 12, 16, 16, 16, 0, 0, 0, 0, 0], "cell_bits": [32] + [0] * 15,
               "band_min_rows": 2048, "packed_warps": [2, 4, 8, 4], "band_min_rows_packed": 3000,
               "pipeline_chunk_kb": 8192, "packed_step_cost": [100, 170, 240, 320], "band_min_rows_few": 700,
-              "band_min_rows_compare": 1500, "band_wait_polls": 1000}
+              "band_min_rows_compare": 1500, "band_wait_polls": 1000, "short_max_rows": 32}
     engine.set_tuning(tuning)
     assert engine.get_tuning() == tuning
     for bad in ({"packed_rows": [3] * 16}, {"cell_bits": [16] * 16}, {"packed_warps": [9, 0, 0, 0]},
