@@ -116,11 +116,14 @@ class Strs:
         if array.null_count:
             raise ValueError("null strings are not supported")
         self._as_bytes = pa.types.is_binary(array.type) or pa.types.is_large_binary(array.type)
+        # Zero copy: both views alias Arrow's own buffers, and 32-bit offsets reach the `_u32tape` entry points as
+        # they are (python/stringzillas/stringzillas.h:158-174 exports Arrow tapes the same way). A sliced array keeps
+        # its parent's offsets, so the first offset is generally not zero.
         _, offsets_buffer, data_buffer = array.buffers()
         offsets = np.frombuffer(offsets_buffer, dtype=offset_dtype)[array.offset:array.offset + len(array) + 1]
         data = (np.frombuffer(data_buffer, dtype=np.uint8) if data_buffer is not None
                 else np.zeros(0, dtype=np.uint8))
-        self._set(data, offsets.astype(np.uint64), 0, len(array))
+        self._set(data, offsets, 0, len(array))
         self._keep = array
 
     @classmethod

@@ -176,3 +176,34 @@ def test_pairwise_u32tape(env, port, name, family, costs):
             ctypes.c_void_p(out.ctypes.data), ctypes.byref(err))
         assert status == 0, err.value
         np.testing.assert_array_equal(out, want)
+
+
+def test_arrow_tapes_used_in_place(env, port):
+    """Arrow string arrays (32-bit offsets) and large-string arrays (64-bit) reach the engine without copies or
+    widening, sliced or whole; where pyarrow is absent, numpy buffers laid out the same way stand in for them."""
+    szs, native = env
+    rng = np.random.default_rng(31)
+    strings = [bytes(rng.choice(DNA, size=int(n))) for n in rng.integers(0, 300, size=120)]
+    others = [bytes(rng.choice(DNA, size=int(n))) for n in rng.integers(0, 300, size=120)]
+    try:
+        import pyarrow as pa
+        a32 = szs.Strs(pa.array(strings, type=pa.binary()))
+        b32 = szs.Strs(pa.array(others, type=pa.binary()))
+        a64 = szs.Strs(pa.array(strings, type=pa.large_binary()))
+        sliced = szs.Strs(pa.array(strings, type=pa.binary()).slice(7, 50))
+    except ImportError:
+        def tape32(items):
+            data, offsets = tape(items)
+            return szs.Strs.from_buffers(data.copy(), offsets.astype(np.uint32))
+        a32, b32 = tape32(strings), tape32(others)
+        a64 = szs.Strs.from_buffers(*tape(strings))
+        sliced = tape32(strings)[7:57]
+    assert a32.tape()[1] == 32 and a64.tape()[1] == 64
+    engine = szs.LevenshteinDistances(0, 2, 3, 1)
+    costs = oracle.levenshtein_costs(0, 2, 3, 1)
+    want = port.pairs(costs, tape(strings), tape(others))
+    np.testing.assert_array_equal(engine.pairwise(a32, b32).astype(np.int64), want)
+    np.testing.assert_array_equal(engine.pairwise(a64, b32).astype(np.int64), want)  # mixed widths
+    np.testing.assert_array_equal(engine(sliced).astype(np.int64), port.cross(costs, tape(strings[7:57])))
+    np.testing.assert_array_equal(engine(a32[:20], b32[5:30]).astype(np.int64),
+                                  port.cross(costs, tape(strings[:20]), tape(others[5:30])))

@@ -75,6 +75,15 @@ def test_strs_from_pyarrow():
     s = szs.Strs(arrow)
     assert list(s) == ["hello", "", "world", "a"]
     assert list(szs.Strs(arrow.slice(1, 2))) == ["", "world"]
+    # Zero copy: the tape points into Arrow's own buffers, 32-bit offsets stay 32-bit, 64-bit ones stay 64-bit.
+    tape, bits = s.tape()
+    _, offsets_buffer, data_buffer = arrow.buffers()
+    assert bits == 32 and tape.offsets == offsets_buffer.address and tape.data == data_buffer.address
+    sliced, bits = szs.Strs(arrow.slice(1, 2)).tape()
+    assert bits == 32 and sliced.offsets == offsets_buffer.address + 4 and sliced.count == 2
+    large = pa.array(["xy", "z"], type=pa.large_string())
+    tape, bits = szs.Strs(large).tape()
+    assert bits == 64 and tape.offsets == large.buffers()[1].address
 
 
 def test_calls_validate_before_running():
