@@ -33,6 +33,7 @@ UNITS = [
     ("kernels_dp16_compare", "kernels_dp16.cu", ["-DSZS_DP16_COMPARE_UNIT"]),
     ("kernels_band", "kernels_band.cu", []),
     ("kernels_band16", "kernels_band16.cu", []),
+    ("direct", "direct.cu", []),
     ("kernels_short8", "kernels_short.cu", ["-DSZS_SHORT_ROWS=8"]),
     ("kernels_short16", "kernels_short.cu", ["-DSZS_SHORT_ROWS=16"]),
     ("probe", "probe.cu", []),

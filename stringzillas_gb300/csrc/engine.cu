@@ -269,6 +269,15 @@ struct device_context_t {
     batch_alphabet_t *alphabet_host() const noexcept {
         return reinterpret_cast<batch_alphabet_t *>(static_cast<unsigned char *>(readback.data) + sizeof(plan_bins_t));
     }
+    /** 256 spare bytes after the plan and the alphabet, on the device and in the pinned readback area. */
+    std::uint32_t *spare_device() const noexcept {
+        return reinterpret_cast<std::uint32_t *>(static_cast<unsigned char *>(control.data) + sizeof(plan_bins_t) +
+                                                 sizeof(batch_alphabet_t));
+    }
+    std::uint64_t *spare_host() const noexcept {
+        return reinterpret_cast<std::uint64_t *>(static_cast<unsigned char *>(readback.data) + sizeof(plan_bins_t) +
+                                                 sizeof(batch_alphabet_t));
+    }
     void release() noexcept {
         if (!ready) return;
         cudaSetDevice(device);
@@ -718,6 +727,48 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         status = transcode_utf8(context, stream, args.queries, args.candidates, call.has_candidates, wide);
         if (!status.ok()) return status;
         args.wide = wide ? 1 : 0;
+    }
+
+    // Cross products of short tokens under unit costs, into device-resident results: when both tapes hold at most 64
+    // bytes per string on average, one kernel scores every cell in place (one thread per cell, no planning); a
+    // string longer than 64 bytes raises its flag, and the general path below scores the call.
+    if (engine.unit_levenshtein && !engine.utf8 && call.mode == mode_cross_k && schedule != szs_gb300_schedule_plain_k &&
+        !defer && device_accessible(call.out)) {
+        std::uint64_t *ends = context->spare_host(); // offsets[0] and offsets[count] of both tapes
+        tape_t const *tapes[2] = {&args.queries, &args.candidates};
+        for (int k = 0; k < 2; ++k) {
+            std::size_t const width = tapes[k]->offset_bits == 32 ? 4 : 8;
+            auto const *offsets = static_cast<unsigned char const *>(tapes[k]->offsets);
+            ends[2 * k] = ends[2 * k + 1] = 0;
+            SZS_TRY_CUDA(cudaMemcpyAsync(&ends[2 * k], offsets, width, cudaMemcpyDefault, stream));
+            SZS_TRY_CUDA(cudaMemcpyAsync(&ends[2 * k + 1], offsets + tapes[k]->count * width, width, cudaMemcpyDefault,
+                                         stream));
+        }
+        SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+        std::uint64_t const query_bytes = ends[1] - ends[0], candidate_bytes = ends[3] - ends[2];
+        if (query_bytes <= 64 * queries_count && candidate_bytes <= 64 * candidates_count) {
+            std::uint32_t *flag = context->spare_device();
+            SZS_TRY_CUDA(cudaEventRecord(context->start, stream));
+            SZS_TRY_CUDA(cudaMemsetAsync(flag, 0, sizeof(std::uint32_t), stream));
+            SZS_TRY_CUDA(cudaEventRecord(context->compute_start, stream));
+            SZS_TRY_CUDA(launch_myers_direct(args, call.out, call.stride, flag, context->sm_count, stream));
+            SZS_TRY_CUDA(cudaEventRecord(context->compute_stop, stream));
+            auto *flag_host = reinterpret_cast<std::uint32_t *>(ends + 4);
+            *flag_host = 0;
+            SZS_TRY_CUDA(cudaMemcpyAsync(flag_host, flag, sizeof(std::uint32_t), cudaMemcpyDeviceToHost, stream));
+            SZS_TRY_CUDA(cudaEventRecord(context->stop, stream));
+            SZS_TRY_CUDA(cudaStreamSynchronize(stream));
+            if (*flag_host == 0) {
+                float elapsed = 0, compute = 0;
+                cudaEventElapsedTime(&elapsed, context->start, context->stop);
+                cudaEventElapsedTime(&compute, context->compute_start, context->compute_stop);
+                stats.last_call_ms = elapsed, stats.last_compute_ms = compute;
+                stats.last_cells = query_bytes * candidate_bytes; // sum over cells of n x m
+                stats.last_launches = 1;
+                stats.kernel_launches += 1;
+                return {};
+            }
+        }
     }
 
     // Work buffers: tasks, then dense results.

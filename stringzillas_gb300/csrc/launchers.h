@@ -23,6 +23,11 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
 cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
                             batch_alphabet_t *alphabet, int sm_count, cudaStream_t stream,
                             std::uint64_t sample_bytes = 0);
+/** Unit-cost Levenshtein over a cross product (`args.mode == mode_cross_k`) straight into `out` (row stride in
+ *  elements), one thread per cell; sets `*flag` to 1 if a string has more than 64 bytes (its cells are then not
+ *  written). */
+cudaError_t launch_myers_direct(plan_args_t const &args, std::int64_t *out, std::uint64_t stride,
+                                std::uint32_t *flag, int sm_count, cudaStream_t stream);
 cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,
                                   std::uint64_t stride, int sm_count, cudaStream_t stream);
 

@@ -888,3 +888,29 @@ def test_short_pairs_compare_mode(szs, port, costs):
     for schedule in ("batched", "plain"):
         engine.set_schedule(schedule)
         np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
+
+
+@pytest.mark.parametrize("longest", [64, 65], ids=["all-short", "one-long"])
+def test_tiny_token_cross_product_in_place(szs, port, longest):
+    """Unit-cost cross products of tokens of at most 64 bytes into device-resident matrices are scored by one
+    thread per cell without planning; a token of 65 bytes makes the call take the general path. Empty tokens,
+    one- and two-word patterns, 32- and 64-bit offsets, and a row stride wider than the candidates."""
+    import torch
+    rng = np.random.default_rng(longest)
+    letters = np.arange(256, dtype=np.uint8)
+    queries = [bytes(rng.choice(letters, size=int(n))) for n in rng.integers(0, 41, size=150)]
+    candidates = [bytes(rng.choice(letters[:6], size=int(n))) for n in rng.integers(0, 41, size=90)]
+    queries[3], queries[4], candidates[5] = b"", bytes(rng.choice(letters, size=64)), bytes(rng.choice(letters, size=longest))
+    queries[7] = candidates[8] = bytes(rng.choice(letters[:6], size=33))
+    want = port.cross(oracle.levenshtein_costs(), tape(queries), tape(candidates))
+    engine = szs.LevenshteinDistances()
+    for bits in (32, 64):
+        def device(items):
+            data, offsets = tape(items)
+            return szs.Strs.from_buffers(torch.from_numpy(data.copy()).cuda(),
+                                         torch.from_numpy(offsets.astype(np.int32 if bits == 32 else np.int64)).cuda())
+        out = torch.full((len(queries), len(candidates) + 3), -1, dtype=torch.int64, device="cuda")
+        engine(device(queries), device(candidates), out=out)
+        got = out.cpu().numpy()
+        np.testing.assert_array_equal(got[:, :len(candidates)], want)
+        assert (got[:, len(candidates):] == -1).all()
