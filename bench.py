@@ -99,6 +99,7 @@ def parse_args():
     parser.add_argument("--fingerprints-only", action="store_true",
                         help="run only the Min-Hash leg and print its JSON object")
     parser.add_argument("--fp-documents", type=int, default=16384, help="documents of the Min-Hash leg")
+    parser.add_argument("--cross-only", action="store_true", help="run only the all-pairs leg and print its object")
     return parser.parse_args()
 
 
@@ -487,6 +488,82 @@ def serving_leg(szs):
     return out
 
 
+# The reference's published all-pairs figures on an H100 (include/stringzillas/similarities/README.md:13-26):
+# balanced tiles of equal-length `acgt` sequences, unit cost scheme, GCUPS.
+REFERENCE_H100_CROSS_GCUPS = {100: {"levenshtein": 1499.8, "needleman_wunsch": 187.3, "smith_waterman": 164.8},
+                              1000: {"levenshtein": 5910.8, "needleman_wunsch": 711.3, "smith_waterman": 615.8}}
+
+
+def cross_product_leg(szs, torch, scope, steps=10, warmup=3):
+    """All-pairs tiles at the reference's published methodology: a balanced square of 256 pairs per SM (q197 x c198
+    on 152 SMs) of equal-length `acgt` sequences at 100 and 1,000 bytes, unit costs (Levenshtein 0/1/1; NW and SW
+    match 0, mismatch -1, gap -1), device-resident tapes and result matrix, CUDA events over `steps` calls. Plus a
+    tiny-token cross product (2,048 x 2,048 printable tokens of 4-16 bytes) on the one-thread-per-cell path."""
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    pairs = 256 * sms
+    rows = int(np.sqrt(pairs))
+    cols = (pairs + rows - 1) // rows
+    stream = torch.cuda.current_stream()
+    letters = np.frombuffer(b"acgt", dtype=np.uint8)
+    b2c = np.zeros(256, dtype=np.uint8)
+    b2c[letters] = [1, 2, 3, 4]
+    table = np.zeros((32, 32), dtype=np.int8)
+    table[1:5, 1:5] = -1
+    np.fill_diagonal(table[1:5, 1:5], 0)
+    engines = {"levenshtein": szs.LevenshteinDistances(),
+               "needleman_wunsch": szs.NeedlemanWunschScores(b2c, table, open=-1, extend=-1),
+               "smith_waterman": szs.SmithWatermanScores(b2c, table, open=-1, extend=-1)}
+
+    def device_strs(data, count, length):
+        offsets = np.arange(count + 1, dtype=np.int64) * length
+        return szs.Strs.from_buffers(torch.from_numpy(data).cuda(), torch.from_numpy(offsets).cuda())
+
+    def timed(engine, queries, candidates, out):
+        for _ in range(warmup):
+            engine(queries, candidates, device=scope, out=out)
+        begin, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        begin.record(stream)
+        for _ in range(steps):
+            engine(queries, candidates, device=scope, out=out)
+        end.record(stream)
+        torch.cuda.synchronize()
+        return begin.elapsed_time(end) / steps
+
+    out = {"method": f"balanced all-pairs tile q{rows} x c{cols} (256 pairs per SM x {sms} SMs), equal-length acgt "
+                     "sequences, unit costs, device-resident inputs and results, one call per step",
+           "tile": [rows, cols]}
+    rng = np.random.Generator(np.random.PCG64(11))
+    for length in (100, 1000):
+        queries = device_strs(letters[rng.integers(0, 4, size=rows * length)], rows, length)
+        candidates = device_strs(letters[rng.integers(0, 4, size=cols * length)], cols, length)
+        result = torch.empty((rows, cols), dtype=torch.int64, device="cuda")
+        cells = rows * cols * length * length
+        row = {}
+        for name, engine in engines.items():
+            ms = timed(engine, queries, candidates, result)
+            row[name] = {"GCUPS": cells / (ms * 1e-3) / 1e9, "ms_per_call": ms,
+                         "reference_h100_GCUPS": REFERENCE_H100_CROSS_GCUPS[length][name]}
+        out[f"{length}_bytes"] = row
+    # Tiny tokens: the one-thread-per-cell path.
+    count = 2048
+    lengths = rng.integers(4, 17, size=2 * count)
+    data = rng.integers(32, 127, size=int(lengths.sum()), dtype=np.uint8)
+    offsets = np.zeros(2 * count + 1, dtype=np.int64)
+    np.cumsum(lengths, out=offsets[1:])
+    queries = szs.Strs.from_buffers(torch.from_numpy(data[:offsets[count]].copy()).cuda(),
+                                    torch.from_numpy(offsets[:count + 1].copy()).cuda())
+    candidates = szs.Strs.from_buffers(torch.from_numpy(data[offsets[count]:].copy()).cuda(),
+                                       torch.from_numpy((offsets[count:] - offsets[count]).copy()).cuda())
+    result = torch.empty((count, count), dtype=torch.int64, device="cuda")
+    ms = timed(engines["levenshtein"], queries, candidates, result)
+    cells = int(lengths[:count].sum()) * int(lengths[count:].sum())
+    out["tiny_tokens"] = {"workload": "unit-cost Levenshtein, 2,048 x 2,048 printable tokens of 4-16 bytes",
+                          "GCUPS": cells / (ms * 1e-3) / 1e9, "ms_per_call": ms,
+                          "cells_per_second": count * count / (ms * 1e-3)}
+    return out
+
+
 FINGERPRINT_WORKLOAD = ("Min-Hash fingerprints: 16,384 documents, len U[1,000, 3,000] printable bytes, 1,024 dimensions, "
                         "default widths {3,4,5,7,9,11,15,31} (64-dimension slices), seed 0")
 # Integer operations per byte and dimension, counted from the rolling step: x = state*a + D*out + (D + 1 + in) (two
@@ -721,6 +798,7 @@ def run_ours(args):
             extra[name] = row
             del batch
         line["extra"] = extra
+        line["cross_product"] = cross_product_leg(szs, torch, scope)
         line["serving"] = serving_leg(szs)
         line["fingerprints"] = fingerprints_leg(szs, torch, scope, peaks)
     elif rank == 0:
@@ -741,9 +819,19 @@ def run_fingerprints_only(args):
     print(json.dumps(leg), flush=True)
 
 
+def run_cross_only(args):
+    import torch
+    import stringzillas_gb300 as szs
+    torch.cuda.set_device(0)
+    scope = szs.DeviceScope(gpu_device=0, stream=torch.cuda.current_stream())
+    print(json.dumps(cross_product_leg(szs, torch, scope, steps=args.steps, warmup=args.warmup)), flush=True)
+
+
 def main():
     args = parse_args()
-    if args.fingerprints_only:
+    if args.cross_only:
+        run_cross_only(args)
+    elif args.fingerprints_only:
         run_fingerprints_only(args)
     elif args.impl == "reference":
         run_reference(args)
