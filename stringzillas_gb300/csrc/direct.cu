@@ -2,15 +2,15 @@
  *  @file direct.cu
  *  @brief Cross products of short tokens under unit-cost Levenshtein: one thread per output cell, no planning.
  *
- *  A cross-product (or symmetric) call over strings of at most 64 bytes spends most of its time in planning when it
+ *  A cross-product call over strings of at most 64 bytes spends most of its time in planning when it
  *  takes the general path: the pair enumeration, binning and task scatter touch every pair, and a host round trip
  *  separates planning from scoring. When every string of both tapes has at most 64 bytes, each output cell is one
  *  bit-parallel distance over a pattern of at most two 32-bit words, cheap enough to compute where it lands. So one
- *  kernel takes one cell per thread: it reads the two strings through the tapes' offsets, lays the shorter one's
- *  bytes out as 8 bit planes of two words, runs the Myers / Hyyrö step over the longer one's bytes (match masks from
- *  the planes, one logic operation per plane and word), and writes the distance into the caller's matrix (both
- *  mirrored cells for the symmetric form). A string longer than 64 bytes raises a flag instead; the host then runs
- *  the general path for the whole call, which writes every cell again.
+ *  kernel takes one cell per thread (a query per grid row, candidates across the row, so no division per cell): it
+ *  reads the two strings through the tapes' offsets, lays the shorter one's bytes out as 8 bit planes of one or two
+ *  words, runs the Myers / Hyyrö step over the longer one's bytes (match masks from the planes, one logic operation
+ *  per plane and word), and writes the distance into the caller's matrix. A string longer than 64 bytes raises a
+ *  flag instead; the host then runs the general path for the whole call, which writes every cell again.
  *
  *  Counterpart of the reference's single-word direct path for tiny-token cross products
  *  (include/stringzillas/similarities/cuda.cuh:3892-3936); the distances are those of the serial engine
@@ -20,6 +20,8 @@
 #include "planner.cuh"
 
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 namespace szs_gb300 {
 
@@ -40,76 +42,89 @@ __device__ __forceinline__ void direct_string(tape_t const &tape, std::uint64_t 
     length = end - begin;
 }
 
-/** Unit-cost edit distance of a pattern of 1..64 bytes against a text of 1..64 bytes. */
+/** Unit-cost edit distance of a pattern of 1..32 x `words_` bytes against a text of 1..64 bytes. */
+template <int words_>
 __device__ __forceinline__ std::uint32_t direct_distance(std::uint8_t const *pattern, std::uint32_t n,
                                                         std::uint8_t const *text, std::uint32_t m) {
-    std::uint32_t planes[8][2];
+    constexpr int W = words_;
+    std::uint32_t planes[8][W];
 #pragma unroll
-    for (int b = 0; b < 8; ++b) planes[b][0] = planes[b][1] = 0u;
-    for (std::uint32_t i = 0; i < n; ++i) {
-        std::uint32_t const byte = pattern[i];
-        std::uint32_t const bit = 1u << (i & 31u);
-        bool const high = i >= 32u;
+    for (int w = 0; w < W; ++w) {
 #pragma unroll
-        for (int b = 0; b < 8; ++b)
-            if ((byte >> b) & 1u) {
-                if (high) planes[b][1] |= bit;
-                else planes[b][0] |= bit;
-            }
+        for (int b = 0; b < 8; ++b) planes[b][w] = 0u;
+        std::uint32_t const rows = n > 32u * w ? min(32u, n - 32u * w) : 0u;
+        for (std::uint32_t k = 0; k < rows; ++k) {
+            std::uint32_t const byte = pattern[32u * w + k];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) planes[b][w] |= ((byte >> b) & 1u) << k;
+        }
     }
-    std::uint32_t pv[2] = {0xFFFFFFFFu, 0xFFFFFFFFu}, mv[2] = {0u, 0u};
+    std::uint32_t pv[W], mv[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) pv[w] = 0xFFFFFFFFu, mv[w] = 0u;
     for (std::uint32_t j = 0; j < m; ++j) {
         std::uint32_t const byte = text[j];
-        std::uint32_t eq[2] = {0xFFFFFFFFu, 0xFFFFFFFFu};
+        std::uint32_t eq[W], xv[W], sum[W];
 #pragma unroll
-        for (int b = 0; b < 8; ++b) {
-            std::uint32_t const select = ((byte >> b) & 1u) - 1u; // all-ones where the text bit is 0
-            eq[0] &= planes[b][0] ^ select;
-            eq[1] &= planes[b][1] ^ select;
+        for (int w = 0; w < W; ++w) {
+            eq[w] = 0xFFFFFFFFu;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) eq[w] &= planes[b][w] ^ (((byte >> b) & 1u) - 1u);
+            xv[w] = eq[w] | mv[w];
+            sum[w] = eq[w] & pv[w];
         }
-        std::uint32_t const xv0 = eq[0] | mv[0], xv1 = eq[1] | mv[1];
-        std::uint32_t sum0 = eq[0] & pv[0], sum1 = eq[1] & pv[1];
-        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(sum0), "+r"(sum1) : "r"(pv[0]), "r"(pv[1]));
-        std::uint32_t const xh0 = (sum0 ^ pv[0]) | eq[0], xh1 = (sum1 ^ pv[1]) | eq[1];
-        std::uint32_t const ph0 = mv[0] | ~(xh0 | pv[0]), ph1 = mv[1] | ~(xh1 | pv[1]);
-        std::uint32_t const mh0 = pv[0] & xh0, mh1 = pv[1] & xh1;
-        std::uint32_t const ph_shift0 = (ph0 << 1) | 1u, ph_shift1 = __funnelshift_l(ph0, ph1, 1);
-        std::uint32_t const mh_shift0 = mh0 << 1, mh_shift1 = __funnelshift_l(mh0, mh1, 1);
-        pv[0] = mh_shift0 | ~(xv0 | ph_shift0), pv[1] = mh_shift1 | ~(xv1 | ph_shift1);
-        mv[0] = ph_shift0 & xv0, mv[1] = ph_shift1 & xv1;
+        if constexpr (W == 1) sum[0] += pv[0];
+        else asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(sum[0]), "+r"(sum[1]) : "r"(pv[0]), "r"(pv[1]));
+        std::uint32_t ph_prev = 1u << 31, mh_prev = 0u; // +1 shifted into row 0
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            std::uint32_t const xh = (sum[w] ^ pv[w]) | eq[w];
+            std::uint32_t const ph = mv[w] | ~(xh | pv[w]);
+            std::uint32_t const mh = pv[w] & xh;
+            std::uint32_t const ph_shifted = __funnelshift_l(ph_prev, ph, 1);
+            std::uint32_t const mh_shifted = __funnelshift_l(mh_prev, mh, 1);
+            pv[w] = mh_shifted | ~(xv[w] | ph_shifted);
+            mv[w] = ph_shifted & xv[w];
+            ph_prev = ph, mh_prev = mh;
+        }
     }
     // D[n][m] = m + (rows 1..n of the last column's +1 deltas) - (its -1 deltas).
-    std::uint32_t const mask0 = n >= 32u ? 0xFFFFFFFFu : (1u << n) - 1u;
-    std::uint32_t const mask1 = n >= 64u ? 0xFFFFFFFFu : (n > 32u ? (1u << (n - 32u)) - 1u : 0u);
-    return m + __popc(pv[0] & mask0) + __popc(pv[1] & mask1) - __popc(mv[0] & mask0) - __popc(mv[1] & mask1);
+    std::uint32_t distance = m;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        std::uint32_t const base = 32u * w;
+        std::uint32_t const mask = n >= base + 32u ? 0xFFFFFFFFu : (n > base ? (1u << (n - base)) - 1u : 0u);
+        distance += __popc(pv[w] & mask) - __popc(mv[w] & mask);
+    }
+    return distance;
 }
 
+/** One output cell per thread: queries along the grid's y dimension, candidates along x (no division per cell). */
 __global__ void __launch_bounds__(256) myers_direct_kernel(plan_args_t const args, std::int64_t *__restrict__ out,
                                                            std::uint64_t stride, std::uint32_t *__restrict__ flag) {
-    for (std::uint64_t p = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < args.pairs;
-         p += (std::uint64_t)gridDim.x * blockDim.x) {
-        std::uint64_t q, c;
-        if (args.mode == mode_cross_k) q = p / args.candidates_count, c = p % args.candidates_count;
-        else {
-            std::uint64_t row = (std::uint64_t)((sqrt(8.0 * (double)p + 1.0) - 1.0) / 2.0);
-            while (row * (row + 1) / 2 > p) --row;
-            while ((row + 1) * (row + 2) / 2 <= p) ++row;
-            q = row, c = p - row * (row + 1) / 2;
-        }
-        std::uint8_t const *first, *second;
-        std::uint64_t n, m;
+    std::uint64_t const queries = args.queries.count, candidates = args.candidates_count;
+    for (std::uint64_t q = blockIdx.y; q < queries; q += gridDim.y) {
+        std::uint8_t const *first;
+        std::uint64_t n;
         direct_string(args.queries, q, first, n);
-        direct_string(args.mode == mode_symmetric_k ? args.queries : args.candidates, c, second, m);
-        if (n > 64u || m > 64u) {
-            atomicOr(flag, 1u);
-            continue;
+        for (std::uint64_t c = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < candidates;
+             c += (std::uint64_t)gridDim.x * blockDim.x) {
+            std::uint8_t const *second;
+            std::uint64_t m;
+            direct_string(args.candidates, c, second, m);
+            if (n > 64u || m > 64u) {
+                atomicOr(flag, 1u);
+                continue;
+            }
+            std::uint32_t distance;
+            bool const swap = m < n;
+            std::uint8_t const *pattern = swap ? second : first, *text = swap ? first : second;
+            std::uint32_t const rows = (std::uint32_t)(swap ? m : n), cols = (std::uint32_t)(swap ? n : m);
+            if (rows == 0) distance = cols;
+            else if (rows <= 32u) distance = direct_distance<1>(pattern, rows, text, cols);
+            else distance = direct_distance<2>(pattern, rows, text, cols);
+            out[q * stride + c] = distance;
         }
-        std::uint32_t distance;
-        if (n == 0 || m == 0) distance = (std::uint32_t)(n > m ? n : m);
-        else if (n <= m) distance = direct_distance(first, (std::uint32_t)n, second, (std::uint32_t)m);
-        else distance = direct_distance(second, (std::uint32_t)m, first, (std::uint32_t)n);
-        out[q * stride + c] = distance;
-        if (args.mode == mode_symmetric_k && q != c) out[c * stride + q] = distance;
     }
 }
 
@@ -117,10 +132,13 @@ __global__ void __launch_bounds__(256) myers_direct_kernel(plan_args_t const arg
 
 cudaError_t launch_myers_direct(plan_args_t const &args, std::int64_t *out, std::uint64_t stride,
                                 std::uint32_t *flag, int sm_count, cudaStream_t stream) {
-    std::uint64_t const needed = (args.pairs + 255) / 256;
-    std::uint64_t const cap = (std::uint64_t)sm_count * 8;
-    int const grid = (int)(needed < cap ? (needed ? needed : 1) : cap);
-    myers_direct_kernel<<<grid, 256, 0, stream>>>(args, out, stride, flag);
+    if (args.mode != mode_cross_k) return cudaErrorInvalidValue;
+    std::uint64_t const columns = (args.candidates_count + 255) / 256;
+    unsigned const grid_x = (unsigned)(columns < 64 ? (columns ? columns : 1) : 64);
+    std::uint64_t const rows_wanted = ((std::uint64_t)sm_count * 16 + grid_x - 1) / grid_x;
+    unsigned const grid_y = (unsigned)std::min<std::uint64_t>(std::min<std::uint64_t>(args.queries.count, rows_wanted),
+                                                              65535);
+    myers_direct_kernel<<<dim3(grid_x, grid_y ? grid_y : 1), 256, 0, stream>>>(args, out, stride, flag);
     return cudaGetLastError();
 }
 
