@@ -569,6 +569,9 @@ typedef struct szs_gb300_server_config_t {
     sz_size_t max_batch_cells;    /**< cells (sum of len(a) * len(b)) merged into one batch at most while another lane
                                        is idle, so small requests do not wait behind a large one's batch (default
                                        2^33; a larger request still runs, alone; without an idle lane all merge) */
+    sz_size_t aging_ms;           /**< 0: batches start from the oldest waiting request (arrival order); otherwise from
+                                       the smallest one by cells, unless the oldest has waited this many milliseconds
+                                       (size-aware admission: small requests pass large ones, none waits forever) */
 } szs_gb300_server_config_t;
 
 /** What happened to one request. Times are host wall-clock milliseconds from its submission. */

@@ -184,6 +184,7 @@ class ServerConfig(ctypes.Structure):
         ("max_batch_requests", c_size_t),
         ("schedule", c_int),
         ("max_batch_cells", c_size_t),
+        ("aging_ms", c_size_t),
     ]
 
 

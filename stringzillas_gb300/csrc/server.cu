@@ -7,6 +7,8 @@
  *  arena:
  *
  *  - Requests wait in arrival order. Whenever a lane is free, the admission thread takes the first waiting request
+ *    (with `aging_ms` set: the smallest by cells, unless the oldest has waited that long - size-aware admission, so
+ *    small requests are not queued behind large ones while no request starves)
  *    and every later waiting request of the same engine that still fits the batch caps (requests, pairs, cells) and
  *    the arena (continuous batching: whatever arrived while the other lanes were busy rides along; the cells cap
  *    keeps small requests out of a large request's batch), reserves one contiguous arena region
@@ -237,15 +239,24 @@ void server_t::admit_loop() {
         });
         if (waiting.empty()) break; // stopping, nothing left
 
-        // Merge: the first waiter, then later waiters of the same engine while the caps and the arena allow.
+        // The batch's head: the oldest waiter, or under size-aware admission the smallest one unless the oldest has
+        // waited past the aging bound.
+        auto head = waiting.begin();
+        if (config.aging_ms && ms_between(waiting.front()->submitted, steady_t::now()) < (double)config.aging_ms)
+            head = std::min_element(waiting.begin(), waiting.end(),
+                                    [](request_t const *a, request_t const *b) { return a->cells < b->cells; });
+        // Merge: the head, then other waiters of the same engine in arrival order while the caps and the arena allow.
         auto batch = std::make_unique<batch_t>();
-        batch->engine = waiting.front()->engine;
+        batch->engine = (*head)->engine;
         std::uint64_t pairs = 0, first_bytes = 0, second_bytes = 0, cells = 0;
         std::size_t largest_free = 0;
         for (auto const &block : allocator.free_blocks) largest_free = std::max(largest_free, block.second);
         std::size_t const max_requests = config.max_batch_requests ? config.max_batch_requests : ~std::size_t(0);
         std::vector<std::list<request_t *>::iterator> taken;
-        for (auto it = waiting.begin(); it != waiting.end(); ++it) {
+        for (int pass = 0; pass < 2; ++pass)
+        for (auto it = (pass == 0 ? head : waiting.begin()); it != waiting.end(); ++it) {
+            if (pass == 0 && it != head) break; // the head first, alone
+            if (pass == 1 && it == head) continue;
             request_t *request = *it;
             if (request->engine != batch->engine) continue;
             if (batch->requests.size() >= max_requests) break;
@@ -269,9 +280,9 @@ void server_t::admit_loop() {
         std::size_t const region = allocator.allocate(batch->layout.total);
         if (region == arena_allocator_t::none_k) {
             if (batch->layout.total > allocator.capacity || inflight == 0) {
-                // Can never fit (or nothing in flight will ever free enough): fail the first waiter alone.
-                request_t *request = waiting.front();
-                waiting.pop_front();
+                // Can never fit (or nothing in flight will ever free enough): fail the head alone.
+                request_t *request = *head;
+                waiting.erase(head);
                 request->admitted = steady_t::now();
                 finish({request}, sz_bad_alloc_k, 0, request->pairs);
                 continue;

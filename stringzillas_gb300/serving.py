@@ -55,16 +55,20 @@ class Ticket:
 
 class Server:
     """``Server(gpu_device=0, arena_bytes=1 << 30, lanes=4, max_batch_pairs=1 << 22, max_batch_requests=0,
-    schedule="batched", max_batch_cells=1 << 33)``.
+    schedule="batched", max_batch_cells=1 << 33, aging_ms=0)``.
+
+    ``aging_ms > 0`` admits the smallest waiting request (by cells) first unless the oldest has waited that long;
+    0 keeps arrival order.
 
     ``max_batch_requests=1, lanes=1, schedule="plain"`` gives the per-request form: every request on its own,
     one after another, with one plain launch each.
     """
 
     def __init__(self, gpu_device=0, arena_bytes=1 << 30, lanes=4, max_batch_pairs=1 << 22, max_batch_requests=0,
-                 schedule="batched", max_batch_cells=1 << 33):
+                 schedule="batched", max_batch_cells=1 << 33, aging_ms=0):
         config = _native.ServerConfig(int(gpu_device), int(arena_bytes), int(lanes), int(max_batch_pairs),
-                                      int(max_batch_requests), _SCHEDULES[schedule], int(max_batch_cells))
+                                      int(max_batch_requests), _SCHEDULES[schedule], int(max_batch_cells),
+                                      int(aging_ms))
         self._handle = ctypes.c_void_p()
         err = ctypes.c_char_p()
         status = lib.szs_gb300_server_init(ctypes.byref(config), ctypes.byref(self._handle), ctypes.byref(err))

@@ -107,7 +107,7 @@ def test_server_validation_without_a_gpu():
     """The serving loop needs a GPU; the ABI structs match the header's layout."""
     from stringzillas_gb300 import _native
     import ctypes
-    assert ctypes.sizeof(_native.ServerConfig) == 7 * 8
+    assert ctypes.sizeof(_native.ServerConfig) == 8 * 8
     assert ctypes.sizeof(_native.RequestInfo) == 7 * 8
     assert ctypes.sizeof(_native.ServerStats) == 10 * 8
     if "cuda" in szs.__capabilities__:

@@ -57,14 +57,16 @@ def _requests(rng, count, max_pairs, max_length):
     return out
 
 
-def test_mixed_stream_equals_alone(szs, engines, port):
+@pytest.mark.parametrize("aging_ms", [0, 40], ids=["arrival-order", "size-aware"])
+def test_mixed_stream_equals_alone(szs, engines, port, aging_ms):
+    """Both admission orders: arrival order, and smallest request first with a 40 ms aging bound."""
     rng = np.random.default_rng(2024)
     requests = _requests(rng, 60, 48, 700)
     # A few long pairs ride along (band and 32-bit routes inside merged batches).
     long_a = bytes(rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=2600))
     requests.append(("sw", [long_a, long_a[:1500]], [long_a[300:2900], long_a[::-1][:1400]]))
     requests.append(("lev", [long_a[:1200]], [long_a[50:1300]]))
-    with szs.Server(lanes=3, arena_bytes=64 << 20) as server:
+    with szs.Server(lanes=3, arena_bytes=64 << 20, aging_ms=aging_ms) as server:
         tickets = [None] * len(requests)
 
         def submitter():
@@ -158,3 +160,26 @@ def test_device_resident_request(szs, engines):
         ticket = server.submit(engine, dev_a, dev_b, out=out)
         ticket.result()
     np.testing.assert_array_equal(out.cpu().numpy(), engine.pairwise(host_a, host_b))
+
+
+def test_size_aware_admission_order(szs, engines):
+    """With one lane busy, a small request submitted after a large one of another engine runs first under
+    size-aware admission, and after it in arrival order; results are the same either way."""
+    rng = np.random.default_rng(17)
+    dna = np.frombuffer(b"ACGT", dtype=np.uint8)
+    protein = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+    blocker = [bytes(rng.choice(protein, size=4000)) for _ in range(1500)]  # ~10 ms on the device
+    large = [bytes(rng.choice(protein, size=1500)) for _ in range(200)]
+    small = [bytes(rng.choice(dna, size=50)) for _ in range(4)]
+    order = {}
+    for aging_ms in (0, 10_000):
+        with szs.Server(lanes=1, aging_ms=aging_ms) as server:
+            first = server.submit(engines["nw"][0], szs.Strs(blocker), szs.Strs(blocker[::-1]))
+            time.sleep(0.001)
+            big = server.submit(engines["sw"][0], szs.Strs(large), szs.Strs(large[::-1]))
+            tiny = server.submit(engines["lev"][0], szs.Strs(small), szs.Strs(small[::-1]))
+            first.result(), big.result(), tiny.result()
+            order[aging_ms] = (big.info["batch"], tiny.info["batch"])
+            np.testing.assert_array_equal(tiny.result(), engines["lev"][0].pairwise(szs.Strs(small), szs.Strs(small[::-1])))
+    assert order[0][0] < order[0][1], "arrival order: the earlier large request runs first"
+    assert order[10_000][1] < order[10_000][0], "size-aware: the small request passes the large one"
