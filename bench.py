@@ -100,6 +100,7 @@ def parse_args():
                         help="run only the Min-Hash leg and print its JSON object")
     parser.add_argument("--fp-documents", type=int, default=16384, help="documents of the Min-Hash leg")
     parser.add_argument("--cross-only", action="store_true", help="run only the all-pairs leg and print its object")
+    parser.add_argument("--serving-only", action="store_true", help="run only the serving leg and print its object")
     return parser.parse_args()
 
 
@@ -389,7 +390,8 @@ def cpu_baseline(first, second, kind_and_tables, seconds_budget):
             "sample": f"first {k} of {count} pairs ({cells:.3e} cells, {elapsed:.2f} s), oracle C restatement"}
 
 
-SERVING_RATE = 120.0      # offered load, requests per second (Poisson arrivals)
+SERVING_RATES = (120.0, 400.0)  # offered loads, requests per second (Poisson arrivals)
+SERVING_AGING_MS = 50     # size-aware admission: a request waiting this long goes first
 SERVING_REQUESTS = 240    # requests per run, drawn from a pool of 48 distinct ones
 NW_SW_BURST = 64          # requests of the NW / SW-only burst, drawn from a pool of 32
 
@@ -443,30 +445,41 @@ def serving_leg(szs):
     engines = serving_engines(szs)
     rng = np.random.Generator(np.random.PCG64(7))
     order = rng.integers(0, len(pool), size=SERVING_REQUESTS)
-    arrivals = np.cumsum(rng.exponential(1.0 / SERVING_RATE, size=SERVING_REQUESTS))
+    gaps = rng.exponential(1.0, size=SERVING_REQUESTS)  # one seeded arrival pattern, scaled to each load
     cells = int(sum(pool[k]["cells"] for k in order))
     forms = {"serving": dict(lanes=4, arena_bytes=4 << 30),
+             "serving_size_aware": dict(lanes=4, arena_bytes=4 << 30, aging_ms=SERVING_AGING_MS),
              "per_request_plain": dict(lanes=1, max_batch_requests=1, schedule="plain", arena_bytes=4 << 30)}
     # The same four lanes without batching: one request per batch, plain schedule (isolates what batching buys).
     same_lanes = {"per_request_plain_4_lanes": dict(lanes=4, max_batch_requests=1, schedule="plain",
                                                     arena_bytes=4 << 30)}
-    out = {"offered_requests_per_s": SERVING_RATE, "requests": SERVING_REQUESTS,
-           "offered_gcups": cells / arrivals[-1] / 1e9, "cells": cells,
-           "mix": "Levenshtein:NW:SW 2:1:1, 1-4,096 pairs per request, pair lengths log-uniform [16, 16,384]"}
+    out = {"offered_requests_per_s": list(SERVING_RATES), "requests": SERVING_REQUESTS, "cells": cells,
+           "offered_gcups": [cells / (np.cumsum(gaps / rate))[-1] / 1e9 for rate in SERVING_RATES],
+           "mix": "Levenshtein:NW:SW 2:1:1, 1-4,096 pairs per request, pair lengths log-uniform [16, 16,384]",
+           "admission": f"serving: oldest waiting request first; serving_size_aware: smallest first, aging bound "
+                        f"{SERVING_AGING_MS} ms"}
     for name, config in forms.items():
+        row = {}
         with szs.Server(**config) as server:
             serve_stream(szs, server, engines, pool, order[:8], np.zeros(8))  # warm-up: builds lane buffers
-            infos, wall = serve_stream(szs, server, engines, pool, order, arrivals)
-            latencies = np.array([i["done_ms"] for i in infos])
+            rates = SERVING_RATES if name != "per_request_plain" else SERVING_RATES[:1]
+            for rate in rates:
+                arrivals = np.cumsum(gaps / rate)
+                infos, wall = serve_stream(szs, server, engines, pool, order, arrivals)
+                latencies = np.array([i["done_ms"] for i in infos])
+                queued = np.array([i["admitted_ms"] for i in infos])
+                row[f"{rate:g}_per_s"] = {
+                    "p50_ms": float(np.percentile(latencies, 50)), "p99_ms": float(np.percentile(latencies, 99)),
+                    "mean_ms": float(latencies.mean()), "queue_p50_ms": float(np.percentile(queued, 50)),
+                    "queue_p99_ms": float(np.percentile(queued, 99)),
+                    "achieved_gcups_at_offered_load": cells / wall / 1e9}
             burst_infos, burst_wall = serve_stream(szs, server, engines, pool, order, np.zeros(len(order)))
             stats = server.stats()
-        out[name] = {
-            "p50_ms": float(np.percentile(latencies, 50)), "p99_ms": float(np.percentile(latencies, 99)),
-            "mean_ms": float(latencies.mean()), "achieved_gcups_at_offered_load": cells / wall / 1e9,
-            "saturated_gcups": cells / burst_wall / 1e9,
-            "saturated_p99_ms": float(np.percentile([i["done_ms"] for i in burst_infos], 99)),
-            "batches": stats["batches"], "peak_inflight_batches": stats["peak_inflight"],
-            "arena_peak_bytes": stats["arena_peak_bytes"], "kernel_launches": stats["kernel_launches"]}
+        row.update({"saturated_gcups": cells / burst_wall / 1e9,
+                    "saturated_p99_ms": float(np.percentile([i["done_ms"] for i in burst_infos], 99)),
+                    "batches": stats["batches"], "peak_inflight_batches": stats["peak_inflight"],
+                    "arena_peak_bytes": stats["arena_peak_bytes"], "kernel_launches": stats["kernel_launches"]})
+        out[name] = row
     out["saturated_serving_over_plain"] = (out["serving"]["saturated_gcups"] /
                                            out["per_request_plain"]["saturated_gcups"])
     # Mixed-length NW / SW only: a saturating burst of alignment requests, both forms.
@@ -829,7 +842,10 @@ def run_cross_only(args):
 
 def main():
     args = parse_args()
-    if args.cross_only:
+    if args.serving_only:
+        import stringzillas_gb300 as szs
+        print(json.dumps(serving_leg(szs)), flush=True)
+    elif args.cross_only:
         run_cross_only(args)
     elif args.fingerprints_only:
         run_fingerprints_only(args)
