@@ -101,6 +101,7 @@ def parse_args():
     parser.add_argument("--fp-documents", type=int, default=16384, help="documents of the Min-Hash leg")
     parser.add_argument("--cross-only", action="store_true", help="run only the all-pairs leg and print its object")
     parser.add_argument("--serving-only", action="store_true", help="run only the serving leg and print its object")
+    parser.add_argument("--long-only", action="store_true", help="run only the long-pair leg and print its object")
     return parser.parse_args()
 
 
@@ -577,6 +578,56 @@ def cross_product_leg(szs, torch, scope, steps=10, warmup=3):
     return out
 
 
+def long_pairs_leg(szs, torch, scope, steps=3, warmup=1):
+    """Single very long pairs, one call each, device-resident: unit-cost Levenshtein at 50,000 and 100,000
+    characters a side (a 3% substitution + 1% indel mutant), Smith-Waterman affine DNA (+2/-3, -5/-2) and
+    Needleman-Wunsch affine protein (-11/-1) at 30,000 with a planted shared segment. GCUPS from CUDA events."""
+    from stringzillas_gb300 import workloads as w
+    stream = torch.cuda.current_stream()
+    rng = np.random.Generator(np.random.PCG64(5))
+    dna = np.frombuffer(b"ACGT", dtype=np.uint8)
+    protein = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+
+    def pair(alphabet, length, mutate=True):
+        a = alphabet[rng.integers(0, len(alphabet), size=length)]
+        if mutate:
+            b, _ = w._mutate(rng, a, np.array([0, length]), alphabet, 0.03, 0.01)
+        else:
+            b = alphabet[rng.integers(0, len(alphabet), size=length)]
+            b[length // 3:length // 3 + 5000] = a[length // 2:length // 2 + 5000]
+        return a, b
+
+    def device(strings):
+        data = np.concatenate(strings)
+        offsets = np.zeros(len(strings) + 1, dtype=np.int64)
+        np.cumsum([len(x) for x in strings], out=offsets[1:])
+        return szs.Strs.from_buffers(torch.from_numpy(data).cuda(), torch.from_numpy(offsets).cuda())
+
+    protein_b2c, protein_table = w.protein_table(seed=42)
+    cases = [("levenshtein_50k", szs.LevenshteinDistances(), pair(dna, 50000)),
+             ("levenshtein_100k", szs.LevenshteinDistances(), pair(dna, 100000)),
+             ("smith_waterman_30k", szs.SmithWatermanScores(*w.dna_table(2, -3), open=-5, extend=-2),
+              pair(dna, 30000, mutate=False)),
+             ("needleman_wunsch_30k", szs.NeedlemanWunschScores(protein_b2c, protein_table, open=-11, extend=-1),
+              pair(protein, 30000, mutate=False))]
+    out = {}
+    for name, engine, (a, b) in cases:
+        first, second = device([a]), device([b])
+        result = torch.empty(1, dtype=torch.int64, device="cuda")
+        for _ in range(warmup):
+            engine.pairwise(first, second, device=scope, out=result)
+        begin, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        begin.record(stream)
+        for _ in range(steps):
+            engine.pairwise(first, second, device=scope, out=result)
+        end.record(stream)
+        torch.cuda.synchronize()
+        ms = begin.elapsed_time(end) / steps
+        out[name] = {"GCUPS": len(a) * len(b) / (ms * 1e-3) / 1e9, "ms_per_call": ms, "lengths": [len(a), len(b)]}
+    return out
+
+
 FINGERPRINT_WORKLOAD = ("Min-Hash fingerprints: 16,384 documents, len U[1,000, 3,000] printable bytes, 1,024 dimensions, "
                         "default widths {3,4,5,7,9,11,15,31} (64-dimension slices), seed 0")
 # Integer operations per byte and dimension, counted from the rolling step: x = state*a + D*out + (D + 1 + in) (two
@@ -812,6 +863,7 @@ def run_ours(args):
             del batch
         line["extra"] = extra
         line["cross_product"] = cross_product_leg(szs, torch, scope)
+        line["long_pairs"] = long_pairs_leg(szs, torch, scope)
         line["serving"] = serving_leg(szs)
         line["fingerprints"] = fingerprints_leg(szs, torch, scope, peaks)
     elif rank == 0:
@@ -842,7 +894,13 @@ def run_cross_only(args):
 
 def main():
     args = parse_args()
-    if args.serving_only:
+    if args.long_only:
+        import torch
+        import stringzillas_gb300 as szs
+        torch.cuda.set_device(0)
+        scope = szs.DeviceScope(gpu_device=0, stream=torch.cuda.current_stream())
+        print(json.dumps(long_pairs_leg(szs, torch, scope)), flush=True)
+    elif args.serving_only:
         import stringzillas_gb300 as szs
         print(json.dumps(serving_leg(szs)), flush=True)
     elif args.cross_only:

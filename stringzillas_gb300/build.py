@@ -44,6 +44,7 @@ UNITS = [
     ("myers_wide", "kernels_myers_wide.cu", []),
     ("myers_p2", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=2"]),
     ("myers_table", "kernels_myers_table.cu", []),
+    ("myers_chain", "kernels_myers_chain.cu", []),
     ("myers_p3", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=3"]),
     ("myers_p5", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=5"]),
     ("myers_p8", "kernels_myers.cu", ["-DSZS_MYERS_PLANES=8"]),

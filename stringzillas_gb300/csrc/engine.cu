@@ -969,7 +969,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
 
     // The launch list, longest pairs first (64- and 32-bit wavefront, packed with the most rows per lane, then the
     // bit-parallel kernels by word count), so the routes' tails overlap each other instead of adding up.
-    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k, job_myers_warp_k, job_short_k };
+    enum job_kind_t { job_dp_k, job_dp16_k, job_myers_k, job_band_k, job_band16_k, job_myers_warp_k, job_short_k,
+                      job_myers_chain_k };
     struct job_t {
         job_kind_t kind;
         int variant; // cell bits, rows per lane, or words
@@ -1105,8 +1106,30 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * shape.ctas_per_sm;
     }
     int myers_planes = 0;
+    std::uint32_t chain_strips = 0;
+    std::uint64_t chain_link_stride = 0;
     if (engine.unit_levenshtein) {
         myers_planes = wide ? 16 : myers_planes_for((int)alphabet_host.bits);
+        // Very long patterns: a chain of warps per pair, the fewest words per lane whose chain fits the GPU at once.
+        if (std::uint64_t const chained = pairs_in(bin_myers_chain_k, bin_myers_chain_k + 1)) {
+            int words = 0, ctas = 0;
+            for (int w : {1, 2, 4}) {
+                std::uint32_t const strips =
+                    (std::uint32_t)(((std::uint64_t)plan.max_chain_rows + 1024u * w - 1) / (1024u * w));
+                int const needed = (int)((strips + 7) / 8);
+                if (needed <= context->sm_count * myers_chain_ctas_per_sm(w, myers_planes)) {
+                    words = w, ctas = needed, chain_strips = strips;
+                    break;
+                }
+            }
+            if (!words) return {sz_status_unknown_k, "A long pattern's chain of warps does not fit the device"};
+            chain_link_stride = align_up((std::size_t)plan.max_cols + 1, 256);
+            std::size_t const bytes =
+                align_up(myers_chain_links_offset(chain_strips) + (std::size_t)chain_strips * chain_link_stride, 256);
+            jobs[job_count++] = {job_myers_chain_k, words, 0, bin_myers_chain_k, bin_myers_chain_k + 1, chained, ctas,
+                                 scratch_total, bytes};
+            scratch_total += bytes;
+        }
         // The plain form keeps each bit-parallel route in one bin and launches the word count of the batch's longest
         // pattern on it (the binned form launches each bin with its own word count).
         bool const plain = schedule == szs_gb300_schedule_plain_k;
@@ -1201,6 +1224,13 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                 SZS_TRY_CUDA(launch_dp16(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
                                          lane_stream, compare_mode, wide));
+            else if (job.kind == job_myers_chain_k) {
+                // One cooperative launch per pair, one after another on this lane (they share the chain scratch).
+                for (std::uint64_t index = 0; index < job.pairs; ++index)
+                    SZS_TRY_CUDA(launch_myers_chain(job.variant, myers_planes, tasks, bins, job.key_begin, (int)index,
+                                                    alphabet, results, scratch, chain_link_stride, chain_strips,
+                                                    job.ctas, costs.wait_polls, lane_stream));
+            }
             else if (job.kind == job_short_k)
                 SZS_TRY_CUDA(launch_short(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end,
                                           tasks, bins, packed_costs, results, job.ctas, job.warps, lane_stream,
@@ -1299,8 +1329,8 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     stats.last_compute_ms = compute;
     if (tracing) {
         static char const *const names[] = {"wavefront bits", "packed16 rows", "bit-parallel words", "band bits",
-                                            "band16 bits", "warp bit-parallel", "short shape"};
-        static_assert(sizeof(names) / sizeof(names[0]) == job_short_k + 1, "a name per job kind");
+                                            "band16 bits", "warp bit-parallel", "short shape", "chained words"};
+        static_assert(sizeof(names) / sizeof(names[0]) == job_myers_chain_k + 1, "a name per job kind");
         for (int i = 0; i < job_count && 2 * i + 1 < 64; ++i) {
             float ms = 0, offset = 0;
             cudaEventElapsedTime(&ms, context->trace_events[2 * i], context->trace_events[2 * i + 1]);

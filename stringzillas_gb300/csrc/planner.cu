@@ -86,6 +86,10 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         info.key = bin_myers_begin_k + words * 16 + text_class;
         return info;
     }
+    if (args.unit_levenshtein && !args.wide && n > 32u * 32u * myers_warp_max_words_k && n <= myers_chain_max_rows_k) {
+        info.key = bin_myers_chain_k; // one bin in both forms: a chain of warps per pair, one launch each
+        return info;
+    }
     if (args.unit_levenshtein && n <= 32u * 32u * myers_warp_max_words_k) {
         // Longer patterns: one warp per pair, W words per lane.
         if (args.force_route >= 0) {
@@ -203,12 +207,13 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
                                   std::int64_t *__restrict__ results) {
     __shared__ std::uint32_t histogram[bin_keys_k];
     __shared__ unsigned long long block_cells;
-    __shared__ std::uint32_t block_max_cols, block_max_myers, block_max_myers_warp;
+    __shared__ std::uint32_t block_max_cols, block_max_myers, block_max_myers_warp, block_max_chain;
     for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x) histogram[i] = 0;
-    if (threadIdx.x == 0) block_cells = 0, block_max_cols = 0, block_max_myers = 0, block_max_myers_warp = 0;
+    if (threadIdx.x == 0)
+        block_cells = 0, block_max_cols = 0, block_max_myers = 0, block_max_myers_warp = 0, block_max_chain = 0;
     __syncthreads();
     std::uint64_t thread_cells = 0;
-    std::uint32_t thread_max_cols = 0, thread_max_myers = 0, thread_max_myers_warp = 0;
+    std::uint32_t thread_max_cols = 0, thread_max_myers = 0, thread_max_myers_warp = 0, thread_max_chain = 0;
     for (std::uint64_t p = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < args.pairs;
          p += (std::uint64_t)gridDim.x * blockDim.x) {
         pair_route_info_t const info = route_of_pair(args, p);
@@ -221,6 +226,7 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
         if (info.key >= bin_dp32_begin_k) thread_max_cols = max(thread_max_cols, info.m);
         if (info.key >= bin_myers_warp_begin_k && info.key < bin_short_begin_k)
             thread_max_myers_warp = max(thread_max_myers_warp, info.n);
+        else if (info.key == bin_myers_chain_k) thread_max_chain = max(thread_max_chain, info.n);
         else if (info.key < bin_myers_begin_k + (myers_max_words_k + 1) * 16)
             thread_max_myers = max(thread_max_myers, info.n);
     }
@@ -228,6 +234,7 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
     atomicMax(&block_max_cols, thread_max_cols);
     atomicMax(&block_max_myers, thread_max_myers);
     atomicMax(&block_max_myers_warp, thread_max_myers_warp);
+    atomicMax(&block_max_chain, thread_max_chain);
     __syncthreads();
     for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x)
         if (histogram[i]) atomicAdd(&bins->count[i], histogram[i]);
@@ -236,6 +243,7 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
         atomicMax(&bins->max_cols, block_max_cols);
         atomicMax(&bins->max_myers_rows, block_max_myers);
         atomicMax(&bins->max_myers_warp_rows, block_max_myers_warp);
+        atomicMax(&bins->max_chain_rows, block_max_chain);
     }
 }
 

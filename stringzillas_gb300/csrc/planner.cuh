@@ -22,6 +22,7 @@
  *                 + (7 - text class), W = words per lane = ceil(n / 1024), text class ~ log2(m) - 9
  *    [1488, 1680) short pairs on 16x2 cells (shorter side <= 128): key = 1488 + 48 * shape + (47 - m class),
  *                 shape 0/1/2/3 for n <= 16/32/64/128, m class = m / 16 below 512, then 32 + log2(m) - 9
+ *    1680         unit-cost Levenshtein beyond the warp kernel (shorter side 8,193 .. 2^20): a chain of warps per pair
  */
 #pragma once
 #include "engine_types.cuh"
@@ -62,6 +63,8 @@ constexpr int short_shapes_k = 4;      // segments holding 16, 32, 64 and 128 ro
 constexpr int short_m_classes_k = 48;  // text-length classes per shape
 constexpr int short_max_rows_k = 128;  // default: shorter sides up to this take the short route
 static_assert(bin_short_begin_k + short_shapes_k * short_m_classes_k <= bin_keys_k, "bin layout exceeds the key space");
+constexpr int bin_myers_chain_k = bin_short_begin_k + short_shapes_k * short_m_classes_k; // 1680
+constexpr std::uint32_t myers_chain_max_rows_k = 1u << 20; // longest pattern a chain of warps takes
 
 /** Which pairs a call scores. */
 enum pair_mode_t : int {
@@ -117,6 +120,8 @@ struct plan_bins_t {
     std::uint64_t scheduled;
     std::uint32_t max_myers_rows;      // longest pattern on the thread-per-pair bit-parallel route
     std::uint32_t max_myers_warp_rows; // longest pattern on the warp-per-pair bit-parallel route
+    std::uint32_t max_chain_rows;      // longest pattern on the chained bit-parallel route
+    std::uint32_t reserved;
 };
 
 } // namespace szs_gb300

@@ -914,3 +914,39 @@ def test_tiny_token_cross_product_in_place(szs, port, longest):
         got = out.cpu().numpy()
         np.testing.assert_array_equal(got[:, :len(candidates)], want)
         assert (got[:, len(candidates):] == -1).all()
+
+
+@pytest.mark.parametrize("schedule", ["batched", "plain"])
+def test_long_unit_levenshtein_chain(szs, port, schedule):
+    """Unit-cost pairs whose shorter side passes 8,192 characters take a chain of warps (1,024 rows each, bits handed
+    from warp to warp through global memory): lengths just past the limit, across warp and CTA boundaries, a 50,000
+    character mutant pair, a pair with the pattern on the second side, and one pair per chain launch."""
+    from stringzillas_gb300 import workloads as w
+    rng = np.random.default_rng(123)
+    first, second = [], []
+    for n in (8193, 9216, 10000, 20480 + 7):
+        first.append(bytes(rng.choice(DNA, size=n)))
+        second.append(bytes(rng.choice(DNA, size=n + int(rng.integers(-100, 3000)))))
+    a = DNA[rng.integers(0, 4, size=50000)]
+    b, _ = w._mutate(rng, a, np.array([0, 50000]), DNA, 0.03, 0.01)
+    first.append(bytes(b)), second.append(bytes(a))  # the shorter string on either side
+    first.append(bytes(rng.choice(DNA, size=40))), second.append(bytes(rng.choice(DNA, size=9000)))
+    engine = szs.LevenshteinDistances()
+    engine.set_schedule(schedule)
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(), tape(first), tape(second)))
+
+
+def test_long_unit_levenshtein_chain_wait_gives_up(szs, port):
+    """The chain's waits are bounded like the bands': tuned down to one poll they give up, the call reports an error,
+    and the next call at the built-in bound is exact."""
+    rng = np.random.default_rng(124)
+    first = [bytes(rng.choice(DNA, size=30000))]
+    second = [bytes(rng.choice(DNA, size=30500))]
+    engine = szs.LevenshteinDistances()
+    engine.set_tuning({"band_wait_polls": 1})
+    with pytest.raises(RuntimeError, match="bounded wait"):
+        engine.pairwise(szs.Strs(first), szs.Strs(second))
+    engine.set_tuning(None)
+    np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64),
+                                  port.pairs(oracle.levenshtein_costs(), tape(first), tape(second)))
