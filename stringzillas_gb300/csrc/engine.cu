@@ -1106,27 +1106,30 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         jobs[job_count - 1].fills = needed >= (std::uint64_t)context->sm_count * shape.ctas_per_sm;
     }
     int myers_planes = 0;
-    std::uint32_t chain_strips = 0;
+    std::uint32_t chain_strips = 0, chain_wave = 0; // warps per chained pair, pairs per cooperative launch
     std::uint64_t chain_link_stride = 0;
     if (engine.unit_levenshtein) {
         myers_planes = wide ? 16 : myers_planes_for((int)alphabet_host.bits);
-        // Very long patterns: a chain of warps per pair, the fewest words per lane whose chain fits the GPU at once.
+        // Very long patterns: a chain of warps per pair, the fewest words per lane whose chain fits the GPU at once;
+        // as many pairs per cooperative launch (a wave) as fit beside each other.
         if (std::uint64_t const chained = pairs_in(bin_myers_chain_k, bin_myers_chain_k + 1)) {
-            int words = 0, ctas = 0;
+            int words = 0;
+            std::uint64_t capacity = 0; // resident warps of one launch
             for (int w : {1, 2, 4}) {
                 std::uint32_t const strips =
                     (std::uint32_t)(((std::uint64_t)plan.max_chain_rows + 1024u * w - 1) / (1024u * w));
-                int const needed = (int)((strips + 7) / 8);
-                if (needed <= context->sm_count * myers_chain_ctas_per_sm(w, myers_planes)) {
-                    words = w, ctas = needed, chain_strips = strips;
+                capacity = (std::uint64_t)context->sm_count * myers_chain_ctas_per_sm(w, myers_planes) * 8u;
+                if (strips <= capacity) {
+                    words = w, chain_strips = strips;
                     break;
                 }
             }
             if (!words) return {sz_status_unknown_k, "A long pattern's chain of warps does not fit the device"};
             chain_link_stride = align_up((std::size_t)plan.max_cols + 1, 256);
+            chain_wave = (std::uint32_t)std::min<std::uint64_t>(chained, capacity / chain_strips);
             std::size_t const bytes =
-                align_up(myers_chain_links_offset(chain_strips) + (std::size_t)chain_strips * chain_link_stride, 256);
-            jobs[job_count++] = {job_myers_chain_k, words, 0, bin_myers_chain_k, bin_myers_chain_k + 1, chained, ctas,
+                align_up(myers_chain_scratch_bytes(chain_strips, chain_link_stride, chain_wave), 256);
+            jobs[job_count++] = {job_myers_chain_k, words, 0, bin_myers_chain_k, bin_myers_chain_k + 1, chained, 0,
                                  scratch_total, bytes};
             scratch_total += bytes;
         }
@@ -1225,11 +1228,13 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                          bins, packed_costs, results, scratch, cells_per_warp, job.ctas, job.warps,
                                          lane_stream, compare_mode, wide));
             else if (job.kind == job_myers_chain_k) {
-                // One cooperative launch per pair, one after another on this lane (they share the chain scratch).
-                for (std::uint64_t index = 0; index < job.pairs; ++index)
-                    SZS_TRY_CUDA(launch_myers_chain(job.variant, myers_planes, tasks, bins, job.key_begin, (int)index,
-                                                    alphabet, results, scratch, chain_link_stride, chain_strips,
-                                                    job.ctas, costs.wait_polls, lane_stream));
+                // One cooperative launch per wave of pairs, one after another on this lane (they share the scratch).
+                for (std::uint64_t first = 0; first < job.pairs; first += chain_wave)
+                    SZS_TRY_CUDA(launch_myers_chain(job.variant, myers_planes, tasks, bins, job.key_begin,
+                                                    (std::uint32_t)first,
+                                                    (std::uint32_t)std::min<std::uint64_t>(chain_wave, job.pairs - first),
+                                                    chain_strips, alphabet, results, scratch, chain_link_stride,
+                                                    costs.wait_polls, lane_stream));
             }
             else if (job.kind == job_short_k)
                 SZS_TRY_CUDA(launch_short(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end,

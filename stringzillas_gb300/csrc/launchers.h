@@ -152,16 +152,17 @@ cudaError_t launch_short(int kind, bool affine, int shape, int key_begin, int ke
                          plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, int ctas, int warps,
                          cudaStream_t stream, int compare = 0);
 
-/** Very long unit-cost pairs on a chain of warps (myers_chain.cuh): one cooperative launch scores pair `index` of bin
- *  `key` with `words` (1, 2, 4) words per lane and `planes` code planes over `strips` warps (1,024 x words rows
- *  each). `scratch` holds the chain's state and progress (`myers_chain_links_offset(strips)` bytes, cleared by the
- *  launch) and then `strips - 1` links of `link_stride` bytes (at least the pair's longer side). */
-std::size_t myers_chain_links_offset(std::uint32_t strips);
+/** Very long unit-cost pairs on chains of warps (myers_chain.cuh): one cooperative launch scores pairs
+ *  [first, first + pairs) of bin `key` with `words` (1, 2, 4) words per lane and `planes` code planes, each pair on
+ *  `strips_per_pair` warps (1,024 x words rows each) and its share of `scratch`
+ *  (`myers_chain_scratch_bytes(strips_per_pair, link_stride, pairs)` bytes in all; `link_stride` at least the
+ *  longest text). 8 warps per CTA; the launch clears the state it needs. */
+std::uint64_t myers_chain_scratch_bytes(std::uint32_t strips_per_pair, std::uint64_t link_stride, std::uint32_t pairs);
 int myers_chain_ctas_per_sm(int words, int planes);
 cudaError_t launch_myers_chain(int words, int planes, pair_task_t const *tasks, plan_bins_t *bins, int key,
-                               int index, batch_alphabet_t const *alphabet, std::int64_t *results, void *scratch,
-                               std::uint64_t link_stride, std::uint32_t strips, int ctas, std::uint32_t wait_polls,
-                               cudaStream_t stream);
+                               std::uint32_t first, std::uint32_t pairs, std::uint32_t strips_per_pair,
+                               batch_alphabet_t const *alphabet, std::int64_t *results, void *scratch,
+                               std::uint64_t link_stride, std::uint32_t wait_polls, cudaStream_t stream);
 
 /** Bit-parallel kernels over strings of 16-bit codes (UTF-8 calls over more than 256 code points, 16 code planes):
  *  thread per pair over the bins of `words` words (1..8), and warp per pair over the warp bins (1..8 words per

@@ -40,23 +40,39 @@ struct myers_chain_state_t {
     long long delta_sum;
 };
 
+/** Bytes of one pair's chain scratch: its state, `strips` progress words, then `strips - 1` links. */
+__host__ __device__ inline std::uint64_t myers_chain_pair_bytes(std::uint32_t strips, std::uint64_t link_stride) {
+    return 256 + ((std::uint64_t)strips * 4 + 255) / 256 * 256 + (std::uint64_t)strips * link_stride;
+}
+
+/**
+ *  One wave of chains: pairs [first, first + pairs) of bin `key`, each given `strips` consecutive warps (its own
+ *  chain needs ceil(n / (1,024 W)) of them; the rest exit) and `myers_chain_pair_bytes(strips, link_stride)` bytes of
+ *  `scratch`, whose head (state and progress) the launcher clears.
+ */
 template <int words_, int bits_>
 __global__ void __launch_bounds__(myers_chain_threads_k)
-    myers_chain_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t *__restrict__ bins, int key, int index,
+    myers_chain_kernel(pair_task_t const *__restrict__ tasks, plan_bins_t *__restrict__ bins, int key,
+                       std::uint32_t first, std::uint32_t pairs, std::uint32_t strips_per_pair,
                        batch_alphabet_t const *__restrict__ alphabet, std::int64_t *__restrict__ results,
-                       myers_chain_state_t *__restrict__ state, std::uint32_t *__restrict__ progress,
-                       std::uint8_t *__restrict__ links, std::uint64_t link_stride, std::uint32_t wait_polls) {
+                       unsigned char *__restrict__ scratch, std::uint64_t link_stride, std::uint32_t wait_polls) {
     constexpr int W = words_, B = bits_;
     __shared__ std::uint8_t code_s[256];
     __shared__ std::uint8_t ring_s[myers_chain_threads_k / 32][128];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) code_s[i] = alphabet->code[i];
     __syncthreads();
-    pair_task_t const task = tasks[bins->begin[key] + index];
+    std::uint32_t const global_warp = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    std::uint32_t const pair_in_wave = global_warp / strips_per_pair, warp = global_warp % strips_per_pair;
+    if (pair_in_wave >= pairs) return; // whole warps past the wave
+    pair_task_t const task = tasks[bins->begin[key] + first + pair_in_wave];
     std::uint32_t const n = task.rows_length, m = task.cols_length;
     constexpr std::uint32_t rows_per_warp = 32u * 32u * W;
     std::uint32_t const strips = (n + rows_per_warp - 1) / rows_per_warp;
-    std::uint32_t const warp = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    if (warp >= strips) return; // a whole warp: nobody waits on chain links past the last strip
+    if (warp >= strips) return; // a whole warp: nobody waits on chain links past the pair's last strip
+    unsigned char *const pair_scratch = scratch + (std::uint64_t)pair_in_wave * myers_chain_pair_bytes(strips_per_pair, link_stride);
+    auto *state = reinterpret_cast<myers_chain_state_t *>(pair_scratch);
+    auto *progress = reinterpret_cast<std::uint32_t *>(pair_scratch + 256);
+    std::uint8_t *links = pair_scratch + 256 + ((std::uint64_t)strips_per_pair * 4 + 255) / 256 * 256;
     int const lane = threadIdx.x & 31;
     bool const first_strip = warp == 0, last_strip = warp + 1 == strips;
 

@@ -950,3 +950,15 @@ def test_long_unit_levenshtein_chain_wait_gives_up(szs, port):
     engine.set_tuning(None)
     np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64),
                                   port.pairs(oracle.levenshtein_costs(), tape(first), tape(second)))
+
+
+def test_long_unit_levenshtein_chain_waves(szs, port):
+    """Many long unit-cost pairs at once: chains side by side in waves of cooperative launches (several waves here),
+    each pair's result equal to the oracle's."""
+    rng = np.random.default_rng(125)
+    count = 1500
+    lengths = rng.integers(8193, 9000, size=count)
+    first = [bytes(rng.choice(DNA, size=int(n))) for n in lengths]
+    second = [bytes(rng.choice(DNA, size=int(n) + int(rng.integers(0, 200)))) for n in lengths]
+    got = szs.LevenshteinDistances().pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle.levenshtein_costs(), tape(first), tape(second)))
