@@ -79,11 +79,12 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
             info.key = bin_myers_begin_k + thread_words * 16; // plain form: one bin, one kernel shape
             return info;
         }
+        // A warp's threads take as long as its longest text: classes of 16 columns over the shortest text a pattern
+        // of this word count can face (no text is shorter than its pattern), then four octaves; longest first.
         int const words = int((n + 31) / 32);
-        int text_class;
-        if (m < 512) text_class = int(m / 64);
-        else text_class = min(15, 8 + floor_log2_u64(m) - 9);
-        info.key = bin_myers_begin_k + words * 16 + text_class;
+        std::uint64_t const over = m - 32u * (words - 1) - 1;
+        int const text_class = over < 12 * 16 ? int(over / 16) : min(15, 12 + floor_log2_u64(over / (12 * 16)));
+        info.key = bin_myers_begin_k + words * 16 + (15 - text_class);
         return info;
     }
     if (args.unit_levenshtein && !args.wide && n > 32u * 32u * myers_warp_max_words_k && n <= myers_chain_max_rows_k) {
@@ -214,15 +215,25 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
     __syncthreads();
     std::uint64_t thread_cells = 0;
     std::uint32_t thread_max_cols = 0, thread_max_myers = 0, thread_max_myers_warp = 0, thread_max_chain = 0;
-    for (std::uint64_t p = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < args.pairs;
-         p += (std::uint64_t)gridDim.x * blockDim.x) {
-        pair_route_info_t const info = route_of_pair(args, p);
+    int const lane = threadIdx.x & 31;
+    // Warp-wide rounds, so that the lanes of a warp that share a bin (most of them, in a batch of similar pairs)
+    // count with one shared-memory atomic instead of contending for the same counter.
+    std::uint64_t const stride = (std::uint64_t)gridDim.x * blockDim.x;
+    for (std::uint64_t base = (std::uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < args.pairs;
+         base += stride) {
+        std::uint64_t const p = base + lane;
+        pair_route_info_t info;
+        info.key = -1, info.n = info.m = 0;
+        if (p < args.pairs) info = route_of_pair(args, p);
+        unsigned const key = info.key < 0 ? 0xFFFFFFFFu : (unsigned)info.key;
+        unsigned const peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (key != 0xFFFFFFFFu && lane == __ffs(peers) - 1) atomicAdd(&histogram[key], (unsigned)__popc(peers));
+        if (p >= args.pairs) continue;
         thread_cells += (std::uint64_t)info.n * info.m;
         if (info.key < 0) {
             results[p] = trivial_score(args, info.n, info.m);
             continue;
         }
-        atomicAdd(&histogram[info.key], 1u);
         if (info.key >= bin_dp32_begin_k) thread_max_cols = max(thread_max_cols, info.m);
         if (info.key >= bin_myers_warp_begin_k && info.key < bin_short_begin_k)
             thread_max_myers_warp = max(thread_max_myers_warp, info.n);
