@@ -222,21 +222,29 @@ struct device_context_t {
     static constexpr int max_chunks_k = 64;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copied[max_chunks_k] = {nullptr};
-    cudaEvent_t pipe_start = nullptr, pipe_stop = nullptr;
+    cudaEvent_t pipe_start = nullptr, pipe_stop = nullptr, offsets_copied = nullptr;
     device_buffer_t chunk_inputs;
-    device_context_t *partner = nullptr; // second context of pipelined calls: its chunks alternate with this one's
+    static constexpr int pipeline_depth_k = 12; // chunks of a pipelined call in flight at once
+    device_context_t *partners[pipeline_depth_k] = {nullptr}; // the contexts a pipelined call's chunks rotate over
     device_buffer_t utf8;                // UTF-8 calls: code-point set, counts, offsets and transcoded tapes
     device_buffer_t dense_table;         // the 256 x 256 table of the dense engine last run here over > 32 bytes
     std::uint64_t dense_table_id = 0;    // that engine's `dense_id` (0: none)
     bool deferred = false, deferred_compute = false;
     std::uint64_t deferred_launches = 0;
+    int traced_jobs = 0;             // under SZS_GB300_TRACE: the deferred call's jobs, for the chunk timeline
+    int traced_kind[32] = {0}, traced_variant[32] = {0};
+    std::uint64_t traced_pairs[32] = {0};
 
-    status_t prepare(int device_index) noexcept {
+    /** @p urgent: the context's own stream takes the device's highest priority (the contexts of pipelined chunks,
+     *  whose planning kernels should start as soon as their chunk lands, ahead of queued scoring work). */
+    status_t prepare(int device_index, bool urgent = false) noexcept {
         if (ready) return {};
         device = device_index;
         SZS_TRY_CUDA(cudaSetDevice(device));
         SZS_TRY_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
-        SZS_TRY_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+        int least = 0, greatest = 0;
+        SZS_TRY_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SZS_TRY_CUDA(cudaStreamCreateWithPriority(&own_stream, cudaStreamNonBlocking, urgent ? greatest : least));
         SZS_TRY_CUDA(cudaEventCreate(&start));
         SZS_TRY_CUDA(cudaEventCreate(&stop));
         SZS_TRY_CUDA(cudaEventCreate(&compute_start));
@@ -244,9 +252,14 @@ struct device_context_t {
         for (auto &event : trace_events) SZS_TRY_CUDA(cudaEventCreate(&event));
         SZS_TRY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
         SZS_TRY_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
-        for (auto &event : copied) SZS_TRY_CUDA(cudaEventCreateWithFlags(&event, cudaEventDisableTiming));
+        // Timed only under SZS_GB300_TRACE or SZS_GB300_TRACE_CHUNKS, which print each pipelined chunk's timeline.
+        unsigned const copied_flags = std::getenv("SZS_GB300_TRACE") || std::getenv("SZS_GB300_TRACE_CHUNKS")
+                                          ? cudaEventDefault
+                                          : cudaEventDisableTiming;
+        for (auto &event : copied) SZS_TRY_CUDA(cudaEventCreateWithFlags(&event, copied_flags));
         SZS_TRY_CUDA(cudaEventCreate(&pipe_start));
         SZS_TRY_CUDA(cudaEventCreate(&pipe_stop));
+        SZS_TRY_CUDA(cudaEventCreateWithFlags(&offsets_copied, cudaEventDisableTiming));
         for (int i = 0; i < lanes_k; ++i) {
             SZS_TRY_CUDA(cudaStreamCreateWithFlags(&lanes[i], cudaStreamNonBlocking));
             SZS_TRY_CUDA(cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming));
@@ -288,14 +301,16 @@ struct device_context_t {
             if (event) cudaEventDestroy(event);
         if (pipe_start) cudaEventDestroy(pipe_start);
         if (pipe_stop) cudaEventDestroy(pipe_stop);
+        if (offsets_copied) cudaEventDestroy(offsets_copied);
         chunk_inputs.release();
         utf8.release();
         dense_table.release(), dense_table_id = 0;
-        if (partner) {
-            partner->release();
-            delete partner;
-            partner = nullptr;
-        }
+        for (auto &partner : partners)
+            if (partner) {
+                partner->release();
+                delete partner;
+                partner = nullptr;
+            }
         control.release(), inputs.release(), work.release(), scratch.release();
         readback.release(), results_host.release();
         if (start) cudaEventDestroy(start);
@@ -572,6 +587,14 @@ struct call_t {
     bool pre_staged = false;           // the tapes below are already on the device (a chunk of a pipelined call)
     tape_t staged_queries {}, staged_candidates {};
     bool exact_alphabet = false;       // mark every byte of the batch, no sampled guess
+    // Pipelined chunks: planning waits for `plan_after` (the offsets, or the chunk's bytes when the plan reads
+    // them), scoring for `scoring_after` (the chunk's bytes); a sampled alphabet comes from `sample_*` (the first
+    // chunk's tapes, on the device before the later chunks), so the plan of a chunk can run before its bytes land.
+    cudaEvent_t plan_after = nullptr, scoring_after = nullptr;
+    tape_t const *sample_queries = nullptr, *sample_candidates = nullptr;
+    // Two phases on one context: `plan_only` returns once the plan is read back and kept in the context; a later
+    // call with `reuse_plan` (same tapes and costs) scores that plan without planning again.
+    bool plan_only = false, reuse_plan = false;
 };
 
 static status_t resolve_scope(void *scope_handle, int &device, cudaStream_t &stream, device_context_t *contexts,
@@ -823,7 +846,9 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     // them, and the shared-table kernel checks every byte it reads against the guess. A guess with more than four
     // symbols, a plan with pairs on other routes, or a byte the guess missed is answered by scoring the call again
     // with the exact alphabet, so results never depend on the guess.
-    bool const speculative = alphabet_pass && engine.unit_levenshtein && !call.exact_alphabet && !defer;
+    // Deferred calls (pipelined chunks) guess from the sample they are given and are checked when they are settled.
+    bool const speculative = alphabet_pass && engine.unit_levenshtein && !call.exact_alphabet &&
+                             (!defer || call.sample_queries != nullptr);
 
     static bool const tracing = std::getenv("SZS_GB300_TRACE") != nullptr;
     // Device-resident inputs make every launch of the call a function of bytes the call can key on, so both phases
@@ -858,38 +883,52 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         return {};
     };
 
+    if (call.plan_after && !call.reuse_plan) SZS_TRY_CUDA(cudaStreamWaitEvent(stream, call.plan_after, 0));
     SZS_TRY_CUDA(cudaEventRecord(context->start, stream));
     std::uint64_t launches = 0;
     plan_bins_t *bins = context->bins_device();
     batch_alphabet_t *alphabet = context->alphabet_device();
     if (alphabet_pass) args.alphabet = alphabet;
-    std::vector<unsigned char> prologue_key;
-    if (graphs) {
-        key_append(prologue_key, args);
-        key_append(prologue_key, bins), key_append(prologue_key, tasks), key_append(prologue_key, results);
-        key_append(prologue_key, context->readback.data), key_append(prologue_key, context->sm_count);
-        key_append(prologue_key, call.has_candidates), key_append(prologue_key, speculative);
+    if (!call.reuse_plan) {
+        std::vector<unsigned char> prologue_key;
+        if (graphs) {
+            key_append(prologue_key, args);
+            key_append(prologue_key, bins), key_append(prologue_key, tasks), key_append(prologue_key, results);
+            key_append(prologue_key, context->readback.data), key_append(prologue_key, context->sm_count);
+            key_append(prologue_key, call.has_candidates), key_append(prologue_key, speculative);
+            for (tape_t const *sample : {call.sample_queries, call.sample_candidates})
+                if (sample) {
+                    key_append(prologue_key, sample->base), key_append(prologue_key, sample->offsets);
+                    key_append(prologue_key, sample->count), key_append(prologue_key, sample->offset_bits);
+                }
+        }
+        status = issue_or_replay(context->prologue_graphs, prologue_key, prologue_replayed, [&](cudaStream_t s) -> status_t {
+            // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code
+            // planes by it, and the 16x2 route builds its substitution profile over it (when it has at most 32
+            // symbols).
+            if (alphabet_pass) {
+                bool const sampled_elsewhere = speculative && call.sample_queries;
+                tape_t const &sample_queries = sampled_elsewhere ? *call.sample_queries : args.queries;
+                tape_t const &sample_candidates = sampled_elsewhere ? *call.sample_candidates : args.candidates;
+                SZS_TRY_CUDA(launch_alphabet(sample_queries, sample_candidates, call.has_candidates, alphabet,
+                                             context->sm_count, s, speculative ? alphabet_sample_bytes_k : 0));
+            }
+            SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, s));
+            // Read the plan (and the alphabet, stored right after it) back: which bins are non-empty, column lengths.
+            SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t) + sizeof(batch_alphabet_t),
+                                         cudaMemcpyDeviceToHost, s));
+            return {};
+        });
+        if (!status.ok()) return status;
+        launches += 3 + (alphabet_pass ? 2 : 0);
+        SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     }
-    status = issue_or_replay(context->prologue_graphs, prologue_key, prologue_replayed, [&](cudaStream_t s) -> status_t {
-        // Levenshtein engines need the batch alphabet before planning: the bit-parallel route sizes its code planes
-        // by it, and the 16x2 route builds its substitution profile over it (when it has at most 32 symbols).
-        if (alphabet_pass)
-            SZS_TRY_CUDA(launch_alphabet(args.queries, args.candidates, call.has_candidates, alphabet,
-                                         context->sm_count, s, speculative ? alphabet_sample_bytes_k : 0));
-        SZS_TRY_CUDA(launch_plan(args, bins, tasks, results, context->sm_count, s));
-        // Read the plan (and the alphabet, stored right after it) back: which bins are non-empty, column lengths.
-        SZS_TRY_CUDA(cudaMemcpyAsync(context->bins_host(), bins, sizeof(plan_bins_t) + sizeof(batch_alphabet_t),
-                                     cudaMemcpyDeviceToHost, s));
-        return {};
-    });
-    if (!status.ok()) return status;
-    launches += 3 + (alphabet_pass ? 2 : 0);
-    SZS_TRY_CUDA(cudaStreamSynchronize(stream));
     plan_bins_t const &plan = *context->bins_host();
     batch_alphabet_t const &alphabet_host = *context->alphabet_host();
     auto run_exact = [&]() -> status_t {
         call_t exact = call;
         exact.exact_alphabet = true;
+        if (exact.scoring_after) exact.plan_after = exact.scoring_after; // the exact pass reads the chunk's bytes
         return run_on(engine, context, stream, exact, schedule, stats, defer);
     };
     if (speculative) {
@@ -897,6 +936,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         for (int key = bin_dp32_begin_k; key < bin_keys_k && thread_route_only; ++key)
             thread_route_only = plan.count[key] == 0;
         if (!thread_route_only) return run_exact();
+    }
+    if (call.plan_only) {
+        stats.last_launches = launches; // the planning launches; the scoring phase counts its own
+        return {};
     }
     stats.last_cells = plan.cells;
     auto pairs_in = [&](int key_begin, int key_end) {
@@ -1177,6 +1220,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                                                                    : std::min(job_count, (int)device_context_t::lanes_k);
     // Scoring kernels are bracketed by their own events so the stats isolate them from planning and copies.
     bool compute_recorded = false;
+    if (call.scoring_after) SZS_TRY_CUDA(cudaStreamWaitEvent(stream, call.scoring_after, 0));
     if (job_count) {
         SZS_TRY_CUDA(cudaEventRecord(context->compute_start, stream));
         compute_recorded = true;
@@ -1294,6 +1338,10 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
                 context->deferred = true;
                 context->deferred_compute = compute_recorded;
                 context->deferred_launches = launches;
+                context->traced_jobs = tracing ? std::min(job_count, 32) : 0;
+                for (int i = 0; i < context->traced_jobs; ++i)
+                    context->traced_kind[i] = (int)jobs[i].kind, context->traced_variant[i] = jobs[i].variant,
+                    context->traced_pairs[i] = jobs[i].pairs;
                 return {};
             }
             SZS_TRY_CUDA(cudaStreamSynchronize(stream));
@@ -1381,91 +1429,110 @@ static bool pinned_host(void const *pointer) noexcept {
 constexpr std::size_t pipeline_chunk_bytes_k = std::size_t(64) << 20; // default input bytes per pipelined chunk
 
 /**
- *  Pairwise calls on large pinned-host tapes: the pairs are cut into chunks of about equal input bytes and every
- *  chunk's host-to-device copy is queued at once on the context's copy stream, each into its own slot; chunk c is
- *  planned and scored on the call's stream as soon as its own copy has landed, while the later copies continue, so
- *  the link stays busy and scoring hides behind it. Each chunk is one ordinary call on device-resident tapes
- *  (`pre_staged`), so results equal the unchunked call's.
+ *  Pairwise calls on large pinned-host tapes: both tapes' offsets are copied first, then the strings in chunks of
+ *  about `chunk_bytes` input bytes, each into its own slot, all queued at once on the context's copy stream. Chunk c
+ *  is planned and scored as soon as its copy has landed, on one of `pipeline_depth_k` chunk contexts whose streams
+ *  have the device's highest priority, so its planning kernels start ahead of the scoring still queued from earlier
+ *  chunks while the later copies continue: the link stays busy and scoring hides behind it. The last chunks halve in
+ *  size down to a quarter chunk, so little work remains once the last byte has landed. Each chunk is one ordinary
+ *  call on device-resident tapes (`pre_staged`), so results equal the unchunked call's.
  */
 static status_t run_pipelined(engine_t const &engine, device_context_t *context, cudaStream_t stream,
-                              call_t const &call, int schedule, szs_gb300_stats_t &stats, int chunks) noexcept {
+                              call_t const &call, int schedule, szs_gb300_stats_t &stats,
+                              std::uint64_t chunk_bytes) noexcept {
     tape_view_t const tapes[2] = {call.queries, call.candidates};
     std::uint64_t const pairs = call.queries.count;
     auto bytes_before = [&](std::uint64_t p) { // input bytes of pairs [0, p) of both tapes
         return (host_offset(tapes[0], p) - host_offset(tapes[0], 0)) + (host_offset(tapes[1], p) - host_offset(tapes[1], 0));
     };
     std::uint64_t const total = bytes_before(pairs);
-    std::vector<std::uint64_t> cuts(chunks + 1, pairs);
-    cuts[0] = 0;
-    for (int c = 1; c < chunks; ++c) { // first pair whose prefix reaches c / chunks of the bytes
-        std::uint64_t const target = total / chunks * c;
-        std::uint64_t low = cuts[c - 1], high = pairs;
+    // Chunk sizes: whole chunks while more than two remain, then halves down to a quarter chunk, then the rest.
+    std::vector<std::uint64_t> targets; // byte prefix at the end of each chunk but the last
+    {
+        std::uint64_t done = 0, remaining = total;
+        std::uint64_t const smallest = std::max<std::uint64_t>(chunk_bytes / 4, 1);
+        while (remaining > 2 * chunk_bytes && targets.size() + 2 < device_context_t::max_chunks_k)
+            done += chunk_bytes, remaining -= chunk_bytes, targets.push_back(done);
+        while (remaining > 2 * smallest && targets.size() + 2 < device_context_t::max_chunks_k)
+            done += remaining / 2, remaining -= remaining / 2, targets.push_back(done);
+    }
+    std::vector<std::uint64_t> cuts(1, 0);
+    for (std::uint64_t const target : targets) { // first pair whose prefix reaches the target
+        std::uint64_t low = cuts.back(), high = pairs;
         while (low < high) {
             std::uint64_t const mid = low + (high - low) / 2;
             if (bytes_before(mid) < target) low = mid + 1;
             else high = mid;
         }
-        cuts[c] = low;
+        if (low > cuts.back() && low < pairs) cuts.push_back(low);
     }
+    cuts.push_back(pairs);
+    int const chunks = (int)cuts.size() - 1;
     std::size_t const offset_size = call.queries.offset_bits == 32 ? 4 : 8;
-    std::vector<std::size_t> slot(chunks + 1, 0); // byte offset of each chunk's slot
-    for (int c = 0; c < chunks; ++c) {
-        std::uint64_t const count = cuts[c + 1] - cuts[c];
-        std::size_t area = 0;
-        for (auto const &tape : tapes)
-            area += align_up((count + 1) * offset_size, 256) +
-                    align_up(host_offset(tape, cuts[c + 1]) - host_offset(tape, cuts[c]), 256);
-        slot[c + 1] = slot[c] + area;
-    }
-    status_t status = context->chunk_inputs.reserve(slot[chunks], stream);
+    // Slots: the offsets of both tapes, then each chunk's bytes of both tapes.
+    std::size_t offsets_at[2], cursor = 0;
+    for (int t = 0; t < 2; ++t) offsets_at[t] = cursor, cursor += align_up((pairs + 1) * offset_size, 256);
+    std::vector<std::size_t> data_at(2 * chunks);
+    for (int c = 0; c < chunks; ++c)
+        for (int t = 0; t < 2; ++t)
+            data_at[2 * c + t] = cursor,
+                          cursor += align_up(host_offset(tapes[t], cuts[c + 1]) - host_offset(tapes[t], cuts[c]), 256);
+    status_t status = context->chunk_inputs.reserve(cursor, stream);
     if (!status.ok()) return status;
     auto *area = static_cast<unsigned char *>(context->chunk_inputs.data);
 
-    std::vector<tape_t> staged(2 * chunks);
     SZS_TRY_CUDA(cudaEventRecord(context->pipe_start, stream));
     // Earlier work on the call's stream may still read the slots: the copies wait for it.
     SZS_TRY_CUDA(cudaStreamWaitEvent(context->copy_stream, context->pipe_start, 0));
+    for (int t = 0; t < 2; ++t)
+        SZS_TRY_CUDA(cudaMemcpyAsync(area + offsets_at[t], tapes[t].offsets, (pairs + 1) * offset_size,
+                                     cudaMemcpyHostToDevice, context->copy_stream));
+    SZS_TRY_CUDA(cudaEventRecord(context->offsets_copied, context->copy_stream));
+    std::vector<tape_t> staged(2 * chunks);
     for (int c = 0; c < chunks; ++c) {
-        unsigned char *cursor = area + slot[c];
         std::uint64_t const first = cuts[c], count = cuts[c + 1] - cuts[c];
         for (int t = 0; t < 2; ++t) {
-            tape_view_t const &tape = tapes[t];
-            std::size_t const offsets_bytes = (count + 1) * offset_size;
-            SZS_TRY_CUDA(cudaMemcpyAsync(cursor, static_cast<unsigned char const *>(tape.offsets) + first * offset_size,
-                                         offsets_bytes, cudaMemcpyHostToDevice, context->copy_stream));
-            tape_t &out = staged[2 * c + t];
-            out.offsets = cursor;
-            out.count = count;
-            out.offset_bits = tape.offset_bits;
-            cursor += align_up(offsets_bytes, 256);
-            std::uint64_t const begin = host_offset(tape, first), end = host_offset(tape, first + count);
+            std::uint64_t const begin = host_offset(tapes[t], first), end = host_offset(tapes[t], first + count);
             if (end > begin)
-                SZS_TRY_CUDA(cudaMemcpyAsync(cursor, tape.data + begin, end - begin, cudaMemcpyHostToDevice,
-                                             context->copy_stream));
-            out.base = reinterpret_cast<std::uint8_t const *>(cursor) - begin; // offsets stay absolute
-            cursor += align_up(end - begin, 256);
+                SZS_TRY_CUDA(cudaMemcpyAsync(area + data_at[2 * c + t], tapes[t].data + begin, end - begin,
+                                             cudaMemcpyHostToDevice, context->copy_stream));
+            tape_t &out = staged[2 * c + t];
+            out.offsets = area + offsets_at[t] + first * offset_size;
+            out.count = count;
+            out.offset_bits = tapes[t].offset_bits;
+            out.base = reinterpret_cast<std::uint8_t const *>(area + data_at[2 * c + t]) - begin; // absolute offsets
         }
         SZS_TRY_CUDA(cudaEventRecord(context->copied[c], context->copy_stream));
     }
-    // Chunks alternate between this context (on the call's stream) and its partner (on the partner's stream), so
-    // chunk c + 1 is planned and launched while chunk c's kernels still drain.
-    if (!context->partner) {
-        context->partner = new (std::nothrow) device_context_t();
-        if (!context->partner) return {sz_bad_alloc_k, nullptr};
-        status = context->partner->prepare(context->device);
-        if (!status.ok()) {
-            context->partner->release();
-            delete context->partner;
-            context->partner = nullptr;
-            return status;
+    int const depth = std::min(chunks, device_context_t::pipeline_depth_k);
+    device_context_t *contexts[device_context_t::pipeline_depth_k] = {nullptr};
+    cudaStream_t streams[device_context_t::pipeline_depth_k] = {nullptr};
+    for (int i = 0; i < depth; ++i) {
+        device_context_t *&partner = context->partners[i];
+        if (!partner) {
+            partner = new (std::nothrow) device_context_t();
+            if (!partner) return {sz_bad_alloc_k, nullptr};
+            status = partner->prepare(context->device, true);
+            if (!status.ok()) {
+                partner->release();
+                delete partner;
+                partner = nullptr;
+                return status;
+            }
         }
+        contexts[i] = partner, streams[i] = partner->own_stream;
+        SZS_TRY_CUDA(cudaStreamWaitEvent(streams[i], context->pipe_start, 0));
     }
-    device_context_t *const contexts[2] = {context, context->partner};
-    cudaStream_t const streams[2] = {stream, context->partner->own_stream};
-    SZS_TRY_CUDA(cudaStreamWaitEvent(streams[1], context->pipe_start, 0));
-    szs_gb300_stats_t chunk_stats[2] {};
+    szs_gb300_stats_t chunk_stats[device_context_t::pipeline_depth_k] {};
+    call_t chunk_calls[device_context_t::pipeline_depth_k];
     std::uint64_t cells = 0, launches = 0, graph_replays = 0;
     double compute_ms = 0;
+    // SZS_GB300_TRACE prints each chunk's timeline and jobs (graphs off); SZS_GB300_TRACE_CHUNKS only the chunks'
+    // timelines, with the graphs of ordinary calls.
+    static bool const tracing =
+        std::getenv("SZS_GB300_TRACE") != nullptr || std::getenv("SZS_GB300_TRACE_CHUNKS") != nullptr;
+    int in_flight[device_context_t::pipeline_depth_k];
+    for (int &chunk : in_flight) chunk = -1; // the chunk each context runs
     auto settle = [&](int which) -> status_t { // waits for the chunk in flight on contexts[which], if any
         if (!contexts[which]->deferred) return {};
         std::uint64_t const before = chunk_stats[which].kernel_launches;
@@ -1473,41 +1540,102 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
         if (!finished.ok()) return finished;
         launches += chunk_stats[which].kernel_launches - before;
         compute_ms += chunk_stats[which].last_compute_ms;
+        if (contexts[which]->bins_host()->error_flags & 2u) { // the sampled alphabet missed a byte of this chunk
+            call_t exact = chunk_calls[which];
+            exact.exact_alphabet = true;
+            exact.plan_after = exact.scoring_after = nullptr; // its bytes landed before its scoring ran
+            exact.sample_queries = exact.sample_candidates = nullptr;
+            exact.plan_only = exact.reuse_plan = false;
+            std::uint64_t const again = chunk_stats[which].kernel_launches;
+            status_t const rescored = run_on(engine, contexts[which], streams[which], exact, schedule,
+                                             chunk_stats[which], false);
+            if (!rescored.ok()) return rescored;
+            launches += chunk_stats[which].kernel_launches - again;
+            compute_ms += chunk_stats[which].last_compute_ms;
+        }
+        if (tracing && in_flight[which] >= 0) { // the chunk's timeline from the start of the call, in ms
+            float at[5] = {0, 0, 0, 0, 0};
+            cudaEvent_t const marks[5] = {context->copied[in_flight[which]], contexts[which]->start,
+                                          contexts[which]->compute_start, contexts[which]->compute_stop,
+                                          contexts[which]->stop};
+            for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&at[i], context->pipe_start, marks[i]);
+            cudaGetLastError(); // a mark that was not recorded leaves no error behind for the next call
+            std::fprintf(stderr,
+                         "[szs_gb300] chunk %3d  pairs %8llu  copied %8.3f  planning %8.3f  scoring %8.3f - %8.3f  "
+                         "done %8.3f\n",
+                         in_flight[which], (unsigned long long)(cuts[in_flight[which] + 1] - cuts[in_flight[which]]),
+                         at[0], at[1], at[2], at[3], at[4]);
+            for (int i = 0; i < contexts[which]->traced_jobs; ++i) {
+                float from = 0, to = 0;
+                cudaEventElapsedTime(&from, context->pipe_start, contexts[which]->trace_events[2 * i]);
+                cudaEventElapsedTime(&to, context->pipe_start, contexts[which]->trace_events[2 * i + 1]);
+                cudaGetLastError();
+                std::fprintf(stderr, "[szs_gb300]      job kind %d variant %3d  pairs %8llu  %8.3f - %8.3f\n",
+                             contexts[which]->traced_kind[i], contexts[which]->traced_variant[i],
+                             (unsigned long long)contexts[which]->traced_pairs[i], from, to);
+            }
+        }
         return {};
     };
-    for (int c = 0; c < chunks && status.ok(); ++c) {
-        int const which = c & 1;
-        status = settle(which); // the chunk this context ran two chunks ago
-        if (!status.ok()) break;
-        call_t chunk = call;
+    // A chunk is planned before its bytes land whenever its plan does not read them: engines without an alphabet
+    // pass plan from the offsets alone, and unit-cost Levenshtein guesses its alphabet from the first chunk's bytes
+    // (checked per pair by the kernels, a missed byte rescoring the chunk exactly). The first `depth` chunks are
+    // then all planned before any scoring is queued, while the GPU only waits for the link, and only scoring waits
+    // for each chunk's own copy; planning kernels queued behind scoring would wait for its CTAs to retire.
+    bool const alphabet_pass = (engine.kind == kind_levenshtein_k || !engine.dense.empty()) && !engine.utf8;
+    bool const sampled = alphabet_pass && engine.unit_levenshtein;
+    bool const plan_ahead = !alphabet_pass || sampled;
+    auto plan = [&](int c) -> status_t { // plans chunk c on context c % depth, once its previous chunk is settled
+        int const which = c % depth;
+        status_t settled = settle(which);
+        if (!settled.ok()) return settled;
+        call_t &chunk = chunk_calls[which];
+        chunk = call;
         chunk.pre_staged = true;
         chunk.staged_queries = staged[2 * c];
         chunk.staged_candidates = staged[2 * c + 1];
         chunk.queries.count = chunk.candidates.count = cuts[c + 1] - cuts[c];
         chunk.out = call.out + cuts[c];
-        if (!chunk.queries.count) continue;
-        cudaError_t const waited = cudaStreamWaitEvent(streams[which], context->copied[c], 0);
-        if (waited != cudaSuccess) {
-            status = from_cuda(waited);
-            break;
-        }
+        chunk.scoring_after = context->copied[c];
+        chunk.plan_after = !alphabet_pass ? context->offsets_copied : sampled ? context->copied[0] : context->copied[c];
+        if (sampled) chunk.sample_queries = &staged[0], chunk.sample_candidates = &staged[1];
+        chunk.plan_only = true;
         chunk_stats[which].graph_replays = 0;
-        status = run_on(engine, contexts[which], streams[which], chunk, schedule, chunk_stats[which], true);
-        if (!status.ok()) break;
+        status_t const planned = run_on(engine, contexts[which], streams[which], chunk, schedule, chunk_stats[which]);
+        launches += chunk_stats[which].last_launches;
+        return planned;
+    };
+    auto launch = [&](int c) -> status_t { // queues the scoring of chunk c's plan, without waiting for it
+        int const which = c % depth;
+        call_t &chunk = chunk_calls[which];
+        chunk.plan_only = false, chunk.reuse_plan = true;
+        status_t const queued = run_on(engine, contexts[which], streams[which], chunk, schedule, chunk_stats[which], true);
+        if (!queued.ok()) return queued;
+        in_flight[which] = c;
         cells += chunk_stats[which].last_cells, graph_replays += chunk_stats[which].graph_replays;
+        return {};
+    };
+    int const window = plan_ahead ? depth : 1;
+    for (int c = 0; c < std::min(window, chunks) && status.ok(); ++c) status = plan(c);
+    for (int c = 0; c < std::min(window, chunks) && status.ok(); ++c) status = launch(c);
+    for (int c = std::min(window, chunks); c < chunks && status.ok(); ++c) {
+        status = plan(c);
+        if (status.ok()) status = launch(c);
     }
-    for (int which = 0; which < 2; ++which) {
+    for (int which = 0; which < depth; ++which) {
         status_t const settled = settle(which);
         if (status.ok()) status = settled;
     }
     if (!status.ok()) {
         cudaStreamSynchronize(context->copy_stream);
-        cudaStreamSynchronize(streams[1]);
+        for (int which = 0; which < depth; ++which) cudaStreamSynchronize(streams[which]);
         cudaStreamSynchronize(stream);
         return status;
     }
-    SZS_TRY_CUDA(cudaEventRecord(context->partner->stop, streams[1]));
-    SZS_TRY_CUDA(cudaStreamWaitEvent(stream, context->partner->stop, 0));
+    for (int which = 0; which < depth; ++which) {
+        SZS_TRY_CUDA(cudaEventRecord(contexts[which]->stop, streams[which]));
+        SZS_TRY_CUDA(cudaStreamWaitEvent(stream, contexts[which]->stop, 0));
+    }
     SZS_TRY_CUDA(cudaEventRecord(context->pipe_stop, stream));
     SZS_TRY_CUDA(cudaEventSynchronize(context->pipe_stop));
     float elapsed = 0;
@@ -1532,9 +1660,8 @@ static status_t run_call(engine_t &engine, void *scope_handle, call_t const &cal
         std::size_t const chunk_bytes = engine.tuning.pipeline_chunk_kb
                                             ? std::size_t(engine.tuning.pipeline_chunk_kb) << 10
                                             : pipeline_chunk_bytes_k;
-        int const chunks = (int)std::min<std::uint64_t>(device_context_t::max_chunks_k,
-                                                        std::min<std::uint64_t>(call.queries.count, bytes / chunk_bytes));
-        if (chunks >= 2) return run_pipelined(engine, context, stream, call, engine.schedule, engine.stats, chunks);
+        if (bytes >= 2 * chunk_bytes)
+            return run_pipelined(engine, context, stream, call, engine.schedule, engine.stats, chunk_bytes);
     }
     return run_on(engine, context, stream, call, engine.schedule, engine.stats);
 }

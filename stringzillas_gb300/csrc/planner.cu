@@ -241,11 +241,21 @@ __global__ void plan_count_kernel(plan_args_t const args, plan_bins_t *__restric
         else if (info.key < bin_myers_begin_k + (myers_max_words_k + 1) * 16)
             thread_max_myers = max(thread_max_myers, info.n);
     }
-    atomicAdd(&block_cells, (unsigned long long)thread_cells);
-    atomicMax(&block_max_cols, thread_max_cols);
-    atomicMax(&block_max_myers, thread_max_myers);
-    atomicMax(&block_max_myers_warp, thread_max_myers_warp);
-    atomicMax(&block_max_chain, thread_max_chain);
+    // Reduce over the warp first: 32 lanes' atomics on one shared word would serialise.
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1)
+        thread_cells += __shfl_xor_sync(0xFFFFFFFFu, thread_cells, offset);
+    thread_max_cols = __reduce_max_sync(0xFFFFFFFFu, thread_max_cols);
+    thread_max_myers = __reduce_max_sync(0xFFFFFFFFu, thread_max_myers);
+    thread_max_myers_warp = __reduce_max_sync(0xFFFFFFFFu, thread_max_myers_warp);
+    thread_max_chain = __reduce_max_sync(0xFFFFFFFFu, thread_max_chain);
+    if (lane == 0) {
+        atomicAdd(&block_cells, (unsigned long long)thread_cells);
+        atomicMax(&block_max_cols, thread_max_cols);
+        atomicMax(&block_max_myers, thread_max_myers);
+        atomicMax(&block_max_myers_warp, thread_max_myers_warp);
+        atomicMax(&block_max_chain, thread_max_chain);
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < bin_keys_k; i += blockDim.x)
         if (histogram[i]) atomicAdd(&bins->count[i], histogram[i]);
@@ -437,6 +447,27 @@ __global__ void scatter_output_kernel(plan_args_t const args, std::int64_t const
     }
 }
 
+/** Launches @p kernel with its stream's priority as an explicit launch attribute, so that a graph captured from a
+ *  high-priority stream keeps the priority in its kernel nodes (the planning of pipelined chunks runs ahead of
+ *  queued scoring). */
+template <typename... params_, typename... args_>
+static cudaError_t launch_prioritised(void (*kernel)(params_...), unsigned grid, unsigned block, cudaStream_t stream,
+                                      args_ const &...args) {
+    int priority = 0;
+    cudaError_t const queried = cudaStreamGetPriority(stream, &priority);
+    if (queried != cudaSuccess) return queried;
+    cudaLaunchConfig_t config = {};
+    config.gridDim = dim3(grid);
+    config.blockDim = dim3(block);
+    config.stream = stream;
+    cudaLaunchAttribute attribute;
+    attribute.id = cudaLaunchAttributePriority;
+    attribute.val.priority = priority;
+    config.attrs = &attribute;
+    config.numAttrs = 1;
+    return cudaLaunchKernelEx(&config, kernel, args...);
+}
+
 static int grid_for(std::uint64_t items, int block, int sm_count, int per_sm = 8) {
     std::uint64_t const needed = (items + block - 1) / block;
     std::uint64_t const cap = (std::uint64_t)sm_count * per_sm;
@@ -448,10 +479,11 @@ cudaError_t launch_plan(plan_args_t const &args, plan_bins_t *bins, pair_task_t 
     cudaError_t status = cudaMemsetAsync(bins, 0, sizeof(plan_bins_t), stream);
     if (status != cudaSuccess) return status;
     if (args.pairs == 0) return cudaSuccess;
-    plan_count_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, bins, results);
-    plan_scan_kernel<<<1, bin_keys_k / 2, 0, stream>>>(bins);
-    plan_scatter_kernel<<<grid_for(args.pairs, 256, sm_count), 256, 0, stream>>>(args, bins, tasks);
-    return cudaGetLastError();
+    status = launch_prioritised(plan_count_kernel, grid_for(args.pairs, 256, sm_count), 256, stream, args, bins, results);
+    if (status != cudaSuccess) return status;
+    status = launch_prioritised(plan_scan_kernel, 1, bin_keys_k / 2, stream, bins);
+    if (status != cudaSuccess) return status;
+    return launch_prioritised(plan_scatter_kernel, grid_for(args.pairs, 256, sm_count), 256, stream, args, bins, tasks);
 }
 
 cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, bool has_candidates,
@@ -461,10 +493,11 @@ cudaError_t launch_alphabet(tape_t const &queries, tape_t const &candidates, boo
     unsigned const per_tape = sample_bytes ? (unsigned)std::min<std::uint64_t>((std::uint64_t)sm_count * 8,
                                                                                 sample_bytes / (256 * 16 * 4) + 1)
                                            : (unsigned)sm_count * 8;
-    alphabet_mark_kernel<<<has_candidates ? 2 * per_tape : per_tape, 256, 0, stream>>>(
-        queries, has_candidates ? candidates : queries, per_tape, sample_bytes, mask);
-    alphabet_codes_kernel<<<1, 32, 0, stream>>>(mask, alphabet);
-    return cudaGetLastError();
+    cudaError_t const status = launch_prioritised(alphabet_mark_kernel, has_candidates ? 2 * per_tape : per_tape, 256,
+                                                  stream, queries, has_candidates ? candidates : queries, per_tape,
+                                                  sample_bytes, mask);
+    if (status != cudaSuccess) return status;
+    return launch_prioritised(alphabet_codes_kernel, 1, 32, stream, mask, alphabet);
 }
 
 cudaError_t launch_scatter_output(plan_args_t const &args, std::int64_t const *results, std::int64_t *out,

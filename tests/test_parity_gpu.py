@@ -525,6 +525,36 @@ def test_pipelined_pinned_host_call(szs, port, family):
     np.testing.assert_array_equal(engine.pairwise(device, device_b).astype(np.int64), want)
 
 
+def test_pipelined_chunks_planned_from_a_sample(szs, port):
+    """Pipelined unit-cost calls plan every chunk before its bytes land, from the alphabet of the first chunk's bytes:
+    later chunks with a fifth symbol in a shorter or a longer string, or with a pair too long for the thread route,
+    are scored again exactly and equal the oracle."""
+    torch = pytest.importorskip("torch")
+    from stringzillas_gb300 import workloads as w
+    count = 200_000
+    (fd, fo), (sd, so) = w.levenshtein_reads(count, 100, 300, 0.05, 0.02, seed=8)
+    first = [bytes(fd[fo[i]:fo[i + 1]]) for i in range(count)]
+    second = [bytes(sd[so[i]:so[i + 1]]) for i in range(count)]
+    first[150_000] = first[150_000][:40] + b"N" + first[150_000][41:]
+    second[180_000] = second[180_000][:90] + b"NN" + second[180_000][92:]
+    rng = np.random.default_rng(8)
+    first[190_000] = bytes(rng.choice(DNA, size=1500))
+    second[190_000] = bytes(rng.choice(DNA, size=1700))
+    (fd, fo), (sd, so) = tape(first), tape(second)
+    engine = szs.LevenshteinDistances()
+    pinned = [torch.from_numpy(x).pin_memory() for x in (fd, fo.astype(np.uint64).view(np.int64),
+                                                          sd, so.astype(np.uint64).view(np.int64))]
+    a = szs.Strs.from_buffers(pinned[0], pinned[1])
+    b = szs.Strs.from_buffers(pinned[2], pinned[3])
+    want = port.pairs(oracle.levenshtein_costs(), (fd, fo), (sd, so))
+    for chunk_kb in (4096, 16384):  # about twenty chunks (more than the contexts in flight), then five
+        engine.set_tuning({"pipeline_chunk_kb": chunk_kb})
+        for _ in range(2):  # the second call replays the captured graphs
+            out = torch.full((count,), -7, dtype=torch.int64).pin_memory()
+            engine.pairwise(a, b, out=out)
+            np.testing.assert_array_equal(out.numpy(), want)
+
+
 @pytest.mark.parametrize("family,costs", [("lev", (0, 1, 1, 1)), ("lev", (0, 2, 3, 1)), ("lev", (0, 3, 2, 2)),
                                           ("nw", (-11, -1)), ("nw", (-4, -4)), ("sw", (-5, -2)), ("sw", (-3, -3))])
 def test_band16_route(szs, port, family, costs):
