@@ -485,6 +485,20 @@ def serving_leg(szs):
         out[name] = row
     out["saturated_serving_over_plain"] = (out["serving"]["saturated_gcups"] /
                                            out["per_request_plain"]["saturated_gcups"])
+    # The latency floor: each distinct request of the pool served alone on an idle server (one lane, one request
+    # per batch, batched schedule), admission to delivery, weighted by how often the stream draws it.
+    alone = np.zeros(len(pool))
+    with szs.Server(lanes=1, max_batch_requests=1, arena_bytes=4 << 30) as server:
+        strs = [(szs.Strs.from_buffers(*r["first"]), szs.Strs.from_buffers(*r["second"])) for r in pool]
+        server.submit(engines[pool[0]["kind"]], *strs[0]).result()  # warm-up
+        for k, request in enumerate(pool):
+            ticket = server.submit(engines[request["kind"]], *strs[k])
+            ticket.result()
+            alone[k] = ticket.info["done_ms"] - ticket.info["admitted_ms"]
+    drawn = alone[order]
+    out["service_alone"] = {"p50_ms": float(np.percentile(drawn, 50)), "p99_ms": float(np.percentile(drawn, 99)),
+                            "max_ms": float(drawn.max()),
+                            "note": "each request scored alone on an idle server: the floor under its latency"}
     # Mixed-length NW / SW only: a saturating burst of alignment requests, both forms.
     nw_sw = w.serving_requests(32, seed=43, kinds=("nw", "sw"))
     burst = rng.integers(0, len(nw_sw), size=NW_SW_BURST)

@@ -35,6 +35,7 @@ UNITS = [
     ("kernels_band16", "kernels_band16.cu", []),
     ("direct", "direct.cu", []),
     ("kernels_short8", "kernels_short.cu", ["-DSZS_SHORT_ROWS=8"]),
+    ("kernels_short12", "kernels_short.cu", ["-DSZS_SHORT_ROWS=12"]),
     ("kernels_short16", "kernels_short.cu", ["-DSZS_SHORT_ROWS=16"]),
     ("probe", "probe.cu", []),
     ("static_scratch", "static_scratch.cu", []),

@@ -1131,7 +1131,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         scratch_total += bytes;
     }
     // Short pairs: one job per segment shape, most rows first.
-    for (int shape_index = short_shapes_k - 1; shape_index >= 0; --shape_index) {
+    for (int shape_index : {3, 6, 2, 5, 1, 4, 0}) {
         int const key_begin = bin_short_begin_k + shape_index * short_m_classes_k;
         int const key_end = key_begin + short_m_classes_k;
         std::uint64_t const pairs_here = pairs_in(key_begin, key_end);
@@ -1140,8 +1140,9 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         dp_launch_shape_t const shape =
             short_shape(engine.kind, costs.affine != 0, shape_index, packed_costs.classes, warps, compare_mode);
         if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Short-pair kernel cannot be resident"};
-        int const rows = short_rows_for(packed_costs.classes, compare_mode);
-        std::uint64_t const per_warp = 2u * (32u / (std::uint64_t)((16 << shape_index) / rows)); // pairs per warp
+        int const rows = short_rows_for(packed_costs.classes, compare_mode, shape_index);
+        std::uint64_t const lanes = (std::uint64_t)(short_segment_rows(shape_index) / rows);
+        std::uint64_t const per_warp = 2u * (32u / lanes); // pairs per warp
         std::uint64_t const warps_needed = (pairs_here + per_warp - 1) / per_warp;
         std::uint64_t const needed = (warps_needed + warps - 1) / warps;
         int const ctas = (int)std::min<std::uint64_t>(needed, (std::uint64_t)context->sm_count * shape.ctas_per_sm);

@@ -143,10 +143,11 @@ cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pai
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
                           int group_ctas = 1, int compare = 0, bool wide = false);
 
-/** Short pairs (shorter side at most 128) on the segmented 16x2 kernel: `shape` 0, 1, 2, 3 for shorter sides up to
- *  16, 32, 64, 128; segments of 16 rows per lane when `short_rows_for` says 16 (compare mode or at most 8 classes),
- *  else of 8 rows per lane; `compare` as for the 16x2 wavefront (Levenshtein only). */
-int short_rows_for(int classes, int compare);
+/** Short pairs (shorter side at most 128) on the segmented 16x2 kernel: `shape` 0-6 for shorter sides up to 16, 32,
+ *  64, 128, 24, 48, 96 (`short_segment_rows`); shapes 4-6 have 12 rows per lane, shapes 0-3 16 when compare mode or
+ *  at most 8 classes, else 8 (`short_rows_for`); `compare` as for the 16x2 wavefront (Levenshtein only). */
+int short_rows_for(int classes, int compare, int shape);
+int short_segment_rows(int shape);
 dp_launch_shape_t short_shape(int kind, bool affine, int shape, int classes, int warps, int compare = 0);
 cudaError_t launch_short(int kind, bool affine, int shape, int key_begin, int key_end, pair_task_t const *tasks,
                          plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, int ctas, int warps,

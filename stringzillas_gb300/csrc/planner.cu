@@ -134,7 +134,13 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
             info.key = bin_short_begin_k + 3 * short_m_classes_k; // plain form: one bin (128-row segments), input order
             return info;
         }
-        int const shape = n <= 16 ? 0 : (n <= 32 ? 1 : (n <= 64 ? 2 : 3));
+        int const shape = n <= 16   ? 0
+                          : n <= 24 ? 4
+                          : n <= 32 ? 1
+                          : n <= 48 ? 5
+                          : n <= 64 ? 2
+                          : n <= 96 ? 6
+                                    : 3;
         int m_class = m < 512 ? int(m / 16) : 32 + floor_log2_u64(m) - 9;
         m_class = m_class > short_m_classes_k - 1 ? short_m_classes_k - 1 : m_class;
         info.key = bin_short_begin_k + shape * short_m_classes_k + (short_m_classes_k - 1 - m_class);

@@ -20,9 +20,10 @@
  *    [1392, 1424) 16-bit band (one CTA per pair, 16x2 cells): same layout from 1392
  *    [1424, 1488) warp-per-pair Myers (unit Levenshtein, shorter side 513..8,192): key = 1424 + 8 * (8 - W)
  *                 + (7 - text class), W = words per lane = ceil(n / 1024), text class ~ log2(m) - 9
- *    [1488, 1680) short pairs on 16x2 cells (shorter side <= 128): key = 1488 + 48 * shape + (47 - m class),
- *                 shape 0/1/2/3 for n <= 16/32/64/128, m class = m / 16 below 512, then 32 + log2(m) - 9
- *    1680         unit-cost Levenshtein beyond the warp kernel (shorter side 8,193 .. 2^20): a chain of warps per pair
+ *    [1488, 1824) short pairs on 16x2 cells (shorter side <= 128): key = 1488 + 48 * shape + (47 - m class),
+ *                 shape 0/4/1/5/2/6/3 for n <= 16/24/32/48/64/96/128, m class = m / 16 below 512, then
+ *                 32 + log2(m) - 9
+ *    1824         unit-cost Levenshtein beyond the warp kernel (shorter side 8,193 .. 2^20): a chain of warps per pair
  */
 #pragma once
 #include "engine_types.cuh"
@@ -59,11 +60,12 @@ constexpr int bin_myers_warp_begin_k = bin_band16_begin_k + bin_dp_classes_k; //
 static_assert(bin_myers_warp_begin_k + myers_warp_max_words_k * myers_warp_classes_k <= bin_keys_k,
               "bin layout exceeds the key space");
 constexpr int bin_short_begin_k = bin_myers_warp_begin_k + myers_warp_max_words_k * myers_warp_classes_k; // 1488
-constexpr int short_shapes_k = 4;      // segments holding 16, 32, 64 and 128 rows
+constexpr int short_shapes_k = 7;      // segments holding 16, 32, 64, 128, then 24, 48 and 96 rows
 constexpr int short_m_classes_k = 48;  // text-length classes per shape
 constexpr int short_max_rows_k = 128;  // default: shorter sides up to this take the short route
 static_assert(bin_short_begin_k + short_shapes_k * short_m_classes_k <= bin_keys_k, "bin layout exceeds the key space");
-constexpr int bin_myers_chain_k = bin_short_begin_k + short_shapes_k * short_m_classes_k; // 1680
+constexpr int bin_myers_chain_k = bin_short_begin_k + short_shapes_k * short_m_classes_k; // 1824
+static_assert(bin_myers_chain_k < bin_keys_k, "bin layout exceeds the key space");
 constexpr std::uint32_t myers_chain_max_rows_k = 1u << 20; // longest pattern a chain of warps takes
 
 /** Which pairs a call scores. */

@@ -875,13 +875,15 @@ def test_sampled_alphabet_with_other_routes(szs, port):
 @pytest.mark.parametrize("name,family,costs", ENGINES, ids=[e[0] for e in ENGINES])
 def test_short_pairs_every_segment_shape(szs, port, name, family, costs):
     """Shorter sides up to 128 take the segmented short-pair kernel (segments of 16 to 128 rows, two pairs per
-    segment; 8 rows per lane for protein profiles, 16 for DNA): every shape, partners from 1 to 600 characters, odd
-    counts that leave segments and halves empty, both schedules, and the short threshold tuned down."""
+    segment; 8 rows per lane for protein profiles, 16 for DNA, 12 for the 24-, 48- and 96-row shapes): every shape and
+    both sides of each shape's limit, partners from 1 to 600 characters, odd counts that leave segments and halves
+    empty, both schedules, and the short threshold tuned down."""
     rng = np.random.default_rng(zlib_seed(name))
     alphabet = DNA if family != "nw" or name == "nw-positive-gaps" else PROTEIN
     b2c, table = dna_tables() if alphabet is DNA else protein_tables(rng, symmetric=False)
     lengths = [(int(rng.integers(1, 129)), int(rng.integers(1, 300))) for _ in range(333)]
-    lengths += [(n, m) for n in (1, 2, 15, 16, 17, 31, 32, 33, 63, 64, 65, 127, 128) for m in (1, 3, 64, 65, 600)]
+    lengths += [(n, m) for n in (1, 2, 15, 16, 17, 23, 24, 25, 31, 32, 33, 47, 48, 49, 63, 64, 65, 95, 96, 97, 127, 128)
+                for m in (1, 3, 64, 65, 600)]
     first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
     second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
     for k in range(0, len(first), 7):
@@ -894,7 +896,7 @@ def test_short_pairs_every_segment_shape(szs, port, name, family, costs):
         bad = np.flatnonzero(got != want)
         assert bad.size == 0, f"{name} {schedule}: {bad.size} mismatches, first {bad[:5]}: {got[bad[:5]]} vs {want[bad[:5]]}"
     engine.set_schedule("batched")
-    for short_rows in (16, 32, 64):
+    for short_rows in (16, 24, 32, 48, 64, 96):
         engine.set_tuning({"short_max_rows": short_rows})
         np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
     engine.set_tuning(None)
