@@ -86,7 +86,7 @@ WORKLOADS = {
 
 # DRAM bytes per step of the dominant kernels, from one ncu capture of the same command
 # (profiles/myers_table_c2_dram_traffic.txt: dram__bytes_read.sum + dram__bytes_write.sum over one step's launches).
-DRAM_TRAFFIC_PER_STEP = {"c2": 699.0e6 + 0.7e6}
+DRAM_TRAFFIC_PER_STEP = {"c2": 702.2e6 + 1.1e6}
 
 
 def parse_args():
