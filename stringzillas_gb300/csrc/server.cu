@@ -15,9 +15,12 @@
  *    for the merged batch and hands it to the lane. A batch that does not fit waits until a finishing batch returns
  *    its region (admission by HBM budget); a request larger than the whole arena fails alone.
  *  - A lane lays the batch out as one pair of u64 tapes over the region - offsets of all first strings, offsets of
- *    all second strings, results, then the first strings' bytes and the second strings' bytes back to back - copies
- *    it in with one host-to-device copy through pinned staging, scores it with one planned pairwise call on its own
- *    stream and device context, and copies the results out. Lanes run concurrently, so several batches are on the
+ *    all second strings, results, then the first strings' bytes and the second strings' bytes back to back - and
+ *    fills it without staging what needs none: the offsets (rebased onto the region) and the bytes of pageable host
+ *    inputs go through a pinned host image, one copy per run of consecutive pageable requests; the bytes of pinned
+ *    host inputs (Arrow or torch buffers in page-locked memory) are copied straight from the caller's buffers, and
+ *    device or managed inputs device-to-device. It scores the batch with one planned pairwise call on its own stream
+ *    and device context, and copies the results out. Lanes run concurrently, so several batches are on the
  *    device at once and their kernels overlap.
  *
  *  Every pair is scored by the same planned call as a direct `szs_*_pairwise_*` call, and the routes' results do not
@@ -71,11 +74,22 @@ bool device_accessible(void const *pointer) {
     return attributes.type == cudaMemoryTypeDevice || attributes.type == cudaMemoryTypeManaged;
 }
 
+bool pinned_host(void const *pointer) {
+    if (!pointer) return false;
+    cudaPointerAttributes attributes;
+    if (cudaPointerGetAttributes(&attributes, pointer) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attributes.type == cudaMemoryTypeHost;
+}
+
 /** One side of a request: its offsets (copied at submission) and where its bytes live. */
 struct side_t {
     char const *data = nullptr;
     std::vector<std::uint64_t> offsets; // count + 1 entries, as the caller gave them
     bool on_device = false;
+    bool pinned = false; // page-locked host memory: copied into the arena without staging
     std::uint64_t bytes() const { return offsets.back() - offsets.front(); }
 };
 
@@ -310,7 +324,8 @@ sz_status_t server_t::run_batch(lane_t *lane, batch_t &batch) {
     cudaStream_t const stream = exec_context_stream(lane->exec);
     unsigned char *region = arena + batch.region;
 
-    // Host image of the region up to the end of the data: offsets of both sides, then the bytes of host inputs.
+    // Host image of the region up to the end of the data: offsets of both sides, then the bytes of pageable host
+    // inputs (the slots of other inputs stay unused in the image).
     std::size_t const image_bytes = layout.total;
     if (!lane->reserve_staging(image_bytes)) return sz_bad_alloc_k;
     auto *image = static_cast<unsigned char *>(lane->staging);
@@ -324,9 +339,9 @@ sz_status_t server_t::run_batch(lane_t *lane, batch_t &batch) {
             first_offsets[pair] = first_at + (request->first.offsets[i] - first_base);
             second_offsets[pair] = second_at + (request->second.offsets[i] - second_base);
         }
-        if (!request->first.on_device && request->first.bytes())
+        if (!request->first.on_device && !request->first.pinned && request->first.bytes())
             std::memcpy(image + first_at, request->first.data + first_base, request->first.bytes());
-        if (!request->second.on_device && request->second.bytes())
+        if (!request->second.on_device && !request->second.pinned && request->second.bytes())
             std::memcpy(image + second_at, request->second.data + second_base, request->second.bytes());
         first_at += request->first.bytes();
         second_at += request->second.bytes();
@@ -335,29 +350,32 @@ sz_status_t server_t::run_batch(lane_t *lane, batch_t &batch) {
     second_offsets[pair] = second_at;
 
     if (cudaEventRecord(lane->start, stream) != cudaSuccess) return sz_status_unknown_k;
-    // Offsets (results area skipped), then the data sections, host inputs from the image.
+    // Offsets (results area skipped).
     if (cudaMemcpyAsync(region, image, layout.results, cudaMemcpyHostToDevice, stream) != cudaSuccess)
         return sz_status_unknown_k;
-    bool any_device_input = false;
-    for (request_t *request : batch.requests) any_device_input |= request->first.on_device || request->second.on_device;
-    if (image_bytes > layout.first_data &&
-        cudaMemcpyAsync(region + layout.first_data, image + layout.first_data, image_bytes - layout.first_data,
-                        cudaMemcpyHostToDevice, stream) != cudaSuccess)
-        return sz_status_unknown_k;
-    if (any_device_input) {
-        first_at = layout.first_data, second_at = layout.second_data;
+    // The bytes of each side: runs of consecutive pageable requests from the image, the others from their buffers.
+    for (int which = 0; which < 2; ++which) {
+        std::uint64_t at = which ? layout.second_data : layout.first_data, run_begin = at;
+        auto flush = [&](std::uint64_t run_end) -> bool {
+            bool const ok = run_end == run_begin || cudaMemcpyAsync(region + run_begin, image + run_begin,
+                                                                    run_end - run_begin, cudaMemcpyHostToDevice,
+                                                                    stream) == cudaSuccess;
+            return ok;
+        };
         for (request_t *request : batch.requests) {
-            if (request->first.on_device && request->first.bytes() &&
-                cudaMemcpyAsync(region + first_at, request->first.data + request->first.offsets.front(),
-                                request->first.bytes(), cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
-                return sz_status_unknown_k;
-            if (request->second.on_device && request->second.bytes() &&
-                cudaMemcpyAsync(region + second_at, request->second.data + request->second.offsets.front(),
-                                request->second.bytes(), cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
-                return sz_status_unknown_k;
-            first_at += request->first.bytes();
-            second_at += request->second.bytes();
+            side_t const &side = which ? request->second : request->first;
+            std::uint64_t const bytes = side.bytes();
+            if ((side.on_device || side.pinned) && bytes) {
+                if (!flush(at)) return sz_status_unknown_k;
+                if (cudaMemcpyAsync(region + at, side.data + side.offsets.front(), bytes,
+                                    side.on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                    stream) != cudaSuccess)
+                    return sz_status_unknown_k;
+                run_begin = at + bytes;
+            }
+            at += bytes;
         }
+        if (!flush(at)) return sz_status_unknown_k;
     }
 
     sz_sequence_u64tape_t first_tape {reinterpret_cast<sz_cptr_t>(region),
@@ -441,6 +459,7 @@ bool read_side(sz_sequence_u64tape_t const *tape, side_t &side) {
         return false;
     }
     side.on_device = device_accessible(tape->data);
+    side.pinned = !side.on_device && pinned_host(tape->data);
     return true;
 }
 

@@ -162,6 +162,45 @@ def test_device_resident_request(szs, engines):
     np.testing.assert_array_equal(out.cpu().numpy(), engine.pairwise(host_a, host_b))
 
 
+def test_merged_batch_of_pageable_pinned_device_and_managed_inputs(szs, engines, port):
+    """One merged batch whose requests hold their strings in pageable host memory, page-locked host memory (copied
+    into the arena straight from the caller's buffers), device memory and managed memory, on either side and mixed
+    within a request, slices with non-zero first offsets among them: every request equals the oracle."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(31)
+    engine, costs = engines["lev-affine"]
+    alphabet = np.frombuffer(b"ACGT", dtype=np.uint8)
+
+    def strings(count):
+        return [bytes(rng.choice(alphabet, size=int(rng.integers(0, 300)))) for _ in range(count)]
+
+    def placed(items, where):
+        host = szs.Strs(items)
+        data, offsets = host._data.copy(), host._offsets.astype(np.int64)
+        if where == "pageable":
+            return host
+        if where == "pinned":
+            return szs.Strs.from_buffers(torch.from_numpy(data).pin_memory(), torch.from_numpy(offsets).pin_memory())
+        if where == "device":
+            return szs.Strs.from_buffers(torch.from_numpy(data).cuda(), torch.from_numpy(offsets).cuda())
+        return szs.to_device(host)  # managed
+
+    places = ["pageable", "pinned", "device", "managed"]
+    requests = []
+    for k in range(12):
+        count = int(rng.integers(1, 60))
+        first, second = strings(count + 3), strings(count + 3)
+        a, b = placed(first, places[k % 4]), placed(second, places[(k // 4 + k) % 4])
+        requests.append((a[3:], b[3:], first[3:], second[3:]))  # slices: offsets start past zero
+    with szs.Server(lanes=1, max_batch_requests=16) as server:
+        blocker = server.submit(engines["nw"][0], szs.Strs(strings(200)), szs.Strs(strings(200)))
+        tickets = [server.submit(engine, a, b) for a, b, _, _ in requests]  # merged while the blocker runs
+        blocker.result()
+        for ticket, (_, _, first, second) in zip(tickets, requests):
+            np.testing.assert_array_equal(ticket.result(), port.pairs(costs, tape(first), tape(second)))
+    assert max(t.info["batch_requests"] for t in tickets) > 1
+
+
 def test_size_aware_admission_order(szs, engines):
     """With one lane busy, a small request submitted after a large one of another engine runs first under
     size-aware admission, and after it in arrival order; results are the same either way."""
