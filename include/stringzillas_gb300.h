@@ -456,7 +456,8 @@ SZS_GB300_API sz_status_t szs_gb300_device_scope_init_stream(sz_size_t gpu_devic
  */
 typedef struct szs_gb300_tuning_t {
     sz_u8_t packed_rows[16]; /**< rows per lane of the 16x2 route (4, 8, 12 or 16); 0 = per-pair step-cost model */
-    sz_u8_t cell_bits[16];   /**< 0 = the narrowest cells the length bound proves safe; 32 = never 16-bit cells */
+    sz_u8_t cell_bits[16];   /**< 0 = the narrowest cells the length bound proves safe; 32 = never 16-bit cells;
+                                  64 = 64-bit cells (the route of spans near 2^31 / magnitude) */
     sz_u32_t band_min_rows;  /**< pairs on 32-bit cells whose shorter side exceeds this take the band (0 = 1,024) */
     sz_u32_t packed_warps[4]; /**< warps per CTA (1..8) of the 16x2 launches with 4, 8, 12, 16 rows (0 = 4) */
     sz_u32_t band_min_rows_packed; /**< the same threshold for pairs that fit 16-bit cells (0 = 2,048) */

@@ -1749,8 +1749,8 @@ sz_status_t set_tuning(void *engine_handle, szs_gb300_tuning_t const *tuning, ch
         int const rows = tuning->packed_rows[k], bits = tuning->cell_bits[k];
         if (rows != 0 && rows != 4 && rows != 8 && rows != 12 && rows != 16)
             return report({sz_unexpected_dimensions_k, "Rows per lane must be 0, 4, 8, 12 or 16"}, error_message);
-        if (bits != 0 && bits != 32)
-            return report({sz_unexpected_dimensions_k, "Cell bits must be 0 or 32"}, error_message);
+        if (bits != 0 && bits != 32 && bits != 64)
+            return report({sz_unexpected_dimensions_k, "Cell bits must be 0, 32 or 64"}, error_message);
     }
     for (int choice = 0; choice < 4; ++choice)
         if (tuning->packed_warps[choice] > 8)

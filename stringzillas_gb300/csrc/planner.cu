@@ -119,15 +119,18 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
     bool const profile_fits = (args.kind != kind_levenshtein_k && !args.dense) ||
                               (args.alphabet && args.alphabet->symbols <= 32);
     bool const compare_fits = args.kind == kind_levenshtein_k && (args.alphabet != nullptr || args.wide);
+    // A tuned cell width: 32 keeps the class off 16-bit cells, 64 puts it on the 64-bit wavefront (the route the
+    // reach bound takes for spans near 2^31 / magnitude, reachable on any pair this way).
+    bool const force64 = args.cell_bits[length_class] == 64;
     bool const packed = args.packed_allowed && (profile_fits || compare_fits) && reach16 < 32767 &&
-                        args.cell_bits[length_class] != 32;
+                        args.cell_bits[length_class] == 0;
     std::uint64_t const band_rows = !packed        ? args.band_min_rows
                                     : profile_fits ? args.band_min_rows_packed
                                                    : args.band_min_rows_compare;
     // Local scores with non-positive gaps take the 16-bit band even beyond their proven bound: the kernel checks the
     // running maximum against the 16-bit limit and scores a pair that reached it again on 32-bit cells.
     bool const local_band16 =
-        args.local_gain >= 0 && args.packed_allowed && profile_fits && args.cell_bits[length_class] != 32;
+        args.local_gain >= 0 && args.packed_allowed && profile_fits && args.cell_bits[length_class] == 0;
     // Short pairs: a few lanes per pair instead of a warp (dp_short.cuh).
     if (packed && !args.wide && n <= args.short_max_rows) {
         if (args.force_route >= 0) {
@@ -146,7 +149,7 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         info.key = bin_short_begin_k + shape * short_m_classes_k + (short_m_classes_k - 1 - m_class);
         return info;
     }
-    if (n > band_rows && fits32_early) {
+    if (n > band_rows && fits32_early && !force64) {
         // Long pairs take a band in both forms (16-bit cells when they fit); the plain form keeps them in one bin,
         // in input order.
         int const band_begin = (packed || local_band16) ? bin_band16_begin_k : bin_band_begin_k;
@@ -187,7 +190,7 @@ __device__ __forceinline__ pair_route_info_t route_pair(plan_args_t const &args,
         info.key = bin_dp16_begin_k + best_choice * dp16_classes_per_rows_k + 8 * (31 - n_class) + (7 - ratio_class);
         return info;
     }
-    bool const fits32 = reach < (1ull << 31) - 1;
+    bool const fits32 = reach < (1ull << 31) - 1 && !force64;
     int const base = fits32 ? bin_dp32_begin_k : bin_dp64_begin_k;
     if (args.force_route >= 0) {
         info.key = base; // one bin, input order is kept by the caller's launch

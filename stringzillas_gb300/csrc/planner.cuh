@@ -102,7 +102,7 @@ struct plan_args_t {
     batch_alphabet_t const *alphabet; // Levenshtein: the batch alphabet, read on the device (may be null)
     // Tuning by length class k = floor(log2(shorter side)), 15 for everything longer.
     std::uint8_t packed_rows[16];     // 0: per-pair step-cost model; else rows per lane 4, 8, 12, 16
-    std::uint8_t cell_bits[16];       // 0: narrowest safe; 32: never 16-bit cells
+    std::uint8_t cell_bits[16];       // 0: narrowest safe; 32: never 16-bit cells; 64: 64-bit cells
     std::uint32_t band_min_rows;      // shorter sides above this take the band (pairs on 32-bit cells)
     std::uint32_t band_min_rows_packed; // the same for pairs that fit 16-bit cells
     std::uint16_t packed_step_cost[4];  // relative cost of one lane step with 4, 8, 12, 16 rows per lane

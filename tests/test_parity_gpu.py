@@ -70,6 +70,32 @@ def make_engine(szs, family, costs, b2c, table):
     return cls(b2c, table, open=costs[0], extend=costs[1]), oracle.alignment_costs(kind, b2c, table, *costs)
 
 
+@pytest.mark.parametrize("family,costs", [("lev", (0, 2, 3, 1)), ("lev", (0, 3, 2, 2)), ("nw", (-11, -1)),
+                                          ("nw", (-4, -4)), ("sw", (-5, -2)), ("sw", (-3, -3))])
+def test_forced_64bit_cells(szs, port, family, costs):
+    """The 64-bit wavefront is the route the reach bound takes for spans near 2^31 / magnitude (pairs of millions of
+    characters); the tuning forces it onto ordinary pairs: every cost family, empty sides, multi-strip and long pairs
+    (no band: 64-bit pairs stay on the wavefront), cross products, both schedules, all equal to the oracle."""
+    rng = np.random.default_rng(zlib_seed(f"{family}{costs}"))
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = protein_tables(rng) if family == "nw" else dna_tables()
+    lengths = [(int(rng.integers(0, 300)), int(rng.integers(0, 300))) for _ in range(150)]
+    lengths += [(0, 40), (40, 0), (1, 1), (700, 1900), (1500, 3100)]
+    first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+    second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    want = port.pairs(oracle_costs, tape(first), tape(second))
+    engine.set_tuning({"cell_bits": [64] * 16})
+    for schedule in ("batched", "plain"):
+        engine.set_schedule(schedule)
+        np.testing.assert_array_equal(engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64), want)
+    engine.set_schedule("batched")
+    queries, candidates = first[:31], second[:29]
+    np.testing.assert_array_equal(engine(szs.Strs(queries), szs.Strs(candidates)).astype(np.int64),
+                                  port.cross(oracle_costs, tape(queries), tape(candidates)))
+    engine.set_tuning(None)
+
+
 @pytest.mark.parametrize("name,family,costs", ENGINES, ids=[e[0] for e in ENGINES])
 @pytest.mark.parametrize("lengths", [(0, 6), (1, 40), (50, 600), (900, 2100)], ids=["tiny", "short", "strips", "long"])
 def test_pairwise_matches_oracle(szs, port, name, family, costs, lengths):

@@ -150,8 +150,8 @@ def test_tuning_round_trip_and_validation():
               "band_min_rows_compare": 1500, "band_wait_polls": 1000, "short_max_rows": 32}
     engine.set_tuning(tuning)
     assert engine.get_tuning() == tuning
-    for bad in ({"packed_rows": [3] * 16}, {"cell_bits": [16] * 16}, {"packed_warps": [9, 0, 0, 0]},
-                {"packed_rows": [4] * 15}, {"bogus": 1}):
+    for bad in ({"packed_rows": [3] * 16}, {"cell_bits": [16] * 16}, {"cell_bits": [48] * 16},
+                {"packed_warps": [9, 0, 0, 0]}, {"packed_rows": [4] * 15}, {"bogus": 1}):
         with pytest.raises(ValueError):
             engine.set_tuning(bad)
     assert engine.get_tuning() == tuning  # rejected tunings leave the installed one
