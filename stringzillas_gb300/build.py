@@ -31,8 +31,10 @@ UNITS = [
     ("kernels_dp", "kernels_dp.cu", []),
     ("kernels_dp16", "kernels_dp16.cu", []),
     ("kernels_dp16_compare", "kernels_dp16.cu", ["-DSZS_DP16_COMPARE_UNIT"]),
-    ("kernels_band", "kernels_band.cu", []),
-    ("kernels_band16", "kernels_band16.cu", []),
+    ("kernels_band", "kernels_band.cu", ["-DSZS_BAND_ROWS=8"]),
+    ("kernels_band4", "kernels_band.cu", ["-DSZS_BAND_ROWS=4"]),
+    ("kernels_band16", "kernels_band16.cu", ["-DSZS_BAND16_ROWS=8"]),
+    ("kernels_band16_4", "kernels_band16.cu", ["-DSZS_BAND16_ROWS=4"]),
     ("direct", "direct.cu", []),
     ("kernels_short8", "kernels_short.cu", ["-DSZS_SHORT_ROWS=8"]),
     ("kernels_short12", "kernels_short.cu", ["-DSZS_SHORT_ROWS=12"]),

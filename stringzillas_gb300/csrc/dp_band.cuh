@@ -96,14 +96,21 @@ __device__ __forceinline__ band_ring_t band_cta_ring(band_shared_t &shared, int 
     return {shared.progress, &shared.failed, band_warps_k, warp, false, wait_polls};
 }
 
-/** Lane 0 of a warp waits (bounded) until ring slot `slot` has reached `target`; the warp then proceeds together. */
+/** Lane 0 of a warp waits (bounded) until ring slot `slot` has reached `target`; the warp then proceeds together
+ *  (the caller's `__syncwarp` orders the other lanes' ring reads after lane 0's wait). In a group's ring the
+ *  progress word is read with GPU-scope acquire loads, which order the ring-row reads after it without a full fence,
+ *  and the first polls do not sleep: a consumer running just behind its producer resumes within a poll. */
 __device__ __forceinline__ bool band_wait(band_ring_t const &ring, int slot, unsigned long long target) {
     int const lane = threadIdx.x & 31;
     int ok = 1;
     if (lane == 0) {
         std::uint32_t polls = 0;
         while (true) {
-            unsigned long long const seen = *reinterpret_cast<volatile unsigned long long *>(&ring.progress[slot]);
+            unsigned long long seen;
+            if (ring.grid_scope)
+                asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(seen) : "l"(&ring.progress[slot]) : "memory");
+            else
+                seen = *reinterpret_cast<volatile unsigned long long *>(&ring.progress[slot]);
             if (seen >= target) break;
             if (*reinterpret_cast<volatile std::uint32_t *>(ring.failed)) {
                 ok = 0;
@@ -114,24 +121,28 @@ __device__ __forceinline__ bool band_wait(band_ring_t const &ring, int slot, uns
                 ok = 0;
                 break;
             }
-            __nanosleep(100);
+            if (!ring.grid_scope || polls > 16) __nanosleep(ring.grid_scope ? 64 : 100);
         }
-        if (ring.grid_scope) __threadfence();
-        else __threadfence_block();
+        if (!ring.grid_scope) __threadfence_block();
     }
     ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
-    if (ring.grid_scope) __threadfence(); // every lane's ring reads come after the producer's release
     return ok != 0;
 }
 
+/** Publishes `value` in ring slot `slot`. Called by the lane that wrote the published ring row, so a GPU-scope
+ *  release store orders the row before the word in a group's ring. */
 __device__ __forceinline__ void band_publish(band_ring_t const &ring, int slot, unsigned long long value) {
-    if (ring.grid_scope) __threadfence();
-    else __threadfence_block();
-    *reinterpret_cast<volatile unsigned long long *>(&ring.progress[slot]) = value;
+    if (ring.grid_scope) {
+        asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(&ring.progress[slot]), "l"(value) : "memory");
+    }
+    else {
+        __threadfence_block();
+        *reinterpret_cast<volatile unsigned long long *>(&ring.progress[slot]) = value;
+    }
 }
 
 /** Most CTAs one long pair can share, and the ring words of a group. */
-constexpr int band_group_max_ctas_k = 16;
+constexpr int band_group_max_ctas_k = 32;
 constexpr int band_group_max_members_k = band_group_max_ctas_k * band_warps_k;
 
 /** One pass over a pair (16-bit or 32-bit cells): ring progress and the combined result. */

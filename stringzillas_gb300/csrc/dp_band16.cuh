@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
             if (threadIdx.x < band_warps_k) shared.progress[threadIdx.x] = 0ull;
             __syncthreads();
             if (shared.redo) {
-                using wide_t = band_policy_t<policy_::kind_k, policy_::affine_k, 8>;
+                using wide_t = band_policy_t<policy_::kind_k, policy_::affine_k, policy_::rows_per_lane_k>;
                 static_assert(band_profile_bytes_per_warp<wide_t>(32) <= band16_profile_bytes_per_warp<policy_>(32),
                               "the 32-bit profile must fit the 16-bit one's space");
                 static_assert(sizeof(band_chunk_t) <= sizeof(band16_chunk_t), "chunk staging must fit");
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(band_warps_k * 32)
         if constexpr (policy_::local_k) {
             // The group's maximum decides, identically in every CTA, whether 16-bit values may have wrapped.
             if (*reinterpret_cast<volatile std::int32_t *>(&pass->best) >= costs_s.local_limit16) {
-                using wide_t = band_policy_t<policy_::kind_k, policy_::affine_k, 8>;
+                using wide_t = band_policy_t<policy_::kind_k, policy_::affine_k, policy_::rows_per_lane_k>;
                 std::size_t const wide_profile = (std::size_t)band_profile_bytes_per_warp<wide_t>(costs.classes);
                 pass = &state->pass[parity][1];
                 band_ring_t const sync {pass->progress, &state->failed, members, member, true, costs_s.wait_polls};

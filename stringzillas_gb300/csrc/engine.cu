@@ -1023,6 +1023,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         int ctas;
         std::size_t scratch_offset, scratch_bytes;
         int group_ctas = 1;            // band jobs: CTAs sharing one pair (1 = one CTA per pair)
+        int rows = 8;                  // band jobs: rows per lane (4 for groups of CTAs per pair)
         std::size_t state_offset = 0;  // grouped band jobs: the groups' state records in the scratch buffer
         std::size_t state_bytes = 0;
         bool fills = true;             // the grid takes every resident CTA slot of its kernel on the device
@@ -1054,11 +1055,18 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            dp_launch_shape_t const shape =
-                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide);
-            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
+            // Groups of CTAs per pair (a few long pairs) take 4 rows per lane: twice the super-strips, so one pair
+            // spreads over twice the warps, each step about half as long.
+            dp_launch_shape_t shape =
+                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide, 4);
             int ctas = 0, group_ctas = 1;
-            band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            if (shape.ctas_per_sm > 0)
+                band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            if (group_ctas < 2) {
+                shape = band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide, 8);
+                if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
+                band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            }
             // Local scores keep room for a 32-bit ring: a pair that reaches the 16-bit limit is scored again.
             std::size_t const ring_scale = engine.kind == kind_smith_waterman_k ? 2 : 1;
             std::size_t const bytes = align_up(band16_words_per_slot * 4 * ring_scale * (std::size_t)ctas *
@@ -1066,6 +1074,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             job_t job {job_band16_k, 16, 0, bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k, pairs_here,
                        ctas, scratch_total, bytes};
             job.fills = group_ctas > 1 || ctas >= context->sm_count * shape.ctas_per_sm;
+            job.rows = shape.rows_per_lane;
             scratch_total += bytes;
             if (group_ctas > 1) {
                 job.group_ctas = group_ctas, job.state_offset = scratch_total;
@@ -1078,16 +1087,22 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            dp_launch_shape_t const shape =
-                band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide);
-            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
+            dp_launch_shape_t shape =
+                band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide, 4);
             int ctas = 0, group_ctas = 1;
-            band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            if (shape.ctas_per_sm > 0)
+                band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            if (group_ctas < 2) {
+                shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide, 8);
+                if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
+                band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            }
             std::size_t const bytes =
                 align_up(cells_per_warp * 4 * (std::size_t)ctas * (std::size_t)band_warps_per_cta(), 256);
             job_t job {job_band_k, 32, 0, bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k, pairs_here, ctas,
                        scratch_total, bytes};
             job.fills = group_ctas > 1 || ctas >= context->sm_count * shape.ctas_per_sm;
+            job.rows = shape.rows_per_lane;
             scratch_total += bytes;
             if (group_ctas > 1) {
                 job.group_ctas = group_ctas, job.state_offset = scratch_total;
@@ -1234,6 +1249,7 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             key_append(launch_key, jobs[i].key_begin), key_append(launch_key, jobs[i].key_end);
             key_append(launch_key, jobs[i].ctas), key_append(launch_key, jobs[i].scratch_offset);
             key_append(launch_key, jobs[i].group_ctas), key_append(launch_key, jobs[i].state_offset);
+            key_append(launch_key, jobs[i].rows);
         }
         key_append(launch_key, packed_costs), key_append(launch_key, call_costs);
         key_append(launch_key, tasks), key_append(launch_key, bins), key_append(launch_key, results);
@@ -1259,11 +1275,11 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
             if (job.kind == job_band_k)
                 SZS_TRY_CUDA(launch_band(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                          call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,
-                                         group_states, job.group_ctas, wide));
+                                         group_states, job.group_ctas, wide, job.rows));
             else if (job.kind == job_band16_k)
                 SZS_TRY_CUDA(launch_band16(engine.kind, costs.affine != 0, job.key_begin, job.key_end, tasks, bins,
                                            packed_costs, results, scratch, band16_words_per_slot, job.ctas,
-                                           lane_stream, group_states, job.group_ctas, compare_mode, wide));
+                                           lane_stream, group_states, job.group_ctas, compare_mode, wide, job.rows));
             else if (job.kind == job_dp_k)
                 SZS_TRY_CUDA(launch_dp(engine.kind, costs.affine != 0, job.variant, job.key_begin, job.key_end, tasks,
                                        bins, call_costs, results, scratch, cells_per_warp, job.ctas, lane_stream,

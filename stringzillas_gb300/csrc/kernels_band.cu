@@ -1,6 +1,8 @@
 /**
  *  @file kernels_band.cu
- *  @brief Instantiations and launcher of the band kernel (dp_band.cuh).
+ *  @brief Instantiations and launcher of the band kernel (dp_band.cuh). Compiled twice, with `SZS_BAND_ROWS` 8 (one
+ *         CTA per pair, and groups for a few long pairs) or 4 (groups of CTAs per pair: strips of 128 rows, so a
+ *         single long pair spreads over twice the warps, each step half as long).
  */
 #include "dp_band.cuh"
 #include "launchers.h"
@@ -9,7 +11,10 @@ namespace szs_gb300 {
 
 namespace {
 
-constexpr int band_rows_per_lane_k = 8;
+#ifndef SZS_BAND_ROWS
+#error "compile with -DSZS_BAND_ROWS=<8|4>"
+#endif
+constexpr int band_rows_per_lane_k = SZS_BAND_ROWS;
 
 template <int kind_, bool affine_>
 using band_instance_t = band_policy_t<kind_, affine_, band_rows_per_lane_k>;
@@ -78,6 +83,9 @@ cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks,
 
 } // namespace
 
+#define SZS_CONCAT_(a, b) a##b
+#define SZS_CONCAT(a, b) SZS_CONCAT_(a, b)
+
 #define SZS_BAND_DISPATCH(call_, ...)                                                                                \
     switch (kind * 2 + (affine ? 1 : 0)) {                                                                           \
     case 0: return call_<kind_levenshtein_k, false>(__VA_ARGS__);                                                    \
@@ -107,9 +115,7 @@ cudaError_t band_launch_of(int key_begin, int key_end, pair_task_t const *tasks,
     default: break;                                                                                                  \
     }
 
-int band_warps_per_cta() { return band_warps_k; }
-
-dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct, bool wide) {
+dp_launch_shape_t SZS_CONCAT(band_shape_rows, SZS_BAND_ROWS)(int kind, bool affine, int classes, bool direct, bool wide) {
     if (wide) {
         SZS_BAND_WIDE_DISPATCH(band_shape_of, classes)
     }
@@ -122,10 +128,11 @@ dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct, bo
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
-cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
-                        score_costs_t const &costs, std::int64_t *results, void *scratch,
-                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
-                        int group_ctas, bool wide) {
+cudaError_t SZS_CONCAT(launch_band_rows, SZS_BAND_ROWS)(int kind, bool affine, int key_begin, int key_end,
+                                                      pair_task_t const *tasks, plan_bins_t *bins,
+                                                      score_costs_t const &costs, std::int64_t *results, void *scratch,
+                                                      std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream,
+                                                      void *group_states, int group_ctas, bool wide) {
     if (wide) {
         SZS_BAND_WIDE_DISPATCH(band_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
                                ring_cells_per_slot, ctas, stream, group_states, group_ctas)
@@ -141,7 +148,35 @@ cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_
     return cudaErrorInvalidValue;
 }
 
+#if SZS_BAND_ROWS == 8
+
+dp_launch_shape_t band_shape_rows4(int kind, bool affine, int classes, bool direct, bool wide);
+cudaError_t launch_band_rows4(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
+                              plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                              std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
+                              int group_ctas, bool wide);
+
+int band_warps_per_cta() { return band_warps_k; }
+
+dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct, bool wide, int rows_per_lane) {
+    return rows_per_lane == 4 ? band_shape_rows4(kind, affine, classes, direct, wide)
+                              : band_shape_rows8(kind, affine, classes, direct, wide);
+}
+
+cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
+                        score_costs_t const &costs, std::int64_t *results, void *scratch,
+                        std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states,
+                        int group_ctas, bool wide, int rows_per_lane) {
+    if (rows_per_lane == 4)
+        return launch_band_rows4(kind, affine, key_begin, key_end, tasks, bins, costs, results, scratch,
+                                 ring_cells_per_slot, ctas, stream, group_states, group_ctas, wide);
+    return launch_band_rows8(kind, affine, key_begin, key_end, tasks, bins, costs, results, scratch,
+                             ring_cells_per_slot, ctas, stream, group_states, group_ctas, wide);
+}
+
 std::size_t band_group_state_bytes() { return sizeof(band_group_state_t); }
 int band_group_max_ctas() { return band_group_max_ctas_k; }
+
+#endif
 
 } // namespace szs_gb300

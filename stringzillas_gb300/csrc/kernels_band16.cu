@@ -1,6 +1,7 @@
 /**
  *  @file kernels_band16.cu
- *  @brief Instantiations and launcher of the 16-bit band kernel (dp_band16.cuh).
+ *  @brief Instantiations and launcher of the 16-bit band kernel (dp_band16.cuh). Compiled twice, with
+ *         `SZS_BAND16_ROWS` 8 (512-row super-strips) or 4 (256-row super-strips, for groups of CTAs per pair).
  */
 #include "dp_band16.cuh"
 #include "launchers.h"
@@ -9,7 +10,10 @@ namespace szs_gb300 {
 
 namespace {
 
-constexpr int band16_rows_per_lane_k = 8;
+#ifndef SZS_BAND16_ROWS
+#error "compile with -DSZS_BAND16_ROWS=<8|4>"
+#endif
+constexpr int band16_rows_per_lane_k = SZS_BAND16_ROWS;
 
 template <int kind_, bool affine_, int compare_ = compare_none_k, bool wide_ = false>
 using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_, wide_>;
@@ -70,6 +74,9 @@ cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *task
 
 } // namespace
 
+#define SZS_CONCAT_(a, b) a##b
+#define SZS_CONCAT(a, b) SZS_CONCAT_(a, b)
+
 #define SZS_BAND16_DISPATCH(call_, ...)                                                                              \
     switch (kind * 2 + (affine ? 1 : 0)) {                                                                           \
     case 0: return call_<kind_levenshtein_k, false>(__VA_ARGS__);                                                    \
@@ -94,7 +101,8 @@ cudaError_t band16_launch_of(int key_begin, int key_end, pair_task_t const *task
     default: return call_<kind_levenshtein_k, true, compare_multiply_k, true>(__VA_ARGS__);                          \
     }
 
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare, bool wide) {
+dp_launch_shape_t SZS_CONCAT(band16_shape_rows, SZS_BAND16_ROWS)(int kind, bool affine, int classes, int compare,
+                                                                 bool wide) {
     if (compare != compare_none_k || wide) {
         if (kind != kind_levenshtein_k || compare == compare_none_k) return dp_launch_shape_t {0, 0, 0, 0, 0};
         SZS_BAND16_COMPARE_DISPATCH(band16_shape_of, classes)
@@ -103,10 +111,12 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare, 
     return dp_launch_shape_t {0, 0, 0, 0, 0};
 }
 
-cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
-                          plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
-                          std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
-                          int group_ctas, int compare, bool wide) {
+cudaError_t SZS_CONCAT(launch_band16_rows, SZS_BAND16_ROWS)(int kind, bool affine, int key_begin, int key_end,
+                                                          pair_task_t const *tasks, plan_bins_t *bins,
+                                                          score_costs_t const &costs, std::int64_t *results,
+                                                          void *scratch, std::size_t ring_words_per_slot, int ctas,
+                                                          cudaStream_t stream, void *group_states, int group_ctas,
+                                                          int compare, bool wide) {
     if (compare != compare_none_k || wide) {
         if (kind != kind_levenshtein_k || compare == compare_none_k) return cudaErrorInvalidValue;
         SZS_BAND16_COMPARE_DISPATCH(band16_launch_of, key_begin, key_end, tasks, bins, costs, results, scratch,
@@ -116,5 +126,31 @@ cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pai
                         ring_words_per_slot, ctas, stream, group_states, group_ctas)
     return cudaErrorInvalidValue;
 }
+
+#if SZS_BAND16_ROWS == 8
+
+dp_launch_shape_t band16_shape_rows4(int kind, bool affine, int classes, int compare, bool wide);
+cudaError_t launch_band16_rows4(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
+                                plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                                std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
+                                int group_ctas, int compare, bool wide);
+
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare, bool wide, int rows_per_lane) {
+    return rows_per_lane == 4 ? band16_shape_rows4(kind, affine, classes, compare, wide)
+                              : band16_shape_rows8(kind, affine, classes, compare, wide);
+}
+
+cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
+                          plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
+                          std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states,
+                          int group_ctas, int compare, bool wide, int rows_per_lane) {
+    if (rows_per_lane == 4)
+        return launch_band16_rows4(kind, affine, key_begin, key_end, tasks, bins, costs, results, scratch,
+                                   ring_words_per_slot, ctas, stream, group_states, group_ctas, compare, wide);
+    return launch_band16_rows8(kind, affine, key_begin, key_end, tasks, bins, costs, results, scratch,
+                               ring_words_per_slot, ctas, stream, group_states, group_ctas, compare, wide);
+}
+
+#endif
 
 } // namespace szs_gb300

@@ -113,8 +113,9 @@ cudaError_t launch_dp16_compare(bool affine, int rows, int key_begin, int key_en
                                 int compare, bool wide);
 
 /** Launch shape of the band kernel (one CTA of several warps per long pair, 32-bit cells); `direct`: the
- *  direct-table instance. */
-dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct = false, bool wide = false);
+ *  direct-table instance; `rows_per_lane` 8 (strips of 256 rows) or 4 (128 rows: for groups of CTAs per pair). */
+dp_launch_shape_t band_shape(int kind, bool affine, int classes, bool direct = false, bool wide = false,
+                             int rows_per_lane = 8);
 /** Warps per band CTA (ring slots per CTA). */
 int band_warps_per_cta();
 
@@ -125,15 +126,17 @@ int band_warps_per_cta();
 cudaError_t launch_band(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                         score_costs_t const &costs, std::int64_t *results, void *scratch,
                         std::size_t ring_cells_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
-                        int group_ctas = 1, bool wide = false); // costs with a `direct_table` run the
-                                                                 // direct-table instance; `wide`: 16-bit codes
+                        int group_ctas = 1, bool wide = false, // costs with a `direct_table` run the direct-table
+                        int rows_per_lane = 8);                // instance; `wide`: 16-bit codes
 /** Bytes of one group's state record, and the most CTAs a group may have. */
 std::size_t band_group_state_bytes();
 int band_group_max_ctas();
 
 /** Launch shape of the 16-bit band kernel (one CTA per long pair, two row strips per warp in 16x2 cells);
- *  `compare` (a `compare_mode_t`): the Levenshtein instances that compare codes instead of reading a profile. */
-dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare = 0, bool wide = false);
+ *  `compare` (a `compare_mode_t`): the Levenshtein instances that compare codes instead of reading a profile;
+ *  `rows_per_lane` 8 (512-row super-strips) or 4 (256 rows: for groups of CTAs per pair). */
+dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare = 0, bool wide = false,
+                               int rows_per_lane = 8);
 
 /** Runs the 16-bit band kernel over bins [key_begin, key_end). `scratch` holds `ctas * band_warps_per_cta()` ring
  *  slots of `ring_words_per_slot` 32-bit words (twice that for local scores, which may rescore a pair on 32-bit
@@ -141,7 +144,7 @@ dp_launch_shape_t band16_shape(int kind, bool affine, int classes, int compare =
 cudaError_t launch_band16(int kind, bool affine, int key_begin, int key_end, pair_task_t const *tasks,
                           plan_bins_t *bins, score_costs_t const &costs, std::int64_t *results, void *scratch,
                           std::size_t ring_words_per_slot, int ctas, cudaStream_t stream, void *group_states = nullptr,
-                          int group_ctas = 1, int compare = 0, bool wide = false);
+                          int group_ctas = 1, int compare = 0, bool wide = false, int rows_per_lane = 8);
 
 /** Short pairs (shorter side at most 128) on the segmented 16x2 kernel: `shape` 0-6 for shorter sides up to 16, 32,
  *  64, 128, 24, 48, 96 (`short_segment_rows`); shapes 4-6 have 12 rows per lane, shapes 0-3 16 when compare mode or

@@ -399,7 +399,7 @@ def test_band_route_long_pairs(szs, port, family, costs):
 @pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 1, 1, 1)),
                                           ("lev", (0, 2, 3, 1)), ("sw", (-3, -3))])
 def test_grouped_band_few_long_pairs(szs, port, family, costs):
-    """One or a few long pairs: each gets a group of up to 16 CTAs (one cooperative launch) whose warps share the
+    """One or a few long pairs: each gets a group of up to 32 CTAs (one cooperative launch) whose warps share the
     strip ring through global memory. Pairs with fewer strips than the group has warps leave warps idle."""
     rng = np.random.default_rng(31)
     alphabet = PROTEIN if family == "nw" else DNA
