@@ -1055,17 +1055,21 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
     {
         std::uint64_t const pairs_here = pairs_in(bin_band16_begin_k, bin_band16_begin_k + bin_dp_classes_k);
         if (pairs_here) {
-            // Groups of CTAs per pair (a few long pairs) take 4 rows per lane: twice the super-strips, so one pair
-            // spreads over twice the warps, each step about half as long.
             dp_launch_shape_t shape =
-                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide, 4);
+                band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide, 8);
+            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
-            if (shape.ctas_per_sm > 0)
-                band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
-            if (group_ctas < 2) {
-                shape = band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide, 8);
-                if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "16-bit band kernel cannot be resident"};
-                band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            band_groups(pairs_here, shape, 2u * 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            // Groups limited by their pairs' super-strips while the GPU has CTA slots to spare (a handful of long
+            // pairs) take 4 rows per lane: twice the super-strips, so a pair spreads over twice the warps, each step
+            // about half as long. Groups that fill the GPU keep 8 rows, which do more cells per step's overhead.
+            if (group_ctas > 1 && ctas * 2 <= context->sm_count * shape.group_ctas_per_sm) {
+                dp_launch_shape_t const narrow =
+                    band16_shape(engine.kind, costs.affine != 0, packed_costs.classes, compare_mode, wide, 4);
+                int narrow_ctas = 0, narrow_group = 1;
+                if (narrow.ctas_per_sm > 0)
+                    band_groups(pairs_here, narrow, 2u * 32u * 4u, narrow_ctas, narrow_group);
+                if (narrow_group > group_ctas) shape = narrow, ctas = narrow_ctas, group_ctas = narrow_group;
             }
             // Local scores keep room for a 32-bit ring: a pair that reaches the 16-bit limit is scored again.
             std::size_t const ring_scale = engine.kind == kind_smith_waterman_k ? 2 : 1;
@@ -1088,14 +1092,17 @@ static status_t run_on(engine_t const &engine, device_context_t *context, cudaSt
         std::uint64_t const pairs_here = pairs_in(bin_band_begin_k, bin_band_begin_k + bin_dp_classes_k);
         if (pairs_here) {
             dp_launch_shape_t shape =
-                band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide, 4);
+                band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide, 8);
+            if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
             int ctas = 0, group_ctas = 1;
-            if (shape.ctas_per_sm > 0)
-                band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
-            if (group_ctas < 2) {
-                shape = band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide, 8);
-                if (shape.ctas_per_sm <= 0) return {sz_status_unknown_k, "Band kernel cannot be resident"};
-                band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            band_groups(pairs_here, shape, 32u * (std::uint64_t)shape.rows_per_lane, ctas, group_ctas);
+            // As for the 16-bit band: 4 rows per lane only while the groups leave half the GPU's CTA slots free.
+            if (group_ctas > 1 && ctas * 2 <= context->sm_count * shape.group_ctas_per_sm) {
+                dp_launch_shape_t const narrow =
+                    band_shape(engine.kind, call_costs.affine != 0, call_costs.classes, direct, wide, 4);
+                int narrow_ctas = 0, narrow_group = 1;
+                if (narrow.ctas_per_sm > 0) band_groups(pairs_here, narrow, 32u * 4u, narrow_ctas, narrow_group);
+                if (narrow_group > group_ctas) shape = narrow, ctas = narrow_ctas, group_ctas = narrow_group;
             }
             std::size_t const bytes =
                 align_up(cells_per_warp * 4 * (std::size_t)ctas * (std::size_t)band_warps_per_cta(), 256);
