@@ -75,6 +75,9 @@ WORKLOADS = {
              "(16-bit codes; 16x2 wavefront in compare mode)",
     "p_long_lev": "profiling case, unit-cost Levenshtein on long DNA reads: 16,384 pairs, len U[1,000, 4,000], partner 3% "
                   "subs + 1% indels (warp-per-pair bit-parallel kernel)",
+    "p_dense": "profiling case, Needleman-Wunsch affine over a dense 256 x 256 table: 131,072 pairs, len U[100,300] over all "
+               "256 byte values, partner 10% subs + 2% indels, seeded table (diagonal 4..11, elsewhere -9..3), open -11 "
+               "extend -1 (32-bit wavefront reading the whole table from shared memory)",
     "short_nw": "short pairs, Needleman-Wunsch affine protein: 1,048,576 pairs, len U[16, 128], 70% identity, the protein "
                 "configuration's table, open -11 extend -1 (segmented short-pair kernel)",
     "short_sw": "short pairs, Smith-Waterman affine DNA: 1,048,576 pairs, len U[16, 128], partner 10% subs + 2% indels, "
@@ -152,6 +155,9 @@ def make_workload(name, seed):
     if name == "short_lev":
         first, second = w.short_pairs(1 << 20, 16, 128, "dna", 0.05, 0.02, seed=seed)
         return first, second, ("levp", (0, 2, 3, 1))
+    if name == "p_dense":
+        first, second = w.byte_pairs(131072, 100, 300, 0.10, 0.02, seed=seed)
+        return first, second, ("nwd", (w.dense_table(seed=seed), -11, -1))
     if name == "p_dp32":
         first, second = w.protein_pairs(65536, seed=seed)
         byte_to_class, table = w.protein_table(seed=seed)
@@ -178,6 +184,8 @@ def make_engine(kind_and_tables):
         engine = szs.NeedlemanWunschScores(*tables, open=-11, extend=-1)
     elif kind == "nw32":  # profiling cases of the 32-bit routes: (byte_to_class, table, open, extend)
         engine = szs.NeedlemanWunschScores(*tables[:2], open=tables[2], extend=tables[3])
+    elif kind == "nwd":  # a dense 256 x 256 table: (table, open, extend)
+        engine = szs.NeedlemanWunschScores.dense(tables[0], open=tables[1], extend=tables[2])
     else:
         engine = szs.SmithWatermanScores(*tables, open=-5, extend=-2)
     autotune.apply(engine)
@@ -214,6 +222,8 @@ def oracle_costs(kind_and_tables):
         return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables, -11, -1)
     if kind == "nw32":
         return oracle.alignment_costs(oracle.NEEDLEMAN_WUNSCH, *tables)
+    if kind == "nwd":
+        return oracle.dense_costs(oracle.NEEDLEMAN_WUNSCH, *tables)
     return oracle.alignment_costs(oracle.SMITH_WATERMAN, *tables, -5, -2)
 
 
@@ -221,7 +231,7 @@ def ops_per_cell(kind_and_tables):
     kind = kind_and_tables[0]
     if kind == "lev":
         return OPS_PER_CELL["myers_dna_table"]
-    if kind == "nw32":
+    if kind in ("nw32", "nwd"):
         return OPS_PER_CELL["dp_affine"]
     if kind in ("levc", "levu"):
         return OPS_PER_CELL["packed_compare_affine"]
@@ -823,7 +833,7 @@ def run_ours(args):
         int_ops = cells_per_step * ops_per_cell(kind_and_tables)
         int_peak = None
         if peaks:
-            int_peak = {"lev": peaks["lop3"], "nw32": peaks["dpx_viaddmax_s32"]}.get(
+            int_peak = {"lev": peaks["lop3"], "nw32": peaks["dpx_viaddmax_s32"], "nwd": peaks["dpx_viaddmax_s32"]}.get(
                 kind_and_tables[0], peaks["dpx_viaddmax_s16x2"])
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,

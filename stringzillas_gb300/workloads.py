@@ -92,6 +92,25 @@ def text_pairs(count, low, high, substitution_rate, indel_rate, seed=42):
     return (first, offsets), (second, second_offsets)
 
 
+def byte_pairs(count, low, high, substitution_rate, indel_rate, seed=42):
+    """Pairs over all 256 byte values (uniform), for dense 256 x 256 substitution tables."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = rng.integers(low, high + 1, size=count)
+    offsets = _offsets(lengths)
+    every = np.arange(256, dtype=np.uint8)
+    first = _letters(rng, every, int(offsets[-1]))
+    second, second_offsets = _mutate(rng, first, offsets, every, substitution_rate, indel_rate)
+    return (first, offsets), (second, second_offsets)
+
+
+def dense_table(seed=42):
+    """A seeded asymmetric 256 x 256 int8 table: diagonal 4..11, elsewhere -9..3."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    table = rng.integers(-9, 4, size=(256, 256)).astype(np.int8)
+    np.fill_diagonal(table, rng.integers(4, 12, size=256).astype(np.int8))
+    return table
+
+
 CJK_FIRST, CJK_COUNT = 0x4E00, 3000  # the first 3,000 CJK unified ideographs: three UTF-8 bytes each
 
 
