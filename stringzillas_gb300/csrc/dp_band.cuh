@@ -244,6 +244,11 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
             std::int64_t const i = row0 + r;
             row_bytes[r] = i <= (std::int64_t)n ? symbol_at<policy_::wide_k>(task.rows, i - 1) : 0u;
         }
+        // Dense tables: each row's part of the table index, oriented once per strip.
+        if constexpr (policy_::direct_k) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) row_bytes[r] = task.transposed ? row_bytes[r] : row_bytes[r] << 8;
+        }
         __syncwarp();
         if constexpr (!policy_::uniform_k && !policy_::direct_k) {
 #pragma unroll
@@ -320,9 +325,9 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                 }
                 else if constexpr (policy_::direct_k) {
                     // table[first byte][second byte]: rows are the first string unless the pair was transposed.
+                    std::uint32_t const column_key = task.transposed ? code_now << 8 : code_now;
 #pragma unroll
-                    for (int r = 0; r < R; ++r)
-                        subs[r] = table_s[task.transposed ? (code_now << 8) | row_bytes[r] : (row_bytes[r] << 8) | code_now];
+                    for (int r = 0; r < R; ++r) subs[r] = table_s[row_bytes[r] | column_key];
                 }
                 else {
 #pragma unroll

@@ -123,6 +123,12 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
             std::int64_t const i = row0 + r;
             row_bytes[r] = i <= (std::int64_t)n ? symbol_at<policy_::wide_k>(task.rows, i - 1) : 0u;
         }
+        // Dense tables: each row's part of the table index, oriented once per strip (the column's part is one shift
+        // per step), so a cell's gather address is one OR.
+        if constexpr (policy_::direct_k) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) row_bytes[r] = task.transposed ? row_bytes[r] : row_bytes[r] << 8;
+        }
         if constexpr (!policy_::uniform_k && !policy_::direct_k) {
             // profile[cc * S + row_in_strip] = cost(row class, column class cc), oriented by `transposed`.
             __syncwarp();
@@ -204,10 +210,9 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
                 }
                 else if constexpr (policy_::direct_k) {
                     // table[first byte][second byte]: rows are the first string unless the pair was transposed.
+                    std::uint32_t const column_key = task.transposed ? (std::uint32_t)code << 8 : (std::uint32_t)code;
 #pragma unroll
-                    for (int r = 0; r < R; ++r)
-                        subs[r] = (cell_t)table_s[task.transposed ? (code << 8) | (int)row_bytes[r]
-                                                                  : ((int)row_bytes[r] << 8) | code];
+                    for (int r = 0; r < R; ++r) subs[r] = (cell_t)table_s[row_bytes[r] | column_key];
                 }
                 else {
                     static_assert(R % 8 == 0, "profile loads are 8 bytes wide");
