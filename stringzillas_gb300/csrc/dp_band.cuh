@@ -331,9 +331,11 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                 }
                 else {
 #pragma unroll
-                    for (int w = 0; w < words; ++w)
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) subs[4 * w + b] = (std::int32_t)(std::int8_t)(p_now[w] >> (8 * b));
+                    for (int w = 0; w < words; ++w) {
+                        // One byte permute per cost (the byte, its sign bit copied above it).
+                        subs[4 * w + 0] = signed_byte<0>(p_now[w]), subs[4 * w + 1] = signed_byte<1>(p_now[w]);
+                        subs[4 * w + 2] = signed_byte<2>(p_now[w]), subs[4 * w + 3] = signed_byte<3>(p_now[w]);
+                    }
                 }
 #pragma unroll
                 for (int r = 0; r < R; ++r) {

@@ -19,6 +19,17 @@
 
 namespace szs_gb300 {
 
+/** Byte `b_` of `x` as a signed 32-bit value: one byte permute whose selector copies the byte's sign bit into the
+ *  three bytes above it. */
+template <int b_>
+__device__ __forceinline__ std::int32_t signed_byte(std::uint32_t x) {
+    constexpr std::uint32_t sign = std::uint32_t(8 + b_);
+    constexpr std::uint32_t selector = std::uint32_t(b_) | (sign << 4) | (sign << 8) | (sign << 12);
+    std::uint32_t r;
+    asm("prmt.b32 %0, %1, %1, %2;" : "=r"(r) : "r"(x), "r"(selector));
+    return (std::int32_t)r;
+}
+
 template <typename cell_t, bool maximize_>
 struct cell_ops_t;
 

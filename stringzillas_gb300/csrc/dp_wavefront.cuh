@@ -219,11 +219,11 @@ __device__ __forceinline__ std::int64_t dp_score_pair_warp(pair_task_t const &ta
 #pragma unroll
                     for (int r8 = 0; r8 < R; r8 += 8) {
                         uint2 const packed = *reinterpret_cast<uint2 const *>(profile + code * S + lane * R + r8);
-#pragma unroll
-                        for (int b = 0; b < 8; ++b) {
-                            std::uint32_t const word = b < 4 ? packed.x : packed.y;
-                            subs[r8 + b] = (cell_t)(std::int8_t)((word >> (8 * (b & 3))) & 0xFF);
-                        }
+                        // One byte permute per cost (the byte, its sign bit copied above it).
+                        subs[r8 + 0] = (cell_t)signed_byte<0>(packed.x), subs[r8 + 1] = (cell_t)signed_byte<1>(packed.x);
+                        subs[r8 + 2] = (cell_t)signed_byte<2>(packed.x), subs[r8 + 3] = (cell_t)signed_byte<3>(packed.x);
+                        subs[r8 + 4] = (cell_t)signed_byte<0>(packed.y), subs[r8 + 5] = (cell_t)signed_byte<1>(packed.y);
+                        subs[r8 + 6] = (cell_t)signed_byte<2>(packed.y), subs[r8 + 7] = (cell_t)signed_byte<3>(packed.y);
                     }
                 }
 #pragma unroll
