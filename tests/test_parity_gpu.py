@@ -522,18 +522,22 @@ def test_any_tuning_keeps_scores(szs, port, tuning, family, costs):
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
-@pytest.mark.parametrize("family", ["lev", "sw"])
-def test_pipelined_pinned_host_call(szs, port, family):
+@pytest.mark.parametrize("family,costs", [("lev", (0, 1, 1, 1)), ("sw", (-5, -2)), ("lev", (0, 2, 3, 1))],
+                         ids=["lev-unit", "sw", "lev-affine"])
+def test_pipelined_pinned_host_call(szs, port, family, costs):
     """Pairwise calls on large pinned host tapes are cut into chunks whose copies overlap the previous chunk's
-    scoring; the chunked call must equal the oracle and the device-resident call."""
+    scoring (planned ahead from a sample of the first chunk for unit costs, from the offsets alone for alignment
+    engines, after each chunk's bytes for the other Levenshtein costs); the chunked call must equal the oracle and
+    the device-resident call."""
     torch = pytest.importorskip("torch")
     from stringzillas_gb300 import workloads as w
-    count = 420_000 if family == "lev" else 700_000
-    (fd, fo), (sd, so) = w.levenshtein_reads(count, 100, 300, 0.05, 0.02, seed=3) if family == "lev" else \
+    unit = costs == (0, 1, 1, 1)
+    count = 420_000 if unit else 700_000
+    (fd, fo), (sd, so) = w.levenshtein_reads(count, 100, 300, 0.05, 0.02, seed=3) if unit else \
         w.levenshtein_reads(count, 60, 100, 0.10, 0.02, seed=4)
     assert fd.nbytes + sd.nbytes > 2 * (48 << 20), "the call must span several chunks"
     b2c, table = dna_tables()
-    engine, oracle_costs = make_engine(szs, family, (0, 1, 1, 1) if family == "lev" else (-5, -2), b2c, table)
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
     pinned = [torch.from_numpy(x).pin_memory() for x in (fd, fo.astype(np.uint64).view(np.int64),
                                                           sd, so.astype(np.uint64).view(np.int64))]
     first = szs.Strs.from_buffers(pinned[0], pinned[1])
