@@ -572,8 +572,8 @@ def test_pipelined_chunks_planned_from_a_sample(szs, port):
     second[190_000] = bytes(rng.choice(DNA, size=1700))
     (fd, fo), (sd, so) = tape(first), tape(second)
     engine = szs.LevenshteinDistances()
-    pinned = [torch.from_numpy(x).pin_memory() for x in (fd, fo.astype(np.uint64).view(np.int64),
-                                                          sd, so.astype(np.uint64).view(np.int64))]
+    pinned = [torch.from_numpy(np.array(x)).pin_memory() for x in (fd, fo.astype(np.uint64).view(np.int64),
+                                                                    sd, so.astype(np.uint64).view(np.int64))]
     a = szs.Strs.from_buffers(pinned[0], pinned[1])
     b = szs.Strs.from_buffers(pinned[2], pinned[3])
     want = port.pairs(oracle.levenshtein_costs(), (fd, fo), (sd, so))
