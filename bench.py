@@ -91,6 +91,12 @@ WORKLOADS = {
 # (profiles/myers_table_c2_dram_traffic.txt: dram__bytes_read.sum + dram__bytes_write.sum over one step's launches).
 DRAM_TRAFFIC_PER_STEP = {"c2": 702.2e6 + 1.1e6}
 
+# What ncu shows about the dominant kernel's integer pipe, beside the algorithmic fraction above
+# (profiles/myers_table_c2_batched_levenshtein.txt).
+PIPE_EVIDENCE = {"c2": "ncu, shared-table bit-parallel kernel (W = 8 and 7): ALU pipe 84 % busy, 12.4 ALU instructions "
+                       "executed per pattern word and text column against the step's 10 (byte extraction, table "
+                       "address, alphabet check, pattern setup)"}
+
 
 def parse_args():
     parser = argparse.ArgumentParser()
@@ -851,7 +857,8 @@ def run_ours(args):
                              "peak": None if int_peak is None else int_peak / 1e12, "unit": "Tops/s",
                              "frac": None if int_peak is None else int_ops / step_compute_s / int_peak,
                              "ops_per_cell": ops_per_cell(kind_and_tables), "measured_peaks_tops":
-                                 None if peaks is None else {k: v / 1e12 for k, v in peaks.items()}},
+                                 None if peaks is None else {k: v / 1e12 for k, v in peaks.items()},
+                             "pipe_evidence": PIPE_EVIDENCE.get(args.workload)},
             "plain": {"value": plain_cells / (plain_ms * 1e-3) / 1e9, "unit": "GCUPS",
                       "ms_per_step": plain_ms / plain_steps, "compute_ms_per_step": plain_compute_ms / plain_steps},
             "batched_over_plain": value / (plain_cells / (plain_ms * 1e-3) / 1e9 * world),
