@@ -341,13 +341,26 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
                 for (int r = 0; r < R; ++r) {
                     std::int32_t const substitution = diag + subs[r];
                     std::int32_t h;
-                    if constexpr (affine) {
+                    if constexpr (affine && R == 4) {
+                        // Groups of CTAs per pair (4 rows per lane) are bound by each warp's step latency: the row
+                        // chain here is two fused add-max deep, at five of them per cell.
                         std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
                         std::int32_t const x = ops::add_opt(e_new, open, substitution);
                         std::int32_t const via_f = ops::add_opt(f_up, extend_open, x);
                         if constexpr (local) h = ops::add_opt_relu(h_up, open, via_f);
                         else h = ops::add_opt(h_up, open, via_f);
                         f_up = ops::add_opt(f_up, extend, h_up);
+                        e_col[r] = e_new;
+                    }
+                    else if constexpr (affine) {
+                        // CTAs per pair (8 rows per lane) fill the GPU and are bound by the integer ALU pipe: three
+                        // fused operations per cell, the adds of the gap opening and the substitution left to the
+                        // multiply-add pipe. e_col and f_up hold E and F minus the opening cost.
+                        std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
+                        std::int32_t const f_new = ops::add_opt(f_up, extend, h_up);
+                        if constexpr (local) h = ops::opt3_relu(substitution, e_new + open, f_new + open);
+                        else h = ops::opt3(substitution, e_new + open, f_new + open);
+                        f_up = f_new;
                         e_col[r] = e_new;
                     }
                     else {
