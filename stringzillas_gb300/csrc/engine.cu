@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1506,6 +1507,10 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
     auto *area = static_cast<unsigned char *>(context->chunk_inputs.data);
 
     SZS_TRY_CUDA(cudaEventRecord(context->pipe_start, stream));
+    auto const host_zero = std::chrono::steady_clock::now();
+    auto host_ms = [&] {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_zero).count();
+    };
     // Earlier work on the call's stream may still read the slots: the copies wait for it.
     SZS_TRY_CUDA(cudaStreamWaitEvent(context->copy_stream, context->pipe_start, 0));
     for (int t = 0; t < 2; ++t)
@@ -1528,6 +1533,8 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
         }
         SZS_TRY_CUDA(cudaEventRecord(context->copied[c], context->copy_stream));
     }
+    double const copies_queued_ms = host_ms();
+    std::vector<double> host_marks(3 * chunks, 0.0); // per chunk: plan queued from, plan read back at, scoring queued at
     int const depth = std::min(chunks, device_context_t::pipeline_depth_k);
     device_context_t *contexts[device_context_t::pipeline_depth_k] = {nullptr};
     cudaStream_t streams[device_context_t::pipeline_depth_k] = {nullptr};
@@ -1613,6 +1620,7 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
         int const which = c % depth;
         status_t settled = settle(which);
         if (!settled.ok()) return settled;
+        host_marks[3 * c] = host_ms();
         call_t &chunk = chunk_calls[which];
         chunk = call;
         chunk.pre_staged = true;
@@ -1627,6 +1635,7 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
         chunk_stats[which].graph_replays = 0;
         status_t const planned = run_on(engine, contexts[which], streams[which], chunk, schedule, chunk_stats[which]);
         launches += chunk_stats[which].last_launches;
+        host_marks[3 * c + 1] = host_ms();
         return planned;
     };
     auto launch = [&](int c) -> status_t { // queues the scoring of chunk c's plan, without waiting for it
@@ -1637,6 +1646,7 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
         if (!queued.ok()) return queued;
         in_flight[which] = c;
         cells += chunk_stats[which].last_cells, graph_replays += chunk_stats[which].graph_replays;
+        host_marks[3 * c + 2] = host_ms();
         return {};
     };
     int const window = plan_ahead ? depth : 1;
@@ -1664,6 +1674,12 @@ static status_t run_pipelined(engine_t const &engine, device_context_t *context,
     SZS_TRY_CUDA(cudaEventSynchronize(context->pipe_stop));
     float elapsed = 0;
     cudaEventElapsedTime(&elapsed, context->pipe_start, context->pipe_stop);
+    if (tracing) { // the host's side of the timeline, in ms from the call's start
+        std::fprintf(stderr, "[szs_gb300] host: copies queued %8.3f, call returns %8.3f\n", copies_queued_ms, host_ms());
+        for (int c = 0; c < chunks; ++c)
+            std::fprintf(stderr, "[szs_gb300] host: chunk %3d  plan queued %8.3f  read back %8.3f  scoring queued %8.3f\n",
+                         c, host_marks[3 * c], host_marks[3 * c + 1], host_marks[3 * c + 2]);
+    }
     stats.last_pairs = pairs, stats.last_cells = cells, stats.last_launches = launches;
     stats.last_call_ms = elapsed, stats.last_compute_ms = compute_ms;
     stats.kernel_launches += launches, stats.graph_replays += graph_replays;
