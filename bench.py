@@ -611,8 +611,9 @@ def cross_product_leg(szs, torch, scope, steps=10, warmup=3):
 
 
 def long_pairs_leg(szs, torch, scope, steps=3, warmup=1):
-    """Single very long pairs, one call each, device-resident: unit-cost Levenshtein at 50,000 and 100,000
-    characters a side (a 3% substitution + 1% indel mutant), Smith-Waterman affine DNA (+2/-3, -5/-2) and
+    """Single very long pairs, one call each, device-resident: unit-cost Levenshtein at 50,000, 100,000 and 200,000
+    characters a side and linear-gap Levenshtein (0, 2, 3, 3) at 50,000 and 100,000 (a 3% substitution + 1% indel
+    mutant), Smith-Waterman affine DNA (+2/-3, -5/-2) and
     Needleman-Wunsch affine protein (-11/-1) at 30,000 with a planted shared segment. GCUPS from CUDA events."""
     from stringzillas_gb300 import workloads as w
     stream = torch.cuda.current_stream()
@@ -640,6 +641,7 @@ def long_pairs_leg(szs, torch, scope, steps=3, warmup=1):
              ("levenshtein_100k", szs.LevenshteinDistances(), pair(dna, 100000)),
              ("levenshtein_200k", szs.LevenshteinDistances(), pair(dna, 200000)),
              ("levenshtein_linear_50k", szs.LevenshteinDistances(0, 2, 3, 3), pair(dna, 50000)),
+             ("levenshtein_linear_100k", szs.LevenshteinDistances(0, 2, 3, 3), pair(dna, 100000)),
              ("smith_waterman_30k", szs.SmithWatermanScores(*w.dna_table(2, -3), open=-5, extend=-2),
               pair(dna, 30000, mutate=False)),
              ("needleman_wunsch_30k", szs.NeedlemanWunschScores(protein_b2c, protein_table, open=-11, extend=-1),

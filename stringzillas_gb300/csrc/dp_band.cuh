@@ -141,8 +141,9 @@ __device__ __forceinline__ void band_publish(band_ring_t const &ring, int slot, 
     }
 }
 
-/** Most CTAs one long pair can share, and the ring words of a group. */
-constexpr int band_group_max_ctas_k = 32;
+/** Most CTAs one long pair can share (enough for every 128-row strip of a 250,000-row pair to have its own warp, so
+ *  no warp sweeps a second strip after its first), and the ring words of a group. */
+constexpr int band_group_max_ctas_k = 256;
 constexpr int band_group_max_members_k = band_group_max_ctas_k * band_warps_k;
 
 /** One pass over a pair (16-bit or 32-bit cells): ring progress and the combined result. */

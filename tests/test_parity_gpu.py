@@ -399,8 +399,8 @@ def test_band_route_long_pairs(szs, port, family, costs):
 @pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 1, 1, 1)),
                                           ("lev", (0, 2, 3, 1)), ("sw", (-3, -3))])
 def test_grouped_band_few_long_pairs(szs, port, family, costs):
-    """One or a few long pairs: each gets a group of up to 32 CTAs (one cooperative launch) whose warps share the
-    strip ring through global memory. Pairs with fewer strips than the group has warps leave warps idle."""
+    """One or a few long pairs: each gets a group of CTAs (one cooperative launch) whose warps share the strip ring
+    through global memory. Pairs with fewer strips than the group has warps leave warps idle."""
     rng = np.random.default_rng(31)
     alphabet = PROTEIN if family == "nw" else DNA
     b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
@@ -412,6 +412,20 @@ def test_grouped_band_few_long_pairs(szs, port, family, costs):
         second[0] = first[0][: lengths[0][0] // 2] + second[0][lengths[0][0] // 2:]  # related: large local scores
         got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
         np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+
+
+@pytest.mark.parametrize("family,costs", [("nw", (-11, -1)), ("lev", (0, 2, 3, 3))])
+def test_grouped_band_more_strips_than_32_ctas_hold(szs, port, family, costs):
+    """One pair of 36,000 x 36,500 on 32-bit cells: 282 strips of 128 rows, so its group takes 36 CTAs (more than a
+    32-CTA group's 256 warps) and every strip has its own warp."""
+    rng = np.random.default_rng(53)
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    first = [bytes(rng.choice(alphabet, size=36000))]
+    second = [first[0][:18000] + bytes(rng.choice(alphabet, size=18500))]
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
 @pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 2, 3, 1))])
