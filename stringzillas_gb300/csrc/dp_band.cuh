@@ -37,7 +37,7 @@ namespace szs_gb300 {
 constexpr int band_warps_k = 8;
 constexpr int band_chunk_k = 32;                      // columns staged and published at a time
 
-template <int kind_, bool affine_, int rows_per_lane_>
+template <int kind_, bool affine_, int rows_per_lane_, int columns_per_step_ = 1>
 struct band_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -45,6 +45,7 @@ struct band_policy_t {
     static constexpr bool local_k = kind_ == kind_smith_waterman_k;
     static constexpr bool uniform_k = kind_ == kind_levenshtein_k;
     static constexpr int rows_per_lane_k = rows_per_lane_;
+    static constexpr int columns_k = columns_per_step_; // columns a lane scores per step of the sweep: 1 or 2
     static constexpr int strip_rows_k = warp_size_k * rows_per_lane_;
     static constexpr bool direct_k = false; // `direct_policy_t<>` reads costs from a dense table in shared memory
     static constexpr bool wide_k = false;   // `wide_policy_t<>`: strings of 16-bit codes
@@ -268,139 +269,308 @@ __device__ __forceinline__ std::int32_t band_score_warp(pair_task_t const &task,
         std::int32_t diag_up = edge.score(row0 - 1);
         int const result_lane = int((n - 1 - strip_base) / R), result_row = int((n - 1 - strip_base) % R);
 
-        std::uint32_t const steps = m + (std::uint32_t)last_lane;
         bool const write_bottom = !last_strip;
-        std::int32_t out_h = 0, out_f = 0;
-        std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
-        __syncwarp();
-        std::uint32_t p_now[words];
-        if constexpr (!policy_::uniform_k && !policy_::direct_k)
-            load_profile_words<R>(profile + (int)code_now * S + lane * R, p_now);
         bool healthy = true;
-
-        // One step of the sweep. `steady` steps are those where every lane is on a real column of a full strip
-        // (31 <= t < m, all 32 lanes hold rows): no range predicates and no corner capture.
-        auto step = [&](std::uint32_t t, auto steady_tag) {
-            constexpr bool steady = decltype(steady_tag)::value;
-            std::uint32_t const e = t & (band_chunk_k - 1);
-            if (e == 0) {
-                // Stage lane 0's next columns; strips below the first wait for the strip above to write them.
-                std::uint32_t const need = min(m, t + band_chunk_k);
-                if (k > 0 && t + 1 <= m) healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
-                __syncwarp();
-                for (int c = lane; c < band_chunk_k; c += 32) {
-                    std::uint32_t const j = t + 1 + c;
-                    std::int32_t h = 0, f = 0;
-                    if (j <= m) {
-                        if (k == 0) h = edge.score(j), f = gap_seed(j);
-                        else h = __ldcg(top + 2 * j), f = __ldcg(top + 2 * j + 1);
-                    }
-                    chunk.top_h[c] = h;
-                    chunk.top_f[c] = f;
-                    chunk.code[c] = j + 1 <= m ? column_code(j + 1) : 0u;
-                }
-                __syncwarp();
-                // The writer of the bottom row publishes its finished columns (it wrote column j at step j + 30).
-                if (write_bottom && lane == 31 && t > 31) {
-                    std::uint32_t const done = min(m, t - 31);
-                    band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | done);
-                }
-            }
-            std::int32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
-            std::int32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0;
-            std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
-            if (lane == 0) up_h = chunk.top_h[e], up_f = chunk.top_f[e], code_next = chunk.code[e];
-            [[maybe_unused]] std::uint32_t p_next[words]; // profile words (unused by uniform and direct instances)
+        if constexpr (policy_::columns_k == 1) {
+            std::uint32_t const steps = m + (std::uint32_t)last_lane;
+            std::int32_t out_h = 0, out_f = 0;
+            std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
+            __syncwarp();
+            std::uint32_t p_now[words];
             if constexpr (!policy_::uniform_k && !policy_::direct_k)
-                load_profile_words<R>(profile + (int)code_next * S + lane * R, p_next);
+                load_profile_words<R>(profile + (int)code_now * S + lane * R, p_now);
 
-            std::int64_t const j = (std::int64_t)t + 1 - lane;
-            if (steady || (j >= 1 && j <= (std::int64_t)m && lane <= last_lane)) {
-                std::int32_t diag = diag_up;
-                diag_up = up_h;
-                std::int32_t h_up = up_h, f_up = up_f;
-                std::int32_t subs[R];
+            // One step of the sweep. `steady` steps are those where every lane is on a real column of a full strip
+            // (31 <= t < m, all 32 lanes hold rows): no range predicates and no corner capture.
+            auto step = [&](std::uint32_t t, auto steady_tag) {
+                constexpr bool steady = decltype(steady_tag)::value;
+                std::uint32_t const e = t & (band_chunk_k - 1);
+                if (e == 0) {
+                    // Stage lane 0's next columns; strips below the first wait for the strip above to write them.
+                    std::uint32_t const need = min(m, t + band_chunk_k);
+                    if (k > 0 && t + 1 <= m) healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
+                    __syncwarp();
+                    for (int c = lane; c < band_chunk_k; c += 32) {
+                        std::uint32_t const j = t + 1 + c;
+                        std::int32_t h = 0, f = 0;
+                        if (j <= m) {
+                            if (k == 0) h = edge.score(j), f = gap_seed(j);
+                            else h = __ldcg(top + 2 * j), f = __ldcg(top + 2 * j + 1);
+                        }
+                        chunk.top_h[c] = h;
+                        chunk.top_f[c] = f;
+                        chunk.code[c] = j + 1 <= m ? column_code(j + 1) : 0u;
+                    }
+                    __syncwarp();
+                    // The writer of the bottom row publishes its finished columns (it wrote column j at step j + 30).
+                    if (write_bottom && lane == 31 && t > 31) {
+                        std::uint32_t const done = min(m, t - 31);
+                        band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | done);
+                    }
+                }
+                std::int32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
+                std::int32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0;
+                std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
+                if (lane == 0) up_h = chunk.top_h[e], up_f = chunk.top_f[e], code_next = chunk.code[e];
+                [[maybe_unused]] std::uint32_t p_next[words]; // profile words (unused by uniform and direct instances)
+                if constexpr (!policy_::uniform_k && !policy_::direct_k)
+                    load_profile_words<R>(profile + (int)code_next * S + lane * R, p_next);
+
+                std::int64_t const j = (std::int64_t)t + 1 - lane;
+                if (steady || (j >= 1 && j <= (std::int64_t)m && lane <= last_lane)) {
+                    std::int32_t diag = diag_up;
+                    diag_up = up_h;
+                    std::int32_t h_up = up_h, f_up = up_f;
+                    std::int32_t subs[R];
+                    if constexpr (policy_::uniform_k) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r) subs[r] = row_bytes[r] == code_now ? costs.match : costs.mismatch;
+                    }
+                    else if constexpr (policy_::direct_k) {
+                        // table[first byte][second byte]: rows are the first string unless the pair was transposed.
+                        std::uint32_t const column_key = task.transposed ? code_now << 8 : code_now;
+#pragma unroll
+                        for (int r = 0; r < R; ++r) subs[r] = table_s[row_bytes[r] | column_key];
+                    }
+                    else {
+#pragma unroll
+                        for (int w = 0; w < words; ++w) {
+                            // One byte permute per cost (the byte, its sign bit copied above it).
+                            subs[4 * w + 0] = signed_byte<0>(p_now[w]), subs[4 * w + 1] = signed_byte<1>(p_now[w]);
+                            subs[4 * w + 2] = signed_byte<2>(p_now[w]), subs[4 * w + 3] = signed_byte<3>(p_now[w]);
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        std::int32_t const substitution = diag + subs[r];
+                        std::int32_t h;
+                        if constexpr (affine && R == 4) {
+                            // Groups of CTAs per pair (4 rows per lane) are bound by each warp's step latency: the row
+                            // chain here is two fused add-max deep, at five of them per cell.
+                            std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
+                            std::int32_t const x = ops::add_opt(e_new, open, substitution);
+                            std::int32_t const via_f = ops::add_opt(f_up, extend_open, x);
+                            if constexpr (local) h = ops::add_opt_relu(h_up, open, via_f);
+                            else h = ops::add_opt(h_up, open, via_f);
+                            f_up = ops::add_opt(f_up, extend, h_up);
+                            e_col[r] = e_new;
+                        }
+                        else if constexpr (affine) {
+                            // CTAs per pair (8 rows per lane) fill the GPU and are bound by the integer ALU pipe: three
+                            // fused operations per cell, the adds of the gap opening and the substitution left to the
+                            // multiply-add pipe. e_col and f_up hold E and F minus the opening cost.
+                            std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
+                            std::int32_t const f_new = ops::add_opt(f_up, extend, h_up);
+                            if constexpr (local) h = ops::opt3_relu(substitution, e_new + open, f_new + open);
+                            else h = ops::opt3(substitution, e_new + open, f_new + open);
+                            f_up = f_new;
+                            e_col[r] = e_new;
+                        }
+                        else {
+                            std::int32_t const x = ops::add_opt(h_col[r], open, substitution);
+                            if constexpr (local) h = ops::add_opt_relu(h_up, open, x);
+                            else h = ops::add_opt(h_up, open, x);
+                        }
+                        diag = h_col[r];
+                        h_col[r] = h;
+                        h_up = h;
+                        if constexpr (local) best_row[r] = max(best_row[r], h);
+                    }
+                    out_h = h_up, out_f = f_up;
+                    if (write_bottom && lane == 31) {
+                        __stcg(bottom + 2 * j, out_h);
+                        __stcg(bottom + 2 * j + 1, out_f);
+                    }
+                    if constexpr (!local && !steady)
+                        if (last_strip && lane == result_lane && j == (std::int64_t)m) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == result_row) result = h_col[r];
+                        }
+                }
+                code_now = code_next;
+                if constexpr (!policy_::uniform_k && !policy_::direct_k) {
+#pragma unroll
+                    for (int w = 0; w < words; ++w) p_now[w] = p_next[w];
+                }
+            };
+
+            std::uint32_t const fill_end = min(steps, 31u);
+            std::uint32_t const steady_end = (last_lane == 31 && m >= 32u) ? max(fill_end, min(steps, m)) : fill_end;
+            std::uint32_t t = 0;
+            for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
+            // Two steps per iteration: the row state alternates between two register sets instead of being copied
+            // back.
+#pragma unroll 2
+            for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
+            for (; t < steps && healthy; ++t) step(t, std::false_type {});
+        }
+        else {
+            // Two columns per step: at step t lane l scores columns 2(t - l) + 1 and 2(t - l) + 2 of its R rows, so a
+            // shuffle, a profile lookup and the step's fixed work serve 2R cells, and the second column's cells run
+            // beside the first column's next row (the chain is R + 1 cells deep instead of 2R). A sweep takes
+            // ceil(m / 2) + 31 steps, and the strip below may start 48 steps behind (32 columns staged at a time).
+            constexpr std::uint32_t steps_per_chunk = band_chunk_k / 2;
+            std::uint32_t const column_pairs = (m + 1) / 2;
+            std::uint32_t const steps = column_pairs + (std::uint32_t)last_lane;
+            std::int32_t out_ha = 0, out_hb = 0, out_fa = 0, out_fb = 0;
+            // The codes of the lane's two current columns: column a in bits 0-15, column b in bits 16-31.
+            std::uint32_t codes_now = lane == 0 ? column_code(1) | (m >= 2 ? column_code(2) << 16 : 0u) : 0u;
+            __syncwarp();
+            std::uint32_t pa_now[words], pb_now[words];
+            if constexpr (!policy_::uniform_k && !policy_::direct_k) {
+                load_profile_words<R>(profile + (int)(codes_now & 0xFFFFu) * S + lane * R, pa_now);
+                load_profile_words<R>(profile + (int)(codes_now >> 16) * S + lane * R, pb_now);
+            }
+            auto substitutions = [&](std::uint32_t code, std::uint32_t const (&p)[words], std::int32_t (&subs)[R]) {
                 if constexpr (policy_::uniform_k) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) subs[r] = row_bytes[r] == code_now ? costs.match : costs.mismatch;
+                    for (int r = 0; r < R; ++r) subs[r] = row_bytes[r] == code ? costs.match : costs.mismatch;
                 }
                 else if constexpr (policy_::direct_k) {
-                    // table[first byte][second byte]: rows are the first string unless the pair was transposed.
-                    std::uint32_t const column_key = task.transposed ? code_now << 8 : code_now;
+                    std::uint32_t const column_key = task.transposed ? code << 8 : code;
 #pragma unroll
                     for (int r = 0; r < R; ++r) subs[r] = table_s[row_bytes[r] | column_key];
                 }
                 else {
 #pragma unroll
                     for (int w = 0; w < words; ++w) {
-                        // One byte permute per cost (the byte, its sign bit copied above it).
-                        subs[4 * w + 0] = signed_byte<0>(p_now[w]), subs[4 * w + 1] = signed_byte<1>(p_now[w]);
-                        subs[4 * w + 2] = signed_byte<2>(p_now[w]), subs[4 * w + 3] = signed_byte<3>(p_now[w]);
+                        subs[4 * w + 0] = signed_byte<0>(p[w]), subs[4 * w + 1] = signed_byte<1>(p[w]);
+                        subs[4 * w + 2] = signed_byte<2>(p[w]), subs[4 * w + 3] = signed_byte<3>(p[w]);
                     }
                 }
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    std::int32_t const substitution = diag + subs[r];
-                    std::int32_t h;
-                    if constexpr (affine && R == 4) {
-                        // Groups of CTAs per pair (4 rows per lane) are bound by each warp's step latency: the row
-                        // chain here is two fused add-max deep, at five of them per cell.
-                        std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
-                        std::int32_t const x = ops::add_opt(e_new, open, substitution);
-                        std::int32_t const via_f = ops::add_opt(f_up, extend_open, x);
-                        if constexpr (local) h = ops::add_opt_relu(h_up, open, via_f);
-                        else h = ops::add_opt(h_up, open, via_f);
-                        f_up = ops::add_opt(f_up, extend, h_up);
-                        e_col[r] = e_new;
-                    }
-                    else if constexpr (affine) {
-                        // CTAs per pair (8 rows per lane) fill the GPU and are bound by the integer ALU pipe: three
-                        // fused operations per cell, the adds of the gap opening and the substitution left to the
-                        // multiply-add pipe. e_col and f_up hold E and F minus the opening cost.
-                        std::int32_t const e_new = ops::add_opt(e_col[r], extend, h_col[r]);
-                        std::int32_t const f_new = ops::add_opt(f_up, extend, h_up);
-                        if constexpr (local) h = ops::opt3_relu(substitution, e_new + open, f_new + open);
-                        else h = ops::opt3(substitution, e_new + open, f_new + open);
-                        f_up = f_new;
-                        e_col[r] = e_new;
-                    }
-                    else {
-                        std::int32_t const x = ops::add_opt(h_col[r], open, substitution);
-                        if constexpr (local) h = ops::add_opt_relu(h_up, open, x);
-                        else h = ops::add_opt(h_up, open, x);
-                    }
-                    diag = h_col[r];
-                    h_col[r] = h;
-                    h_up = h;
-                    if constexpr (local) best_row[r] = max(best_row[r], h);
+            };
+            // One cell from its left (H, and E as E - open), its upper H and F - open (updated for the cell below)
+            // and its substitution score; the forms are those of the one-column sweep.
+            auto cell = [&](std::int32_t left_h, std::int32_t &e, std::int32_t up_h, std::int32_t &f_up,
+                            std::int32_t substitution) -> std::int32_t {
+                std::int32_t h;
+                if constexpr (affine && R == 4) {
+                    std::int32_t const e_new = ops::add_opt(e, extend, left_h);
+                    std::int32_t const x = ops::add_opt(e_new, open, substitution);
+                    std::int32_t const via_f = ops::add_opt(f_up, extend_open, x);
+                    if constexpr (local) h = ops::add_opt_relu(up_h, open, via_f);
+                    else h = ops::add_opt(up_h, open, via_f);
+                    f_up = ops::add_opt(f_up, extend, up_h);
+                    e = e_new;
                 }
-                out_h = h_up, out_f = f_up;
-                if (write_bottom && lane == 31) {
-                    __stcg(bottom + 2 * j, out_h);
-                    __stcg(bottom + 2 * j + 1, out_f);
+                else if constexpr (affine) {
+                    std::int32_t const e_new = ops::add_opt(e, extend, left_h);
+                    std::int32_t const f_new = ops::add_opt(f_up, extend, up_h);
+                    if constexpr (local) h = ops::opt3_relu(substitution, e_new + open, f_new + open);
+                    else h = ops::opt3(substitution, e_new + open, f_new + open);
+                    f_up = f_new;
+                    e = e_new;
                 }
-                if constexpr (!local && !steady)
-                    if (last_strip && lane == result_lane && j == (std::int64_t)m) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if (r == result_row) result = h_col[r];
-                    }
-            }
-            code_now = code_next;
-            if constexpr (!policy_::uniform_k && !policy_::direct_k) {
-#pragma unroll
-                for (int w = 0; w < words; ++w) p_now[w] = p_next[w];
-            }
-        };
+                else {
+                    std::int32_t const x = ops::add_opt(left_h, open, substitution);
+                    if constexpr (local) h = ops::add_opt_relu(up_h, open, x);
+                    else h = ops::add_opt(up_h, open, x);
+                }
+                return h;
+            };
 
-        std::uint32_t const fill_end = min(steps, 31u);
-        std::uint32_t const steady_end = (last_lane == 31 && m >= 32u) ? max(fill_end, min(steps, m)) : fill_end;
-        std::uint32_t t = 0;
-        for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
-        // Two steps per iteration: the row state alternates between two register sets instead of being copied back.
+            auto step = [&](std::uint32_t t, auto steady_tag) {
+                constexpr bool steady = decltype(steady_tag)::value;
+                std::uint32_t const e = t & (steps_per_chunk - 1);
+                if (e == 0) {
+                    // Stage lane 0's next 32 columns; strips below the first wait for the strip above to write them.
+                    std::uint32_t const first_column = 2 * t + 1;
+                    std::uint32_t const need = min(m, 2 * t + band_chunk_k);
+                    if (k > 0 && first_column <= m)
+                        healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
+                    __syncwarp();
+                    for (int c = lane; c < band_chunk_k; c += 32) {
+                        std::uint32_t const j = first_column + c;
+                        std::int32_t h = 0, f = 0;
+                        if (j <= m) {
+                            if (k == 0) h = edge.score(j), f = gap_seed(j);
+                            else {
+                                int2 const cell_hf = __ldcg(reinterpret_cast<int2 const *>(top) + j);
+                                h = cell_hf.x, f = cell_hf.y;
+                            }
+                        }
+                        chunk.top_h[c] = h;
+                        chunk.top_f[c] = f;
+                        chunk.code[c] = j + 2 <= m ? column_code(j + 2) : 0u; // lane 0's codes one step ahead
+                    }
+                    __syncwarp();
+                    // The writer of the bottom row publishes its finished columns (before step t: up to 2(t - 31)).
+                    if (write_bottom && lane == 31 && t > 31) {
+                        std::uint32_t const done = min(m, 2 * (t - 31));
+                        band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | done);
+                    }
+                }
+                std::int32_t up_ha = __shfl_up_sync(0xFFFFFFFFu, out_ha, 1);
+                std::int32_t up_hb = __shfl_up_sync(0xFFFFFFFFu, out_hb, 1);
+                std::int32_t up_fa = affine ? __shfl_up_sync(0xFFFFFFFFu, out_fa, 1) : 0;
+                std::int32_t up_fb = affine ? __shfl_up_sync(0xFFFFFFFFu, out_fb, 1) : 0;
+                std::uint32_t codes_next = __shfl_up_sync(0xFFFFFFFFu, codes_now, 1);
+                if (lane == 0) {
+                    up_ha = chunk.top_h[2 * e], up_hb = chunk.top_h[2 * e + 1];
+                    up_fa = chunk.top_f[2 * e], up_fb = chunk.top_f[2 * e + 1];
+                    codes_next = chunk.code[2 * e] | chunk.code[2 * e + 1] << 16;
+                }
+                [[maybe_unused]] std::uint32_t pa_next[words], pb_next[words];
+                if constexpr (!policy_::uniform_k && !policy_::direct_k) {
+                    load_profile_words<R>(profile + (int)(codes_next & 0xFFFFu) * S + lane * R, pa_next);
+                    load_profile_words<R>(profile + (int)(codes_next >> 16) * S + lane * R, pb_next);
+                }
+
+                std::int64_t const ja = 2 * ((std::int64_t)t - lane) + 1;
+                if (steady || (ja >= 1 && ja <= (std::int64_t)m && lane <= last_lane)) {
+                    bool const valid_b = steady || ja + 1 <= (std::int64_t)m;
+                    std::int32_t diag_a = diag_up, diag_b = up_ha;
+                    diag_up = up_hb;
+                    std::int32_t h_up_a = up_ha, h_up_b = up_hb, f_up_a = up_fa, f_up_b = up_fb;
+                    std::int32_t subs_a[R], subs_b[R];
+                    substitutions(codes_now & 0xFFFFu, pa_now, subs_a);
+                    substitutions(codes_now >> 16, pb_now, subs_b);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        std::int32_t e_left = e_col[r];
+                        std::int32_t const h_a = cell(h_col[r], e_left, h_up_a, f_up_a, diag_a + subs_a[r]);
+                        std::int32_t const h_b = cell(h_a, e_left, h_up_b, f_up_b, diag_b + subs_b[r]);
+                        diag_a = h_col[r];
+                        diag_b = h_a;
+                        h_col[r] = h_b;
+                        e_col[r] = e_left;
+                        h_up_a = h_a;
+                        h_up_b = h_b;
+                        if constexpr (local) {
+                            best_row[r] = max(best_row[r], h_a);
+                            if (valid_b) best_row[r] = max(best_row[r], h_b);
+                        }
+                        if constexpr (!local && !steady)
+                            if (last_strip && lane == result_lane && r == result_row) {
+                                if (ja == (std::int64_t)m) result = h_a;
+                                if (ja + 1 == (std::int64_t)m) result = h_b;
+                            }
+                    }
+                    out_ha = h_up_a, out_hb = h_up_b, out_fa = f_up_a, out_fb = f_up_b;
+                    if (write_bottom && lane == 31) {
+                        __stcg(reinterpret_cast<int2 *>(bottom) + ja, make_int2(out_ha, out_fa));
+                        if (valid_b) __stcg(reinterpret_cast<int2 *>(bottom) + ja + 1, make_int2(out_hb, out_fb));
+                    }
+                }
+                codes_now = codes_next;
+                if constexpr (!policy_::uniform_k && !policy_::direct_k) {
+#pragma unroll
+                    for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
+                }
+            };
+
+            // Steady steps: lane 31 on column pair >= 0 (t >= 31) and lane 0's second column within the pair
+            // (2t + 2 <= m), all 32 lanes holding rows.
+            std::uint32_t const fill_end = min(steps, 31u);
+            std::uint32_t const steady_end =
+                (last_lane == 31 && m / 2 > 31u) ? max(fill_end, min(steps, m / 2)) : fill_end;
+            std::uint32_t t = 0;
+            for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
 #pragma unroll 2
-        for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
-        for (; t < steps && healthy; ++t) step(t, std::false_type {});
+            for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
+            for (; t < steps && healthy; ++t) step(t, std::false_type {});
+        }
         __syncwarp();
         if (write_bottom && lane == 31) band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | m);
         if constexpr (local) {

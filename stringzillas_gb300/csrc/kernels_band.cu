@@ -16,8 +16,9 @@ namespace {
 #endif
 constexpr int band_rows_per_lane_k = SZS_BAND_ROWS;
 
+// Groups of CTAs per pair (the 4-row build) are bound by each warp's step latency: they take two columns per step.
 template <int kind_, bool affine_>
-using band_instance_t = band_policy_t<kind_, affine_, band_rows_per_lane_k>;
+using band_instance_t = band_policy_t<kind_, affine_, band_rows_per_lane_k, band_rows_per_lane_k == 4 ? 2 : 1>;
 
 /** The instance for (direct table, 16-bit codes): at most one of the two. */
 template <int kind_, bool affine_, bool direct_, bool wide_>

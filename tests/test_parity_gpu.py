@@ -428,6 +428,52 @@ def test_grouped_band_more_strips_than_32_ctas_hold(szs, port, family, costs):
     np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
 
 
+@pytest.mark.parametrize("family,costs", [("lev", (0, 2, 3, 1)), ("lev", (0, 2, 3, 3)), ("nw", (-11, -1)),
+                                          ("nw", (-4, -4)), ("sw", (-5, -2)), ("sw", (-3, -3))])
+def test_grouped_band_two_columns_per_step(szs, port, family, costs):
+    """Groups of CTAs on 4-row strips score two columns per lane-step: odd and even column counts (the last step's
+    second column past the end), the corner in either column, related pairs (large local scores), both orientations,
+    one pair alone and three at once. 32-bit cells are forced so that local scores take the 32-bit band too."""
+    rng = np.random.default_rng(zlib_seed(f"two-columns{family}{costs}"))
+    alphabet = PROTEIN if family == "nw" else DNA
+    b2c, table = protein_tables(rng) if family == "nw" else dna_tables()
+    engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
+    engine.set_tuning({"cell_bits": [32] * 16})
+    for lengths in ([(5001, 6001)], [(6003, 4097)], [(3001, 3003), (2999, 7002), (4000, 4001)], [(7000, 7000)]):
+        first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
+        second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
+        half = min(lengths[0]) // 2
+        second[0] = first[0][:half] + second[0][half:]
+        got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+        np.testing.assert_array_equal(got, port.pairs(oracle_costs, tape(first), tape(second)))
+    engine.set_tuning(None)
+
+
+@pytest.mark.parametrize("case", ["dense-nw-affine", "dense-sw-linear", "utf8-wide"])
+def test_grouped_band_two_columns_dense_and_wide(szs, port, case):
+    """The two-column sweep over a dense 256 x 256 table (every byte value) and over 16-bit codes (UTF-8 with more
+    than 256 code points), one long pair with an odd number of columns, against the oracle."""
+    rng = np.random.default_rng(zlib_seed(case))
+    if case.startswith("dense"):
+        family, costs = ("nw", (-11, -1)) if case == "dense-nw-affine" else ("sw", (-3, -3))
+        cls = szs.NeedlemanWunschScores if family == "nw" else szs.SmithWatermanScores
+        kind = oracle.NEEDLEMAN_WUNSCH if family == "nw" else oracle.SMITH_WATERMAN
+        table = rng.integers(-9, 10, size=(256, 256)).astype(np.int8)
+        engine = cls.dense(table, open=costs[0], extend=costs[1])
+        want_costs = oracle.dense_costs(kind, table, *costs)
+        everything = np.arange(256, dtype=np.uint8)
+        first, second = [bytes(rng.choice(everything, size=2601))], [bytes(rng.choice(everything, size=3001))]
+    else:
+        letters = [chr(c) for c in range(0x4E00, 0x4E00 + 3000)]
+        first = ["".join(rng.choice(letters, size=4001))]
+        second = [first[0][:2000] + "".join(rng.choice(letters, size=3001))]
+        engine = szs.LevenshteinDistancesUTF8(0, 2, 3, 1)
+        want_costs = oracle.levenshtein_utf8_costs(0, 2, 3, 1)
+        engine.set_tuning({"cell_bits": [32] * 16})
+    got = engine.pairwise(szs.Strs(first), szs.Strs(second)).astype(np.int64)
+    np.testing.assert_array_equal(got, port.pairs(want_costs, tape(first), tape(second)))
+
+
 @pytest.mark.parametrize("family,costs", [("sw", (-5, -2)), ("nw", (-11, -1)), ("lev", (0, 2, 3, 1))])
 def test_grouped_band_beside_small_launches(szs, port, family, costs):
     """A cooperative grouped-band launch queued behind small launches that take a few CTA slots first (grids that
