@@ -30,7 +30,8 @@ namespace szs_gb300 {
 
 /** `compare_`: Levenshtein over more than 32 byte values, costs from comparing codes (`compare_mode_t`); `wide_`
  *  (compare modes only): strings of 16-bit codes. */
-template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k, bool wide_ = false>
+template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k, bool wide_ = false,
+          int columns_per_step_ = 1>
 struct band16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -42,6 +43,7 @@ struct band16_policy_t {
     static constexpr bool compare_k = compare_ != compare_none_k;
     static constexpr bool multiply_k = compare_ == compare_multiply_k;
     static constexpr bool wide_k = wide_;
+    static constexpr int columns_k = columns_per_step_; // columns each half of a lane scores per step: 1 or 2
     static_assert(!compare_k || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
     static_assert(!wide_ || compare_k, "16-bit codes have no profile");
 };
@@ -158,71 +160,174 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
         int const capture_lane = last_strip ? (v_n & 31) : -1;
         bool const capture_hi = v_n >= 32;
 
-        std::uint32_t const steps = m + (std::uint32_t)last_vlane;
         bool const bottom_writer = !last_strip && lane == 31;
-        std::uint32_t out_h = 0, out_f = 0;
-        std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
-        __syncwarp();
-        [[maybe_unused]] std::uint32_t p_lo[words], p_hi[words]; // profile words (unused in compare mode)
-        if constexpr (!compare) {
-            load_profile_words<R>(profile_lo + (code_now & 0xFF) * S + lane_rows, p_lo);
-            load_profile_words<R>(profile_hi + ((code_now >> 8) & 0xFF) * S + lane_rows, p_hi);
-        }
         bool healthy = true;
-
-        // `steady`: every lane's two columns are real and below m (63 <= t < m - 1): no masks, no capture.
-        auto step = [&](std::uint32_t t, auto steady_tag) {
-            constexpr bool steady = decltype(steady_tag)::value;
-            std::uint32_t const e = t & (band16_chunk_k - 1);
-            if (e == 0) {
-                // The strip above must have published the columns staged now; this strip publishes its own.
-                std::uint32_t const need = min(m, t + band16_chunk_k);
-                if (k > 0 && t + 1 <= m) healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
-                if (bottom_writer && t > 63)
-                    band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | min(m, t - 63));
-                __syncwarp();
-#pragma unroll
-                for (int c = lane; c < band16_chunk_k; c += 32) {
-                    std::uint32_t const j = t + 1 + c;
-                    std::uint32_t word = 0;
-                    if (j <= m) {
-                        if (k == 0) word = pack16(edge.score(j) + h_shift, gap_seed(j));
-                        else word = __ldcg(top + j);
-                    }
-                    chunk.top[c] = word;
-                    chunk.code[c] = j + 1 <= m ? column_code(j + 1) : 0u;
-                }
-                __syncwarp();
-            }
-            std::uint32_t const staged_top = chunk.top[e], staged_code = chunk.code[e];
-            std::uint32_t up_h = __shfl_sync(0xFFFFFFFFu, out_h, from_lane);
-            std::uint32_t up_f = affine ? __shfl_sync(0xFFFFFFFFu, out_f, from_lane) : 0u;
-            std::uint32_t code_next = __shfl_sync(0xFFFFFFFFu, code_now, from_lane);
-            if (lane == 0) {
-                // Low half: the strip's top row; high half: lane 31's low half (the row just above).
-                up_h = __byte_perm(staged_top, up_h, 0x5410);
-                up_f = __byte_perm(staged_top, up_f, 0x5432);
-                // Codes: the low half's in byte 0 and the high half's in byte 1 (profiles; the staged codes are below
-                // 256, so their byte 1 is a zero byte), or in bits 0-15 and 16-31 (compare mode).
-                code_next = __byte_perm(staged_code, code_next, compare ? 0x5410 : 0x1140);
-            }
-            [[maybe_unused]] std::uint32_t q_lo[words], q_hi[words];
+        if constexpr (policy_::columns_k == 1) {
+            std::uint32_t const steps = m + (std::uint32_t)last_vlane;
+            std::uint32_t out_h = 0, out_f = 0;
+            std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
+            __syncwarp();
+            [[maybe_unused]] std::uint32_t p_lo[words], p_hi[words]; // profile words (unused in compare mode)
             if constexpr (!compare) {
-                load_profile_words<R>(profile_lo + (code_next & 0xFF) * S + lane_rows, q_lo);
-                load_profile_words<R>(profile_hi + ((code_next >> 8) & 0xFF) * S + lane_rows, q_hi);
+                load_profile_words<R>(profile_lo + (code_now & 0xFF) * S + lane_rows, p_lo);
+                load_profile_words<R>(profile_hi + ((code_now >> 8) & 0xFF) * S + lane_rows, p_hi);
             }
 
-            int const j_lo = (int)t + 1 - lane, j_hi = j_lo - 32;
-            // Low half past m, high half not yet started: a lane with neither real column skips the update.
-            bool const active = steady || (j_lo >= 1 && j_hi <= (int)m);
-            if (active) {
-                // A high half that has not reached column 1 keeps its column-0 state (blended back below).
-                std::uint32_t const keep = (steady || j_hi >= 1) ? 0u : 0xFFFF0000u;
-                std::uint32_t diag = diag_up;
-                diag_up = steady ? up_h : ((up_h & ~keep) | (diag_up & keep));
-                std::uint32_t h_up = up_h, f_up = up_f;
-                std::uint32_t subs[R], cell_h[R];
-                if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code_now, subs);
+            // `steady`: every lane's two columns are real and below m (63 <= t < m - 1): no masks, no capture.
+            auto step = [&](std::uint32_t t, auto steady_tag) {
+                constexpr bool steady = decltype(steady_tag)::value;
+                std::uint32_t const e = t & (band16_chunk_k - 1);
+                if (e == 0) {
+                    // The strip above must have published the columns staged now; this strip publishes its own.
+                    std::uint32_t const need = min(m, t + band16_chunk_k);
+                    if (k > 0 && t + 1 <= m) healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
+                    if (bottom_writer && t > 63)
+                        band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | min(m, t - 63));
+                    __syncwarp();
+#pragma unroll
+                    for (int c = lane; c < band16_chunk_k; c += 32) {
+                        std::uint32_t const j = t + 1 + c;
+                        std::uint32_t word = 0;
+                        if (j <= m) {
+                            if (k == 0) word = pack16(edge.score(j) + h_shift, gap_seed(j));
+                            else word = __ldcg(top + j);
+                        }
+                        chunk.top[c] = word;
+                        chunk.code[c] = j + 1 <= m ? column_code(j + 1) : 0u;
+                    }
+                    __syncwarp();
+                }
+                std::uint32_t const staged_top = chunk.top[e], staged_code = chunk.code[e];
+                std::uint32_t up_h = __shfl_sync(0xFFFFFFFFu, out_h, from_lane);
+                std::uint32_t up_f = affine ? __shfl_sync(0xFFFFFFFFu, out_f, from_lane) : 0u;
+                std::uint32_t code_next = __shfl_sync(0xFFFFFFFFu, code_now, from_lane);
+                if (lane == 0) {
+                    // Low half: the strip's top row; high half: lane 31's low half (the row just above).
+                    up_h = __byte_perm(staged_top, up_h, 0x5410);
+                    up_f = __byte_perm(staged_top, up_f, 0x5432);
+                    // Codes: the low half's in byte 0 and the high half's in byte 1 (profiles; the staged codes are
+                    // below 256, so their byte 1 is a zero byte), or in bits 0-15 and 16-31 (compare mode).
+                    code_next = __byte_perm(staged_code, code_next, compare ? 0x5410 : 0x1140);
+                }
+                [[maybe_unused]] std::uint32_t q_lo[words], q_hi[words];
+                if constexpr (!compare) {
+                    load_profile_words<R>(profile_lo + (code_next & 0xFF) * S + lane_rows, q_lo);
+                    load_profile_words<R>(profile_hi + ((code_next >> 8) & 0xFF) * S + lane_rows, q_hi);
+                }
+
+                int const j_lo = (int)t + 1 - lane, j_hi = j_lo - 32;
+                // Low half past m, high half not yet started: a lane with neither real column skips the update.
+                bool const active = steady || (j_lo >= 1 && j_hi <= (int)m);
+                if (active) {
+                    // A high half that has not reached column 1 keeps its column-0 state (blended back below).
+                    std::uint32_t const keep = (steady || j_hi >= 1) ? 0u : 0xFFFF0000u;
+                    std::uint32_t diag = diag_up;
+                    diag_up = steady ? up_h : ((up_h & ~keep) | (diag_up & keep));
+                    std::uint32_t h_up = up_h, f_up = up_f;
+                    std::uint32_t subs[R], cell_h[R];
+                    if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code_now, subs);
+                    else {
+#pragma unroll
+                        for (int w = 0; w < words; ++w) {
+                            subs[4 * w + 0] = interleave_signed_bytes<0>(p_lo[w], p_hi[w]);
+                            subs[4 * w + 1] = interleave_signed_bytes<1>(p_lo[w], p_hi[w]);
+                            subs[4 * w + 2] = interleave_signed_bytes<2>(p_lo[w], p_hi[w]);
+                            subs[4 * w + 3] = interleave_signed_bytes<3>(p_lo[w], p_hi[w]);
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        std::uint32_t h, kept;
+                        [[maybe_unused]] std::uint32_t e_new = 0; // affine tracks only
+                        if constexpr (affine) {
+                            e_new = ops::add_opt(e_col[r], extend2, h_col[r]);
+                            std::uint32_t const x = ops::add_opt(diag, subs[r], e_new);
+                            f_up = ops::add_opt(f_up, extend2, h_up);
+                            h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
+                            kept = ops::add(h, open2);
+                        }
+                        else {
+                            std::uint32_t const substitution = ops::add(diag, subs[r]);
+                            std::uint32_t const x = ops::add_opt(h_col[r], open2, substitution);
+                            if constexpr (local) h = ops::add_opt_relu(h_up, open2, x);
+                            else h = ops::add_opt(h_up, open2, x);
+                            kept = h;
+                        }
+                        cell_h[r] = h;
+                        diag = h_col[r];
+                        if constexpr (steady) {
+                            h_col[r] = kept;
+                            if constexpr (affine) e_col[r] = e_new;
+                        }
+                        else {
+                            h_col[r] = (kept & ~keep) | (h_col[r] & keep);
+                            if constexpr (affine) e_col[r] = (e_new & ~keep) | (e_col[r] & keep);
+                        }
+                        h_up = kept;
+                    }
+                    if constexpr (local) {
+                        if constexpr (steady) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r], 0u);
+                        }
+                        else {
+                            std::uint32_t const mask = ((j_lo >= 1 && j_lo <= (int)m) ? 0x0000FFFFu : 0u) |
+                                                       ((j_hi >= 1 && j_hi <= (int)m) ? 0xFFFF0000u : 0u);
+#pragma unroll
+                            for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r] & mask, 0u);
+                        }
+                    }
+                    else if constexpr (!steady) {
+                        if (lane == capture_lane && (capture_hi ? j_hi : j_lo) == (int)m) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == r_n) result = capture_hi ? high16(cell_h[r]) : low16(cell_h[r]);
+                        }
+                    }
+                    out_h = h_up, out_f = f_up;
+                    if (bottom_writer && (steady || (j_hi >= 1 && j_hi <= (int)m)))
+                        __stcg(bottom + j_hi, __byte_perm(out_h, out_f, 0x7632));
+                }
+                code_now = code_next;
+                if constexpr (!compare) {
+#pragma unroll
+                    for (int w = 0; w < words; ++w) p_lo[w] = q_lo[w], p_hi[w] = q_hi[w];
+                }
+            };
+
+            std::uint32_t const fill_end = min(steps, 63u);
+            std::uint32_t const steady_end = m >= 64u ? max(fill_end, min(steps, m - 1u)) : fill_end;
+            std::uint32_t t = 0;
+            for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
+            // Two steps per iteration: the row state alternates between two register sets instead of being copied
+            // back.
+#pragma unroll 2
+            for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
+            for (; t < steps && healthy; ++t) step(t, std::false_type {});
+        }
+        else {
+            // Two columns per step: at step t the low half of lane l scores columns 2(t - l) + 1 and 2(t - l) + 2, its
+            // high half the pair 32 steps (64 columns) behind; as in the 32-bit band, a round of shuffles and the
+            // step's fixed work serve twice the cells and the second column's cells run beside the first column's
+            // next row. A sweep takes ceil(m / 2) + 63 steps; staging stays 64 columns (32 steps) at a time.
+            constexpr std::uint32_t steps_per_chunk = band16_chunk_k / 2;
+            std::uint32_t const column_pairs = (m + 1) / 2;
+            std::uint32_t const steps = column_pairs + (std::uint32_t)last_vlane;
+            std::uint32_t out_ha = 0, out_hb = 0, out_fa = 0, out_fb = 0;
+            // Each column's codes as in the one-column sweep (low half in byte 0 or bits 0-15, high half above).
+            std::uint32_t code_a = lane == 0 ? column_code(1) : 0u;
+            std::uint32_t code_b = lane == 0 && m >= 2 ? column_code(2) : 0u;
+            __syncwarp();
+            [[maybe_unused]] std::uint32_t pa_lo[words], pa_hi[words], pb_lo[words], pb_hi[words];
+            if constexpr (!compare) {
+                load_profile_words<R>(profile_lo + (code_a & 0xFF) * S + lane_rows, pa_lo);
+                load_profile_words<R>(profile_hi + ((code_a >> 8) & 0xFF) * S + lane_rows, pa_hi);
+                load_profile_words<R>(profile_lo + (code_b & 0xFF) * S + lane_rows, pb_lo);
+                load_profile_words<R>(profile_hi + ((code_b >> 8) & 0xFF) * S + lane_rows, pb_hi);
+            }
+            auto substitutions = [&](std::uint32_t code, std::uint32_t const (&p_lo)[words],
+                                     std::uint32_t const (&p_hi)[words], std::uint32_t (&subs)[R]) {
+                if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code, subs);
                 else {
 #pragma unroll
                     for (int w = 0; w < words; ++w) {
@@ -232,74 +337,161 @@ __device__ __forceinline__ std::int32_t band16_score_warp(pair_task_t const &tas
                         subs[4 * w + 3] = interleave_signed_bytes<3>(p_lo[w], p_hi[w]);
                     }
                 }
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    std::uint32_t h, kept;
-                    [[maybe_unused]] std::uint32_t e_new = 0; // affine tracks only
-                    if constexpr (affine) {
-                        e_new = ops::add_opt(e_col[r], extend2, h_col[r]);
-                        std::uint32_t const x = ops::add_opt(diag, subs[r], e_new);
-                        f_up = ops::add_opt(f_up, extend2, h_up);
-                        h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
-                        kept = ops::add(h, open2);
-                    }
-                    else {
-                        std::uint32_t const substitution = ops::add(diag, subs[r]);
-                        std::uint32_t const x = ops::add_opt(h_col[r], open2, substitution);
-                        if constexpr (local) h = ops::add_opt_relu(h_up, open2, x);
-                        else h = ops::add_opt(h_up, open2, x);
-                        kept = h;
-                    }
-                    cell_h[r] = h;
-                    diag = h_col[r];
-                    if constexpr (steady) {
-                        h_col[r] = kept;
-                        if constexpr (affine) e_col[r] = e_new;
-                    }
-                    else {
-                        h_col[r] = (kept & ~keep) | (h_col[r] & keep);
-                        if constexpr (affine) e_col[r] = (e_new & ~keep) | (e_col[r] & keep);
-                    }
-                    h_up = kept;
+            };
+            // One packed cell pair: returns H and sets `kept` (H + open for affine tracks, else H), updating E
+            // (from its left) and F (for the cell below) as the one-column sweep does.
+            auto cell = [&](std::uint32_t diag, std::uint32_t left_kept, std::uint32_t &e, std::uint32_t up_kept,
+                            std::uint32_t &f_up, std::uint32_t substitution, std::uint32_t &kept) -> std::uint32_t {
+                std::uint32_t h;
+                if constexpr (affine) {
+                    e = ops::add_opt(e, extend2, left_kept);
+                    std::uint32_t const x = ops::add_opt(diag, substitution, e);
+                    f_up = ops::add_opt(f_up, extend2, up_kept);
+                    h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
+                    kept = ops::add(h, open2);
                 }
-                if constexpr (local) {
-                    if constexpr (steady) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r], 0u);
-                    }
-                    else {
-                        std::uint32_t const mask = ((j_lo >= 1 && j_lo <= (int)m) ? 0x0000FFFFu : 0u) |
-                                                   ((j_hi >= 1 && j_hi <= (int)m) ? 0xFFFF0000u : 0u);
-#pragma unroll
-                        for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r] & mask, 0u);
-                    }
+                else {
+                    std::uint32_t const x = ops::add_opt(left_kept, open2, ops::add(diag, substitution));
+                    if constexpr (local) h = ops::add_opt_relu(up_kept, open2, x);
+                    else h = ops::add_opt(up_kept, open2, x);
+                    kept = h;
                 }
-                else if constexpr (!steady) {
-                    if (lane == capture_lane && (capture_hi ? j_hi : j_lo) == (int)m) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if (r == r_n) result = capture_hi ? high16(cell_h[r]) : low16(cell_h[r]);
-                    }
-                }
-                out_h = h_up, out_f = f_up;
-                if (bottom_writer && (steady || (j_hi >= 1 && j_hi <= (int)m)))
-                    __stcg(bottom + j_hi, __byte_perm(out_h, out_f, 0x7632));
-            }
-            code_now = code_next;
-            if constexpr (!compare) {
-#pragma unroll
-                for (int w = 0; w < words; ++w) p_lo[w] = q_lo[w], p_hi[w] = q_hi[w];
-            }
-        };
+                return h;
+            };
 
-        std::uint32_t const fill_end = min(steps, 63u);
-        std::uint32_t const steady_end = m >= 64u ? max(fill_end, min(steps, m - 1u)) : fill_end;
-        std::uint32_t t = 0;
-        for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
-        // Two steps per iteration: the row state alternates between two register sets instead of being copied back.
+            // `steady`: every lane's four columns are real and below m (63 <= t, 2t + 2 < m): no masks, no capture.
+            auto step = [&](std::uint32_t t, auto steady_tag) {
+                constexpr bool steady = decltype(steady_tag)::value;
+                std::uint32_t const e = t & (steps_per_chunk - 1);
+                if (e == 0) {
+                    // The strip above must have published the columns staged now; this strip publishes its own
+                    // (before step t its last lane's high half has finished columns up to 2(t - 63)).
+                    std::uint32_t const first_column = 2 * t + 1;
+                    std::uint32_t const need = min(m, 2 * t + band16_chunk_k);
+                    if (k > 0 && first_column <= m)
+                        healthy = band_wait(sync, slot_in, ((unsigned long long)k << 32) | need);
+                    if (bottom_writer && t > 63)
+                        band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | min(m, 2 * (t - 63)));
+                    __syncwarp();
+#pragma unroll
+                    for (int c = lane; c < band16_chunk_k; c += 32) {
+                        std::uint32_t const j = first_column + c;
+                        std::uint32_t word = 0;
+                        if (j <= m) {
+                            if (k == 0) word = pack16(edge.score(j) + h_shift, gap_seed(j));
+                            else word = __ldcg(top + j);
+                        }
+                        chunk.top[c] = word;
+                        chunk.code[c] = j + 2 <= m ? column_code(j + 2) : 0u; // lane 0's codes one step ahead
+                    }
+                    __syncwarp();
+                }
+                std::uint32_t const staged_top_a = chunk.top[2 * e], staged_top_b = chunk.top[2 * e + 1];
+                std::uint32_t const staged_code_a = chunk.code[2 * e], staged_code_b = chunk.code[2 * e + 1];
+                std::uint32_t up_ha = __shfl_sync(0xFFFFFFFFu, out_ha, from_lane);
+                std::uint32_t up_hb = __shfl_sync(0xFFFFFFFFu, out_hb, from_lane);
+                std::uint32_t up_fa = affine ? __shfl_sync(0xFFFFFFFFu, out_fa, from_lane) : 0u;
+                std::uint32_t up_fb = affine ? __shfl_sync(0xFFFFFFFFu, out_fb, from_lane) : 0u;
+                std::uint32_t next_a = __shfl_sync(0xFFFFFFFFu, code_a, from_lane);
+                std::uint32_t next_b = __shfl_sync(0xFFFFFFFFu, code_b, from_lane);
+                if (lane == 0) {
+                    // Low half: the strip's top row; high half: lane 31's low half (the row just above).
+                    up_ha = __byte_perm(staged_top_a, up_ha, 0x5410);
+                    up_hb = __byte_perm(staged_top_b, up_hb, 0x5410);
+                    up_fa = __byte_perm(staged_top_a, up_fa, 0x5432);
+                    up_fb = __byte_perm(staged_top_b, up_fb, 0x5432);
+                    next_a = __byte_perm(staged_code_a, next_a, compare ? 0x5410 : 0x1140);
+                    next_b = __byte_perm(staged_code_b, next_b, compare ? 0x5410 : 0x1140);
+                }
+                [[maybe_unused]] std::uint32_t qa_lo[words], qa_hi[words], qb_lo[words], qb_hi[words];
+                if constexpr (!compare) {
+                    load_profile_words<R>(profile_lo + (next_a & 0xFF) * S + lane_rows, qa_lo);
+                    load_profile_words<R>(profile_hi + ((next_a >> 8) & 0xFF) * S + lane_rows, qa_hi);
+                    load_profile_words<R>(profile_lo + (next_b & 0xFF) * S + lane_rows, qb_lo);
+                    load_profile_words<R>(profile_hi + ((next_b >> 8) & 0xFF) * S + lane_rows, qb_hi);
+                }
+
+                int const ja_lo = 2 * ((int)t - lane) + 1, ja_hi = ja_lo - 64;
+                // Low half past m, high half not yet started: a lane with neither real column skips the update.
+                bool const active = steady || (ja_lo >= 1 && ja_hi <= (int)m);
+                if (active) {
+                    // A high half that has not reached column 1 keeps its column-0 state (blended back below).
+                    std::uint32_t const keep = (steady || ja_hi >= 1) ? 0u : 0xFFFF0000u;
+                    std::uint32_t diag_a = diag_up, diag_b = up_ha;
+                    diag_up = steady ? up_hb : ((up_hb & ~keep) | (diag_up & keep));
+                    std::uint32_t h_up_a = up_ha, h_up_b = up_hb, f_up_a = up_fa, f_up_b = up_fb;
+                    std::uint32_t subs_a[R], subs_b[R], cell_a[R], cell_b[R];
+                    substitutions(code_a, pa_lo, pa_hi, subs_a);
+                    substitutions(code_b, pb_lo, pb_hi, subs_b);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        std::uint32_t e_left = e_col[r], kept_a, kept_b;
+                        cell_a[r] = cell(diag_a, h_col[r], e_left, h_up_a, f_up_a, subs_a[r], kept_a);
+                        cell_b[r] = cell(diag_b, kept_a, e_left, h_up_b, f_up_b, subs_b[r], kept_b);
+                        diag_a = h_col[r];
+                        diag_b = kept_a;
+                        if constexpr (steady) {
+                            h_col[r] = kept_b;
+                            if constexpr (affine) e_col[r] = e_left;
+                        }
+                        else {
+                            h_col[r] = (kept_b & ~keep) | (h_col[r] & keep);
+                            if constexpr (affine) e_col[r] = (e_left & ~keep) | (e_col[r] & keep);
+                        }
+                        h_up_a = kept_a;
+                        h_up_b = kept_b;
+                    }
+                    if constexpr (local) {
+                        if constexpr (steady) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_a[r], cell_b[r]);
+                        }
+                        else {
+                            auto half_mask = [&](int j_lo, int j_hi) {
+                                return ((j_lo >= 1 && j_lo <= (int)m) ? 0x0000FFFFu : 0u) |
+                                       ((j_hi >= 1 && j_hi <= (int)m) ? 0xFFFF0000u : 0u);
+                            };
+                            std::uint32_t const mask_a = half_mask(ja_lo, ja_hi);
+                            std::uint32_t const mask_b = half_mask(ja_lo + 1, ja_hi + 1);
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                best_row[r] = __vimax3_s16x2(best_row[r], cell_a[r] & mask_a, cell_b[r] & mask_b);
+                        }
+                    }
+                    else if constexpr (!steady) {
+                        int const ja = capture_hi ? ja_hi : ja_lo;
+                        if (lane == capture_lane && (ja == (int)m || ja + 1 == (int)m)) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == r_n) {
+                                    std::uint32_t const cell_m = ja == (int)m ? cell_a[r] : cell_b[r];
+                                    result = capture_hi ? high16(cell_m) : low16(cell_m);
+                                }
+                        }
+                    }
+                    out_ha = h_up_a, out_hb = h_up_b, out_fa = f_up_a, out_fb = f_up_b;
+                    if (bottom_writer && (steady || (ja_hi >= 1 && ja_hi <= (int)m))) {
+                        __stcg(bottom + ja_hi, __byte_perm(out_ha, out_fa, 0x7632));
+                        if (steady || ja_hi + 1 <= (int)m)
+                            __stcg(bottom + ja_hi + 1, __byte_perm(out_hb, out_fb, 0x7632));
+                    }
+                }
+                code_a = next_a, code_b = next_b;
+                if constexpr (!compare) {
+#pragma unroll
+                    for (int w = 0; w < words; ++w)
+                        pa_lo[w] = qa_lo[w], pa_hi[w] = qa_hi[w], pb_lo[w] = qb_lo[w], pb_hi[w] = qb_hi[w];
+                }
+            };
+
+            std::uint32_t const fill_end = min(steps, 63u);
+            std::uint32_t const steady_end = m / 2 > 64u ? max(fill_end, min(steps, m / 2 - 1u)) : fill_end;
+            std::uint32_t t = 0;
+            for (; t < fill_end && healthy; ++t) step(t, std::false_type {});
 #pragma unroll 2
-        for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
-        for (; t < steps && healthy; ++t) step(t, std::false_type {});
+            for (; t < steady_end && healthy; ++t) step(t, std::true_type {});
+            for (; t < steps && healthy; ++t) step(t, std::false_type {});
+        }
         __syncwarp();
         if (bottom_writer) band_publish(sync, slot_out, ((unsigned long long)(k + 1) << 32) | m);
         if constexpr (local) {

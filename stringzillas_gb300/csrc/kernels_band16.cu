@@ -14,9 +14,14 @@ namespace {
 #error "compile with -DSZS_BAND16_ROWS=<8|4>"
 #endif
 constexpr int band16_rows_per_lane_k = SZS_BAND16_ROWS;
+#ifndef SZS_BAND16_COLUMNS
+#define SZS_BAND16_COLUMNS 2
+#endif
+constexpr int band16_columns_k = SZS_BAND16_COLUMNS; // columns each half of a lane scores per step
 
 template <int kind_, bool affine_, int compare_ = compare_none_k, bool wide_ = false>
-using band16_instance_t = band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_, wide_>;
+using band16_instance_t =
+    band16_policy_t<kind_, affine_, band16_rows_per_lane_k, compare_, wide_, band16_columns_k>;
 
 template <int kind_, bool affine_, int compare_ = compare_none_k, bool wide_ = false>
 dp_launch_shape_t band16_shape_of(int classes) {

@@ -405,7 +405,7 @@ def test_grouped_band_few_long_pairs(szs, port, family, costs):
     alphabet = PROTEIN if family == "nw" else DNA
     b2c, table = (protein_tables(rng) if family == "nw" else dna_tables())
     engine, oracle_costs = make_engine(szs, family, costs, b2c, table)
-    for lengths in ([(6000, 7000)], [(1100, 20000)], [(3000, 3000), (2500, 9000), (1200, 1300)],
+    for lengths in ([(6000, 7000)], [(5001, 7001)], [(1100, 20000)], [(3000, 3000), (2500, 9000), (1200, 1301)],
                     [(1030, 1030)] * 2 + [(4000, 4100)]):
         first = [bytes(rng.choice(alphabet, size=n)) for n, _ in lengths]
         second = [bytes(rng.choice(alphabet, size=m)) for _, m in lengths]
