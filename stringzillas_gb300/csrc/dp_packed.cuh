@@ -39,7 +39,8 @@ namespace szs_gb300 {
 /** `compare_`: a `compare_mode_t` (engine_types.cuh); other than `compare_none_k`, Levenshtein over more than 32 byte
  *  values with costs from comparing codes instead of profiles. `wide_` (compare modes only): strings of 16-bit codes
  *  (UTF-8 calls over more than 256 code points), compared as they are. */
-template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k, bool wide_ = false>
+template <int kind_, bool affine_, int rows_per_lane_, int compare_ = compare_none_k, bool wide_ = false,
+          int columns_per_step_ = 1>
 struct dp16_policy_t {
     static constexpr int kind_k = kind_;
     static constexpr bool affine_k = affine_;
@@ -50,6 +51,7 @@ struct dp16_policy_t {
     static constexpr bool compare_k = compare_ != compare_none_k;
     static constexpr bool multiply_k = compare_ == compare_multiply_k;
     static constexpr bool wide_k = wide_;
+    static constexpr int columns_k = columns_per_step_; // columns a lane scores per step: 1 or 2
     static_assert(!compare_k || kind_ == kind_levenshtein_k, "only Levenshtein costs are a function of equality");
     static_assert(!wide_ || compare_k, "16-bit codes have no profile");
 };
@@ -297,142 +299,319 @@ __device__ __forceinline__ void dp16_score_couple(pair_task_t const &a, pair_tas
         int const b_lane = b_ends_here ? int((n_b - 1 - strip_base) / R) : -1;
         int const a_row = int((n_a - 1 - strip_base) % R), b_row = int((n_b - 1 - strip_base) % R);
 
-        std::uint32_t const steps = m_max + (std::uint32_t)last_lane;
         bool const write_bottom = !last_strip;
         bool const bottom_writer = write_bottom && lane == 31;
-        std::uint32_t out_h = 0, out_f = 0;
-        std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
-        __syncwarp();
-        [[maybe_unused]] std::uint32_t pa_now[words], pb_now[words]; // profile words (unused in compare mode)
-        if constexpr (!compare) {
-            load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
-            load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
-        }
         int const lane_rows = lane * R;
+        if constexpr (policy_::columns_k == 1) {
+            std::uint32_t const steps = m_max + (std::uint32_t)last_lane;
+            std::uint32_t out_h = 0, out_f = 0;
+            std::uint32_t code_now = lane == 0 ? column_code(1) : 0u;
+            __syncwarp();
+            [[maybe_unused]] std::uint32_t pa_now[words], pb_now[words]; // profile words (unused in compare mode)
+            if constexpr (!compare) {
+                load_profile_words<R>(profile_a + (code_now & 0xFF) * S + lane * R, pa_now);
+                load_profile_words<R>(profile_b + (code_now >> 8) * S + lane * R, pb_now);
+            }
 
-        // One step of the sweep. `steady` steps are those where every lane is on a real column below both pairs'
-        // ends (31 <= t < m_min - 1): no range predicates, no masks, no result capture.
-        auto step = [&](std::uint32_t t, auto steady_tag) {
-            constexpr bool steady = decltype(steady_tag)::value;
-            std::uint32_t const e = t & (chunk_columns_k - 1);
-            if (e == 0) {
-                // Stage lane 0's next 64 top-boundary values (columns t+1..) and codes (columns t+2..).
-                __syncwarp();
+            // One step of the sweep. `steady` steps are those where every lane is on a real column below both pairs'
+            // ends (31 <= t < m_min - 1): no range predicates, no masks, no result capture.
+            auto step = [&](std::uint32_t t, auto steady_tag) {
+                constexpr bool steady = decltype(steady_tag)::value;
+                std::uint32_t const e = t & (chunk_columns_k - 1);
+                if (e == 0) {
+                    // Stage lane 0's next 64 top-boundary values (columns t+1..) and codes (columns t+2..).
+                    __syncwarp();
 #pragma unroll
-                for (int k = lane; k < chunk_columns_k; k += 32) {
-                    std::uint32_t const j = t + 1 + k;
-                    std::uint32_t h = 0, f = 0;
-                    if (j <= m_max) {
-                        if (strip_base == 0) {
-                            std::int32_t const v = edge.score(j) + h_shift, g = gap_seed(j);
-                            h = pack16(v, v), f = pack16(g, g);
+                    for (int k = lane; k < chunk_columns_k; k += 32) {
+                        std::uint32_t const j = t + 1 + k;
+                        std::uint32_t h = 0, f = 0;
+                        if (j <= m_max) {
+                            if (strip_base == 0) {
+                                std::int32_t const v = edge.score(j) + h_shift, g = gap_seed(j);
+                                h = pack16(v, v), f = pack16(g, g);
+                            }
+                            else {
+                                uint2 const stored = *reinterpret_cast<uint2 const *>(scratch + 2 * j);
+                                h = stored.x, f = stored.y;
+                            }
                         }
-                        else {
-                            uint2 const stored = *reinterpret_cast<uint2 const *>(scratch + 2 * j);
-                            h = stored.x, f = stored.y;
+                        chunk.top_h[k] = h;
+                        chunk.top_f[k] = f;
+                        chunk.code[k] = j + 1 <= m_max ? column_code(j + 1) : 0u;
+                    }
+                    __syncwarp();
+                }
+                std::uint32_t const staged_h = chunk.top_h[e], staged_f = chunk.top_f[e], staged_code = chunk.code[e];
+                std::uint32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
+                std::uint32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0u;
+                std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
+                if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
+                [[maybe_unused]] std::uint32_t pa_next[words], pb_next[words];
+                if constexpr (!compare) {
+                    load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane_rows, pa_next);
+                    load_profile_words<R>(profile_b + (code_next >> 8) * S + lane_rows, pb_next);
+                }
+
+                int const j = (int)t + 1 - lane;
+                bool const active = steady || (j >= 1 && j <= (int)m_max && lane <= last_lane);
+                if (active) {
+                    std::uint32_t diag = diag_up;
+                    diag_up = up_h;
+                    std::uint32_t h_up = up_h, f_up = up_f;
+                    std::uint32_t subs[R], cell_h[R];
+                    if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code_now, subs);
+                    else {
+#pragma unroll
+                        for (int w = 0; w < words; ++w) {
+                            subs[4 * w + 0] = interleave_signed_bytes<0>(pa_now[w], pb_now[w]);
+                            subs[4 * w + 1] = interleave_signed_bytes<1>(pa_now[w], pb_now[w]);
+                            subs[4 * w + 2] = interleave_signed_bytes<2>(pa_now[w], pb_now[w]);
+                            subs[4 * w + 3] = interleave_signed_bytes<3>(pa_now[w], pb_now[w]);
                         }
                     }
-                    chunk.top_h[k] = h;
-                    chunk.top_f[k] = f;
-                    chunk.code[k] = j + 1 <= m_max ? column_code(j + 1) : 0u;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        std::uint32_t h, kept;
+                        if constexpr (affine) {
+                            // h_col, h_up and diag hold Ĥ = H + open; e_col and f_up hold E and F.
+                            // E = max(E + ext, H + open); x = max(H_diag + s, E); F = max(F + ext, H + open).
+                            std::uint32_t const e_new = ops::add_opt(e_col[r], extend2, h_col[r]);
+                            std::uint32_t const x = ops::add_opt(diag, subs[r], e_new);
+                            f_up = ops::add_opt(f_up, extend2, h_up);
+                            h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
+                            kept = ops::add(h, open2);
+                            e_col[r] = e_new;
+                        }
+                        else {
+                            std::uint32_t const substitution = ops::add(diag, subs[r]);
+                            std::uint32_t const x = ops::add_opt(h_col[r], open2, substitution);
+                            if constexpr (local) h = ops::add_opt_relu(h_up, open2, x);
+                            else h = ops::add_opt(h_up, open2, x);
+                            kept = h;
+                        }
+                        cell_h[r] = h;
+                        diag = h_col[r];
+                        h_col[r] = kept;
+                        h_up = kept;
+                    }
+                    if constexpr (local) {
+                        if constexpr (steady) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r], 0u);
+                        }
+                        else {
+                            // Columns past one pair's end carry filler in that half: mask it out of the maxima
+                            // (H >= 0).
+                            std::uint32_t const mask = j <= (int)m_min ? 0xFFFFFFFFu
+                                                                       : ((j <= (int)m_a ? 0x0000FFFFu : 0u) |
+                                                                          (j <= (int)m_b ? 0xFFFF0000u : 0u));
+#pragma unroll
+                            for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r] & mask, 0u);
+                        }
+                    }
+                    else if constexpr (!steady) {
+                        if (lane == a_lane && j == (int)m_a) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == a_row) result_a = low16(cell_h[r]);
+                        }
+                        if (lane == b_lane && j == (int)m_b) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == b_row) result_b = high16(cell_h[r]);
+                        }
+                    }
+                    out_h = h_up, out_f = f_up;
+                    if (bottom_writer) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
                 }
-                __syncwarp();
-            }
-            std::uint32_t const staged_h = chunk.top_h[e], staged_f = chunk.top_f[e], staged_code = chunk.code[e];
-            std::uint32_t up_h = __shfl_up_sync(0xFFFFFFFFu, out_h, 1);
-            std::uint32_t up_f = affine ? __shfl_up_sync(0xFFFFFFFFu, out_f, 1) : 0u;
-            std::uint32_t code_next = __shfl_up_sync(0xFFFFFFFFu, code_now, 1);
-            if (lane == 0) up_h = staged_h, up_f = staged_f, code_next = staged_code;
-            [[maybe_unused]] std::uint32_t pa_next[words], pb_next[words];
-            if constexpr (!compare) {
-                load_profile_words<R>(profile_a + (code_next & 0xFF) * S + lane_rows, pa_next);
-                load_profile_words<R>(profile_b + (code_next >> 8) * S + lane_rows, pb_next);
-            }
+                code_now = code_next;
+                if constexpr (!compare) {
+#pragma unroll
+                    for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
+                }
+            };
 
-            int const j = (int)t + 1 - lane;
-            bool const active = steady || (j >= 1 && j <= (int)m_max && lane <= last_lane);
-            if (active) {
-                std::uint32_t diag = diag_up;
-                diag_up = up_h;
-                std::uint32_t h_up = up_h, f_up = up_f;
-                std::uint32_t subs[R], cell_h[R];
-                if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code_now, subs);
+            std::uint32_t const fill_end = min(steps, 31u);
+            std::uint32_t const steady_end = m_min >= 1u + 31u ? max(fill_end, m_min - 1u) : fill_end;
+            std::uint32_t t = 0;
+            for (; t < fill_end; ++t) step(t, std::false_type {});
+#pragma unroll 2
+            for (; t < steady_end; ++t) step(t, std::true_type {});
+            for (; t < steps; ++t) step(t, std::false_type {});
+        }
+        else {
+            // Two columns per step: at step t lane l scores columns 2(t - l) + 1 and 2(t - l) + 2 of both pairs, so a
+            // round of shuffles, the code words, the profile lookups and the step's fixed work serve twice the
+            // cells, and the second column's cells run beside the first column's next row. A strip takes
+            // ceil(m_max / 2) + last lane steps; staging stays 64 columns (32 steps) at a time.
+            constexpr std::uint32_t steps_per_chunk = chunk_columns_k / 2;
+            std::uint32_t const steps = (m_max + 1) / 2 + (std::uint32_t)last_lane;
+            std::uint32_t out_ha = 0, out_hb = 0, out_fa = 0, out_fb = 0;
+            std::uint32_t code_a = lane == 0 ? column_code(1) : 0u; // both pairs' codes of the lane's two columns
+            std::uint32_t code_b = lane == 0 && m_max >= 2 ? column_code(2) : 0u;
+            __syncwarp();
+            [[maybe_unused]] std::uint32_t pa_a[words], pb_a[words], pa_b[words], pb_b[words]; // pair, column
+            if constexpr (!compare) {
+                load_profile_words<R>(profile_a + (code_a & 0xFF) * S + lane_rows, pa_a);
+                load_profile_words<R>(profile_b + (code_a >> 8) * S + lane_rows, pb_a);
+                load_profile_words<R>(profile_a + (code_b & 0xFF) * S + lane_rows, pa_b);
+                load_profile_words<R>(profile_b + (code_b >> 8) * S + lane_rows, pb_b);
+            }
+            auto substitutions = [&](std::uint32_t code, std::uint32_t const (&p_a)[words],
+                                     std::uint32_t const (&p_b)[words], std::uint32_t (&subs)[R]) {
+                if constexpr (compare) compared.rows<policy_::multiply_k>(row_codes, code, subs);
                 else {
 #pragma unroll
                     for (int w = 0; w < words; ++w) {
-                        subs[4 * w + 0] = interleave_signed_bytes<0>(pa_now[w], pb_now[w]);
-                        subs[4 * w + 1] = interleave_signed_bytes<1>(pa_now[w], pb_now[w]);
-                        subs[4 * w + 2] = interleave_signed_bytes<2>(pa_now[w], pb_now[w]);
-                        subs[4 * w + 3] = interleave_signed_bytes<3>(pa_now[w], pb_now[w]);
+                        subs[4 * w + 0] = interleave_signed_bytes<0>(p_a[w], p_b[w]);
+                        subs[4 * w + 1] = interleave_signed_bytes<1>(p_a[w], p_b[w]);
+                        subs[4 * w + 2] = interleave_signed_bytes<2>(p_a[w], p_b[w]);
+                        subs[4 * w + 3] = interleave_signed_bytes<3>(p_a[w], p_b[w]);
                     }
                 }
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    std::uint32_t h, kept;
-                    if constexpr (affine) {
-                        // h_col, h_up and diag hold Ĥ = H + open; e_col and f_up hold E and F.
-                        std::uint32_t const e_new = ops::add_opt(e_col[r], extend2, h_col[r]); // max(E + ext, H + open)
-                        std::uint32_t const x = ops::add_opt(diag, subs[r], e_new);            // max(H_diag + s, E)
-                        f_up = ops::add_opt(f_up, extend2, h_up);                              // max(F + ext, H + open)
-                        h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
-                        kept = ops::add(h, open2);
-                        e_col[r] = e_new;
-                    }
-                    else {
-                        std::uint32_t const substitution = ops::add(diag, subs[r]);
-                        std::uint32_t const x = ops::add_opt(h_col[r], open2, substitution);
-                        if constexpr (local) h = ops::add_opt_relu(h_up, open2, x);
-                        else h = ops::add_opt(h_up, open2, x);
-                        kept = h;
-                    }
-                    cell_h[r] = h;
-                    diag = h_col[r];
-                    h_col[r] = kept;
-                    h_up = kept;
+            };
+            // One packed cell pair as in the one-column sweep: returns H, sets `kept` (Ĥ for affine tracks, else H)
+            // and updates E (from the left) and F (for the cell below).
+            auto cell = [&](std::uint32_t diag, std::uint32_t left_kept, std::uint32_t &e, std::uint32_t up_kept,
+                            std::uint32_t &f_up, std::uint32_t substitution, std::uint32_t &kept) -> std::uint32_t {
+                std::uint32_t h;
+                if constexpr (affine) {
+                    e = ops::add_opt(e, extend2, left_kept);
+                    std::uint32_t const x = ops::add_opt(diag, substitution, e);
+                    f_up = ops::add_opt(f_up, extend2, up_kept);
+                    h = local ? ops::opt2_relu(x, f_up) : ops::opt2(x, f_up);
+                    kept = ops::add(h, open2);
                 }
-                if constexpr (local) {
-                    if constexpr (steady) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r], 0u);
-                    }
-                    else {
-                        // Columns past one pair's end carry filler in that half: mask it out of the maxima (H >= 0).
-                        std::uint32_t const mask = j <= (int)m_min ? 0xFFFFFFFFu
-                                                                   : ((j <= (int)m_a ? 0x0000FFFFu : 0u) |
-                                                                      (j <= (int)m_b ? 0xFFFF0000u : 0u));
-#pragma unroll
-                        for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_h[r] & mask, 0u);
-                    }
+                else {
+                    std::uint32_t const x = ops::add_opt(left_kept, open2, ops::add(diag, substitution));
+                    if constexpr (local) h = ops::add_opt_relu(up_kept, open2, x);
+                    else h = ops::add_opt(up_kept, open2, x);
+                    kept = h;
                 }
-                else if constexpr (!steady) {
-                    if (lane == a_lane && j == (int)m_a) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if (r == a_row) result_a = low16(cell_h[r]);
-                    }
-                    if (lane == b_lane && j == (int)m_b) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if (r == b_row) result_b = high16(cell_h[r]);
-                    }
-                }
-                out_h = h_up, out_f = f_up;
-                if (bottom_writer) *reinterpret_cast<uint2 *>(scratch + 2 * j) = make_uint2(out_h, out_f);
-            }
-            code_now = code_next;
-            if constexpr (!compare) {
-#pragma unroll
-                for (int w = 0; w < words; ++w) pa_now[w] = pa_next[w], pb_now[w] = pb_next[w];
-            }
-        };
+                return h;
+            };
 
-        std::uint32_t const fill_end = min(steps, 31u);
-        std::uint32_t const steady_end = m_min >= 1u + 31u ? max(fill_end, m_min - 1u) : fill_end;
-        std::uint32_t t = 0;
-        for (; t < fill_end; ++t) step(t, std::false_type {});
+            // `steady`: every lane's two columns are real and below both pairs' ends (31 <= t, 2t + 2 < m_min).
+            auto step = [&](std::uint32_t t, auto steady_tag) {
+                constexpr bool steady = decltype(steady_tag)::value;
+                std::uint32_t const e = t & (steps_per_chunk - 1);
+                if (e == 0) {
+                    // Stage lane 0's next 64 top-boundary values (columns 2t + 1..) and codes (columns 2t + 3..).
+                    __syncwarp();
+#pragma unroll
+                    for (int k = lane; k < chunk_columns_k; k += 32) {
+                        std::uint32_t const j = 2 * t + 1 + k;
+                        std::uint32_t h = 0, f = 0;
+                        if (j <= m_max) {
+                            if (strip_base == 0) {
+                                std::int32_t const v = edge.score(j) + h_shift, g = gap_seed(j);
+                                h = pack16(v, v), f = pack16(g, g);
+                            }
+                            else {
+                                uint2 const stored = *reinterpret_cast<uint2 const *>(scratch + 2 * j);
+                                h = stored.x, f = stored.y;
+                            }
+                        }
+                        chunk.top_h[k] = h;
+                        chunk.top_f[k] = f;
+                        chunk.code[k] = j + 2 <= m_max ? column_code(j + 2) : 0u;
+                    }
+                    __syncwarp();
+                }
+                std::uint32_t up_ha = __shfl_up_sync(0xFFFFFFFFu, out_ha, 1);
+                std::uint32_t up_hb = __shfl_up_sync(0xFFFFFFFFu, out_hb, 1);
+                std::uint32_t up_fa = affine ? __shfl_up_sync(0xFFFFFFFFu, out_fa, 1) : 0u;
+                std::uint32_t up_fb = affine ? __shfl_up_sync(0xFFFFFFFFu, out_fb, 1) : 0u;
+                std::uint32_t next_a = __shfl_up_sync(0xFFFFFFFFu, code_a, 1);
+                std::uint32_t next_b = __shfl_up_sync(0xFFFFFFFFu, code_b, 1);
+                if (lane == 0) {
+                    up_ha = chunk.top_h[2 * e], up_hb = chunk.top_h[2 * e + 1];
+                    up_fa = chunk.top_f[2 * e], up_fb = chunk.top_f[2 * e + 1];
+                    next_a = chunk.code[2 * e], next_b = chunk.code[2 * e + 1];
+                }
+                [[maybe_unused]] std::uint32_t qa_a[words], qb_a[words], qa_b[words], qb_b[words];
+                if constexpr (!compare) {
+                    load_profile_words<R>(profile_a + (next_a & 0xFF) * S + lane_rows, qa_a);
+                    load_profile_words<R>(profile_b + (next_a >> 8) * S + lane_rows, qb_a);
+                    load_profile_words<R>(profile_a + (next_b & 0xFF) * S + lane_rows, qa_b);
+                    load_profile_words<R>(profile_b + (next_b >> 8) * S + lane_rows, qb_b);
+                }
+
+                int const ja = 2 * ((int)t - lane) + 1;
+                bool const active = steady || (ja >= 1 && ja <= (int)m_max && lane <= last_lane);
+                if (active) {
+                    std::uint32_t diag_a = diag_up, diag_b = up_ha;
+                    diag_up = up_hb;
+                    std::uint32_t h_up_a = up_ha, h_up_b = up_hb, f_up_a = up_fa, f_up_b = up_fb;
+                    std::uint32_t subs_a[R], subs_b[R], cell_a[R], cell_b[R];
+                    substitutions(code_a, pa_a, pb_a, subs_a);
+                    substitutions(code_b, pa_b, pb_b, subs_b);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        std::uint32_t e_left = e_col[r], kept_a, kept_b;
+                        cell_a[r] = cell(diag_a, h_col[r], e_left, h_up_a, f_up_a, subs_a[r], kept_a);
+                        cell_b[r] = cell(diag_b, kept_a, e_left, h_up_b, f_up_b, subs_b[r], kept_b);
+                        diag_a = h_col[r];
+                        diag_b = kept_a;
+                        h_col[r] = kept_b;
+                        if constexpr (affine) e_col[r] = e_left;
+                        h_up_a = kept_a;
+                        h_up_b = kept_b;
+                    }
+                    if constexpr (local) {
+                        if constexpr (steady) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r) best_row[r] = __vimax3_s16x2(best_row[r], cell_a[r], cell_b[r]);
+                        }
+                        else {
+                            // Columns past one pair's end carry filler in that half: masked out of the maxima.
+                            auto half_mask = [&](int j) {
+                                return j <= (int)m_min ? 0xFFFFFFFFu
+                                                       : ((j <= (int)m_a ? 0x0000FFFFu : 0u) |
+                                                          (j <= (int)m_b ? 0xFFFF0000u : 0u));
+                            };
+                            std::uint32_t const mask_a = half_mask(ja), mask_b = half_mask(ja + 1);
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                best_row[r] = __vimax3_s16x2(best_row[r], cell_a[r] & mask_a, cell_b[r] & mask_b);
+                        }
+                    }
+                    else if constexpr (!steady) {
+                        if (lane == a_lane && (ja == (int)m_a || ja + 1 == (int)m_a)) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == a_row) result_a = low16(ja == (int)m_a ? cell_a[r] : cell_b[r]);
+                        }
+                        if (lane == b_lane && (ja == (int)m_b || ja + 1 == (int)m_b)) {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r == b_row) result_b = high16(ja == (int)m_b ? cell_a[r] : cell_b[r]);
+                        }
+                    }
+                    out_ha = h_up_a, out_hb = h_up_b, out_fa = f_up_a, out_fb = f_up_b;
+                    if (bottom_writer) {
+                        *reinterpret_cast<uint2 *>(scratch + 2 * ja) = make_uint2(out_ha, out_fa);
+                        if (steady || ja + 1 <= (int)m_max)
+                            *reinterpret_cast<uint2 *>(scratch + 2 * (ja + 1)) = make_uint2(out_hb, out_fb);
+                    }
+                }
+                code_a = next_a, code_b = next_b;
+                if constexpr (!compare) {
+#pragma unroll
+                    for (int w = 0; w < words; ++w)
+                        pa_a[w] = qa_a[w], pb_a[w] = qb_a[w], pa_b[w] = qa_b[w], pb_b[w] = qb_b[w];
+                }
+            };
+
+            std::uint32_t const fill_end = min(steps, 31u);
+            std::uint32_t const steady_end =
+                m_min >= 1u && (m_min - 1u) / 2u > 31u ? max(fill_end, (m_min - 1u) / 2u) : fill_end;
+            std::uint32_t t = 0;
+            for (; t < fill_end; ++t) step(t, std::false_type {});
 #pragma unroll 2
-        for (; t < steady_end; ++t) step(t, std::true_type {});
-        for (; t < steps; ++t) step(t, std::false_type {});
+            for (; t < steady_end; ++t) step(t, std::true_type {});
+            for (; t < steps; ++t) step(t, std::false_type {});
+        }
         if constexpr (local) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {

@@ -13,9 +13,15 @@ namespace szs_gb300 {
 
 namespace {
 
+// 8 rows per lane (the planner's choice for longer pairs) take two columns per step. 4 rows (short pairs) keep one:
+// with two, the 31 steps by which lane 31 trails lane 0 would idle twice the columns of a short sweep (a cross
+// product of 100-byte strings ran 6 % slower). 12 and 16 rows have no registers to spare.
+template <int kind_, bool affine_, int rows_, int compare_, bool wide_>
+using dp16_instance_t = dp16_policy_t<kind_, affine_, rows_, compare_, wide_, rows_ == 8 ? 2 : 1>;
+
 template <int kind_, bool affine_, int rows_, int compare_, bool wide_>
 dp_launch_shape_t dp16_shape_rows(int classes, int warps) {
-    using policy_t = dp16_policy_t<kind_, affine_, rows_, compare_, wide_>;
+    using policy_t = dp16_instance_t<kind_, affine_, rows_, compare_, wide_>;
     dp_launch_shape_t shape;
     shape.threads_per_cta = warps * 32;
     shape.warps_per_cta = warps;
@@ -46,7 +52,7 @@ template <int kind_, bool affine_, int rows_, int compare_, bool wide_>
 cudaError_t dp16_launch_rows(int key_begin, int key_end, pair_task_t const *tasks, plan_bins_t *bins,
                              score_costs_t const &costs, std::int64_t *results, void *scratch,
                              std::size_t scratch_cells_per_warp, int ctas, int warps, cudaStream_t stream) {
-    using policy_t = dp16_policy_t<kind_, affine_, rows_, compare_, wide_>;
+    using policy_t = dp16_instance_t<kind_, affine_, rows_, compare_, wide_>;
     int const shared = dp16_shared_bytes<policy_t>(warps, costs.classes);
     auto kernel = dp16_wavefront_kernel<policy_t>;
     cudaError_t status = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared);
