@@ -1,4 +1,5 @@
-"""Model check of the band kernels' ring protocol (csrc/dp_band.cuh, csrc/dp_band16.cuh), run on the CPU.
+"""Model check of the band kernels' ring protocol (csrc/dp_band.cuh, csrc/dp_band16.cuh) and of the chain of
+warps' hand-over (csrc/myers_chain.cuh), run on the CPU.
 
 Strips of one pair go round a ring of W warps (strip k on member k mod W, each member sweeping its strips in order).
 A strip writes its bottom row into ring slot k mod W and publishes how many columns it has written; the strip below
@@ -32,7 +33,6 @@ class Strip:
         self.k, self.m, self.skew, self.columns, self.chunk = k, m, skew, columns, chunk
         self.steps = (m + columns - 1) // columns + last_skew
         self.t = 0
-        self.done = False
 
     def staged(self, t):
         """Columns lane 0 stages at step t (a chunk boundary): the chunk starting at its current column."""
@@ -128,3 +128,39 @@ def test_two_columns_shorten_the_ring(variant):
     one_column = play(4000, 24, 24, variant.replace("two-columns", "one-column"))
     if columns == 2:
         assert ticks < 0.7 * one_column
+
+
+def play_chain(m, warps):
+    """The chain of warps (0-based columns): warp k's lane 31 writes the byte of column j = t - 31 at step t and
+    publishes j + 1 after each 32nd column and after the last; at every 32nd step t < m warp k + 1 waits until
+    min(m, t + 32) columns are published, then its lanes read columns t .. t + 31. All warps are resident."""
+    steps = m + 31
+    t = [0] * warps
+    published = [0] * warps
+    written = [set() for _ in range(warps)]
+    while min(t) < steps:
+        progressed = False
+        for k in range(warps):
+            if t[k] >= steps:
+                continue
+            step = t[k]
+            if step % 32 == 0 and k > 0 and step < m:
+                if published[k - 1] < min(m, step + 32):
+                    continue
+                for column in range(step, min(m, step + 32)):
+                    assert column in written[k - 1], (m, warps, k, step, column)
+            j = step - 31
+            if k + 1 < warps and 0 <= j < m:
+                written[k].add(j)
+                if j % 32 == 31 or j + 1 == m:
+                    assert all(c in written[k] for c in range(j + 1))
+                    published[k] = j + 1
+            t[k] += 1
+            progressed = True
+        assert progressed, f"chain stalled: m={m} warps={warps}"
+
+
+@pytest.mark.parametrize("m", [1, 2, 31, 32, 33, 63, 64, 65, 100, 257])
+def test_chain_protocol(m):
+    for warps in (1, 2, 3, 7):
+        play_chain(m, warps)
